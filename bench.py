@@ -1,0 +1,352 @@
+#!/usr/bin/env python3
+"""Benchmark of the EMC hot path on GB300.
+
+Workload (one "step" = one EMC time step of every particle): bulk silicon,
+three paired Delta valleys (m_l 0.916, m_t 0.19, alpha 0.5 /eV), acoustic
+(9 eV) + 3 g + 3 f zero-order intervalley phonons, T = 300 K, field 1e6 V/m
+along <100>, dt = 1 fs, N = 2^20 electrons, 5000 steps; FP32 particle state,
+FP64 observable sums.  Synthetic data (Maxwellian initial electrons).
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl engine|reference]
+
+Prints one JSON line.  --impl reference times the reference's CPU algorithm
+(the oracle port, bit-identical to the reference on the golden vectors) on the
+host cores for the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s, FP32-batched vs plain GPU at ≤1% v_d error; Poisson ms/solve"
+UNIT = "particle-steps/s"
+BYTES_PER_PARTICLE_STEP = {"fp32": 72, "fp64": 136}  # state read + written once
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def reduce_over_ranks(ms: float, units: float, ws: int):
+    """Max time and summed units over ranks (barrier included)."""
+    if ws <= 1:
+        return ms, units
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms, -units], dtype=torch.float64)
+    dist.barrier()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    u = torch.tensor([units], dtype=torch.float64)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(u[0])
+
+
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.p = None
+        self.path = os.path.join("/tmp", f"emcg_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        rows = []
+        for ln in open(self.path):
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def silicon_model(v, precision):
+    return v.silicon_electron("jacoboni", temperature=300.0, n_levels=1000, max_energy=1.0)
+
+
+def run_engine(args):
+    ws, rank, local = _dist()
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1 and not torch.distributed.is_initialized():
+        torch.distributed.init_process_group("nccl")
+    import viennaemc_gb300 as v
+    from viennaemc_gb300.bulk import BulkBatch, EnsembleSpec
+    N, K, W, per = args.n, args.steps, args.warmup, args.steps_per_launch
+    pt = silicon_model(v, "fp32")
+    spec = EnsembleSpec(0, N, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 1234 + rank, 0, 300.0)
+    b = BulkBatch([pt], [spec], "fp32")
+    b.set_launch(args.block, per)
+    b.init_particles(0)
+    # warm-up (untimed)
+    b.step(W)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    sampler = ClockSampler(local)
+    n_launch = (K + per - 1) // per
+    kernel_ms = 0.0
+    obs_all = []
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    sampler.start()
+    t0 = time.perf_counter()
+    done = 0
+    for _ in range(n_launch):
+        ns = min(per, K - done)
+        flush.zero_()
+        torch.cuda.synchronize()
+        obs_all.append(b.step(ns))
+        kernel_ms += b.last_kernel_ms()
+        done += ns
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    ms, units = reduce_over_ranks(kernel_ms, float(N) * K, ws)
+    value = units / (ms / 1e3)
+    obs = np.concatenate(obs_all, axis=1)
+    avg = BulkBatch.averages(obs, [N])
+    b.close()
+
+    # end to end through the C ABI: host state in, per-step observables out
+    st = _host_state(v, N)
+    b2 = BulkBatch([pt], [spec], "fp32")
+    b2.set_launch(args.block, per)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b2.set_state(0, st)
+    o2 = b2.step(K)
+    e2e_s = time.perf_counter() - t0
+    b2.close()
+    e2e_units = float(N) * K
+    h2d = N * (9 * 4 + 4) / K
+    d2h = o2.shape[-2] * 3 * 8
+
+    # plain FP64 engine on the same configuration, and the FP32 v_d error
+    k64 = min(K, args.fp64_steps)
+    spec64 = EnsembleSpec(0, N, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 999 + rank, 0, 300.0)
+    b64 = BulkBatch([pt], [spec64], "fp64")
+    b64.set_launch(args.block, per)
+    b64.init_particles(0)
+    b64.step(W)
+    ms64 = 0.0
+    obs64 = []
+    for d0 in range(0, k64, per):
+        obs64.append(b64.step(min(per, k64 - d0)))
+        ms64 += b64.last_kernel_ms()
+    b64.close()
+    a64 = BulkBatch.averages(np.concatenate(obs64, axis=1), [N])
+    win = slice(max(0, k64 - 500), k64)
+    vd32 = float(avg["drift_velocity"][0, win, 0].mean())
+    vd64 = float(a64["drift_velocity"][0, win, 0].mean())
+    value64 = N * k64 / (ms64 / 1e3)
+
+    peak, peak_src = _peaks()
+    bpp = BYTES_PER_PARTICLE_STEP["fp32"]
+    achieved = bpp * value / 1e9
+    traffic = _profiled_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "bulk Si, 2^20 electrons, 1e6 V/m <100>, dt 1 fs, 5000 steps",
+                   "particles": N, "steps_per_launch": per, "block_threads": args.block,
+                   "l2": "flushed (256 MB write) between timed launches",
+                   "observables": "per-step FP64 sums of E, v.dir, count"},
+        "e2e": {"value": e2e_units / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": n_launch,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": peak_src,
+                     "bytes_per_unit": bpp, "unit_of_work": "particle-step"},
+        "fp64_engine": {"value": value64, "unit": UNIT, "steps": k64,
+                        "fp32_speedup": value / value64},
+        "vd_error": {"fp32_mps": vd32, "fp64_mps": vd64,
+                     "rel": abs(vd32 - vd64) / abs(vd64) if vd64 else None,
+                     "window_steps": [win.start, win.stop]},
+        "wall_s": wall,
+    }
+    if clocks:
+        line["clocks"] = clocks
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(N, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _host_state(v, N):
+    """A host-side Maxwellian state (the public API's input form)."""
+    rs = np.random.default_rng(5)
+    from viennaemc_gb300.bulk import ParticleState
+    st = ParticleState(N)
+    E = -1.5 * (1.38066e-23 / 1.60219e-19 * 300.0) * np.log(rs.uniform(1e-6, 1, N))
+    k = np.sqrt(2 * 0.2586 * 9.11e-31 * E * (1 + 0.5 * E) * 1.60219e-19) / 1.05459e-34
+    ct = 1 - 2 * rs.random(N)
+    ph = 2 * np.pi * rs.random(N)
+    stt = np.sqrt(1 - ct * ct)
+    st.kx[:], st.ky[:], st.kz[:] = k * stt * np.cos(ph), k * stt * np.sin(ph), k * ct
+    st.px[:], st.py[:], st.pz[:] = (rs.random((3, N)) * 1e-6)
+    st.energy[:] = E
+    st.tau[:] = -np.log(rs.uniform(1e-6, 1, N)) * 8.7e-15
+    st.grain_tau[:] = 1.0
+    st.sub[:] = rs.integers(0, 3, N)
+    return st
+
+
+def _profiled_traffic():
+    """DRAM bytes per launch of the bulk kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "bulk_step_fp32_traffic.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["dram_bytes_per_launch"])
+    except Exception:
+        return None
+
+
+def cpu_baseline(N, seconds):
+    """The reference algorithm (oracle port) on all host cores, bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    po.build()
+    threads = os.cpu_count() or 1
+    m = po.silicon_model("jacoboni")
+    n = min(N, 1 << 18)
+    st = _oracle_state(po, n)
+    force = [-1.60219e-19 * 1e6, 0, 0]
+    t0 = time.perf_counter()
+    m.bulk_run_philox(st, 1e-15, force, [1e-6] * 3, [1, 0, 0], 7, 0, 0, 20, threads, False)
+    dt20 = time.perf_counter() - t0
+    steps = int(max(20, min(2000, seconds / max(dt20 / 20, 1e-9))))
+    t0 = time.perf_counter()
+    m.bulk_run_philox(st, 1e-15, force, [1e-6] * 3, [1, 0, 0], 7, 0, 20, steps, threads, True)
+    el = time.perf_counter() - t0
+    return {"value": n * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} electrons x {steps} steps of the same workload (FP64, per-step "
+                      f"observables), OpenMP over particles"}
+
+
+def _oracle_state(po, n):
+    rs = np.random.default_rng(3)
+    st = po.State(n)
+    E = -1.5 * (1.38066e-23 / 1.60219e-19 * 300.0) * np.log(rs.uniform(1e-6, 1, n))
+    k = np.sqrt(2 * 0.2586 * 9.11e-31 * E * (1 + 0.5 * E) * 1.60219e-19) / 1.05459e-34
+    ct = 1 - 2 * rs.random(n)
+    ph = 2 * np.pi * rs.random(n)
+    stt = np.sqrt(1 - ct * ct)
+    st.kx[:], st.ky[:], st.kz[:] = k * stt * np.cos(ph), k * stt * np.sin(ph), k * ct
+    st.E[:] = E
+    st.tau[:] = -np.log(rs.uniform(1e-6, 1, n)) * 8.7e-15
+    st.gtau[:] = 1.0
+    st.sub[:] = rs.integers(0, 3, n)
+    return st
+
+
+def run_reference(args):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    po.build()
+    threads = os.cpu_count() or 1
+    m = po.silicon_model("jacoboni")
+    N, K, W = args.n, args.steps, args.warmup
+    st = _oracle_state(po, N)
+    force = [-1.60219e-19 * 1e6, 0, 0]
+    m.bulk_run_philox(st, 1e-15, force, [1e-6] * 3, [1, 0, 0], 7, 0, 0, max(W, 3), threads, True)
+    # each timed step is the full 2^20-electron step; cap the count so the run
+    # stays within a few minutes
+    t0 = time.perf_counter()
+    m.bulk_run_philox(st, 1e-15, force, [1e-6] * 3, [1, 0, 0], 7, 0, W, 5, threads, True)
+    per = (time.perf_counter() - t0) / 5
+    k_run = int(max(5, min(K, 120.0 / max(per, 1e-9))))
+    t0 = time.perf_counter()
+    m.bulk_run_philox(st, 1e-15, force, [1e-6] * 3, [1, 0, 0], 7, 0, W + 5, k_run, threads, True)
+    el = time.perf_counter() - t0
+    value = N * k_run / el
+    sample = (f"{N} electrons x {k_run} steps (of {K} requested) of the same workload, "
+              f"FP64, per-step observables, OpenMP over particles on {threads} threads")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": k_run,
+            "warmup": W, "ms_per_step": el / k_run * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "bulk Si, 2^20 electrons, 1e6 V/m <100>, dt 1 fs, 5000 steps",
+                       "particles": N},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5000)
+    ap.add_argument("--warmup", type=int, default=200)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--steps-per-launch", type=int, default=500)
+    ap.add_argument("--block", type=int, default=256)
+    ap.add_argument("--fp64-steps", type=int, default=1500)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,238 @@
+/*
+ * emcgpu.h -- C ABI of libemcgpu, the sm_103a engine for the ViennaEMC
+ * per-particle hot path (free flight, scatter selection and final states,
+ * particle-mesh assignment / force interpolation, grid Poisson solve).
+ *
+ * Plain C: POD descriptors, plain pointers and sizes, no C++ or torch types.
+ * Every entry point returns an int status (EMCG_OK == 0); emcg_last_error()
+ * gives the message of the most recent failure on the calling thread.
+ *
+ * The reference interface each entry point replaces is cited beside it
+ * (paths relative to the ViennaEMC project root).  A maintainer binds this
+ * header from the reference's C++ through the adapter shown in
+ * INTEGRATION.md; the Python package viennaemc_gb300 binds it with ctypes.
+ *
+ * Units are SI throughout (m, s, J, kg, V/m) except energies in eV, exactly
+ * as in the reference.  Particle state crosses the boundary as
+ * structure-of-arrays doubles/int32, whatever precision the engine computes in.
+ */
+#ifndef EMCGPU_H
+#define EMCGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- limits ------------------------------------------------------------ */
+#define EMCG_MAX_VALLEYS 4
+#define EMCG_MAX_DEG 8       /* subvalleys per valley */
+#define EMCG_MAX_MECH 32     /* mechanisms per model */
+#define EMCG_MAX_NF 8        /* final subvalleys per initial subvalley */
+#define EMCG_MAX_REGIONS 16  /* doping regions */
+#define EMCG_MAX_TABLESETS (EMCG_MAX_VALLEYS * EMCG_MAX_REGIONS)
+
+/* ---- status codes ------------------------------------------------------ */
+#define EMCG_OK 0
+#define EMCG_ERR_ARG (-1)          /* invalid argument (host-side check)   */
+#define EMCG_ERR_CUDA (-2)         /* CUDA runtime failure                 */
+#define EMCG_ERR_TIMEOUT (-3)      /* a bounded device wait gave up        */
+#define EMCG_ERR_NONCONVERGED (-4) /* Poisson solve did not converge       */
+#define EMCG_ERR_OUT_OF_TABLE (-5) /* particle in a (valley, region) pair
+                                      without a rate-table set (the
+                                      reference's std::map::at throws)    */
+#define EMCG_ERR_REPLAY (-6)       /* replay word stream exhausted         */
+#define EMCG_ERR_CAPACITY (-7)     /* particle capacity exceeded           */
+
+/* ---- precision --------------------------------------------------------- */
+#define EMCG_FP64 0 /* double state and arithmetic (parity engine)         */
+#define EMCG_FP32 1 /* float state and arithmetic, double observable sums  */
+
+/* ---- mechanism kinds (include/ScatterMechanisms/) ---------------------- */
+#define EMCG_MECH_ACOUSTIC 0     /* emcAcousticScatterMechanism.hpp:124-126 */
+#define EMCG_MECH_ZERO_IV_ABS 1  /* emcZeroOrderInterValleyScatterMechanism.hpp:247-257 */
+#define EMCG_MECH_ZERO_IV_EMI 2  /* emcZeroOrderInterValleyScatterMechanism.hpp:390-400 */
+#define EMCG_MECH_FIRST_IV_ABS 3 /* emcFirstOrderInterValleyScatterMechanism.hpp:121-131 */
+#define EMCG_MECH_FIRST_IV_EMI 4 /* emcFirstOrderInterValleyScatterMechanism.hpp:269-279 */
+#define EMCG_MECH_COULOMB 5      /* emcCoulombScatterMechanism.hpp:48-59 */
+
+/* ---- random-number modes ----------------------------------------------- */
+#define EMCG_RNG_PHILOX 0 /* counter-based Philox4x32-10                   */
+#define EMCG_RNG_REPLAY 1 /* consume a recorded std::mt19937_64 word stream */
+
+/* One valley: emcNonParabolicAnisotropValley
+   (include/ValleyTypes/emcNonParabolicAnistropValley.hpp:22-204).
+   rot[s] holds the normalised ellipse-frame axes of subvalley s as rows
+   (setSubValleyEllipseCoordSystem, :68-80). */
+typedef struct {
+  int32_t deg;
+  int32_t pad_;
+  double rel_mass[3];
+  double particle_mass; /* kg */
+  double alpha;         /* non-parabolicity [1/eV] */
+  double bottom;        /* valley bottom energy [eV] */
+  double rot[EMCG_MAX_DEG][9];
+} emcg_valley_desc;
+
+/* One scatter mechanism's final-state sampler.  The rates stay on the host
+   (getScatterRate of the reference classes) and arrive as tables.
+   shift:  energy change of an intervalley event [eV]
+           (absorption: +(phononEnergy - deltaValley),
+            emission:   -(phononEnergy + deltaValley));
+   coulomb_sc2: 8 eps0 epsR Vt / hbar^2 (emcCoulombScatterMechanism.hpp:31). */
+typedef struct {
+  int32_t kind;
+  int32_t valley;
+  int32_t final_valley;
+  int32_t n_final;
+  double shift;
+  double coulomb_sc2;
+  int32_t final_sub[EMCG_MAX_DEG][EMCG_MAX_NF];
+} emcg_mech_desc;
+
+/* One (valley, region) table set (emcScatterHandler::scatterTables entry,
+   include/emcScatterHandler.hpp:58-59).  mech[t] is the model mechanism index
+   of table t in registration order; tau_max = 1 / Gamma_max (:271). */
+typedef struct {
+  int32_t valley;
+  int32_t region;
+  int32_t n_tables;
+  int32_t pad_;
+  int32_t mech[EMCG_MAX_MECH];
+  double tau_max;
+} emcg_tableset_desc;
+
+/* A particle type's band + scattering model (emcParticleType +
+   emcScatterHandler, include/ParticleType/emcParticleType.hpp:25-189).
+   tables: for each table set in order, n_tables x n_levels doubles of the
+   cumulative, Gamma_max-normalised rates (renormalizeTables, :248-273),
+   table-major: tables[ts_offset + t * n_levels + level].
+   region_doping: net doping per region [1/m^3] (Coulomb final state). */
+typedef struct {
+  int32_t n_valleys;
+  int32_t n_mechs;
+  int32_t n_tablesets;
+  int32_t n_levels;
+  double max_energy; /* eV; dE = max_energy / n_levels */
+  double grain_tau;  /* grain free-flight constant (1.0 without a grain
+                        mechanism, include/emcScatterHandler.hpp:62) */
+  const emcg_valley_desc *valleys;
+  const emcg_mech_desc *mechs;
+  const emcg_tableset_desc *tablesets;
+  const double *tables;
+  double region_doping[EMCG_MAX_REGIONS];
+} emcg_model_desc;
+
+/* One bulk ensemble (basicBulkParticleHandler,
+   examples/bulkSimulation/basicBulkParticleHandler.hpp:93-120):
+   force = charge * field (:186), periodic box [0, box] (:600-613),
+   field_dir = normalised field direction for the drift velocity (:326-347). */
+typedef struct {
+  int32_t model;      /* index into the handle's models */
+  int32_t pad_;
+  int64_t capacity;   /* particle slots reserved for this ensemble */
+  double field[3];    /* V/m */
+  double charge;      /* C (-q for electrons) */
+  double field_dir[3];
+  double box[3];      /* m */
+  double dt;          /* s */
+  uint64_t seed;
+  uint32_t stream;
+  uint32_t pad2_;
+} emcg_ensemble_desc;
+
+/* Host-side structure-of-arrays particle state (emcParticle +
+   positionsParticles, include/emcParticle.hpp:10-18). */
+typedef struct {
+  double *kx, *ky, *kz;
+  double *px, *py, *pz;
+  double *energy;
+  double *tau;
+  double *grain_tau;
+  int32_t *valley, *sub, *region;
+  int64_t n;
+} emcg_state;
+
+typedef struct emcg_handle emcg_handle;
+
+/* ---- errors ------------------------------------------------------------ */
+/* Text of the last failure on this thread (replaces emcMessage::addError,
+   include/emcMessage.hpp:43-66, which aborts). */
+const char *emcg_last_error(void);
+int32_t emcg_version(void);
+
+/* ---- bulk engine (examples/bulkSimulation/basicBulkParticleHandler.hpp) -- */
+
+/* Create a bulk engine holding n_models particle-type models and n_ens
+   ensembles (one ensemble = one basicBulkParticleHandler; several ensembles
+   advance together in one launch).  precision: EMCG_FP64 | EMCG_FP32.
+   Replaces the basicBulkParticleHandler constructor (:93-120) once the
+   particle type's initScatterTables has run. */
+int32_t emcg_bulk_create(const emcg_model_desc *models, int32_t n_models,
+                         const emcg_ensemble_desc *ens, int32_t n_ens,
+                         int32_t precision, emcg_handle **out);
+int32_t emcg_destroy(emcg_handle *h);
+
+/* Replace ensemble e's field, charge, direction, box, dt and Philox stream
+   (resetAppliedFieldStrength, :135-137); model and capacity must not change. */
+int32_t emcg_bulk_update_ensemble(emcg_handle *h, int32_t ens,
+                                  const emcg_ensemble_desc *desc);
+
+/* Upload / download ensemble e's particles (replaces direct access to the
+   handler's particles / positionsParticles vectors, :58-59). */
+int32_t emcg_set_state(emcg_handle *h, int32_t ens, const emcg_state *s);
+int32_t emcg_get_state(emcg_handle *h, int32_t ens, emcg_state *s);
+int64_t emcg_num_particles(emcg_handle *h, int32_t ens);
+
+/* Generate n initial particles of ensemble e on the GPU (Philox stream
+   (seed, stream), counter = (particle, 0xFFFFFFFF, call, stream)):
+   emcElectron::generateInitialParticle + initParticlePos
+   (include/ParticleType/emcElectron.hpp:75-90,
+    include/emcParticleInitialization.hpp:14-51) at grid nodes coord[i]
+   (3 x int64 per particle) of a grid with the given extent and spacing.
+   coords == NULL places particles at nodes drawn uniformly. */
+int32_t emcg_bulk_init(emcg_handle *h, int32_t ens, int64_t n,
+                       const int64_t *coords, const int64_t extent[3],
+                       const double spacing[3], double thermal_voltage);
+
+/* Advance every ensemble by n_steps time steps (moveParticles(dt), :181-225)
+   starting at global step index step0 (Philox counter).  obs (optional,
+   host) receives, per ensemble, step and valley, the sums
+   {sum E, sum v.field_dir, count}:
+   obs[((e * n_steps + s) * n_valleys_max + v) * 3 + q]
+   with n_valleys_max the largest n_valleys over the models.  Averages and
+   occupations as returned by getAvgEnergy / getAvgDriftVelocity /
+   getValleyOccupationProbability (:289-347) are sum/count and count/N. */
+int32_t emcg_bulk_step(emcg_handle *h, int32_t n_steps, uint32_t step0,
+                       double *obs);
+
+/* Replay mode: the next emcg_bulk_step (n_steps must be 1) of ensemble 0
+   consumes words[offsets[i] .. offsets[i+1]) for particle i instead of
+   Philox (the sequential std::mt19937_64 stream of the reference built
+   without OpenMP, attributed to particles).  words/offsets are host
+   arrays of nwords / n+1 entries; NULL words switches replay off. */
+int32_t emcg_set_replay(emcg_handle *h, const uint64_t *words, int64_t nwords,
+                        const int64_t *offsets, int64_t n_offsets);
+
+/* Per-launch timing of the last emcg_bulk_step (device milliseconds). */
+int32_t emcg_last_kernel_ms(emcg_handle *h, double *ms);
+
+/* Tuning: threads per block (multiple of 32, <= 1024) and steps fused per
+   kernel launch (observables flushed every chunk). 0 keeps the current. */
+int32_t emcg_set_launch(emcg_handle *h, int32_t block_threads,
+                        int32_t steps_per_launch);
+
+/* ---- single-particle kernels (known-answer tests of the reference) ----- */
+/* drift() of include/emcParticleDrift.hpp:11-36 for n independent
+   particles of valley v of model 0: k, pos (3 x n, SoA) and energy in/out,
+   force 3 x n, dt per particle.  Runs in the handle's precision. */
+int32_t emcg_drift_kat(emcg_handle *h, int32_t valley, int64_t n,
+                       const int32_t *sub, const double *dt,
+                       const double *force, double *k, double *pos,
+                       double *energy);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EMCGPU_H */

@@ -1,0 +1,387 @@
+"""ctypes bindings for the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the engine in viennaemc_gb300/.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
+
+ACOUSTIC, ZERO_IV_ABS, ZERO_IV_EMI, FIRST_IV_ABS, FIRST_IV_EMI, COULOMB = range(6)
+RNG_MT, RNG_PHILOX, RNG_REPLAY = range(3)
+
+_lib = None
+
+
+def build(force: bool = False) -> None:
+    """Compile liboracle.so with the Makefile beside this file."""
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+class Particles(C.Structure):
+    _fields_ = [(n, C.POINTER(C.c_double)) for n in
+                ("kx", "ky", "kz", "px", "py", "pz", "E", "tau", "gtau")] + \
+               [(n, C.POINTER(C.c_int32)) for n in ("valley", "sub", "region")] + \
+               [("n", C.c_int64)]
+
+
+class Rng(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("stream", C.c_uint32), ("seed", C.c_uint64),
+                ("mt", C.c_uint64 * 312), ("mt_idx", C.c_int32), ("pad_", C.c_int32),
+                ("words", C.POINTER(C.c_uint64)), ("nwords", C.c_int64), ("pos", C.c_int64),
+                ("rec", C.POINTER(C.c_uint64)), ("rec_cap", C.c_int64), ("rec_n", C.c_int64),
+                ("rec_overflow", C.c_int32), ("pad2_", C.c_int32)]
+
+
+def _declare(L):
+    d, i32, i64, u32, u64, vp = C.c_double, C.c_int32, C.c_int64, C.c_uint32, C.c_uint64, C.c_void_p
+    P = C.POINTER
+    L.oc_model_new.restype = vp
+    L.oc_model_new.argtypes = [d, d, d, d, d, i32, d]
+    L.oc_model_free.argtypes = [vp]
+    L.oc_add_valley.restype = i32
+    L.oc_add_valley.argtypes = [vp, P(d), d, i32, d, d]
+    L.oc_set_frame.restype = i32
+    L.oc_set_frame.argtypes = [vp, i32, i32, P(d), P(d), P(d)]
+    L.oc_add_mech.restype = i32
+    L.oc_add_mech.argtypes = [vp, i32, i32, i32, d, d, i32, P(i32), P(i32), i32]
+    L.oc_set_region_doping.restype = i32
+    L.oc_set_region_doping.argtypes = [vp, i32, d]
+    L.oc_build_tables.restype = i32
+    L.oc_build_tables.argtypes = [vp]
+    for fn in ("oc_get_raw_table", "oc_get_norm_table"):
+        getattr(L, fn).restype = i32
+        getattr(L, fn).argtypes = [vp, i32, i32, i32, P(d)]
+    L.oc_n_tables.restype = i32
+    L.oc_n_tables.argtypes = [vp, i32, i32]
+    L.oc_table_mech.restype = i32
+    L.oc_table_mech.argtypes = [vp, i32, i32, i32]
+    L.oc_get_tau.restype = d
+    L.oc_get_tau.argtypes = [vp, i32, i32]
+    L.oc_valley_consts.argtypes = [vp, i32, P(d)]
+    L.oc_valley_rot.argtypes = [vp, i32, P(d)]
+    L.oc_energy.restype = d
+    L.oc_energy.argtypes = [vp, i32, P(d)]
+    L.oc_norm_wave_vec.restype = d
+    L.oc_norm_wave_vec.argtypes = [vp, i32, d]
+    L.oc_velocity.argtypes = [vp, i32, i32, P(d), d, P(d)]
+    L.oc_drift.argtypes = [vp, d, P(d), P(d), i32, i32, P(d), i32, P(d)]
+    L.oc_mt_seed.argtypes = [P(Rng), u64]
+    L.oc_mt_next.restype = u64
+    L.oc_mt_next.argtypes = [P(Rng)]
+    L.oc_philox4x32_10.argtypes = [P(u32), P(u32), P(u32)]
+    L.oc_canonical.restype = d
+    L.oc_canonical.argtypes = [u64]
+    L.oc_bulk_step.restype = i32
+    L.oc_bulk_step.argtypes = [vp, P(Particles), d, P(d), P(d), P(Rng), u32, P(i64)]
+    L.oc_bulk_run_philox.restype = i32
+    L.oc_bulk_run_philox.argtypes = [vp, P(Particles), d, P(d), P(d), P(d), u64, u32, u32,
+                                     i32, i32, P(d)]
+    L.oc_observables.argtypes = [vp, P(Particles), P(d), P(d)]
+    L.oc_bulk_init.restype = i64
+    L.oc_bulk_init.argtypes = [vp, P(d), P(d), d, P(Rng), P(Particles), i64]
+    L.oc_init_particle.argtypes = [vp, P(i64), P(i64), P(d), i32, i32, d, P(Rng),
+                                   P(Particles), i64, i32]
+    if hasattr(L, "oc_device_declare"):
+        pass
+
+
+def dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def lptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+def uptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint64))
+
+
+def darr(x):
+    return np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+
+
+STATE_F = ("kx", "ky", "kz", "px", "py", "pz", "E", "tau", "gtau")
+STATE_I = ("valley", "sub", "region")
+
+
+class State:
+    """Structure-of-arrays particle state held in numpy (float64 / int32)."""
+
+    def __init__(self, n: int):
+        for f in STATE_F:
+            setattr(self, f, np.zeros(n, np.float64))
+        for f in STATE_I:
+            setattr(self, f, np.zeros(n, np.int32))
+        self.n = n
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "State":
+        n = len(d["E"])
+        s = cls(n)
+        for f in STATE_F:
+            getattr(s, f)[:] = d[f]
+        for f in STATE_I:
+            getattr(s, f)[:] = d[f]
+        return s
+
+    def to_dict(self) -> dict:
+        return {f: getattr(self, f).copy() for f in STATE_F + STATE_I}
+
+    def copy(self) -> "State":
+        return State.from_dict(self.to_dict())
+
+    def resize(self, n: int) -> "State":
+        s = State(n)
+        m = min(n, self.n)
+        for f in STATE_F + STATE_I:
+            getattr(s, f)[:m] = getattr(self, f)[:m]
+        return s
+
+    def cstruct(self) -> Particles:
+        p = Particles()
+        for f in STATE_F:
+            setattr(p, f, dptr(getattr(self, f)))
+        for f in STATE_I:
+            setattr(p, f, iptr(getattr(self, f)))
+        p.n = self.n
+        return p
+
+
+class RngState:
+    def __init__(self, mode=RNG_MT, seed=0, stream=0):
+        self.r = Rng()
+        self.r.mode = mode
+        self.r.seed = seed
+        self.r.stream = stream
+        self._keep = []
+        if mode == RNG_MT:
+            lib().oc_mt_seed(C.byref(self.r), seed)
+
+    def load_mt(self, words):
+        """Load a libstdc++ mt19937_64 text state (312 words + index)."""
+        for i in range(312):
+            self.r.mt[i] = int(words[i])
+        self.r.mt_idx = int(words[312])
+
+    def set_replay(self, words: np.ndarray):
+        w = np.ascontiguousarray(words, dtype=np.uint64)
+        self._keep.append(w)
+        self.r.mode = RNG_REPLAY
+        self.r.words = uptr(w)
+        self.r.nwords = len(w)
+        self.r.pos = 0
+
+    def start_record(self, cap: int):
+        buf = np.zeros(cap, np.uint64)
+        self._rec = buf
+        self.r.rec = uptr(buf)
+        self.r.rec_cap = cap
+        self.r.rec_n = 0
+        self.r.rec_overflow = 0
+
+    def recorded(self) -> np.ndarray:
+        assert not self.r.rec_overflow, "record buffer overflow"
+        return self._rec[: self.r.rec_n].copy()
+
+
+class Model:
+    """Oracle model: valleys, mechanisms and rate tables."""
+
+    def __init__(self, temperature=300.0, rho=2329.0, vsound=9040.0, epsR=11.8,
+                 Ni=1.45e16, n_levels=1000, max_energy=1.0):
+        self.h = lib().oc_model_new(temperature, rho, vsound, epsR, Ni, n_levels, max_energy)
+        self.n_levels = n_levels
+        self.max_energy = max_energy
+        self.temperature = temperature
+        self.nV = 0
+
+    def __del__(self):
+        try:
+            lib().oc_model_free(self.h)
+        except Exception:
+            pass
+
+    def add_valley(self, rel_mass, particle_mass, deg, alpha, bottom=0.0, frames=None):
+        v = lib().oc_add_valley(self.h, dptr(darr(rel_mass)), particle_mass, deg, alpha, bottom)
+        assert v >= 0
+        if frames:
+            for s, (a, b, c) in enumerate(frames):
+                assert lib().oc_set_frame(self.h, v, s, dptr(darr(a)), dptr(darr(b)),
+                                          dptr(darr(c))) == 0
+        self.nV += 1
+        return v
+
+    def add_mech(self, kind, valley, regions, p0=0.0, p1=0.0, final_valley=None,
+                 final_sub=None):
+        fs = np.zeros(1, np.int32) if final_sub is None else \
+            np.ascontiguousarray(np.asarray(final_sub, np.int32))
+        nF = 0 if final_sub is None else fs.shape[1]
+        regs = np.ascontiguousarray(np.asarray(regions, np.int32))
+        fv = valley if final_valley is None else final_valley
+        idx = lib().oc_add_mech(self.h, kind, valley, fv, p0, p1, nF, iptr(fs.reshape(-1)),
+                                iptr(regs), len(regs))
+        assert idx >= 0
+        return idx
+
+    def set_region_doping(self, region, doping):
+        assert lib().oc_set_region_doping(self.h, region, doping) == 0
+
+    def build_tables(self):
+        assert lib().oc_build_tables(self.h) == 0
+
+    def n_tables(self, valley, region):
+        return lib().oc_n_tables(self.h, valley, region)
+
+    def raw_table(self, valley, region, t):
+        out = np.zeros(self.n_levels)
+        assert lib().oc_get_raw_table(self.h, valley, region, t, dptr(out)) == 0
+        return out
+
+    def norm_table(self, valley, region, t):
+        out = np.zeros(self.n_levels)
+        assert lib().oc_get_norm_table(self.h, valley, region, t, dptr(out)) == 0
+        return out
+
+    def tau(self, valley, region):
+        return lib().oc_get_tau(self.h, valley, region)
+
+    def valley_consts(self, v):
+        out = np.zeros(8)
+        lib().oc_valley_consts(self.h, v, dptr(out))
+        return out
+
+    # ---- dynamics -------------------------------------------------------
+    def bulk_step(self, st: State, dt, force, box, rng: RngState, step, offsets=None):
+        p = st.cstruct()
+        off = None
+        if offsets:
+            off = np.zeros(st.n + 1, np.int64)
+        rc = lib().oc_bulk_step(self.h, C.byref(p), dt, dptr(darr(force)), dptr(darr(box)),
+                                C.byref(rng.r), step, lptr(off) if off is not None else None)
+        return rc, off
+
+    def bulk_run_philox(self, st: State, dt, force, box, field_dir, seed, stream, step0,
+                        n_steps, n_threads=0, want_obs=True):
+        p = st.cstruct()
+        obs = np.zeros((n_steps, self.nV, 3)) if want_obs else None
+        rc = lib().oc_bulk_run_philox(self.h, C.byref(p), dt, dptr(darr(force)), dptr(darr(box)),
+                                      dptr(darr(field_dir)), seed, stream, step0, n_steps,
+                                      n_threads, dptr(obs) if want_obs else None)
+        assert rc == 0, rc
+        return obs
+
+    def observables(self, st: State, field_dir):
+        out = np.zeros((self.nV, 3))
+        p = st.cstruct()
+        lib().oc_observables(self.h, C.byref(p), dptr(darr(field_dir)), dptr(out))
+        return out
+
+    def bulk_init(self, max_pos, spacing, doping, rng: RngState, cap=1 << 22):
+        st = State(cap)
+        p = st.cstruct()
+        n = lib().oc_bulk_init(self.h, dptr(darr(max_pos)), dptr(darr(spacing)), doping,
+                               C.byref(rng.r), C.byref(p), cap)
+        assert n >= 0
+        return st.resize(int(n))
+
+
+# ---- canonical silicon models (restated from the reference example) ----------
+SI_FRAMES = [((1, 0, 0), (0, 1, 0), (0, 0, 1)),
+             ((0, 1, 0), (1, 0, 0), (0, 0, 1)),
+             ((0, 0, 1), (0, 1, 0), (1, 0, 0))]
+F_SUB = [[1, 1, 2, 2], [0, 0, 2, 2], [0, 0, 1, 1]]
+G_SUB = [[0], [1], [2]]
+ME = 9.11e-31
+KB, Q = 1.38066e-23, 1.60219e-19
+JACOBONI = [("G1", False, 140., 0.5e10), ("G2", False, 215., 0.8e10),
+            ("G3", False, 720., 11.e10), ("F1", True, 220., 0.3e10),
+            ("F2", True, 550., 2.0e10), ("F3", True, 685., 2.0e10)]
+
+
+def silicon_model(name="jacoboni", temperature=300.0, n_levels=1000, max_energy=1.0,
+                  mt=None, regions=(0,), coulomb=False) -> Model:
+    """Oracle twin of the silicon models used by the reference harness."""
+    m = Model(temperature=temperature, n_levels=n_levels, max_energy=max_energy)
+    if mt is None:
+        mt = 0.196 if name == "refbulk" else 0.19
+    m.add_valley([0.916, mt, mt], ME, 3, 0.5, 0.0, SI_FRAMES)
+    regs = list(regions)
+    if name == "refbulk":
+        m.add_mech(ACOUSTIC, 0, regs, 9.0)
+        for kind in (ZERO_IV_ABS, ZERO_IV_EMI):
+            m.add_mech(kind, 0, regs, 5.23e10, 0.06, 0, F_SUB)
+        for kind in (ZERO_IV_ABS, ZERO_IV_EMI):
+            m.add_mech(kind, 0, regs, 5.23e10, 0.06, 0, G_SUB)
+        for kind in (FIRST_IV_ABS, FIRST_IV_EMI):
+            m.add_mech(kind, 0, regs, 2.5, 0.023, 0, F_SUB)
+        for kind in (FIRST_IV_ABS, FIRST_IV_EMI):
+            m.add_mech(kind, 0, regs, 4.0, 0.018, 0, G_SUB)
+    elif name == "jacoboni":
+        m.add_mech(ACOUSTIC, 0, regs, 9.0)
+        for _, isF, theta, D in JACOBONI:
+            e = KB * theta / Q
+            fs = F_SUB if isF else G_SUB
+            m.add_mech(ZERO_IV_ABS, 0, regs, D, e, 0, fs)
+            m.add_mech(ZERO_IV_EMI, 0, regs, D, e, 0, fs)
+    else:
+        raise ValueError(name)
+    if coulomb:
+        m.add_mech(COULOMB, 0, regs, 11.8)
+    m.build_tables()
+    return m
+
+
+# ---- reference harness output -------------------------------------------------
+def parse_ref(text: str) -> dict:
+    out = {}
+    for line in text.splitlines():
+        parts = line.split()
+        if len(parts) < 2:
+            continue
+        key, n = parts[0], int(parts[1])
+        vals = parts[2:2 + n]
+        if key.startswith("name_"):
+            out[key] = vals[0] if vals else ""
+        elif vals and (vals[0].startswith("0x") or vals[0].startswith("-0x")
+                       or "p" in vals[0] or vals[0] in ("inf", "-inf", "nan")):
+            out[key] = np.array([float.fromhex(v) for v in vals])
+        else:
+            out[key] = np.array([int(v) for v in vals], dtype=np.uint64 if key.startswith("mt")
+                                else np.int64)
+    return out
+
+
+def run_ref(*args) -> dict:
+    if not os.path.exists(REF_DRIVER):
+        raise FileNotFoundError("reference harness not built (make -C oracle ref)")
+    r = subprocess.run([REF_DRIVER] + [str(a) for a in args], check=True,
+                       capture_output=True, text=True)
+    return parse_ref(r.stdout)
+
+
+def state_from_ref(d: dict, tag: str) -> State:
+    return State.from_dict({f: d[f"{tag}_{f}"] for f in STATE_F + STATE_I})

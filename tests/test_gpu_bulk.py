@@ -1,0 +1,314 @@
+"""Bulk engine on the GPU against the reference and the oracle.
+
+* replay: the FP64 engine consumes the reference's own std::mt19937_64 words
+  (tests/golden/, attributed per particle) and must land on the reference's
+  particle states and observables within 1e-12 relative;
+* Philox: FP64 engine and oracle consume the same counter-based stream;
+* statistics: FP32 vs FP64 engine, and FP64 engine vs the reference's
+  algorithm (oracle with mt19937_64) over 16 seeds at 3 sigma.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import BULK_CASES, case_model, golden
+
+pytestmark = pytest.mark.gpu
+
+FIELDS_F = ("kx", "ky", "kz", "px", "py", "pz", "E", "tau", "gtau")
+ENG = {"E": "energy", "gtau": "grain_tau"}
+RTOL = 1e-12  # relative tolerance of the FP64 parity engine
+
+
+def _eng_field(f):
+    return ENG.get(f, f)
+
+
+def _batch(engine, g, precision="fp64", n=None, seed=1, stream=0):
+    name, T, nL, maxE, mt = case_model(g)
+    pt = engine.physics.silicon_electron(name, temperature=T, n_levels=nL, max_energy=maxE, mt=mt)
+    fld = g["applied_field"]
+    strength = float(np.sqrt(np.sum(fld * fld)))
+    spec = engine.EnsembleSpec(0, n if n is not None else len(g["s0_E"]), strength,
+                               tuple(g["field_dir"]), (float(g["box"]),) * 3, float(g["dt"]),
+                               seed, stream, T)
+    return engine.BulkBatch([pt], [spec], precision)
+
+
+def _to_engine_state(engine, g, s):
+    kw = {_eng_field(f): g[f"s{s}_{f}"] for f in FIELDS_F}
+    kw.update({f: g[f"s{s}_{f}"] for f in ("valley", "sub", "region")})
+    return engine.ParticleState.from_arrays(**kw)
+
+
+def _assert_close_state(st, g, s, rtol=RTOL):
+    for f in FIELDS_F:
+        a = getattr(st, _eng_field(f))
+        b = g[f"s{s}_{f}"]
+        scale = max(np.max(np.abs(b)), 1e-300)
+        err = np.max(np.abs(a - b)) / scale
+        assert err <= rtol, (s, f, err)
+    for f in ("valley", "sub", "region"):
+        assert np.array_equal(getattr(st, f), g[f"s{s}_{f}"]), (s, f)
+
+
+def _step_words(g, s):
+    off = g["offsets"][s - 1]
+    return g["words"][off[0]:off[-1]], off - off[0]
+
+
+@pytest.mark.parametrize("case", BULK_CASES)
+def test_replay_each_step_matches_reference(engine, case):
+    g = golden(case)
+    b = _batch(engine, g)
+    n = len(g["s0_E"])
+    for s in range(1, g["offsets"].shape[0] + 1):
+        b.set_state(0, _to_engine_state(engine, g, s - 1))
+        w, off = _step_words(g, s)
+        b.set_replay(w, off)
+        obs = b.step(1, step0=s)
+        _assert_close_state(b.get_state(0), g, s)
+        avg = engine.BulkBatch.averages(obs, [n])
+        ref = g[f"obs{s}"].reshape(-1, 3)
+        assert np.allclose(avg["energy"][0, 0], ref[:, 0], rtol=RTOL, atol=0)
+        assert np.allclose(avg["drift_velocity"][0, 0], ref[:, 1], rtol=1e-10, atol=0)
+        assert np.array_equal(avg["occupation"][0, 0], ref[:, 2])
+    b.close()
+
+
+@pytest.mark.parametrize("case", BULK_CASES)
+def test_replay_trajectory_24_steps(engine, case):
+    g = golden(case)
+    b = _batch(engine, g)
+    b.set_state(0, _to_engine_state(engine, g, 0))
+    steps = g["offsets"].shape[0]
+    for s in range(1, steps + 1):
+        w, off = _step_words(g, s)
+        b.set_replay(w, off)
+        b.step(1, step0=s)
+    _assert_close_state(b.get_state(0), g, steps, rtol=1e-10)
+    b.close()
+
+
+def test_replay_detects_word_mismatch(engine):
+    g = golden(BULK_CASES[0])
+    b = _batch(engine, g)
+    b.set_state(0, _to_engine_state(engine, g, 0))
+    w, off = _step_words(g, 1)
+    off = off.copy()
+    i = int(np.argmax(np.diff(off) > 0))  # a particle that draws words
+    off[i + 1:] += 1  # claim one extra word for it
+    w = np.concatenate([w, np.zeros(1, np.uint64)])
+    b.set_replay(w, off)
+    with pytest.raises(engine._lib.EmcgError) as ei:
+        b.step(1, step0=1)
+    assert ei.value.status == -6
+    b.close()
+
+
+def _oracle_state_to_engine(engine, st):
+    kw = {_eng_field(f): getattr(st, f) for f in FIELDS_F}
+    kw.update({f: getattr(st, f) for f in ("valley", "sub", "region")})
+    return engine.ParticleState.from_arrays(**kw)
+
+
+def test_philox_fp64_matches_oracle(engine, oracle):
+    """Same Philox stream in engine and oracle: states within 1e-12 after 100 steps
+    (particles whose path branched on a last-ulp difference are counted)."""
+    m = oracle.silicon_model("jacoboni")
+    rng = oracle.RngState(oracle.RNG_MT, 99)
+    st = m.bulk_init([2e-6] * 3, [2e-7] * 3, 4e20, rng)
+    assert st.n > 2000
+    g = {"applied_field": np.array([-1e6, 0, 0]), "field_dir": np.array([-1.0, 0, 0]),
+         "box": np.array(2e-6), "dt": np.array(1e-15), "s0_E": st.E,
+         "raw": np.zeros((13, 1)), "params": np.array([300, 1000, 1.0, 0, 0, 0, 0, 0, 0, 0, 0.19])}
+    seed, stream, steps = 0x1234_5678_9ABC, 3, 100
+    b = _batch(engine, g, seed=seed, stream=stream)
+    b.set_state(0, _oracle_state_to_engine(engine, st))
+    obs = b.step(steps, step0=5)
+    ref = st.copy()
+    oobs = m.bulk_run_philox(ref, 1e-15, [1.60219e-19 * 1e6, 0, 0], [2e-6] * 3, [-1.0, 0, 0],
+                             seed, stream, 5, steps, n_threads=1)
+    got = b.get_state(0)
+    bad = np.zeros(st.n, bool)
+    for f in FIELDS_F:
+        a, r = getattr(got, _eng_field(f)), getattr(ref, f)
+        scale = np.max(np.abs(r))
+        bad |= np.abs(a - r) > 1e-12 * scale
+    for f in ("valley", "sub"):
+        bad |= getattr(got, f) != getattr(ref, f)
+    assert bad.sum() <= max(1, st.n // 1000), bad.sum()
+    # observables: sums per step
+    assert np.allclose(obs[0, :, 0, 2], oobs[:, 0, 2])
+    assert np.allclose(obs[0, :, 0, 0], oobs[:, 0, 0], rtol=1e-9)
+    assert np.allclose(obs[0, :, 0, 1], oobs[:, 0, 1], rtol=1e-7, atol=1e-9 * np.abs(oobs[:, 0, 1]).max())
+    b.close()
+
+
+def test_init_fp64_matches_oracle(engine, oracle):
+    m = oracle.silicon_model("jacoboni")
+    n, ext, spacing = 500, np.array([6, 6, 6]), np.array([1e-7] * 3)
+    rs = np.random.default_rng(0)
+    coords = rs.integers(0, 6, size=(n, 3))
+    seed, stream = 777, 2
+    ro = oracle.RngState(oracle.RNG_PHILOX, seed, stream)
+    ost = oracle.State(n)
+    p = ost.cstruct()
+    Vt = 1.38066e-23 / 1.60219e-19 * 300.0
+    for i in range(n):
+        c = np.ascontiguousarray(coords[i].astype(np.int64))
+        oracle.lib().oc_init_particle(m.h, oracle.lptr(c), oracle.lptr(ext.astype(np.int64)),
+                                      oracle.dptr(spacing), 3, 0, Vt, C.byref(ro.r), C.byref(p),
+                                      i, 0)
+    g = {"applied_field": np.array([0.0, 0, 0]), "field_dir": np.array([1.0, 0, 0]),
+         "box": np.array(6e-7), "dt": np.array(1e-15), "s0_E": ost.E,
+         "raw": np.zeros((13, 1)), "params": np.array([300, 1000, 1.0, 0, 0, 0, 0, 0, 0, 0, 0.19])}
+    b = _batch(engine, g, seed=seed, stream=stream)
+    b.init_particles(0, coords=coords, extent=ext, spacing=spacing)
+    got = b.get_state(0)
+    for f in FIELDS_F:
+        a, r = getattr(got, _eng_field(f)), getattr(ost, f)
+        assert np.max(np.abs(a - r)) <= 1e-12 * np.max(np.abs(r)), f
+    for f in ("valley", "sub", "region"):
+        assert np.array_equal(getattr(got, f), getattr(ost, f)), f
+    b.close()
+
+
+@pytest.mark.parametrize("precision,ktol,ptol", [("fp64", 1e-5, 1e-10), ("fp32", None, None)])
+def test_drift_known_answers(engine, precision, ktol, ptol):
+    """tests/testParticleMovement of the reference through the engine's drift."""
+    from viennaemc_gb300 import physics
+    hbar, me, dT = 1.05459e-34, 9.11e-31, 1e-12
+    frames = [((1, 0, 0), (0, 1, 0), (0, 0, 1)), ((0, 1, 0), (1, 0, 0), (0, 0, 1)),
+              ((0, 0, 1), (0, 1, 0), (1, 0, 0)), ((-1, 1, 1), (1, 1, 0), (1, -1, 2)),
+              ((1, 1, 1), (-1, 1, 0), (-1, -1, 2)), ((-1, -1, 1), (1, 0, 1), (-1, 2, 1))]
+    pt = physics.Electron(1000, 1.0)
+    v = physics.NonParabolicAnisotropValley([0.1, 0.5, 1.0], me, 6, 0.5)
+    for s, (a, bb, c) in enumerate(frames):
+        v.setSubValleyEllipseCoordSystem(s, a, bb, c)
+    pt.addValley(v)
+    pt.addScatterMechanism([0], physics.AcousticScatterMechanism(0, 9.0, 300, 2329., 9040.))
+    pt.initScatterTables()
+    spec = engine.EnsembleSpec(0, 1, 0.0, (1, 0, 0), (1e-6,) * 3, 1e-15, 1)
+    b = engine.BulkBatch([pt], [spec], precision)
+    n = 6
+    F = np.full((3, n), 1e-17)
+    k = np.zeros((3, n))
+    pos = np.full((3, n), 1e-7)
+    E = np.zeros(n)
+    sub = np.arange(n, dtype=np.int32)
+    dt = np.full(n, dT)
+    L = engine._lib.lib()
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    engine._lib.check(L.emcg_drift_kat(b.h, 0, n, sub.ctypes.data_as(C.POINTER(C.c_int32)),
+                                       dp(dt), dp(F), dp(k), dp(pos), dp(E)))
+    for s, (d1, d2, d3) in enumerate(frames):
+        D = np.array([np.array(d, float) / np.linalg.norm(d) for d in (d1, d2, d3)])
+        fE = D @ F[:, s]
+        mass = np.array([0.1, 0.5, 1.0])
+        mc = 3.0 / np.sum(1.0 / mass)
+        kE = fE * dT * np.sqrt(mc / mass) / hbar
+        pE = kE / 2.0 * dT / np.sqrt(mass * mc) * hbar
+        ek, ep = D.T @ kE, D.T @ pE + 1e-7
+        eE = v.getEnergy(list(ek))
+        if ktol is not None:
+            assert np.all(np.abs(k[:, s] - ek) <= ktol), s
+            assert np.all(np.abs(pos[:, s] - ep) <= ptol), s
+            assert abs(E[s] - eE) <= 1e-10
+        else:  # float engine: relative agreement
+            assert np.allclose(k[:, s], ek, rtol=2e-6, atol=1e-6 * np.abs(ek).max())
+            assert abs(E[s] - eE) <= 2e-6 * eE
+    b.close()
+
+
+def _steady(engine, precision, n, steps, seed, field=1e6, direction=(1, 0, 0), model="jacoboni",
+            T=300.0):
+    pt = engine.physics.silicon_electron(model, temperature=T)
+    spec = engine.EnsembleSpec(0, n, field, direction, (1e-6,) * 3, 1e-15, seed, 0, T)
+    b = engine.BulkBatch([pt], [spec], precision)
+    b.init_particles(0)
+    obs = b.step(steps)
+    b.close()
+    a = engine.BulkBatch.averages(obs, [n])
+    return a["drift_velocity"][0, :, 0], a["energy"][0, :, 0]
+
+
+def test_fp32_matches_fp64_within_one_percent(engine):
+    n, steps = 1 << 16, 1500
+    v64, e64 = _steady(engine, "fp64", n, steps, 11)
+    v32, e32 = _steady(engine, "fp32", n, steps, 12)
+    vd64, vd32 = v64[-500:].mean(), v32[-500:].mean()
+    ee64, ee32 = e64[-500:].mean(), e32[-500:].mean()
+    assert abs(vd32 - vd64) <= 0.01 * abs(vd64), (vd32, vd64)
+    assert abs(ee32 - ee64) <= 0.01 * ee64, (ee32, ee64)
+    # electrons drift against the field
+    assert vd64 < 0 and 4e4 < abs(vd64) < 2e5
+
+
+def test_ensemble_statistics_match_reference_16_seeds(engine, oracle):
+    """FP64 engine (Philox) vs the reference algorithm with mt19937_64 (oracle,
+    bit-identical to the reference) over 16 seeds: steady drift velocity and
+    energy agree within 3 sigma of the seed-to-seed spread."""
+    n, steps, tail = 1000, 600, 300
+    m = oracle.silicon_model("jacoboni")
+    ref_v, ref_e, gpu_v, gpu_e = [], [], [], []
+    for seed in range(1, 17):
+        rng = oracle.RngState(oracle.RNG_MT, seed)
+        st = m.bulk_init([1e-6] * 3, [2e-7] * 3, 1e21, rng)
+        st = st.resize(n) if st.n > n else st
+        force = [1.60219e-19 * 1e6, 0, 0]
+        vs, es = [], []
+        for s in range(steps):
+            m.bulk_step(st, 1e-15, force, [1e-6] * 3, rng, s)
+            if s >= steps - tail:
+                o = m.observables(st, [-1.0, 0, 0])
+                es.append(o[0, 0])
+                vs.append(o[0, 1])
+        ref_v.append(np.mean(vs))
+        ref_e.append(np.mean(es))
+        v, e = _steady(engine, "fp64", st.n, steps, 1000 + seed, direction=(-1, 0, 0))
+        gpu_v.append(v[-tail:].mean())
+        gpu_e.append(e[-tail:].mean())
+    for ref, gpu in ((ref_v, gpu_v), (ref_e, gpu_e)):
+        ref, gpu = np.array(ref), np.array(gpu)
+        sigma = np.sqrt(ref.var(ddof=1) / len(ref) + gpu.var(ddof=1) / len(gpu))
+        assert abs(ref.mean() - gpu.mean()) <= 3 * sigma, (ref.mean(), gpu.mean(), sigma)
+
+
+def test_uneven_batch_equals_separate_runs(engine):
+    """Ensembles of different size, field and temperature in one launch give the
+    same trajectories as separate runs (same Philox streams)."""
+    pt300 = engine.physics.silicon_electron("jacoboni", temperature=300.0)
+    pt77 = engine.physics.silicon_electron("jacoboni", temperature=77.0)
+    specs = [engine.EnsembleSpec(0, 1000, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 5, 0, 300.0),
+             engine.EnsembleSpec(1, 3333, 3e5, (1, 1, 1), (1e-6,) * 3, 1e-15, 5, 1, 77.0)]
+    batch = engine.BulkBatch([pt300, pt77], specs, "fp64")
+    for e in range(2):
+        batch.init_particles(e)
+    obs = batch.step(40)
+    for e, pt in enumerate((pt300, pt77)):
+        single = engine.BulkBatch([pt], [engine.EnsembleSpec(
+            0, specs[e].n_particles, specs[e].field_strength, specs[e].field_dir,
+            specs[e].box, specs[e].dt, specs[e].seed, specs[e].stream, specs[e].temperature)],
+            "fp64")
+        single.init_particles(0)
+        o1 = single.step(40)
+        a, b_ = batch.get_state(e), single.get_state(0)
+        assert np.array_equal(a.energy, b_.energy) and np.array_equal(a.kx, b_.kx)
+        assert np.allclose(obs[e], o1[0], rtol=1e-12)
+        single.close()
+    batch.close()
+
+
+def test_out_of_table_region_is_reported(engine):
+    g = golden(BULK_CASES[0])
+    b = _batch(engine, g)
+    st = _to_engine_state(engine, g, 0)
+    st.region[:] = 1  # no rate tables registered for region 1
+    st.tau[:] = 0.0   # force a scatter event in the first step
+    b.set_state(0, st)
+    with pytest.raises(engine._lib.EmcgError) as ei:
+        b.step(1)
+    assert ei.value.status == -5
+    b.close()

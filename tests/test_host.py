@@ -1,0 +1,151 @@
+"""Host-side checks that need no GPU: the C ABI library loads and exports every
+entry point of include/emcgpu.h, rejects invalid arguments before touching
+the device, and the host model builder reproduces the reference's tables."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import BULK_CASES, ROOT, case_model, golden
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "emcgpu.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:const char \*|int32_t|int64_t)\s*\n?\s*(emcg_\w+)\(",
+                                 txt, re.M)))
+
+
+def test_header_declares_entry_points():
+    syms = header_symbols()
+    for s in ("emcg_bulk_create", "emcg_bulk_step", "emcg_set_replay", "emcg_destroy",
+              "emcg_last_error", "emcg_set_state", "emcg_get_state", "emcg_bulk_init"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol():
+    from viennaemc_gb300 import _lib
+    path = _lib.build()
+    lib = C.CDLL(path)
+    for s in header_symbols():
+        assert hasattr(lib, s), s
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True,
+                         text=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if ln.strip()}
+    assert set(header_symbols()) <= exported
+
+
+@pytest.mark.parametrize("case", BULK_CASES)
+def test_host_model_builder_matches_reference_tables(case):
+    from viennaemc_gb300 import physics
+    g = golden(case)
+    name, T, nL, maxE, mt = case_model(g)
+    pt = physics.silicon_electron(name, temperature=T, n_levels=nL, max_energy=maxE, mt=mt)
+    raw = pt.scatterHandler.raw[(0, 0)]
+    assert np.array_equal(raw, g["raw"])
+    assert pt.getTau(0, 0) == g["tau"][0]
+    names = [m.getName() for m in pt.scatterHandler.mechanisms]
+    assert names == [str(x) for x in g["names"]]
+
+
+def _desc(**over):
+    from viennaemc_gb300 import physics
+    pt = physics.silicon_electron("jacoboni")
+    d = pt.model_desc()
+    for k, v in over.items():
+        setattr(d, k, v)
+    return pt, d
+
+
+def _create(models, ens, prec=0):
+    from viennaemc_gb300 import _lib
+    L = _lib.lib()
+    h = C.c_void_p()
+    n_models = len(models)
+    marr = (_lib.ModelDesc * max(n_models, 1))(*models)
+    earr = (_lib.EnsembleDesc * max(len(ens), 1))(*ens)
+    st = L.emcg_bulk_create(marr, n_models, earr, len(ens), prec, C.byref(h))
+    return st, L.emcg_last_error().decode()
+
+
+def _ens(**over):
+    from viennaemc_gb300 import _lib
+    e = _lib.EnsembleDesc()
+    e.model, e.capacity, e.charge, e.dt, e.seed = 0, 16, -1.60219e-19, 1e-15, 1
+    for i in range(3):
+        e.box[i] = 5e-7
+        e.field_dir[i] = 1.0 if i == 0 else 0.0
+    for k, v in over.items():
+        setattr(e, k, v)
+    return e
+
+
+@pytest.mark.parametrize("bad,msg", [
+    (dict(n_valleys=0), "n_valleys"),
+    (dict(n_levels=0), "n_levels"),
+    (dict(max_energy=-1.0), "max_energy"),
+    (dict(grain_tau=0.0), "grain_tau"),
+])
+def test_create_rejects_bad_model_without_gpu(bad, msg):
+    pt, d = _desc(**bad)
+    st, err = _create([d], [_ens()])
+    assert st == -1 and msg in err
+
+
+def test_create_rejects_bad_ensembles_and_precision():
+    pt, d = _desc()
+    st, err = _create([d], [_ens(model=3)])
+    assert st == -1 and "model" in err
+    st, err = _create([d], [_ens(dt=0.0)])
+    assert st == -1 and "dt" in err
+    st, err = _create([d], [_ens()], prec=7)
+    assert st == -1 and "precision" in err
+
+
+def test_create_rejects_mechanism_of_another_valley():
+    pt, d = _desc()
+    d.mechs[3].valley = 1  # valley 1 does not exist
+    st, err = _create([d], [_ens()])
+    assert st == -1 and "valley" in err
+
+
+def test_create_rejects_bad_final_subvalley():
+    pt, d = _desc()
+    d.mechs[1].final_sub[0][0] = 7  # valley has 3 subvalleys
+    st, err = _create([d], [_ens()])
+    assert st == -1 and "final subvalley" in err
+
+
+def test_null_handle_calls_fail_cleanly():
+    from viennaemc_gb300 import _lib
+    L = _lib.lib()
+    assert L.emcg_bulk_step(None, 1, 0, None) == -1
+    assert L.emcg_destroy(None) == 0
+    assert L.emcg_num_particles(None, 0) == -1
+
+
+def test_model_descriptor_layout():
+    from viennaemc_gb300 import physics
+    pt = physics.silicon_electron("jacoboni")
+    d = pt.model_desc()
+    assert d.n_valleys == 1 and d.n_mechs == 13 and d.n_tablesets == 1
+    ts = d.tablesets[0]
+    assert ts.n_tables == 13 and list(ts.mech)[:13] == list(range(13))
+    nT, nL = 13, d.n_levels
+    tab = np.ctypeslib.as_array(d.tables, shape=(nT * nL,)).reshape(nT, nL)
+    assert np.array_equal(tab, pt.scatterHandler.norm[(0, 0)])
+    # intervalley energy shifts: absorption +hw, emission -hw
+    for i, m in enumerate(pt.scatterHandler.mechanisms[1:], start=1):
+        sign = 1 if m.absorption else -1
+        assert d.mechs[i].shift == sign * m.phonon_energy
+
+
+def test_bulk_handler_field_and_observable_averaging():
+    from viennaemc_gb300.bulk import BulkBatch
+    sums = np.zeros((1, 2, 1, 3))
+    sums[0, :, 0] = [[3.0, -6.0, 3.0], [0.0, 0.0, 0.0]]
+    a = BulkBatch.averages(sums, [3])
+    assert a["energy"][0, 0, 0] == 1.0 and a["drift_velocity"][0, 0, 0] == -2.0
+    assert a["occupation"][0, 0, 0] == 1.0 and a["energy"][0, 1, 0] == 0.0

@@ -1,0 +1,328 @@
+"""Bulk ensembles on the GPU engine.
+
+BulkParticleHandler mirrors basicBulkParticleHandler
+(examples/bulkSimulation/basicBulkParticleHandler.hpp:43-614): same names,
+argument meaning and observables, with the particle state resident on the
+GPU.  BulkBatch advances many uneven ensembles (different fields,
+temperatures, particle counts) together in one launch.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from .physics import Electron, thermal_voltage
+
+STATE_F = ("kx", "ky", "kz", "px", "py", "pz", "energy", "tau", "grain_tau")
+STATE_I = ("valley", "sub", "region")
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class ParticleState:
+    """Host structure-of-arrays particle state (float64 / int32)."""
+
+    def __init__(self, n: int):
+        self.n = int(n)
+        for f in STATE_F:
+            setattr(self, f, np.zeros(self.n, np.float64))
+        for f in STATE_I:
+            setattr(self, f, np.zeros(self.n, np.int32))
+
+    @classmethod
+    def from_arrays(cls, **kw) -> "ParticleState":
+        n = len(kw["energy"])
+        s = cls(n)
+        for f in STATE_F + STATE_I:
+            if f in kw:
+                getattr(s, f)[:] = kw[f]
+        return s
+
+    def desc(self) -> L.StateDesc:
+        d = L.StateDesc()
+        for f in STATE_F:
+            setattr(d, f, _dp(getattr(self, f)))
+        for f in STATE_I:
+            setattr(d, f, _ip(getattr(self, f)))
+        d.n = self.n
+        return d
+
+
+def _normalize(v):
+    s = 0.0
+    for x in v:
+        s += x * x
+    n = math.sqrt(s)
+    return [float(x) for x in v] if n == 0 else [x / n for x in v]
+
+
+@dataclass
+class EnsembleSpec:
+    """One bulk ensemble: the model it uses, its particle count and field."""
+    model: int
+    n_particles: int
+    field_strength: float
+    field_dir: tuple
+    box: tuple
+    dt: float
+    seed: int
+    stream: int = 0
+    temperature: float = 300.0
+
+
+class BulkBatch:
+    """Several bulk ensembles advanced together on one GPU.
+
+    models: list of Electron particle types (e.g. one per temperature).
+    precision: "fp64" (parity engine) or "fp32" (throughput engine).
+    """
+
+    def __init__(self, models, ensembles, precision="fp64", capacity_slack=0):
+        self._lib = L.lib()
+        self.models = list(models)
+        self.specs = list(ensembles)
+        self.precision = L.FP64 if precision in ("fp64", L.FP64) else L.FP32
+        self._mdesc = [m.model_desc() for m in self.models]
+        marr = (L.ModelDesc * len(self._mdesc))(*self._mdesc)
+        self._marr = marr
+        self.nVmax = max(m.getNrValleys() for m in self.models)
+        earr = (L.EnsembleDesc * len(self.specs))()
+        for i, sp in enumerate(self.specs):
+            self._fill_ens(earr[i], sp, sp.n_particles + capacity_slack)
+        self._earr = earr
+        h = C.c_void_p()
+        L.check(self._lib.emcg_bulk_create(marr, len(self._mdesc), earr, len(self.specs),
+                                           self.precision, C.byref(h)))
+        self.h = h
+        self.step_index = 0
+
+    def _fill_ens(self, d, sp: EnsembleSpec, capacity: int):
+        pt = self.models[sp.model]
+        dirn = _normalize(sp.field_dir)  # basicBulkParticleHandler.hpp:100-101
+        d.model = sp.model
+        d.capacity = capacity
+        for i in range(3):
+            d.field[i] = dirn[i] * sp.field_strength
+            d.field_dir[i] = dirn[i]
+            d.box[i] = sp.box[i]
+        d.charge = pt.getCharge()
+        d.dt = sp.dt
+        d.seed = sp.seed
+        d.stream = sp.stream
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.emcg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- particles -----------------------------------------------------------
+    def init_particles(self, ens: int, n: int | None = None, coords=None, extent=None,
+                       spacing=None):
+        """GPU initial particles (emcElectron::generateInitialParticle)."""
+        sp = self.specs[ens]
+        n = sp.n_particles if n is None else int(n)
+        Vt = thermal_voltage(sp.temperature)
+        if coords is None:
+            L.check(self._lib.emcg_bulk_init(self.h, ens, n, None, None, None, Vt))
+        else:
+            c = np.ascontiguousarray(np.asarray(coords, np.int64).reshape(-1, 3))
+            ext = np.ascontiguousarray(np.asarray(extent, np.int64))
+            spc = np.ascontiguousarray(np.asarray(spacing, np.float64))
+            L.check(self._lib.emcg_bulk_init(
+                self.h, ens, len(c), c.ctypes.data_as(C.POINTER(C.c_int64)),
+                ext.ctypes.data_as(C.POINTER(C.c_int64)), _dp(spc), Vt))
+
+    def set_state(self, ens: int, st: ParticleState):
+        d = st.desc()
+        L.check(self._lib.emcg_set_state(self.h, ens, C.byref(d)))
+
+    def get_state(self, ens: int) -> ParticleState:
+        n = self._lib.emcg_num_particles(self.h, ens)
+        st = ParticleState(n)
+        d = st.desc()
+        L.check(self._lib.emcg_get_state(self.h, ens, C.byref(d)))
+        return st
+
+    def num_particles(self, ens: int) -> int:
+        return int(self._lib.emcg_num_particles(self.h, ens))
+
+    def update_ensemble(self, ens: int, spec: EnsembleSpec):
+        d = L.EnsembleDesc()
+        self._fill_ens(d, spec, self._earr[ens].capacity)
+        L.check(self._lib.emcg_bulk_update_ensemble(self.h, ens, C.byref(d)))
+        self.specs[ens] = spec
+        self._earr[ens] = d
+
+    # ---- dynamics ------------------------------------------------------------
+    def set_launch(self, block_threads=0, steps_per_launch=0):
+        L.check(self._lib.emcg_set_launch(self.h, block_threads, steps_per_launch))
+
+    def step(self, n_steps: int = 1, observables: bool = True, step0: int | None = None):
+        """Advance all ensembles; returns sums [ens, step, valley, {E, v.dir, count}]."""
+        s0 = self.step_index if step0 is None else int(step0)
+        obs = np.zeros((len(self.specs), n_steps, self.nVmax, 3)) if observables else None
+        L.check(self._lib.emcg_bulk_step(self.h, n_steps, s0, _dp(obs) if observables else None))
+        self.step_index = s0 + n_steps
+        return obs
+
+    def set_replay(self, words, offsets):
+        w = np.ascontiguousarray(np.asarray(words, np.uint64))
+        o = np.ascontiguousarray(np.asarray(offsets, np.int64))
+        self._replay_keep = (w, o)
+        L.check(self._lib.emcg_set_replay(self.h, w.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                          len(w), o.ctypes.data_as(C.POINTER(C.c_int64)),
+                                          len(o)))
+
+    def last_kernel_ms(self) -> float:
+        ms = C.c_double()
+        L.check(self._lib.emcg_last_kernel_ms(self.h, C.byref(ms)))
+        return ms.value
+
+    @staticmethod
+    def averages(obs_sums: np.ndarray, n_particles) -> dict:
+        """Per-step getAvgEnergy / getAvgDriftVelocity /
+        getValleyOccupationProbability from observable sums."""
+        cnt = obs_sums[..., 2]
+        with np.errstate(invalid="ignore", divide="ignore"):
+            avgE = np.where(cnt > 0, obs_sums[..., 0] / np.maximum(cnt, 1), 0.0)
+            avgV = np.where(cnt > 0, obs_sums[..., 1] / np.maximum(cnt, 1), 0.0)
+        n = np.asarray(n_particles, np.float64).reshape(-1, *([1] * (cnt.ndim - 1)))
+        occ = np.where(n > 0, cnt / np.maximum(n, 1), 0.0)
+        return {"energy": avgE, "drift_velocity": avgV, "occupation": occ}
+
+
+class BulkParticleHandler:
+    """basicBulkParticleHandler (examples/bulkSimulation/basicBulkParticleHandler.hpp)
+    for one electron type on the GPU.
+
+    handler = BulkParticleHandler(maxPos, particleType, fieldDir, fieldStrength, seed)
+    handler.generateInitialParticles(spacing, doping)    # node-based counts
+    handler.moveParticles(dt)                            # one time step
+    handler.getAvgEnergy(0), getAvgDriftVelocity(0), getValleyOccupationProbability(0)
+    """
+
+    def __init__(self, max_pos, particle_type: Electron, field_dir, field_strength=0.0,
+                 seed=0, temperature=300.0, precision="fp64", capacity=None, dt=1e-15):
+        if seed == 0:  # the reference draws a wall-clock seed for 0 (:110-115)
+            import time
+            seed = time.time_ns() & 0xFFFFFFFFFFFFFFFF
+        self.max_pos = tuple(float(x) for x in max_pos)
+        self.type = particle_type
+        self.field_dir = _normalize(field_dir)
+        self.field_strength = float(field_strength)
+        self.seed = int(seed)
+        self.temperature = float(temperature)
+        self.dt = float(dt)
+        self.precision = precision
+        self._capacity = capacity
+        self._batch = None
+        self._last = None
+        self.n = 0
+
+    def _spec(self, n):
+        return EnsembleSpec(0, n, self.field_strength, tuple(self.field_dir), self.max_pos,
+                            self.dt, self.seed, 0, self.temperature)
+
+    def _ensure(self, n):
+        cap = max(self._capacity or 0, n)
+        if self._batch is None or self._batch._earr[0].capacity < cap:
+            if self._batch is not None:
+                self._batch.close()
+            self._batch = BulkBatch([self.type], [self._spec(cap)], self.precision)
+        return self._batch
+
+    def generateInitialParticles(self, spacing=None, doping=None, n=None):
+        """Initial particles.  With (spacing, doping): the reference's node-based
+        count doping * cellVolume (half per boundary dimension), the
+        fractional part drawn at random (:143-159); with n: n particles uniform
+        in the box."""
+        if n is not None:
+            b = self._ensure(int(n))
+            b.init_particles(0, int(n))
+            self.n = int(n)
+            return
+        ext = [int(round(mp / h)) + 1 for mp, h in zip(self.max_pos, spacing)]
+        cell = 1.0
+        for h in spacing:
+            cell = cell * h
+        rng = np.random.default_rng(self.seed)
+        coords = []
+        for z in range(ext[2]):
+            for y in range(ext[1]):
+                for x in range(ext[0]):
+                    nr = doping
+                    for c, e in zip((x, y, z), ext):
+                        if c == 0 or c == e - 1:
+                            nr *= 0.5
+                    nr = nr * cell
+                    while nr >= 1:
+                        coords.append((x, y, z))
+                        nr -= 1
+                    if rng.random() < nr:
+                        coords.append((x, y, z))
+        b = self._ensure(len(coords))
+        b.init_particles(0, coords=coords, extent=ext, spacing=spacing)
+        self.n = len(coords)
+
+    def resetAppliedFieldStrength(self, strength):
+        self.field_strength = float(strength)
+        if self._batch is not None:
+            self._batch.update_ensemble(0, self._spec(self._batch.specs[0].n_particles))
+
+    def getAppliedField(self):
+        return [d * self.field_strength for d in self.field_dir]
+
+    def getNrParticles(self, idx_type=0):
+        return self.n
+
+    def moveParticles(self, dt, n_steps=1):
+        """Advance by n_steps steps of dt; returns per-step averages."""
+        b = self._batch
+        if dt != self.dt:
+            self.dt = float(dt)
+            b.update_ensemble(0, self._spec(b.specs[0].n_particles))
+        obs = b.step(n_steps)
+        self._last = BulkBatch.averages(obs, [self.n])
+        return self._last
+
+    def getAvgEnergy(self, idx_type=0):
+        return self._current()["energy"]
+
+    def getAvgDriftVelocity(self, idx_type=0):
+        return self._current()["drift_velocity"]
+
+    def getValleyOccupationProbability(self, idx_type=0):
+        return self._current()["occupation"]
+
+    def _current(self):
+        if self._last is None:
+            raise RuntimeError("observables are produced by moveParticles")
+        return {k: v[0, -1] for k, v in self._last.items()}
+
+    def get_state(self):
+        return self._batch.get_state(0)
+
+    def set_state(self, st: ParticleState):
+        self._ensure(st.n).set_state(0, st)
+        self.n = st.n
+
+    def deleteParticles(self):
+        if self._batch is not None:
+            self._batch.set_state(0, ParticleState(0))
+        self.n = 0

@@ -1,0 +1,879 @@
+// Bulk engine: ensembles of electrons in a periodic box under a constant
+// field (examples/bulkSimulation/basicBulkParticleHandler.hpp).  Many
+// time steps run inside one launch with the particle state held in
+// registers; per-step ensemble observables are reduced warp -> block ->
+// device with double accumulators.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "emcg_common.cuh"
+#include "emcg_host.h"
+#include "emcg_model.h"
+
+namespace emcg {
+
+constexpr int kMaxScatterPerStep = 1 << 16; // bound on the per-step scatter loop
+
+// ---------------------------------------------------------------------------
+// device code
+// ---------------------------------------------------------------------------
+// free flight + periodic wrap (basicBulkParticleHandler.hpp:600-613)
+template <class T>
+__device__ __forceinline__ void driftBulk(const ValleyK<T> &V, int sub, const T fv[3], T dt,
+                                          T k[3], T &E, T pos[3], T kN[3], const T box[3]) {
+  drift<T, 3>(V, sub, fv, dt, k, E, pos, kN);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    T c = pos[i];
+    if (c < T(0))
+      pos[i] = c + box[i];
+    else if (c > box[i])
+      pos[i] = c - box[i];
+  }
+}
+
+// One particle, one time step (basicBulkParticleHandler.hpp:195-220).
+template <class T, class Src>
+__device__ __forceinline__ int bulkParticleStep(const ModelK<T> &M, const EnsK<T> &EK, T k[3],
+                                                T pos[3], T &E, T &tau, T &gtau, int &valley,
+                                                int &sub, int region, T kN[3], Src &rng) {
+  const T dt = EK.dt;
+  int err = 0;
+  driftBulk(M.v[valley], sub, EK.fv[valley][sub], dt < tau ? dt : tau, k, E, pos, kN, EK.box);
+  T tRem = dt - tau;
+  int guard = 0;
+  while (tRem > T(0)) {
+    if (++guard > kMaxScatterPerStep) {
+      err = EMCG_ERR_TIMEOUT;
+      break;
+    }
+    int e = scatterParticle(M, k, E, valley, sub, region, rng);
+    if (e) {
+      err = e;
+      break;
+    }
+    T nt = -m_log(rng.ulog()) * tauOf(M, valley, region);
+    tau += nt;
+    driftBulk(M.v[valley], sub, EK.fv[valley][sub], nt < tRem ? nt : tRem, k, E, pos, kN,
+              EK.box);
+    tRem -= nt;
+  }
+  tau -= dt;
+  gtau -= dt;
+  if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
+    gtau = -m_log(rng.ulog()) * M.grainTau;
+  return err;
+}
+
+template <class T> __device__ __forceinline__ T warpSum(T x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+__device__ __forceinline__ void recordError(int *err, int code) {
+  if (code)
+    atomicCAS(err, 0, code);
+}
+
+// Advance all tiles by nSteps time steps.  obs layout:
+// [ens][step][nVmax][3] of {sum E, sum v.dir, count} (doubles).
+template <class T, bool REPLAY>
+__global__ void bulkStepKernel(StateK<T> st, const ModelK<T> *__restrict__ models,
+                               const EnsK<T> *__restrict__ ens, const Tile *__restrict__ tiles,
+                               int nSteps, uint32_t step0, int chunk, int nVmax,
+                               double *__restrict__ obs, const uint64_t *__restrict__ rw,
+                               const int64_t *__restrict__ roff, int *__restrict__ err) {
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  T *sbuf = reinterpret_cast<T *>(smemRaw); // [chunk][nWarps][Q]
+  const Tile tl = tiles[blockIdx.x];
+  const EnsK<T> &EK = ens[tl.ens];
+  const ModelK<T> &M = models[EK.model];
+  const int nV = EK.nV;
+  const int Q = nVmax * 3;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nWarps = blockDim.x >> 5;
+  const int64_t gi = tl.begin + threadIdx.x;
+  const bool active = gi < tl.end;
+  const uint32_t pid = (uint32_t)(gi - EK.begin);
+
+  T k[3] = {0, 0, 0}, pos[3] = {0, 0, 0}, kN[3] = {0, 0, 0}, E = 0, tau = 0, gtau = 0;
+  int valley = 0, sub = 0, region = 0;
+  if (active) {
+    k[0] = st.kx[gi];
+    k[1] = st.ky[gi];
+    k[2] = st.kz[gi];
+    pos[0] = st.px[gi];
+    pos[1] = st.py[gi];
+    pos[2] = st.pz[gi];
+    E = st.E[gi];
+    tau = st.tau[gi];
+    gtau = st.gtau[gi];
+    uint32_t mt = st.meta[gi];
+    valley = mt & 0xff;
+    sub = (mt >> 8) & 0xff;
+    region = mt >> 16;
+  }
+  int myErr = 0;
+  double *obsE = obs + (size_t)tl.ens * nSteps * Q;
+  for (int s = 0; s < nSteps; s++) {
+    if (active && !myErr) {
+      if constexpr (REPLAY) {
+        ReplaySrc src{rw, roff[pid], roff[pid + 1], 0};
+        myErr = bulkParticleStep(M, EK, k, pos, E, tau, gtau, valley, sub, region, kN, src);
+        if (!myErr && (src.bad || src.pos != src.end))
+          myErr = EMCG_ERR_REPLAY;
+      } else {
+        PhiloxSrc<T> src;
+        src.init(pid, step0 + (uint32_t)s, EK.stream, EK.key0, EK.key1);
+        myErr = bulkParticleStep(M, EK, k, pos, E, tau, gtau, valley, sub, region, kN, src);
+      }
+    }
+    // drift velocity v.dir = cX (g . k_ecs) / sqrt(1 + 4 alpha gamma)
+    // (emcNonParabolicAnistropValley.hpp:126-136 projected on the field)
+    T vd = T(0);
+    if (active) {
+      const ValleyK<T> &V = M.v[valley];
+      const T *g = EK.g[valley][sub];
+      T npf = m_sqrt(T(1) + T(4) * V.alpha * gammaOf(V, E));
+      vd = m_div(V.cX * (g[0] * kN[0] + g[1] * kN[1] + g[2] * kN[2]), npf);
+    }
+    T *row = sbuf + ((s % chunk) * nWarps + warp) * Q;
+    for (int v = 0; v < nV; v++) {
+      bool in = active && valley == v;
+      T e = warpSum(in ? E : T(0));
+      T d = warpSum(in ? vd : T(0));
+      unsigned c = __popc(__ballot_sync(0xffffffffu, in));
+      if (lane == 0) {
+        row[v * 3 + 0] = e;
+        row[v * 3 + 1] = d;
+        row[v * 3 + 2] = (T)c;
+      }
+    }
+    if ((s + 1) % chunk == 0 || s == nSteps - 1) {
+      __syncthreads();
+      const int inChunk = s % chunk + 1, sBase = s - s % chunk;
+      const int nQ = nV * 3;
+      for (int idx = threadIdx.x; idx < inChunk * nQ; idx += blockDim.x) {
+        int cs = idx / nQ, q = idx - cs * nQ;
+        double acc = 0.;
+        for (int w = 0; w < nWarps; w++)
+          acc += (double)sbuf[(cs * nWarps + w) * Q + q];
+        atomicAdd(&obsE[(size_t)(sBase + cs) * Q + q], acc);
+      }
+      __syncthreads();
+    }
+  }
+  if (active) {
+    st.kx[gi] = k[0];
+    st.ky[gi] = k[1];
+    st.kz[gi] = k[2];
+    st.px[gi] = pos[0];
+    st.py[gi] = pos[1];
+    st.pz[gi] = pos[2];
+    st.E[gi] = E;
+    st.tau[gi] = tau;
+    st.gtau[gi] = gtau;
+    st.meta[gi] = packMeta(valley, sub, region);
+  }
+  recordError(err, myErr);
+}
+
+// Initial particles (include/ParticleType/emcElectron.hpp:75-90,
+// include/emcParticleInitialization.hpp:14-51), Philox counter
+// (i, 0xFFFFFFFF, call, stream).  coords == nullptr: uniform in the box.
+template <class T>
+__global__ void bulkInitKernel(StateK<T> st, const ModelK<T> *__restrict__ models, int model,
+                               int64_t begin, int64_t n, const int64_t *__restrict__ coords,
+                               int64_t e0, int64_t e1, int64_t e2, double h0, double h1,
+                               double h2, double Vt, double b0, double b1, double b2,
+                               uint32_t key0, uint32_t key1, uint32_t stream) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const ModelK<T> &M = models[model];
+  PhiloxSrc<T> rng;
+  rng.init((uint32_t)i, 0xFFFFFFFFu, stream, key0, key1);
+  T pos[3];
+  int64_t c[3] = {0, 0, 0};
+  const int64_t ext[3] = {e0, e1, e2};
+  const double h[3] = {h0, h1, h2};
+  if (coords) {
+    c[0] = coords[3 * i];
+    c[1] = coords[3 * i + 1];
+    c[2] = coords[3 * i + 2];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      if (c[d] == ext[d] - 1)
+        pos[d] = ((T)c[d] - rng.u01() * T(0.5)) * (T)h[d];
+      else if (c[d] == 0)
+        pos[d] = rng.u01() * T(0.5) * (T)h[d];
+      else
+        pos[d] = ((T)c[d] + rng.u01() - T(0.5)) * (T)h[d];
+    }
+  } else {
+    pos[0] = rng.u01() * (T)b0;
+    pos[1] = rng.u01() * (T)b1;
+    pos[2] = rng.u01() * (T)b2;
+  }
+  int valley = (int)m_floor((T)M.nV * rng.ulog());
+  const ValleyK<T> &V = M.v[valley];
+  int sub = (int)m_floor((T)V.deg * rng.ulog());
+  T E = T(-1.5) * (T)Vt * m_log(rng.ulog());
+  T k[3];
+  randomDirection(V.cK * m_sqrt(gammaOf(V, E)), rng, k);
+  if (coords) {
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+      if ((c[d] == 0 && k[d] < T(0)) || (c[d] == ext[d] - 1 && k[d] > T(0)))
+        k[d] *= T(-1);
+  }
+  T tau = -m_log(rng.ulog()) * tauOf(M, valley, 0);
+  T gtau = -m_log(rng.ulog()) * M.grainTau;
+  int64_t g = begin + i;
+  st.kx[g] = k[0];
+  st.ky[g] = k[1];
+  st.kz[g] = k[2];
+  st.px[g] = pos[0];
+  st.py[g] = pos[1];
+  st.pz[g] = pos[2];
+  st.E[g] = E;
+  st.tau[g] = tau;
+  st.gtau[g] = gtau;
+  st.meta[g] = packMeta(valley, sub, 0);
+}
+
+// drift() known-answer kernel: independent particles, per-particle force/dt
+template <class T>
+__global__ void driftKatKernel(const ModelK<T> *__restrict__ models, int valley, int64_t n,
+                               const int32_t *__restrict__ sub, const double *__restrict__ dt,
+                               const double *__restrict__ force, double *__restrict__ k,
+                               double *__restrict__ pos, double *__restrict__ energy) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const ValleyK<T> &V = models[0].v[valley];
+  int s = sub[i];
+  T F[3] = {(T)force[i], (T)force[n + i], (T)force[2 * n + i]};
+  T fE[3];
+  toEcs(V.rot[s], F[0], F[1], F[2], fE);
+  T fv[3] = {fE[0] * V.cF[0], fE[1] * V.cF[1], fE[2] * V.cF[2]};
+  T kk[3] = {(T)k[i], (T)k[n + i], (T)k[2 * n + i]};
+  T p[3] = {(T)pos[i], (T)pos[n + i], (T)pos[2 * n + i]};
+  T E = (T)energy[i], kN[3];
+  drift<T, 3>(V, s, fv, (T)dt[i], kk, E, p, kN);
+  for (int d = 0; d < 3; d++) {
+    k[d * n + i] = (double)kk[d];
+    pos[d * n + i] = (double)p[d];
+  }
+  energy[i] = (double)E;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct BulkImpl {
+  int precision = EMCG_FP64;
+  size_t tsz = 8;
+  int nModels = 0, nEns = 0, nVmax = 1;
+  std::vector<emcg_ensemble_desc> ens;
+  std::vector<emcg_model_desc> modelDescs;       // shallow copies (valleys)
+  std::vector<std::vector<emcg_valley_desc>> valleyCopies;
+  std::vector<int> ensNV;
+  std::vector<int64_t> begin, count, cap;
+  int64_t totalCap = 0;
+  void *dModels = nullptr;
+  std::vector<void *> dTables;
+  void *dEns = nullptr;
+  Tile *dTiles = nullptr;
+  int nTiles = 0, tilesCap = 0;
+  bool tilesDirty = true;
+  void *dState[9] = {};
+  uint32_t *dMeta = nullptr;
+  double *dObs = nullptr;
+  size_t obsCap = 0;
+  int *dErr = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int blockThreads = 256;
+  int stepsPerLaunch = 0;
+  int chunk = 16;
+  uint64_t *dWords = nullptr;
+  int64_t wordsCap = 0;
+  int64_t *dOff = nullptr;
+  int64_t offCap = 0;
+  bool replay = false;
+  double lastMs = 0;
+  // host staging for state transfer
+  std::vector<unsigned char> stage;
+};
+
+template <class T> static StateK<T> stateOf(BulkImpl *b) {
+  StateK<T> s;
+  T **f[9] = {&s.kx, &s.ky, &s.kz, &s.px, &s.py, &s.pz, &s.E, &s.tau, &s.gtau};
+  for (int i = 0; i < 9; i++)
+    *f[i] = (T *)b->dState[i];
+  s.meta = b->dMeta;
+  return s;
+}
+
+template <class T>
+static void buildEnsK(const emcg_ensemble_desc &d, const ModelK<T> &M,
+                      const emcg_model_desc &md, int64_t begin, int64_t n, EnsK<T> &E) {
+  std::memset(&E, 0, sizeof(E));
+  E.model = d.model;
+  E.nV = md.n_valleys;
+  E.begin = begin;
+  E.n = n;
+  double F[3], dir[3];
+  for (int i = 0; i < 3; i++)
+    F[i] = d.field[i] * d.charge; // scale(appliedField, charge) (:186)
+  double nrm = std::sqrt(d.field_dir[0] * d.field_dir[0] + d.field_dir[1] * d.field_dir[1] +
+                         d.field_dir[2] * d.field_dir[2]);
+  for (int i = 0; i < 3; i++)
+    dir[i] = nrm > 0 ? d.field_dir[i] / nrm : 0.;
+  for (int v = 0; v < md.n_valleys; v++) {
+    const emcg_valley_desc &V = md.valleys[v];
+    ValleyDerived dv = deriveValley(V);
+    for (int s = 0; s < V.deg; s++) {
+      const double *R = V.rot[s];
+      for (int i = 0; i < 3; i++) {
+        double fe = F[0] * R[3 * i] + F[1] * R[3 * i + 1] + F[2] * R[3 * i + 2];
+        double de = dir[0] * R[3 * i] + dir[1] * R[3 * i + 1] + dir[2] * R[3 * i + 2];
+        E.fv[v][s][i] = (T)(fe * dv.vogt[i] / kHBAR);
+        E.g[v][s][i] = (T)(dv.vogt[i] * de);
+      }
+    }
+  }
+  for (int i = 0; i < 3; i++)
+    E.box[i] = (T)d.box[i];
+  E.dt = (T)d.dt;
+  E.key0 = (uint32_t)d.seed;
+  E.key1 = (uint32_t)(d.seed >> 32);
+  E.stream = d.stream;
+  (void)M;
+}
+
+template <class T>
+static int32_t createTyped(BulkImpl *b, const emcg_model_desc *models, int nModels,
+                           const emcg_ensemble_desc *ens, int nEns) {
+  std::vector<ModelK<T>> mk(nModels);
+  b->dTables.assign(nModels, nullptr);
+  for (int i = 0; i < nModels; i++) {
+    std::vector<T> tab;
+    EMCG_TRY(buildModelK<T>(models[i], mk[i], tab));
+    EMCG_CUDA(cudaMalloc(&b->dTables[i], tab.size() * sizeof(T)));
+    EMCG_CUDA(cudaMemcpy(b->dTables[i], tab.data(), tab.size() * sizeof(T),
+                         cudaMemcpyHostToDevice));
+    mk[i].tables = (const T *)b->dTables[i];
+  }
+  EMCG_CUDA(cudaMalloc(&b->dModels, sizeof(ModelK<T>) * nModels));
+  EMCG_CUDA(cudaMemcpy(b->dModels, mk.data(), sizeof(ModelK<T>) * nModels,
+                       cudaMemcpyHostToDevice));
+  std::vector<EnsK<T>> ek(nEns);
+  for (int e = 0; e < nEns; e++)
+    buildEnsK<T>(ens[e], mk[ens[e].model], models[ens[e].model], b->begin[e], 0, ek[e]);
+  EMCG_CUDA(cudaMalloc(&b->dEns, sizeof(EnsK<T>) * nEns));
+  EMCG_CUDA(cudaMemcpy(b->dEns, ek.data(), sizeof(EnsK<T>) * nEns, cudaMemcpyHostToDevice));
+  return EMCG_OK;
+}
+
+static int32_t ensureTiles(BulkImpl *b) {
+  if (!b->tilesDirty)
+    return EMCG_OK;
+  std::vector<Tile> t;
+  for (int e = 0; e < b->nEns; e++) {
+    for (int64_t o = 0; o < b->count[e]; o += b->blockThreads) {
+      Tile x;
+      x.ens = e;
+      x.pad_ = 0;
+      x.begin = b->begin[e] + o;
+      x.end = b->begin[e] + std::min<int64_t>(o + b->blockThreads, b->count[e]);
+      t.push_back(x);
+    }
+  }
+  if ((int)t.size() > b->tilesCap) {
+    cudaFree(b->dTiles);
+    b->dTiles = nullptr;
+    b->tilesCap = std::max<int>((int)t.size(), 1);
+    EMCG_CUDA(cudaMalloc(&b->dTiles, sizeof(Tile) * b->tilesCap));
+  }
+  if (!t.empty())
+    EMCG_CUDA(cudaMemcpyAsync(b->dTiles, t.data(), sizeof(Tile) * t.size(),
+                              cudaMemcpyHostToDevice, b->stream));
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  b->nTiles = (int)t.size();
+  b->tilesDirty = false;
+  return EMCG_OK;
+}
+
+static int32_t readError(BulkImpl *b) {
+  int e = 0;
+  EMCG_CUDA(cudaMemcpyAsync(&e, b->dErr, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  if (e) {
+    EMCG_CUDA(cudaMemsetAsync(b->dErr, 0, sizeof(int), b->stream));
+    setError("bulk kernel reported: %s", statusName(e));
+    return e;
+  }
+  return EMCG_OK;
+}
+
+template <class T>
+static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHost) {
+  EMCG_TRY(ensureTiles(b));
+  const int Q = b->nVmax * 3;
+  int per = b->stepsPerLaunch > 0 ? b->stepsPerLaunch : nSteps;
+  if (b->replay)
+    per = 1;
+  size_t need = (size_t)b->nEns * per * Q;
+  if (need > b->obsCap) {
+    cudaFree(b->dObs);
+    b->dObs = nullptr;
+    EMCG_CUDA(cudaMalloc(&b->dObs, need * sizeof(double)));
+    b->obsCap = need;
+  }
+  const int nWarps = b->blockThreads / 32;
+  const size_t smem = (size_t)b->chunk * nWarps * Q * sizeof(T);
+  StateK<T> st = stateOf<T>(b);
+  double totalMs = 0;
+  for (int done = 0; done < nSteps; done += per) {
+    int ns = std::min(per, nSteps - done);
+    EMCG_CUDA(cudaMemsetAsync(b->dObs, 0, (size_t)b->nEns * ns * Q * sizeof(double), b->stream));
+    EMCG_CUDA(cudaEventRecord(b->ev0, b->stream));
+    if (b->nTiles > 0) {
+      if (b->replay) {
+        if constexpr (sizeof(T) == 8)
+          bulkStepKernel<T, true><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
+              st, (const ModelK<T> *)b->dModels, (const EnsK<T> *)b->dEns, b->dTiles, ns,
+              step0 + done, b->chunk, b->nVmax, b->dObs, b->dWords, b->dOff, b->dErr);
+      } else {
+        bulkStepKernel<T, false><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
+            st, (const ModelK<T> *)b->dModels, (const EnsK<T> *)b->dEns, b->dTiles, ns,
+            step0 + done, b->chunk, b->nVmax, b->dObs, nullptr, nullptr, b->dErr);
+      }
+      EMCG_CUDA(cudaGetLastError());
+    }
+    EMCG_CUDA(cudaEventRecord(b->ev1, b->stream));
+    if (obsHost) {
+      // gather [ens][ns][Q] of this launch into [ens][nSteps][Q]
+      for (int e = 0; e < b->nEns; e++)
+        EMCG_CUDA(cudaMemcpyAsync(obsHost + ((size_t)e * nSteps + done) * Q,
+                                  b->dObs + (size_t)e * ns * Q, (size_t)ns * Q * sizeof(double),
+                                  cudaMemcpyDeviceToHost, b->stream));
+    }
+    EMCG_CUDA(cudaEventSynchronize(b->ev1));
+    float ms = 0;
+    EMCG_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    totalMs += ms;
+  }
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  b->lastMs = totalMs;
+  if (b->replay)
+    b->replay = false;
+  return readError(b);
+}
+
+static void freeBulk(BulkImpl *b) {
+  if (!b)
+    return;
+  if (b->stream)
+    cudaStreamSynchronize(b->stream);
+  for (void *p : b->dTables)
+    cudaFree(p);
+  cudaFree(b->dModels);
+  cudaFree(b->dEns);
+  cudaFree(b->dTiles);
+  for (void *p : b->dState)
+    cudaFree(p);
+  cudaFree(b->dMeta);
+  cudaFree(b->dObs);
+  cudaFree(b->dErr);
+  cudaFree(b->dWords);
+  cudaFree(b->dOff);
+  if (b->ev0)
+    cudaEventDestroy(b->ev0);
+  if (b->ev1)
+    cudaEventDestroy(b->ev1);
+  if (b->stream)
+    cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+static int32_t bulkOf(emcg_handle *h, BulkImpl **out) {
+  EMCG_CHECK_ARG(h && h->kind == 1 && h->bulk, "handle is not a bulk engine");
+  *out = h->bulk;
+  return EMCG_OK;
+}
+
+} // namespace emcg
+
+using namespace emcg;
+
+extern "C" int32_t emcg_bulk_create(const emcg_model_desc *models, int32_t n_models,
+                                    const emcg_ensemble_desc *ens, int32_t n_ens,
+                                    int32_t precision, emcg_handle **out) {
+  EMCG_CHECK_ARG(out, "out is NULL");
+  *out = nullptr;
+  EMCG_CHECK_ARG(models && n_models >= 1, "need at least one model");
+  EMCG_CHECK_ARG(ens && n_ens >= 1, "need at least one ensemble");
+  EMCG_CHECK_ARG(precision == EMCG_FP64 || precision == EMCG_FP32, "bad precision %d",
+                 precision);
+  for (int e = 0; e < n_ens; e++) {
+    const emcg_ensemble_desc &d = ens[e];
+    EMCG_CHECK_ARG(d.model >= 0 && d.model < n_models, "ensemble %d: bad model index", e);
+    EMCG_CHECK_ARG(d.capacity >= 0 && d.capacity < (int64_t(1) << 32),
+                   "ensemble %d: capacity out of range", e);
+    EMCG_CHECK_ARG(d.dt > 0 && std::isfinite(d.dt), "ensemble %d: dt must be positive", e);
+    for (int i = 0; i < 3; i++)
+      EMCG_CHECK_ARG(d.box[i] > 0 && std::isfinite(d.field[i]), "ensemble %d: bad box/field", e);
+  }
+  BulkImpl *b = new BulkImpl();
+  b->precision = precision;
+  b->tsz = precision == EMCG_FP64 ? 8 : 4;
+  b->nModels = n_models;
+  b->nEns = n_ens;
+  b->ens.assign(ens, ens + n_ens);
+  b->valleyCopies.resize(n_models);
+  for (int i = 0; i < n_models; i++) {
+    b->valleyCopies[i].assign(models[i].valleys, models[i].valleys + models[i].n_valleys);
+    emcg_model_desc md = models[i];
+    md.valleys = b->valleyCopies[i].data();
+    md.mechs = nullptr;
+    md.tablesets = nullptr;
+    md.tables = nullptr;
+    b->modelDescs.push_back(md);
+  }
+  b->begin.resize(n_ens);
+  b->count.assign(n_ens, 0);
+  b->cap.resize(n_ens);
+  b->ensNV.resize(n_ens);
+  int64_t off = 0;
+  for (int e = 0; e < n_ens; e++) {
+    b->begin[e] = off;
+    b->cap[e] = ens[e].capacity;
+    off += ens[e].capacity;
+    b->ensNV[e] = models[ens[e].model].n_valleys;
+    b->nVmax = std::max(b->nVmax, models[ens[e].model].n_valleys);
+  }
+  b->totalCap = off;
+  auto fail = [&](int32_t s) {
+    freeBulk(b);
+    return s;
+  };
+  int32_t s = precision == EMCG_FP64
+                  ? createTyped<double>(b, models, n_models, ens, n_ens)
+                  : createTyped<float>(b, models, n_models, ens, n_ens);
+  if (s)
+    return fail(s);
+  size_t n = (size_t)std::max<int64_t>(off, 1);
+  for (int i = 0; i < 9; i++)
+    if (cudaMalloc(&b->dState[i], n * b->tsz) != cudaSuccess) {
+      setError("cudaMalloc of particle state (%zu slots) failed", n);
+      return fail(EMCG_ERR_CUDA);
+    }
+  if (cudaMalloc(&b->dMeta, n * sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc(&b->dErr, sizeof(int)) != cudaSuccess ||
+      cudaMemset(b->dErr, 0, sizeof(int)) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+    setError("CUDA allocation failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return fail(EMCG_ERR_CUDA);
+  }
+  emcg_handle *h = new emcg_handle();
+  h->kind = 1;
+  h->bulk = b;
+  *out = h;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_destroy(emcg_handle *h) {
+  if (!h)
+    return EMCG_OK;
+  if (h->kind == 1)
+    freeBulk(h->bulk);
+  if (h->kind == 2)
+    emcg::destroyDevice(h);
+  delete h;
+  return EMCG_OK;
+}
+
+extern "C" int64_t emcg_num_particles(emcg_handle *h, int32_t e) {
+  BulkImpl *b = nullptr;
+  if (bulkOf(h, &b) || e < 0 || e >= b->nEns)
+    return -1;
+  return b->count[e];
+}
+
+template <class T>
+static int32_t setStateTyped(BulkImpl *b, int e, const emcg_state *s) {
+  const int64_t n = s->n, base = b->begin[e];
+  const double *src[9] = {s->kx, s->ky, s->kz, s->px, s->py, s->pz, s->energy, s->tau,
+                          s->grain_tau};
+  std::vector<T> tmp((size_t)std::max<int64_t>(n, 1));
+  for (int f = 0; f < 9; f++) {
+    EMCG_CHECK_ARG(src[f] != nullptr, "state field %d is NULL", f);
+    for (int64_t i = 0; i < n; i++)
+      tmp[i] = (T)src[f][i];
+    if (n)
+      EMCG_CUDA(cudaMemcpy((T *)b->dState[f] + base, tmp.data(), n * sizeof(T),
+                           cudaMemcpyHostToDevice));
+  }
+  EMCG_CHECK_ARG(s->valley && s->sub && s->region, "state index arrays are NULL");
+  std::vector<uint32_t> meta((size_t)std::max<int64_t>(n, 1));
+  for (int64_t i = 0; i < n; i++) {
+    EMCG_CHECK_ARG(s->valley[i] >= 0 && s->valley[i] < b->ensNV[e] && s->sub[i] >= 0 &&
+                       s->sub[i] < EMCG_MAX_DEG && s->region[i] >= 0 &&
+                       s->region[i] < EMCG_MAX_REGIONS,
+                   "particle %lld: valley/sub/region out of range", (long long)i);
+    meta[i] = packMeta(s->valley[i], s->sub[i], s->region[i]);
+  }
+  if (n)
+    EMCG_CUDA(cudaMemcpy(b->dMeta + base, meta.data(), n * sizeof(uint32_t),
+                         cudaMemcpyHostToDevice));
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_set_state(emcg_handle *h, int32_t e, const emcg_state *s) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(s && e >= 0 && e < b->nEns, "bad ensemble or state");
+  EMCG_CHECK_ARG(s->n >= 0 && s->n <= b->cap[e], "ensemble %d: %lld particles exceed capacity %lld",
+                 e, (long long)s->n, (long long)b->cap[e]);
+  int32_t r = b->precision == EMCG_FP64 ? setStateTyped<double>(b, e, s)
+                                        : setStateTyped<float>(b, e, s);
+  if (r)
+    return r;
+  b->count[e] = s->n;
+  b->tilesDirty = true;
+  return EMCG_OK;
+}
+
+template <class T> static int32_t getStateTyped(BulkImpl *b, int e, emcg_state *s) {
+  const int64_t n = b->count[e], base = b->begin[e];
+  double *dst[9] = {s->kx, s->ky, s->kz, s->px, s->py, s->pz, s->energy, s->tau, s->grain_tau};
+  std::vector<T> tmp((size_t)std::max<int64_t>(n, 1));
+  for (int f = 0; f < 9; f++) {
+    if (!dst[f])
+      continue;
+    if (n)
+      EMCG_CUDA(cudaMemcpy(tmp.data(), (T *)b->dState[f] + base, n * sizeof(T),
+                           cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < n; i++)
+      dst[f][i] = (double)tmp[i];
+  }
+  std::vector<uint32_t> meta((size_t)std::max<int64_t>(n, 1));
+  if (n)
+    EMCG_CUDA(cudaMemcpy(meta.data(), b->dMeta + base, n * sizeof(uint32_t),
+                         cudaMemcpyDeviceToHost));
+  for (int64_t i = 0; i < n; i++) {
+    if (s->valley)
+      s->valley[i] = meta[i] & 0xff;
+    if (s->sub)
+      s->sub[i] = (meta[i] >> 8) & 0xff;
+    if (s->region)
+      s->region[i] = meta[i] >> 16;
+  }
+  s->n = n;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_get_state(emcg_handle *h, int32_t e, emcg_state *s) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(s && e >= 0 && e < b->nEns, "bad ensemble or state");
+  return b->precision == EMCG_FP64 ? getStateTyped<double>(b, e, s)
+                                   : getStateTyped<float>(b, e, s);
+}
+
+extern "C" int32_t emcg_bulk_init(emcg_handle *h, int32_t e, int64_t n, const int64_t *coords,
+                                  const int64_t extent[3], const double spacing[3],
+                                  double thermal_voltage) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(e >= 0 && e < b->nEns, "bad ensemble %d", e);
+  EMCG_CHECK_ARG(n >= 0 && n <= b->cap[e], "ensemble %d: %lld particles exceed capacity", e,
+                 (long long)n);
+  EMCG_CHECK_ARG(thermal_voltage > 0, "thermal voltage must be positive");
+  int64_t ext[3] = {1, 1, 1};
+  double hsp[3] = {1, 1, 1};
+  int64_t *dC = nullptr;
+  if (coords) {
+    EMCG_CHECK_ARG(extent && spacing, "coords need extent and spacing");
+    for (int d = 0; d < 3; d++) {
+      ext[d] = extent[d];
+      hsp[d] = spacing[d];
+      EMCG_CHECK_ARG(ext[d] >= 1 && hsp[d] > 0, "bad extent/spacing");
+    }
+    for (int64_t i = 0; i < 3 * n; i++)
+      EMCG_CHECK_ARG(coords[i] >= 0 && coords[i] < ext[i % 3], "coordinate out of the grid");
+    if (n) {
+      EMCG_CUDA(cudaMalloc(&dC, sizeof(int64_t) * 3 * n));
+      EMCG_CUDA(cudaMemcpy(dC, coords, sizeof(int64_t) * 3 * n, cudaMemcpyHostToDevice));
+    }
+  }
+  const emcg_ensemble_desc &d = b->ens[e];
+  uint32_t k0 = (uint32_t)d.seed, k1 = (uint32_t)(d.seed >> 32);
+  int blocks = (int)((n + 255) / 256);
+  if (n) {
+    if (b->precision == EMCG_FP64)
+      bulkInitKernel<double><<<blocks, 256, 0, b->stream>>>(
+          stateOf<double>(b), (const ModelK<double> *)b->dModels, d.model, b->begin[e], n, dC,
+          ext[0], ext[1], ext[2], hsp[0], hsp[1], hsp[2], thermal_voltage, d.box[0], d.box[1],
+          d.box[2], k0, k1, d.stream);
+    else
+      bulkInitKernel<float><<<blocks, 256, 0, b->stream>>>(
+          stateOf<float>(b), (const ModelK<float> *)b->dModels, d.model, b->begin[e], n, dC,
+          ext[0], ext[1], ext[2], hsp[0], hsp[1], hsp[2], thermal_voltage, d.box[0], d.box[1],
+          d.box[2], k0, k1, d.stream);
+    EMCG_CUDA(cudaGetLastError());
+  }
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  cudaFree(dC);
+  b->count[e] = n;
+  b->tilesDirty = true;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_bulk_step(emcg_handle *h, int32_t n_steps, uint32_t step0, double *obs) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(n_steps >= 0, "n_steps must be >= 0");
+  if (n_steps == 0)
+    return EMCG_OK;
+  if (b->replay) {
+    EMCG_CHECK_ARG(n_steps == 1, "replay mode advances one step per call");
+    EMCG_CHECK_ARG(b->nEns == 1, "replay mode needs exactly one ensemble");
+  }
+  return b->precision == EMCG_FP64 ? stepTyped<double>(b, n_steps, step0, obs)
+                                   : stepTyped<float>(b, n_steps, step0, obs);
+}
+
+extern "C" int32_t emcg_set_replay(emcg_handle *h, const uint64_t *words, int64_t nwords,
+                                   const int64_t *offsets, int64_t n_offsets) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  if (!words) {
+    b->replay = false;
+    return EMCG_OK;
+  }
+  EMCG_CHECK_ARG(b->precision == EMCG_FP64, "replay needs the FP64 engine");
+  EMCG_CHECK_ARG(b->nEns == 1, "replay needs exactly one ensemble");
+  EMCG_CHECK_ARG(offsets && n_offsets == b->count[0] + 1,
+                 "replay: need n+1 = %lld offsets, got %lld", (long long)(b->count[0] + 1),
+                 (long long)n_offsets);
+  EMCG_CHECK_ARG(nwords >= 0, "replay: negative word count");
+  for (int64_t i = 0; i + 1 < n_offsets; i++)
+    EMCG_CHECK_ARG(offsets[i] >= 0 && offsets[i] <= offsets[i + 1] && offsets[i + 1] <= nwords,
+                   "replay: offsets not monotone within [0, nwords]");
+  if (nwords > b->wordsCap) {
+    cudaFree(b->dWords);
+    b->dWords = nullptr;
+    EMCG_CUDA(cudaMalloc(&b->dWords, sizeof(uint64_t) * std::max<int64_t>(nwords, 1)));
+    b->wordsCap = nwords;
+  }
+  if (n_offsets > b->offCap) {
+    cudaFree(b->dOff);
+    b->dOff = nullptr;
+    EMCG_CUDA(cudaMalloc(&b->dOff, sizeof(int64_t) * n_offsets));
+    b->offCap = n_offsets;
+  }
+  if (nwords)
+    EMCG_CUDA(cudaMemcpy(b->dWords, words, sizeof(uint64_t) * nwords, cudaMemcpyHostToDevice));
+  EMCG_CUDA(cudaMemcpy(b->dOff, offsets, sizeof(int64_t) * n_offsets, cudaMemcpyHostToDevice));
+  b->replay = true;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_last_kernel_ms(emcg_handle *h, double *ms) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(ms, "ms is NULL");
+  *ms = b->lastMs;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_set_launch(emcg_handle *h, int32_t block_threads,
+                                   int32_t steps_per_launch) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  if (block_threads) {
+    EMCG_CHECK_ARG(block_threads % 32 == 0 && block_threads >= 32 && block_threads <= 1024,
+                   "block_threads must be a multiple of 32 in [32, 1024]");
+    if (block_threads != b->blockThreads)
+      b->tilesDirty = true;
+    b->blockThreads = block_threads;
+  }
+  if (steps_per_launch) {
+    EMCG_CHECK_ARG(steps_per_launch > 0, "steps_per_launch must be positive");
+    b->stepsPerLaunch = steps_per_launch;
+  }
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_drift_kat(emcg_handle *h, int32_t valley, int64_t n, const int32_t *sub,
+                                  const double *dt, const double *force, double *k, double *pos,
+                                  double *energy) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(n >= 0 && sub && dt && force && k && pos && energy, "bad drift arguments");
+  if (n == 0)
+    return EMCG_OK;
+  // one scratch block: dt | force | k | pos | E (doubles) | sub (int32)
+  void *buf = nullptr;
+  EMCG_CUDA(cudaMalloc(&buf, n * sizeof(double) * 11 + n * sizeof(int32_t)));
+  double *base = (double *)buf;
+  double *dDt = base, *dF = base + n, *dK = base + 4 * n, *dP = base + 7 * n,
+         *dE = base + 10 * n;
+  int32_t *dSub = (int32_t *)(base + 11 * n);
+  EMCG_CUDA(cudaMemcpy(dSub, sub, n * sizeof(int32_t), cudaMemcpyHostToDevice));
+  EMCG_CUDA(cudaMemcpy(dDt, dt, n * sizeof(double), cudaMemcpyHostToDevice));
+  EMCG_CUDA(cudaMemcpy(dF, force, 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+  EMCG_CUDA(cudaMemcpy(dK, k, 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+  EMCG_CUDA(cudaMemcpy(dP, pos, 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+  EMCG_CUDA(cudaMemcpy(dE, energy, n * sizeof(double), cudaMemcpyHostToDevice));
+  int blocks = (int)((n + 127) / 128);
+  if (b->precision == EMCG_FP64)
+    driftKatKernel<double><<<blocks, 128, 0, b->stream>>>((const ModelK<double> *)b->dModels,
+                                                          valley, n, dSub, dDt, dF, dK, dP, dE);
+  else
+    driftKatKernel<float><<<blocks, 128, 0, b->stream>>>((const ModelK<float> *)b->dModels,
+                                                         valley, n, dSub, dDt, dF, dK, dP, dE);
+  EMCG_CUDA(cudaGetLastError());
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  EMCG_CUDA(cudaMemcpy(k, dK, 3 * n * sizeof(double), cudaMemcpyDeviceToHost));
+  EMCG_CUDA(cudaMemcpy(pos, dP, 3 * n * sizeof(double), cudaMemcpyDeviceToHost));
+  EMCG_CUDA(cudaMemcpy(energy, dE, n * sizeof(double), cudaMemcpyDeviceToHost));
+  cudaFree(buf);
+  return EMCG_OK;
+}
+
+template <class T>
+static int32_t updateEnsTyped(BulkImpl *b, int e, const emcg_ensemble_desc &d) {
+  EnsK<T> ek;
+  ModelK<T> dummy;
+  buildEnsK<T>(d, dummy, b->modelDescs[d.model], b->begin[e], 0, ek);
+  EMCG_CUDA(cudaMemcpyAsync((EnsK<T> *)b->dEns + e, &ek, sizeof(EnsK<T>), cudaMemcpyHostToDevice,
+                            b->stream));
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_bulk_update_ensemble(emcg_handle *h, int32_t e,
+                                             const emcg_ensemble_desc *d) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(d && e >= 0 && e < b->nEns, "bad ensemble or descriptor");
+  EMCG_CHECK_ARG(d->model == b->ens[e].model && d->capacity == b->ens[e].capacity,
+                 "ensemble %d: model and capacity cannot change", e);
+  EMCG_CHECK_ARG(d->dt > 0 && std::isfinite(d->dt), "dt must be positive");
+  for (int i = 0; i < 3; i++)
+    EMCG_CHECK_ARG(d->box[i] > 0 && std::isfinite(d->field[i]), "bad box/field");
+  int32_t r = b->precision == EMCG_FP64 ? updateEnsTyped<double>(b, e, *d)
+                                        : updateEnsTyped<float>(b, e, *d);
+  if (r == EMCG_OK)
+    b->ens[e] = *d;
+  return r;
+}

@@ -1,0 +1,59 @@
+// Host-side helpers shared by the translation units of libemcgpu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "emcgpu.h"
+
+namespace emcg {
+
+void setError(const char *fmt, ...);
+
+// Return EMCG_ERR_CUDA (with the CUDA message) if a runtime call failed.
+#define EMCG_CUDA(call)                                                        \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      ::emcg::setError("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                       __FILE__, __LINE__);                                    \
+      return EMCG_ERR_CUDA;                                                    \
+    }                                                                          \
+  } while (0)
+
+#define EMCG_CHECK_ARG(cond, ...)                                              \
+  do {                                                                         \
+    if (!(cond)) {                                                             \
+      ::emcg::setError(__VA_ARGS__);                                           \
+      return EMCG_ERR_ARG;                                                     \
+    }                                                                          \
+  } while (0)
+
+#define EMCG_TRY(expr)                                                         \
+  do {                                                                         \
+    int32_t s_ = (expr);                                                       \
+    if (s_ != EMCG_OK)                                                         \
+      return s_;                                                               \
+  } while (0)
+
+const char *statusName(int32_t s);
+
+struct BulkImpl;
+struct DeviceImpl;
+
+
+} // namespace emcg
+
+struct emcg_handle;
+namespace emcg {
+int32_t destroyDevice(emcg_handle *h); // emcg_device.cu
+}
+
+struct emcg_handle {
+  int kind = 0; // 1 = bulk, 2 = device
+  emcg::BulkImpl *bulk = nullptr;
+  emcg::DeviceImpl *dev = nullptr;
+};
