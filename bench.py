@@ -154,10 +154,28 @@ def run_engine(args):
     avg = BulkBatch.averages(obs, [N])
     b.close()
 
-    # end to end through the C ABI: host state in, per-step observables out
+    if args.skip_e2e:
+        e2e_s, e2e_units, h2d, d2h = float("nan"), 0.0, 0, 0
+    else:
+        e2e_s, e2e_units, h2d, d2h = _e2e(v, pt, spec, args, N, K)
+    if args.fp64_steps > 0:
+        value64, vd32, vd64, win, k64 = _fp64(v, pt, args, N, K, W, per, rank, avg)
+    else:
+        value64 = vd32 = vd64 = k64 = None
+        win = slice(0, 0)
+    _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units, h2d, d2h,
+            value64, vd32, vd64, win, k64, wall, clocks)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _e2e(v, pt, spec, args, N, K):
+    """End to end through the C ABI: host state in, per-step observables out."""
+    import torch
+    from viennaemc_gb300.bulk import BulkBatch
     st = _host_state(v, N)
     b2 = BulkBatch([pt], [spec], "fp32")
-    b2.set_launch(args.block, per)
+    b2.set_launch(args.block, args.steps_per_launch)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     b2.set_state(0, st)
@@ -167,8 +185,12 @@ def run_engine(args):
     e2e_units = float(N) * K
     h2d = N * (9 * 4 + 4) / K
     d2h = o2.shape[-2] * 3 * 8
+    return e2e_s, e2e_units, h2d, d2h
 
-    # plain FP64 engine on the same configuration, and the FP32 v_d error
+
+def _fp64(v, pt, args, N, K, W, per, rank, avg):
+    """Plain FP64 engine on the same configuration, and the FP32 v_d error."""
+    from viennaemc_gb300.bulk import BulkBatch, EnsembleSpec
     k64 = min(K, args.fp64_steps)
     spec64 = EnsembleSpec(0, N, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 999 + rank, 0, 300.0)
     b64 = BulkBatch([pt], [spec64], "fp64")
@@ -186,7 +208,11 @@ def run_engine(args):
     vd32 = float(avg["drift_velocity"][0, win, 0].mean())
     vd64 = float(a64["drift_velocity"][0, win, 0].mean())
     value64 = N * k64 / (ms64 / 1e3)
+    return value64, vd32, vd64, win, k64
 
+
+def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units, h2d, d2h,
+            value64, vd32, vd64, win, k64, wall, clocks):
     peak, peak_src = _peaks()
     bpp = BYTES_PER_PARTICLE_STEP["fp32"]
     achieved = bpp * value / 1e9
@@ -199,28 +225,27 @@ def run_engine(args):
                    "particles": N, "steps_per_launch": per, "block_threads": args.block,
                    "l2": "flushed (256 MB write) between timed launches",
                    "observables": "per-step FP64 sums of E, v.dir, count"},
-        "e2e": {"value": e2e_units / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_units / e2e_s if e2e_units else None, "unit": UNIT,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": n_launch,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_src,
                      "bytes_per_unit": bpp, "unit_of_work": "particle-step"},
-        "fp64_engine": {"value": value64, "unit": UNIT, "steps": k64,
-                        "fp32_speedup": value / value64},
-        "vd_error": {"fp32_mps": vd32, "fp64_mps": vd64,
-                     "rel": abs(vd32 - vd64) / abs(vd64) if vd64 else None,
-                     "window_steps": [win.start, win.stop]},
         "wall_s": wall,
     }
+    if value64:
+        line["fp64_engine"] = {"value": value64, "unit": UNIT, "steps": k64,
+                               "fp32_speedup": value / value64}
+        line["vd_error"] = {"fp32_mps": vd32, "fp64_mps": vd64,
+                            "rel": abs(vd32 - vd64) / abs(vd64) if vd64 else None,
+                            "window_steps": [win.start, win.stop]}
     if clocks:
         line["clocks"] = clocks
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(N, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if ws > 1:
-        torch.distributed.destroy_process_group()
 
 
 def _host_state(v, N):
@@ -340,6 +365,7 @@ def main(argv=None):
     ap.add_argument("--fp64-steps", type=int, default=1500)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

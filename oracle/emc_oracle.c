@@ -7,6 +7,7 @@
  * oracle must reproduce its doubles exactly.
  */
 #include "emc_oracle.h"
+#include "emc_oracle_internal.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -136,18 +137,7 @@ double oc_canonical(uint64_t w) {
   return ret;
 }
 
-/* per particle-step draw context */
-typedef struct {
-  oc_rng *r;
-  int32_t mode;
-  uint32_t ctr[4];
-  uint32_t key[2];
-  uint64_t buf[2];
-  int32_t nbuf;
-  int32_t fail; /* replay log exhausted */
-} dctx;
-
-static void dctx_init(dctx *d, oc_rng *r, uint32_t pid, uint32_t step,
+void oci_dctx_init(dctx *d, oc_rng *r, uint32_t pid, uint32_t step,
                       uint32_t streamWord) {
   d->r = r;
   d->mode = r->mode;
@@ -161,7 +151,7 @@ static void dctx_init(dctx *d, oc_rng *r, uint32_t pid, uint32_t step,
   d->fail = 0;
 }
 
-static uint64_t draw_u64(dctx *d) {
+uint64_t oci_draw_u64(dctx *d) {
   uint64_t w;
   if (d->mode == OC_RNG_MT) {
     w = oc_mt_next(d->r);
@@ -197,9 +187,9 @@ static uint64_t draw_u64(dctx *d) {
 
 /* std::uniform_real_distribution<double>(a, b)(rng) = canonical*(b-a)+a
    (bits/random.h uniform_real_distribution::operator()) */
-static double draw_u01(dctx *d) { return oc_canonical(draw_u64(d)) * (1.0 - 0.0) + 0.0; }
-static double draw_ulog(dctx *d) {
-  return oc_canonical(draw_u64(d)) * (1. - 1e-6) + 1e-6;
+double oci_draw_u01(dctx *d) { return oc_canonical(oci_draw_u64(d)) * (1.0 - 0.0) + 0.0; }
+double oci_draw_ulog(dctx *d) {
+  return oc_canonical(oci_draw_u64(d)) * (1. - 1e-6) + 1e-6;
 }
 
 /* ======================================================================== */
@@ -611,11 +601,11 @@ static void random_direction(double nrm, double r1, double r2, double *o) {
 /* two draws in the compiled reference's argument order */
 static void random_direction_draw(double nrm, dctx *d, double *o) {
 #if OC_ARGS_RIGHT_TO_LEFT
-  double r2 = draw_u01(d);
-  double r1 = draw_u01(d);
+  double r2 = oci_draw_u01(d);
+  double r1 = oci_draw_u01(d);
 #else
-  double r1 = draw_u01(d);
-  double r2 = draw_u01(d);
+  double r1 = oci_draw_u01(d);
+  double r2 = oci_draw_u01(d);
 #endif
   random_direction(nrm, r1, r2, o);
 }
@@ -671,7 +661,7 @@ static void mech_scatter(const oc_model *m, const oc_mech *me, double *k,
   case OC_ZERO_IV_EMI:
   case OC_FIRST_IV_EMI: { /* ...ZeroOrder...hpp:247-257, 390-400 etc. */
     *valley = me->finalValley;
-    uint64_t w = draw_u64(d);
+    uint64_t w = oci_draw_u64(d);
     *sub = me->finalSub[*sub][w % (uint64_t)me->nF];
     if (me->kind == OC_ZERO_IV_ABS || me->kind == OC_FIRST_IV_ABS)
       *E += (me->p1 - me->deltaValley);
@@ -686,11 +676,11 @@ static void mech_scatter(const oc_model *m, const oc_mech *me, double *k,
     double g = gamma_of(v, *E);
     double doping = fabs(m->regionDoping[region]);
     double mc = v->mc * (1 + 2 * 0. * v->alpha);
-    double rnd = draw_u01(d);
+    double rnd = oci_draw_u01(d);
     double debye = doping / (me->sc2 * mc);
     double ct = 1.0 - rnd * 2.0 / ((1 - rnd) * g / debye + 1.0);
     double kin[3] = {k[0], k[1], k[2]};
-    random_direction_wrt_k(kin, ct, draw_u01(d), k);
+    random_direction_wrt_k(kin, ct, oci_draw_u01(d), k);
     break;
   }
   }
@@ -698,7 +688,7 @@ static void mech_scatter(const oc_model *m, const oc_mech *me, double *k,
 
 /* include/emcScatterHandler.hpp:148-170; returns -1 if the (valley, region)
    pair has no table set (the reference's std::map::at throws there) */
-static int32_t handler_scatter(const oc_model *m, double *k, double *E,
+int32_t oci_handler_scatter(const oc_model *m, double *k, double *E,
                                int32_t *valley, int32_t *sub, int32_t region,
                                dctx *d) {
   int v = *valley;
@@ -711,7 +701,7 @@ static int32_t handler_scatter(const oc_model *m, double *k, double *E,
   const double *nt = m->norm[v][region];
   int L = m->nLevels;
   int32_t lvl = energy_level(m, *E);
-  double rnd = draw_u01(d);
+  double rnd = oci_draw_u01(d);
   if (rnd > nt[(nT - 1) * L + lvl])
     return 0;
   double lo = 0, hi;
@@ -728,9 +718,9 @@ static int32_t handler_scatter(const oc_model *m, double *k, double *E,
 }
 
 /* include/ParticleType/emcParticleType.hpp:187-189 */
-static double new_tau(const oc_model *m, int32_t valley, int32_t region,
+double oci_new_tau(const oc_model *m, int32_t valley, int32_t region,
                       dctx *d) {
-  return -log(draw_ulog(d)) * oc_get_tau(m, valley, region);
+  return -log(oci_draw_ulog(d)) * oc_get_tau(m, valley, region);
 }
 
 /* ======================================================================== */
@@ -763,11 +753,11 @@ static int32_t bulk_particle_step(const oc_model *m, oc_particles *p, int64_t i,
   bulk_drift(m, (dt < tau) ? dt : tau, k, &E, valley, sub, pos, force, box);
   double tRem = dt - tau;
   while (tRem > 0) {
-    if (handler_scatter(m, k, &E, &valley, &sub, region, d) < 0) {
+    if (oci_handler_scatter(m, k, &E, &valley, &sub, region, d) < 0) {
       st = -1;
       break;
     }
-    double nt = new_tau(m, valley, region, d);
+    double nt = oci_new_tau(m, valley, region, d);
     tau += nt;
     bulk_drift(m, (nt < tRem) ? nt : tRem, k, &E, valley, sub, pos, force, box);
     tRem -= nt;
@@ -775,7 +765,7 @@ static int32_t bulk_particle_step(const oc_model *m, oc_particles *p, int64_t i,
   tau -= dt;
   gtau -= dt;
   if (gtau <= 0) /* no grain mechanism: scatterParticleAtGrain is a no-op */
-    gtau = -log(draw_ulog(d)) * 1.;
+    gtau = -log(oci_draw_ulog(d)) * 1.;
   p->kx[i] = k[0];
   p->ky[i] = k[1];
   p->kz[i] = k[2];
@@ -796,7 +786,7 @@ int32_t oc_bulk_step(const oc_model *m, oc_particles *p, double dt,
   int32_t st = 0;
   for (int64_t i = 0; i < p->n; i++) {
     dctx d;
-    dctx_init(&d, r, (uint32_t)i, step, r->stream);
+    oci_dctx_init(&d, r, (uint32_t)i, step, r->stream);
     if (offsets)
       offsets[i] = r->rec_n;
     int32_t s = bulk_particle_step(m, p, i, dt, force, box, &d);
@@ -848,7 +838,7 @@ int32_t oc_bulk_run_philox(const oc_model *m, oc_particles *p, double dt,
 #endif
       for (int64_t i = 0; i < p->n; i++) {
         dctx d;
-        dctx_init(&d, &r, (uint32_t)i, step0 + (uint32_t)s, stream);
+        oci_dctx_init(&d, &r, (uint32_t)i, step0 + (uint32_t)s, stream);
         if (bulk_particle_step(m, p, i, dt, force, box, &d))
           status = -1;
         if (obs)
@@ -891,39 +881,39 @@ void oc_observables(const oc_model *m, const oc_particles *p,
 }
 
 /* include/emcParticleInitialization.hpp:14-29 */
-static void init_pos(const int64_t *coord, const int64_t *ext,
+void oci_init_pos(const int64_t *coord, const int64_t *ext,
                      const double *h, int32_t dim, dctx *d, double *pos) {
   for (int i = 0; i < dim; i++) {
     if (coord[i] == ext[i] - 1)
-      pos[i] = ((double)coord[i] - draw_u01(d) * 0.5) * h[i];
+      pos[i] = ((double)coord[i] - oci_draw_u01(d) * 0.5) * h[i];
     else if (coord[i] == 0)
-      pos[i] = draw_u01(d) * 0.5 * h[i];
+      pos[i] = oci_draw_u01(d) * 0.5 * h[i];
     else
-      pos[i] = ((double)coord[i] + draw_u01(d) - 0.5) * h[i];
+      pos[i] = ((double)coord[i] + oci_draw_u01(d) - 0.5) * h[i];
   }
 }
 
 /* include/ParticleType/emcElectron.hpp:75-90 (+ initParticleKSpaceMaxwellian,
    include/emcParticleInitialization.hpp:36-51).  tauRegionIsValley mirrors
    examples/mosfet2D/electronVWD.hpp:73 (getNewTau(valley, valley)). */
-static void init_particle_d(const oc_model *m, const int64_t *coord,
+void oci_init_particle(const oc_model *m, const int64_t *coord,
                             const int64_t *ext, const double *h, int32_t dim,
                             int32_t region, double Vt, dctx *d,
                             oc_particles *p, int64_t idx,
                             int32_t tauRegionIsValley) {
   double pos[3] = {0, 0, 0};
-  init_pos(coord, ext, h, dim, d, pos);
-  int32_t valley = (int32_t)floor((double)m->nV * draw_ulog(d));
-  int32_t sub = (int32_t)floor((double)m->v[valley].deg * draw_ulog(d));
-  double E = -1.5 * Vt * log(draw_ulog(d));
+  oci_init_pos(coord, ext, h, dim, d, pos);
+  int32_t valley = (int32_t)floor((double)m->nV * oci_draw_ulog(d));
+  int32_t sub = (int32_t)floor((double)m->v[valley].deg * oci_draw_ulog(d));
+  double E = -1.5 * Vt * log(oci_draw_ulog(d));
   double k[3];
   random_direction_draw(oc_norm_wave_vec(m, valley, E), d, k);
   for (int i = 0; i < dim; i++)
     if ((coord[i] == 0 && k[i] < 0) || (coord[i] == ext[i] - 1 && k[i] > 0))
       k[i] *= -1;
-  double tau = -log(draw_ulog(d)) *
+  double tau = -log(oci_draw_ulog(d)) *
                oc_get_tau(m, valley, tauRegionIsValley ? valley : region);
-  double gtau = -log(draw_ulog(d)) * 1.;
+  double gtau = -log(oci_draw_ulog(d)) * 1.;
   p->kx[idx] = k[0];
   p->ky[idx] = k[1];
   p->kz[idx] = k[2];
@@ -945,8 +935,8 @@ void oc_init_particle(const oc_model *m, const int64_t coord[3],
                       oc_rng *r, oc_particles *p, int64_t idx,
                       int32_t tauRegionIsValley) {
   dctx d;
-  dctx_init(&d, r, (uint32_t)idx, 0xFFFFFFFFu, r->stream);
-  init_particle_d(m, coord, extent, spacing, dim, region, thermalVoltage, &d, p,
+  oci_dctx_init(&d, r, (uint32_t)idx, 0xFFFFFFFFu, r->stream);
+  oci_init_particle(m, coord, extent, spacing, dim, region, thermalVoltage, &d, p,
                   idx, tauRegionIsValley);
 }
 
@@ -977,21 +967,22 @@ int64_t oc_bulk_init(const oc_model *m, const double maxPos[3],
           if (n >= cap)
             return -1;
           dctx d;
-          dctx_init(&d, r, (uint32_t)n, 0xFFFFFFFFu, r->stream);
-          init_particle_d(m, c, ext, spacing, 3, 0, Vt, &d, p, n, 0);
+          oci_dctx_init(&d, r, (uint32_t)n, 0xFFFFFFFFu, r->stream);
+          oci_init_particle(m, c, ext, spacing, 3, 0, Vt, &d, p, n, 0);
           n++;
           nr--;
         }
         dctx d;
-        dctx_init(&d, r, (uint32_t)n, 0xFFFFFFFEu, r->stream);
-        if (draw_u01(&d) < nr) {
+        oci_dctx_init(&d, r, (uint32_t)n, 0xFFFFFFFEu, r->stream);
+        if (oci_draw_u01(&d) < nr) {
           if (n >= cap)
             return -1;
-          dctx_init(&d, r, (uint32_t)n, 0xFFFFFFFFu, r->stream);
-          init_particle_d(m, c, ext, spacing, 3, 0, Vt, &d, p, n, 0);
+          oci_dctx_init(&d, r, (uint32_t)n, 0xFFFFFFFFu, r->stream);
+          oci_init_particle(m, c, ext, spacing, 3, 0, Vt, &d, p, n, 0);
           n++;
         }
       }
   p->n = n;
   return n;
 }
+int32_t oci_nvalleys(const oc_model *m) { return m->nV; }
