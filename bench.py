@@ -123,7 +123,7 @@ def run_engine(args):
     pt = silicon_model(v, "fp32")
     spec = EnsembleSpec(0, N, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 1234 + rank, 0, 300.0)
     b = BulkBatch([pt], [spec], "fp32")
-    b.set_launch(args.block, per)
+    b.set_launch(args.block, per, args.min_blocks)
     b.init_particles(0)
     # warm-up (untimed)
     b.step(W)
@@ -175,7 +175,7 @@ def _e2e(v, pt, spec, args, N, K):
     from viennaemc_gb300.bulk import BulkBatch
     st = _host_state(v, N)
     b2 = BulkBatch([pt], [spec], "fp32")
-    b2.set_launch(args.block, args.steps_per_launch)
+    b2.set_launch(args.block, args.steps_per_launch, args.min_blocks)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     b2.set_state(0, st)
@@ -223,6 +223,7 @@ def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units,
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": "bulk Si, 2^20 electrons, 1e6 V/m <100>, dt 1 fs, 5000 steps",
                    "particles": N, "steps_per_launch": per, "block_threads": args.block,
+                   "min_blocks_per_sm": args.min_blocks,
                    "l2": "flushed (256 MB write) between timed launches",
                    "observables": "per-step FP64 sums of E, v.dir, count"},
         "e2e": {"value": e2e_units / e2e_s if e2e_units else None, "unit": UNIT,
@@ -362,6 +363,7 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=1 << 20)
     ap.add_argument("--steps-per-launch", type=int, default=500)
     ap.add_argument("--block", type=int, default=256)
+    ap.add_argument("--min-blocks", type=int, default=1, help="register cap variant (1, 3, 4)")
     ap.add_argument("--fp64-steps", type=int, default=1500)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -180,7 +180,8 @@ int32_t emcg_bulk_update_ensemble(emcg_handle *h, int32_t ens,
                                   const emcg_ensemble_desc *desc);
 
 /* Upload / download ensemble e's particles (replaces direct access to the
-   handler's particles / positionsParticles vectors, :58-59). */
+   handler's particles / positionsParticles vectors, :58-59).  For a device
+   engine (emcg_device_create) e must be 0 and pz is ignored. */
 int32_t emcg_set_state(emcg_handle *h, int32_t ens, const emcg_state *s);
 int32_t emcg_get_state(emcg_handle *h, int32_t ens, emcg_state *s);
 int64_t emcg_num_particles(emcg_handle *h, int32_t ens);
@@ -223,6 +224,11 @@ int32_t emcg_last_kernel_ms(emcg_handle *h, double *ms);
 int32_t emcg_set_launch(emcg_handle *h, int32_t block_threads,
                         int32_t steps_per_launch);
 
+/* Tuning: register cap of the step kernel, as the minimum number of resident
+   256-thread blocks per SM (1 = uncapped, 3 or 4); capped variants apply to
+   blocks of at most 256 threads. */
+int32_t emcg_set_occupancy(emcg_handle *h, int32_t min_blocks_per_sm);
+
 /* ---- single-particle kernels (known-answer tests of the reference) ----- */
 /* drift() of include/emcParticleDrift.hpp:11-36 for n independent
    particles of valley v of model 0: k, pos (3 x n, SoA) and energy in/out,
@@ -231,6 +237,95 @@ int32_t emcg_drift_kat(emcg_handle *h, int32_t valley, int64_t n,
                        const int32_t *sub, const double *dt,
                        const double *force, double *k, double *pos,
                        double *energy);
+
+/* ---- device engine (include/emcSimulation.hpp:164-193) ------------------ */
+#define EMCG_PM_NGP 0 /* include/PMSchemes/emcNGPScheme.hpp */
+#define EMCG_PM_CIC 1 /* include/PMSchemes/emcCICScheme.hpp */
+#define EMCG_CONTACT_OHMIC 0
+#define EMCG_CONTACT_SCHOTTKY 1
+#define EMCG_CONTACT_GATE 2
+#define EMCG_GRID_POTENTIAL 0 /* phi / Vt (Debye-normalised)           */
+#define EMCG_GRID_EX 1        /* V/m                                   */
+#define EMCG_GRID_EY 2
+#define EMCG_GRID_NRPART 3    /* particles assigned to each node       */
+#define EMCG_GRID_CONC 4      /* electron concentration / Ni           */
+
+/* A 2-D emcDevice (include/emcDevice.hpp:38-344) flattened; grids are x
+   fastest (include/emcGrid.hpp:242-254).  boundary_contact[b] lists the
+   contact index of every coordinate of boundary b (XMIN, XMAX: ny entries;
+   YMIN, YMAX: nx entries; -1 = artificial boundary), as emcSurface's
+   idxContactGrid (include/emcSurface.hpp:37-64, 199-222). */
+typedef struct {
+  int32_t nx, ny;
+  double hx, hy;       /* m */
+  double max_x, max_y; /* device extent maxPos [m]; 0: (n - 1) h */
+  double width;        /* extent in the third dimension [m] */
+  double temperature;  /* K */
+  double ni;           /* intrinsic density [1/m^3] */
+  double eps_r;
+  const double *doping;  /* net doping [1/m^3] */
+  const int32_t *region; /* doping-region index */
+  const int32_t *boundary_contact[4];
+  int32_t n_contacts;
+  int32_t pad_;
+  const int32_t *contact_type;
+  const double *contact_voltage; /* V */
+  const double *contact_param;   /* 3 per contact: oxide eps_r, oxide
+                                    thickness [m], barrier height [V] */
+} emcg_device_desc;
+
+/* emcSimulationParameter + particle handler + solver settings. */
+typedef struct {
+  int32_t pm_scheme;            /* EMCG_PM_NGP | EMCG_PM_CIC */
+  int32_t tau_region_is_valley; /* injection draws tau with the valley as the
+                                   region (examples/mosfet2D/electronVWD.hpp:87) */
+  int64_t capacity;             /* particle slots */
+  double dt;                    /* s */
+  double charge;                /* C */
+  double carriers_per_particle;
+  uint64_t seed;
+  uint32_t stream;
+  int32_t poisson_max_cycles;   /* Newton / defect-correction iterations */
+  double poisson_rtol;          /* relative residual target */
+  int32_t poisson_smooth;       /* red-black sweeps before and after */
+  int32_t poisson_fp32;         /* 1: float V-cycles in double refinement */
+} emcg_device_config;
+
+/* Create a device engine (emcSimulation constructor: particle handler with
+   expected contact counts, solver, PM scheme). */
+int32_t emcg_device_create(const emcg_model_desc *model, const emcg_device_desc *dev,
+                           const emcg_device_config *cfg, int32_t precision,
+                           emcg_handle **out);
+int32_t emcg_device_set_grid(emcg_handle *h, int32_t which, const double *v);
+int32_t emcg_device_get_grid(emcg_handle *h, int32_t which, double *v);
+/* emcAbstractSolver::calcEquilibriumPotential / calcNonEquilibriumPotential
+   (include/PoissonSolver/emcAbstractSolver.hpp:9-58) on the potential grid,
+   the latter with the current concentration grid. */
+int32_t emcg_device_poisson(emcg_handle *h, int32_t equilibrium, int32_t reset_bc,
+                            double *rel_residual, int32_t *cycles);
+/* emcAbstractPMScheme::calcEField (include/PMSchemes/emcEFieldCalculation.hpp:13-81) */
+int32_t emcg_device_efield(emcg_handle *h);
+/* driftScatterParticles (include/ParticleHandler/emcBasicParticleHandler.hpp:76-145):
+   netto[c] += particles that left through contact c. */
+int32_t emcg_device_move(emcg_handle *h, uint32_t step, int32_t *netto);
+/* handleOhmicContacts (:158-192): rem_inj[c] = injected - removed at c. */
+int32_t emcg_device_contacts(emcg_handle *h, uint32_t step, int32_t *rem_inj);
+/* assignParticlesToMesh + updateCurrentParticleConcentrations
+   (include/emcSimulation.hpp:207-213, include/emcSimulationResults.hpp:98-116) */
+int32_t emcg_device_assign(emcg_handle *h);
+/* performEMCStep (include/emcSimulation.hpp:164-193) n_steps times; netto
+   (n_steps x n_contacts, may be NULL) receives removed - (injected - deleted)
+   per step and contact, as emcSimulationResults::updateCurrent consumes. */
+int32_t emcg_device_step(emcg_handle *h, int32_t n_steps, uint32_t step0, int32_t *netto);
+/* generateInitialParticles (include/ParticleHandler/emcAbstractParticleHandler.hpp:
+   133-148): counts from exp(potential) Ni (potential_based) or the doping. */
+int32_t emcg_device_init(emcg_handle *h, int32_t potential_based, int32_t round_counts);
+/* Replay words for the next move (phase 0, offsets per particle) or
+   contact injection (phase 1, offsets per injected particle). */
+int32_t emcg_device_set_replay(emcg_handle *h, int32_t phase, const uint64_t *words,
+                               int64_t nwords, const int64_t *offsets, int64_t n_offsets);
+/* Device-side time of the last emcg_device_step / poisson call (ms). */
+int32_t emcg_device_timing(emcg_handle *h, double *step_ms, double *poisson_ms);
 
 #ifdef __cplusplus
 }

@@ -158,6 +158,75 @@ void oc_init_particle(const oc_model *m, const int64_t coord[3],
                       oc_rng *r, oc_particles *p, int64_t idx,
                       int32_t tauRegionIsValley);
 
+/* ---- device (2-D) path ------------------------------------------------- */
+enum { OC_NGP = 0, OC_CIC = 1 };
+enum { OC_OHMIC = 0, OC_SCHOTTKY = 1, OC_GATE = 2 };
+enum { OC_XMIN = 0, OC_XMAX = 1, OC_YMIN = 2, OC_YMAX = 3 };
+
+/* A 2-D emcDevice flattened: grids are x fastest (include/emcGrid.hpp:242-254);
+   bnd[b] holds the contact index of each coordinate of boundary b (-1: none),
+   XMIN/XMAX indexed by y, YMIN/YMAX by x (include/emcSurface.hpp:37-64). */
+typedef struct {
+  int32_t nx, ny;
+  double hx, hy;
+  double maxX, maxY;
+  double width;
+  double T, Ni, epsR;
+  const double *doping;
+  const int32_t *region;
+  const int32_t *bnd[4];
+  int32_t nContacts;
+  int32_t pad_;
+  const int32_t *ctype;
+  const double *cvolt;
+  const double *cpar; /* nContacts x 3: epsR oxide, thickness [m], barrier [V] */
+} oc_dev;
+
+double oc_dev_debye(const oc_dev *d);
+double oc_dev_cell_volume(const oc_dev *d);
+int32_t oc_dev_contact_idx(const oc_dev *d, int32_t x, int32_t y);
+int32_t oc_dev_is_reservoir(const oc_dev *d, int32_t x, int32_t y);
+void oc_dev_efield(const oc_dev *d, const double *pot, double *Ex, double *Ey);
+void oc_dev_assign(const oc_dev *d, int32_t scheme, const double *px,
+                   const double *py, int64_t n, double nrCarriers,
+                   double *grid);
+void oc_dev_force(const oc_dev *d, int32_t scheme, const double *Ex,
+                  const double *Ey, double x, double y, double charge,
+                  double F[3]);
+/* driftScatterParticles (include/ParticleHandler/emcBasicParticleHandler.hpp:
+   76-145): moves every particle, removes those that left through an ohmic
+   contact (stable), netto[c] counts them per contact.  offsets (n+1, may be
+   NULL) receive each particle's word offsets into r->rec. */
+int32_t oc_dev_move(const oc_model *m, const oc_dev *d, int32_t scheme,
+                    oc_particles *p, const double *Ex, const double *Ey,
+                    double dt, double charge, oc_rng *r, uint32_t step,
+                    int32_t *netto, int64_t *offsets);
+/* expected particles at reservoir nodes (emcElectron.hpp:63-73) */
+void oc_dev_exp_nr(const oc_dev *d, double *expNr, int32_t roundCounts);
+/* handleOhmicContacts (emcBasicParticleHandler.hpp:158-192 with
+   emcAbstractParticleHandler.hpp:200-216): removes excess particles at
+   reservoir nodes, injects missing ones (appended, grid order).  remInj[c]
+   gets -removed + injected per contact.  Returns the new particle count or a
+   negative status. */
+int64_t oc_dev_contacts(const oc_model *m, const oc_dev *d, oc_particles *p,
+                        int64_t cap, const double *expNr, double nrCarriers,
+                        oc_rng *r, uint32_t step, int32_t *remInj,
+                        int32_t tauRegionIsValley);
+/* generateInitialParticles (emcAbstractParticleHandler.hpp:133-148) with
+   emcElectron::getInitialNrParticles (emcElectron.hpp:48-61): pot != NULL ->
+   exp(pot) Ni, else the doping; roundCounts mirrors electronVWD. */
+int64_t oc_dev_init(const oc_model *m, const oc_dev *d, const double *pot,
+                    int32_t roundCounts, double nrCarriers, oc_rng *r,
+                    oc_particles *p, int64_t cap, int32_t tauRegionIsValley);
+void oc_dev_concentration(const oc_dev *d, const double *nrPart, double *conc);
+void oc_dev_init_potential(const oc_dev *d, double *pot);
+/* emcSORSolver (include/PoissonSolver/emcSORSolver.hpp:49-197): eConc NULL ->
+   equilibrium, else non-equilibrium with the given normalised electron
+   concentration.  Returns sweeps used (<= maxSweeps), negative on error. */
+int64_t oc_dev_sor(const oc_dev *d, double *pot, const double *eConc,
+                   double omega, double accuracyVolt, int32_t resetBC,
+                   int64_t maxSweeps);
+
 #ifdef __cplusplus
 }
 #endif

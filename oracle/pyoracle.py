@@ -385,3 +385,145 @@ def run_ref(*args) -> dict:
 
 def state_from_ref(d: dict, tag: str) -> State:
     return State.from_dict({f: d[f"{tag}_{f}"] for f in STATE_F + STATE_I})
+
+
+# ---- device (2-D) path ----------------------------------------------------------
+NGP, CIC = 0, 1
+
+
+class DevDesc(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("hx", C.c_double), ("hy", C.c_double),
+                ("maxX", C.c_double), ("maxY", C.c_double), ("width", C.c_double),
+                ("T", C.c_double), ("Ni", C.c_double), ("epsR", C.c_double),
+                ("doping", C.POINTER(C.c_double)), ("region", C.POINTER(C.c_int32)),
+                ("bnd", C.POINTER(C.c_int32) * 4), ("nContacts", C.c_int32), ("pad_", C.c_int32),
+                ("ctype", C.POINTER(C.c_int32)), ("cvolt", C.POINTER(C.c_double)),
+                ("cpar", C.POINTER(C.c_double))]
+
+
+def _declare_dev(L):
+    d, i32, i64, u32, vp = C.c_double, C.c_int32, C.c_int64, C.c_uint32, C.c_void_p
+    P = C.POINTER
+    L.oc_dev_debye.restype = d
+    L.oc_dev_debye.argtypes = [P(DevDesc)]
+    L.oc_dev_cell_volume.restype = d
+    L.oc_dev_cell_volume.argtypes = [P(DevDesc)]
+    L.oc_dev_contact_idx.restype = i32
+    L.oc_dev_contact_idx.argtypes = [P(DevDesc), i32, i32]
+    L.oc_dev_is_reservoir.restype = i32
+    L.oc_dev_is_reservoir.argtypes = [P(DevDesc), i32, i32]
+    L.oc_dev_efield.argtypes = [P(DevDesc), P(d), P(d), P(d)]
+    L.oc_dev_assign.argtypes = [P(DevDesc), i32, P(d), P(d), i64, d, P(d)]
+    L.oc_dev_force.argtypes = [P(DevDesc), i32, P(d), P(d), d, d, d, P(d)]
+    L.oc_dev_move.restype = i32
+    L.oc_dev_move.argtypes = [vp, P(DevDesc), i32, P(Particles), P(d), P(d), d, d, P(Rng), u32,
+                              P(i32), P(i64)]
+    L.oc_dev_exp_nr.argtypes = [P(DevDesc), P(d), i32]
+    L.oc_dev_contacts.restype = i64
+    L.oc_dev_contacts.argtypes = [vp, P(DevDesc), P(Particles), i64, P(d), d, P(Rng), u32, P(i32),
+                                  i32]
+    L.oc_dev_concentration.argtypes = [P(DevDesc), P(d), P(d)]
+    L.oc_dev_init_potential.argtypes = [P(DevDesc), P(d)]
+    L.oc_dev_sor.restype = i64
+    L.oc_dev_sor.argtypes = [P(DevDesc), P(d), P(d), d, d, i32, i64]
+    L.oc_dev_init.restype = i64
+    L.oc_dev_init.argtypes = [vp, P(DevDesc), P(d), i32, d, P(Rng), P(Particles), i64, i32]
+
+
+class Device:
+    """Flattened 2-D device for the oracle (arrays kept alive here)."""
+
+    def __init__(self, nx, ny, hx, hy, width, doping, region, bnd, ctype, cvolt, cpar,
+                 T=300.0, Ni=1.45e16, epsR=11.8):
+        L = lib()
+        if not hasattr(L, "_dev_declared"):
+            _declare_dev(L)
+            L._dev_declared = True
+        self.nx, self.ny = nx, ny
+        self.doping = darr(doping)
+        self.region = np.ascontiguousarray(np.asarray(region, np.int32))
+        self.bnd = [np.ascontiguousarray(np.asarray(b, np.int32)) for b in bnd]
+        self.ctype = np.ascontiguousarray(np.asarray(ctype, np.int32))
+        self.cvolt = darr(cvolt)
+        self.cpar = darr(cpar).reshape(-1)
+        d = DevDesc()
+        d.nx, d.ny, d.hx, d.hy = nx, ny, hx, hy
+        d.maxX, d.maxY = hx * (nx - 1), hy * (ny - 1)
+        d.width, d.T, d.Ni, d.epsR = width, T, Ni, epsR
+        d.doping, d.region = dptr(self.doping), iptr(self.region)
+        for b in range(4):
+            d.bnd[b] = iptr(self.bnd[b])
+        d.nContacts = len(self.ctype)
+        d.ctype, d.cvolt, d.cpar = iptr(self.ctype), dptr(self.cvolt), dptr(self.cpar)
+        self.d = d
+
+    def set_max(self, maxX, maxY):
+        self.d.maxX, self.d.maxY = maxX, maxY
+
+    @property
+    def L(self):
+        return lib()
+
+    def efield(self, pot):
+        Ex = np.zeros(self.nx * self.ny)
+        Ey = np.zeros(self.nx * self.ny)
+        self.L.oc_dev_efield(C.byref(self.d), dptr(darr(pot)), dptr(Ex), dptr(Ey))
+        return Ex, Ey
+
+    def sor(self, pot, conc=None, omega=1.8, acc=1e-4, reset=True, max_sweeps=10 ** 7):
+        pot = darr(pot).copy()
+        c = dptr(darr(conc)) if conc is not None else None
+        n = self.L.oc_dev_sor(C.byref(self.d), dptr(pot), c, omega, acc, int(reset), max_sweeps)
+        return pot, n
+
+    def assign(self, scheme, st, nrC=1.0):
+        g = np.zeros(self.nx * self.ny)
+        self.L.oc_dev_assign(C.byref(self.d), scheme, dptr(st.px), dptr(st.py), st.n, nrC, dptr(g))
+        return g
+
+    def concentration(self, nr):
+        c = np.zeros(self.nx * self.ny)
+        self.L.oc_dev_concentration(C.byref(self.d), dptr(darr(nr)), dptr(c))
+        return c
+
+    def exp_nr(self, round_counts=False):
+        e = np.zeros(self.nx * self.ny)
+        self.L.oc_dev_exp_nr(C.byref(self.d), dptr(e), int(round_counts))
+        return e
+
+    def move(self, model, scheme, st, Ex, Ey, dt, rng, step, charge=-1.60219e-19, offsets=False):
+        p = st.cstruct()
+        netto = np.zeros(max(len(self.ctype), 1), np.int32)
+        off = np.zeros(st.n + 1, np.int64) if offsets else None
+        rc = self.L.oc_dev_move(model.h, C.byref(self.d), scheme, C.byref(p), dptr(darr(Ex)),
+                                dptr(darr(Ey)), dt, charge, C.byref(rng.r), step, iptr(netto),
+                                lptr(off) if off is not None else None)
+        st.n = int(p.n)
+        return rc, netto, off
+
+    def contacts(self, model, st, cap, expnr, rng, step, nrC=1.0, tau_region_is_valley=False):
+        """st must have capacity `cap` allocated (State.resize)."""
+        p = st.cstruct()
+        p.n = st.n
+        remInj = np.zeros(max(len(self.ctype), 1), np.int32)
+        n = self.L.oc_dev_contacts(model.h, C.byref(self.d), C.byref(p), cap, dptr(darr(expnr)),
+                                   nrC, C.byref(rng.r), step, iptr(remInj),
+                                   int(tau_region_is_valley))
+        assert n >= 0, n
+        st.n = int(n)
+        return remInj
+
+    def init_particles(self, model, rng, pot=None, round_counts=False, nrC=1.0, cap=1 << 20,
+                       tau_region_is_valley=False):
+        st = State(cap)
+        p = st.cstruct()
+        n = self.L.oc_dev_init(model.h, C.byref(self.d), dptr(darr(pot)) if pot is not None
+                               else None, int(round_counts), nrC, C.byref(rng.r), C.byref(p), cap,
+                               int(tau_region_is_valley))
+        assert n >= 0
+        return st.resize(int(n))
+
+
+def truncate(st: State, n: int) -> State:
+    """View of the first n particles (copy)."""
+    return st.resize(n)

@@ -83,6 +83,95 @@ def make_bulk(case):
     print(f"bulk_{name}: n={st.n} steps={steps} words={len(out['words'])} tables={nT}")
 
 
+# (name, kind, seed, dt, steps, SOR accuracy [V], device width [m])
+DEVICE_CASES = [("resistor_ngp", "resistor", 42, 1e-15, 3, 1e-4, 3e-7),
+                ("mosfet_cic", "mosfet", 7, 1e-15, 3, 1e-4, 3e-8)]
+
+
+def device_of(d):
+    g = d["geom"]
+    nx, ny = int(round(g[0] / g[2])) + 1, int(round(g[1] / g[3])) + 1
+    dev = po.Device(nx, ny, g[2], g[3], g[4], d["doping"], d["region"],
+                    [d[f"bnd{b}"] for b in range(4)], d["ctype"], d["cvolt"],
+                    d["cpar"].reshape(-1, 3))
+    dev.set_max(g[0], g[1])
+    return dev
+
+
+def device_model(d):
+    """Oracle model of the device harness: acoustic, Coulomb and zero-order f/g
+    intervalley phonons on every doping region (4 eV tables)."""
+    nreg = int(d["region"].max()) + 1
+    m = po.Model(n_levels=1000, max_energy=4.0)
+    m.add_valley([0.916, 0.196, 0.196], po.ME, 3, 0.5, 0.0, po.SI_FRAMES)
+    regs = list(range(nreg))
+    for r in regs:
+        m.set_region_doping(r, d["doping"][d["region"] == r][0])
+    m.add_mech(po.ACOUSTIC, 0, regs, 9.0)
+    m.add_mech(po.COULOMB, 0, regs, 11.8)
+    for fs in (po.F_SUB, po.G_SUB):
+        m.add_mech(po.ZERO_IV_ABS, 0, regs, 5.23e10, 0.06, 0, fs)
+        m.add_mech(po.ZERO_IV_EMI, 0, regs, 5.23e10, 0.06, 0, fs)
+    m.build_tables()
+    return m, regs
+
+
+def make_device(case):
+    name, kind, seed, dt, steps, acc, width = case
+    d = po.run_ref("device", kind, seed, dt, steps, acc, width)
+    dev = device_of(d)
+    m, regs = device_model(d)
+    for r in regs:
+        for t in range(6):
+            assert np.array_equal(m.raw_table(0, r, t), d[f"raw_v0_r{r}_t{t}"])
+    out = {k: d[k] for k in ("doping", "region", "bnd0", "bnd1", "bnd2", "bnd3", "ctype",
+                             "cvolt", "cpar", "geom", "pot_init", "pot_eq", "ex_eq", "ey_eq",
+                             "mt_pre", "mt0", "nr0", "conc0", "expnr")}
+    out["raw_r0"] = np.stack([d[f"raw_v0_r0_t{t}"] for t in range(6)])
+    out["raw_coulomb"] = np.stack([d[f"raw_v0_r{r}_t1"] for r in regs])
+    out["params"] = np.array([seed, dt, steps, acc, width])
+    scheme = po.CIC if kind == "mosfet" else po.NGP
+    pot, _ = dev.sor(d["pot_init"], None, 1.8, acc, True)
+    assert np.array_equal(pot, d["pot_eq"])
+    rng = po.RngState(po.RNG_MT, 0)
+    rng.load_mt(d["mt_pre"])
+    st = dev.init_particles(m, rng, pot if kind == "mosfet" else None)
+    for f in po.STATE_F + po.STATE_I:
+        assert np.array_equal(getattr(st, f), d[f"s0_{f}"])
+        out[f"s0_{f}"] = d[f"s0_{f}"]
+    expnr = dev.exp_nr(False)
+    conc = dev.concentration(dev.assign(scheme, st))
+    cap = 1 << 16
+    cur = st.resize(cap)
+    cur.n = st.n
+    for s in range(1, steps + 1):
+        pot, _ = dev.sor(pot, conc, 1.8, acc, s == 1)
+        Ex, Ey = dev.efield(pot)
+        assert np.array_equal(pot, d[f"pot{s}"]) and np.array_equal(Ex, d[f"ex{s}"])
+        n_before = cur.n
+        rng.start_record(1 << 20)
+        rc, netto, off = dev.move(m, scheme, cur, Ex, Ey, dt, rng, s, offsets=True)
+        assert rc == 0
+        out[f"move_words{s}"] = rng.recorded()
+        out[f"move_offsets{s}"] = off
+        out[f"move_n{s}"] = np.array([n_before, cur.n])
+        rng.start_record(1 << 20)
+        rem_inj = dev.contacts(m, cur, cap, expnr, rng, s)
+        out[f"inject_words{s}"] = rng.recorded()
+        out[f"netto{s}"] = d[f"netto{s}"]
+        assert np.array_equal(netto - rem_inj, d[f"netto{s}"])
+        for f in po.STATE_F + po.STATE_I:
+            assert np.array_equal(getattr(cur, f)[:cur.n], d[f"s{s}_{f}"]), (s, f)
+            out[f"s{s}_{f}"] = d[f"s{s}_{f}"]
+        nr = dev.assign(scheme, cur.resize(cur.n))
+        conc = dev.concentration(nr)
+        assert np.array_equal(nr, d[f"nr{s}"]) and np.array_equal(conc, d[f"conc{s}"])
+        for k in ("pot", "ex", "ey", "nr", "conc", "cur"):
+            out[f"{k}{s}"] = d[f"{k}{s}"]
+    np.savez_compressed(os.path.join(HERE, f"device_{name}.npz"), **out)
+    print(f"device_{name}: {dev.nx}x{dev.ny} n0={st.n} steps={steps}")
+
+
 def make_mt():
     d = po.run_ref("mt", 5489, 2000)
     np.savez_compressed(os.path.join(HERE, "mt19937_64.npz"), words=d["mt"], canon=d["canon"])
@@ -94,3 +183,5 @@ if __name__ == "__main__":
     make_mt()
     for c in CASES:
         make_bulk(c)
+    for c in DEVICE_CASES:
+        make_device(c)

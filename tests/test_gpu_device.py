@@ -1,0 +1,196 @@
+"""Device engine on the GPU against the reference's device runs and the oracle.
+
+Replay: the FP64 engine consumes the reference's own random words (move and
+injection phases, attributed per particle) from the reference's state before
+each step and must land on the reference's state after it (1e-12 relative),
+with the same netto contact counts.  Poisson: the multigrid / defect-correction
+solver against the reference's SOR iteration run to 1e-12 V.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from test_oracle_device_golden import DEVICE_CASES, _host_device, _oracle_device, _oracle_model
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-12
+FIELDS_F = ("kx", "ky", "kz", "px", "py", "E", "tau", "gtau")
+ENG = {"E": "energy", "gtau": "grain_tau"}
+
+
+def _electron(engine, dev):
+    """The harness's particle type: acoustic, Coulomb, zero-order f/g
+    absorption/emission, in that registration order, 4 eV tables."""
+    from viennaemc_gb300 import physics as P
+    mat = P.silicon_material()
+    pt = P.Electron(1000, 4.0)
+    P.add_x_valley(pt, 0.196)
+    regs = list(range(dev.n_regions))
+    pt.addScatterMechanism(regs, P.AcousticScatterMechanism(0, 9.0, 300.0, mat.rho, mat.velSound))
+    pt.addScatterMechanism(regs, P.CoulombScatterMechanism(0, mat.epsR, 300.0,
+                                                           dev.getDopingRegionDoping))
+    for fs, sfx in ((P.FINAL_F, "F"), (P.FINAL_G, "G")):
+        pt.addScatterMechanism(regs, P.ZeroOrderInterValleyAbsorptionScatterMechanism(
+            sfx, 0, fs, 5.23e10, 0.06, 300.0, mat.rho))
+        pt.addScatterMechanism(regs, P.ZeroOrderInterValleyEmissionScatterMechanism(
+            sfx, 0, fs, 5.23e10, 0.06, 300.0, mat.rho))
+    pt.initScatterTables()
+    return pt
+
+
+def _sim(engine, g, case, precision="fp64", seed=1, **kw):
+    from viennaemc_gb300 import device as D
+    mos = "mosfet" in case
+    dev = _host_device(g, mos)
+    pt = _electron(engine, dev)
+    return D.DeviceSimulation(dev, pt, scheme=D.CIC if mos else D.NGP, dt=float(g["params"][1]),
+                              seed=seed, capacity=1 << 15, precision=precision,
+                              potential_init=mos, **kw), dev, pt
+
+
+def _engine_state(engine, g, s):
+    kw = {ENG.get(f, f): g[f"s{s}_{f}"] for f in FIELDS_F}
+    kw["pz"] = np.zeros(len(g[f"s{s}_E"]))
+    kw.update({f: g[f"s{s}_{f}"] for f in ("valley", "sub", "region")})
+    return engine.ParticleState.from_arrays(**kw)
+
+
+def _assert_state(st, g, s, rtol=RTOL):
+    assert st.n == len(g[f"s{s}_E"]), (s, st.n)
+    for f in FIELDS_F:
+        a, b = getattr(st, ENG.get(f, f)), g[f"s{s}_{f}"]
+        err = np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+        assert err <= rtol, (s, f, err)
+    for f in ("valley", "sub", "region"):
+        assert np.array_equal(getattr(st, f), g[f"s{s}_{f}"]), (s, f)
+
+
+@pytest.mark.parametrize("case", DEVICE_CASES)
+def test_efield_matches_reference(engine, case):
+    from viennaemc_gb300 import _lib as L
+    g = golden(case)
+    sim, dev, pt = _sim(engine, g, case)
+    for s in (1, 2):
+        sim.set_grid(L.GRID_POTENTIAL, g[f"pot{s}"])
+        sim.efield()
+        ex, ey = sim.get_grid(L.GRID_EX), sim.get_grid(L.GRID_EY)
+        scale = max(np.abs(g[f"ex{s}"]).max(), np.abs(g[f"ey{s}"]).max())
+        assert np.max(np.abs(ex - g[f"ex{s}"])) <= RTOL * scale
+        assert np.max(np.abs(ey - g[f"ey{s}"])) <= RTOL * scale
+    sim.close()
+
+
+@pytest.mark.parametrize("case", DEVICE_CASES)
+def test_replayed_step_matches_reference(engine, case):
+    """move + contacts from the reference's state and random words."""
+    from viennaemc_gb300 import _lib as L
+    g = golden(case)
+    sim, dev, pt = _sim(engine, g, case)
+    for s in range(1, int(g["params"][2]) + 1):
+        sim.set_state(_engine_state(engine, g, s - 1))
+        sim.set_grid(L.GRID_EX, g[f"ex{s}"])
+        sim.set_grid(L.GRID_EY, g[f"ey{s}"])
+        sim.set_replay(0, g[f"move_words{s}"], g[f"move_offsets{s}"])
+        netto = sim.move(step=s)
+        w = g[f"inject_words{s}"]
+        per = 9  # 2 position + 7 particle draws per injected electron
+        sim.set_replay(1, w, np.arange(0, len(w) + 1, per, dtype=np.int64))
+        rem_inj = sim.contacts(step=s)
+        assert np.array_equal(netto - rem_inj, g[f"netto{s}"]), s
+        _assert_state(sim.get_state(), g, s)
+    sim.close()
+
+
+@pytest.mark.parametrize("case", DEVICE_CASES)
+def test_assignment_and_concentration_match_reference(engine, case):
+    from viennaemc_gb300 import _lib as L
+    g = golden(case)
+    sim, dev, pt = _sim(engine, g, case)
+    for s in (0, 1, 3):
+        sim.set_state(_engine_state(engine, g, s))
+        sim.assign()
+        nr, conc = sim.get_grid(L.GRID_NRPART), sim.get_grid(L.GRID_CONC)
+        assert np.allclose(nr, g[f"nr{s}"], rtol=1e-12, atol=1e-12)
+        assert np.allclose(conc, g[f"conc{s}"], rtol=1e-12, atol=0)
+    sim.close()
+
+
+@pytest.mark.parametrize("case", DEVICE_CASES)
+@pytest.mark.parametrize("fp32", [True, False])
+def test_poisson_matches_converged_sor(engine, oracle, case, fp32):
+    """Equilibrium and non-equilibrium potentials: multigrid + double
+    refinement to 1e-10 relative residual vs the reference's SOR to 1e-12 V."""
+    from viennaemc_gb300 import _lib as L
+    g = golden(case)
+    sim, dev, pt = _sim(engine, g, case, poisson_rtol=1e-10, poisson_fp32=fp32,
+                      poisson_max_cycles=200)
+    odev = _oracle_device(oracle, g)
+    # equilibrium from the initial guess asinh(C/2)
+    sim.set_grid(L.GRID_POTENTIAL, g["pot_init"])
+    rel, cyc = sim.poisson(equilibrium=True, reset_bc=True)
+    ref, sweeps = odev.sor(g["pot_init"], None, 1.8, 1e-12, True)
+    assert sweeps > 0 and rel <= 1e-10
+    assert np.max(np.abs(sim.potential - ref)) <= 1e-7, np.max(np.abs(sim.potential - ref))
+    # non-equilibrium with the reference's concentration of step 1
+    sim.set_grid(L.GRID_POTENTIAL, g["pot_eq"])
+    sim.set_grid(L.GRID_CONC, g["conc0"])
+    rel, cyc = sim.poisson(equilibrium=False, reset_bc=True)
+    ref, sweeps = odev.sor(g["pot_eq"], g["conc0"], 1.8, 1e-12, True)
+    assert sweeps > 0 and rel <= 1e-10
+    assert np.max(np.abs(sim.potential - ref)) <= 1e-7, np.max(np.abs(sim.potential - ref))
+    sim.close()
+
+
+@pytest.mark.parametrize("case", DEVICE_CASES)
+def test_philox_step_matches_oracle(engine, oracle, case):
+    """Same potential, same Philox counters: E field, move, contacts and
+    assignment of the FP64 engine equal the oracle's (1e-12)."""
+    from viennaemc_gb300 import _lib as L
+    g = golden(case)
+    seed, stream = 0xBEEF, 0
+    sim, dev, pt = _sim(engine, g, case, seed=seed)
+    odev = _oracle_device(oracle, g)
+    m, regs = _oracle_model(oracle, g)
+    scheme = oracle.CIC if "mosfet" in case else oracle.NGP
+    dt = float(g["params"][1])
+    cur = oracle.State.from_dict({f: g[f"s0_{f}"] for f in oracle.STATE_F + oracle.STATE_I})
+    cur = cur.resize(1 << 15)
+    cur.n = len(g["s0_E"])
+    sim.set_state(_engine_state(engine, g, 0))
+    rng = oracle.RngState(oracle.RNG_PHILOX, seed, stream)
+    expnr = odev.exp_nr(False)
+    for s in range(1, 4):
+        sim.set_grid(L.GRID_POTENTIAL, g[f"pot{s}"])
+        sim.efield()
+        Ex, Ey = odev.efield(g[f"pot{s}"])
+        netto = sim.move(step=s)
+        rem_inj = sim.contacts(step=s)
+        rc, onet, _ = odev.move(m, scheme, cur, Ex, Ey, dt, rng, s)
+        ori = odev.contacts(m, cur, 1 << 15, expnr, rng, s)
+        assert np.array_equal(netto, onet) and np.array_equal(rem_inj, ori)
+        st = sim.get_state()
+        assert st.n == cur.n
+        for f in FIELDS_F:
+            a, b = getattr(st, ENG.get(f, f)), getattr(cur, f)[:cur.n]
+            assert np.max(np.abs(a - b)) <= RTOL * max(np.abs(b).max(), 1e-300), (s, f)
+        sim.assign()
+        nr = odev.assign(scheme, cur.resize(cur.n))
+        assert np.allclose(sim.get_grid(L.GRID_NRPART), nr, rtol=1e-12, atol=1e-12)
+    sim.close()
+
+
+def test_full_device_steps_run_and_conserve_count(engine):
+    """performEMCStep end to end (Poisson -> E -> move -> contacts -> assign),
+    FP64 and FP32: particle count changes only by the contact flux."""
+    g = golden(DEVICE_CASES[0])
+    for precision in ("fp64", "fp32"):
+        sim, dev, pt = _sim(engine, g, DEVICE_CASES[0], precision=precision, seed=3)
+        sim.calcEquilibriumCharacteristics()
+        n0 = sim.num_particles()
+        netto = sim.performEMCStep(20)
+        n1 = sim.num_particles()
+        assert n1 == n0 - int(netto.sum())
+        assert np.all(np.isfinite(sim.potential))
+        sim.close()

@@ -15,8 +15,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 LIB_PATH = os.path.join(PKG, "libemcgpu.so")
-SOURCES = ["emcg_core.cu", "emcg_bulk.cu", "emcg_device.cu"]
-HEADERS = ["emcg_common.cuh", "emcg_host.h", "emcg_model.h"]
+SOURCES = ["emcg_core.cu", "emcg_bulk.cu", "emcg_device.cu", "emcg_poisson.cu"]
+HEADERS = ["emcg_common.cuh", "emcg_host.h", "emcg_model.h", "emcg_poisson.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 MAX_VALLEYS, MAX_DEG, MAX_MECH, MAX_NF, MAX_REGIONS = 4, 8, 32, 8, 16
@@ -158,6 +158,8 @@ def _declare(L):
     L.emcg_last_kernel_ms.argtypes = [vp, P(d)]
     L.emcg_set_launch.restype = i32
     L.emcg_set_launch.argtypes = [vp, i32, i32]
+    L.emcg_set_occupancy.restype = i32
+    L.emcg_set_occupancy.argtypes = [vp, i32]
     L.emcg_drift_kat.restype = i32
     L.emcg_drift_kat.argtypes = [vp, i32, i64, P(i32), P(d), P(d), P(d), P(d), P(d)]
     for name, args in _EXTRA_DECLS:
@@ -174,3 +176,52 @@ def check(status: int) -> None:
     if status != 0:
         msg = lib().emcg_last_error().decode(errors="replace")
         raise EmcgError(status, msg)
+
+
+# ---- device engine ---------------------------------------------------------------
+PM_NGP, PM_CIC = 0, 1
+CONTACT_OHMIC, CONTACT_SCHOTTKY, CONTACT_GATE = 0, 1, 2
+GRID_POTENTIAL, GRID_EX, GRID_EY, GRID_NRPART, GRID_CONC = range(5)
+
+
+class DeviceDesc(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("hx", C.c_double), ("hy", C.c_double),
+                ("max_x", C.c_double), ("max_y", C.c_double), ("width", C.c_double),
+                ("temperature", C.c_double), ("ni", C.c_double), ("eps_r", C.c_double),
+                ("doping", C.POINTER(C.c_double)), ("region", C.POINTER(C.c_int32)),
+                ("boundary_contact", C.POINTER(C.c_int32) * 4), ("n_contacts", C.c_int32),
+                ("pad_", C.c_int32), ("contact_type", C.POINTER(C.c_int32)),
+                ("contact_voltage", C.POINTER(C.c_double)),
+                ("contact_param", C.POINTER(C.c_double))]
+
+
+class DeviceConfig(C.Structure):
+    _fields_ = [("pm_scheme", C.c_int32), ("tau_region_is_valley", C.c_int32),
+                ("capacity", C.c_int64), ("dt", C.c_double), ("charge", C.c_double),
+                ("carriers_per_particle", C.c_double), ("seed", C.c_uint64),
+                ("stream", C.c_uint32), ("poisson_max_cycles", C.c_int32),
+                ("poisson_rtol", C.c_double), ("poisson_smooth", C.c_int32),
+                ("poisson_fp32", C.c_int32)]
+
+
+def _i32p():
+    return C.POINTER(C.c_int32)
+
+
+_EXTRA_DECLS.extend([
+    ("emcg_device_create", [C.POINTER(ModelDesc), C.POINTER(DeviceDesc), C.POINTER(DeviceConfig),
+                            C.c_int32, C.POINTER(C.c_void_p)]),
+    ("emcg_device_set_grid", [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
+    ("emcg_device_get_grid", [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
+    ("emcg_device_poisson", [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_double),
+                             C.POINTER(C.c_int32)]),
+    ("emcg_device_efield", [C.c_void_p]),
+    ("emcg_device_move", [C.c_void_p, C.c_uint32, C.POINTER(C.c_int32)]),
+    ("emcg_device_contacts", [C.c_void_p, C.c_uint32, C.POINTER(C.c_int32)]),
+    ("emcg_device_assign", [C.c_void_p]),
+    ("emcg_device_step", [C.c_void_p, C.c_int32, C.c_uint32, C.POINTER(C.c_int32)]),
+    ("emcg_device_init", [C.c_void_p, C.c_int32, C.c_int32]),
+    ("emcg_device_set_replay", [C.c_void_p, C.c_int32, C.POINTER(C.c_uint64), C.c_int64,
+                                C.POINTER(C.c_int64), C.c_int64]),
+    ("emcg_device_timing", [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+])

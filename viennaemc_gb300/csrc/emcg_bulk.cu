@@ -81,8 +81,10 @@ __device__ __forceinline__ void recordError(int *err, int code) {
 
 // Advance all tiles by nSteps time steps.  obs layout:
 // [ens][step][nVmax][3] of {sum E, sum v.dir, count} (doubles).
-template <class T, bool REPLAY>
-__global__ void bulkStepKernel(StateK<T> st, const ModelK<T> *__restrict__ models,
+// MINB: minimum resident blocks of 256 threads per SM requested from the
+// compiler (register cap); 1 leaves the allocation unconstrained.
+template <class T, bool REPLAY, int MINB>
+__global__ void __launch_bounds__(256, MINB) bulkStepKernel(StateK<T> st, const ModelK<T> *__restrict__ models,
                                const EnsK<T> *__restrict__ ens, const Tile *__restrict__ tiles,
                                int nSteps, uint32_t step0, int chunk, int nVmax,
                                double *__restrict__ obs, const uint64_t *__restrict__ rw,
@@ -298,6 +300,7 @@ struct BulkImpl {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int blockThreads = 256;
+  int minBlocks = 1; // register cap variant of the step kernel (1, 3 or 4)
   int stepsPerLaunch = 0;
   int chunk = 16;
   uint64_t *dWords = nullptr;
@@ -444,15 +447,25 @@ static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHos
     EMCG_CUDA(cudaMemsetAsync(b->dObs, 0, (size_t)b->nEns * ns * Q * sizeof(double), b->stream));
     EMCG_CUDA(cudaEventRecord(b->ev0, b->stream));
     if (b->nTiles > 0) {
+      const ModelK<T> *mp = (const ModelK<T> *)b->dModels;
+      const EnsK<T> *ep = (const EnsK<T> *)b->dEns;
       if (b->replay) {
         if constexpr (sizeof(T) == 8)
-          bulkStepKernel<T, true><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
-              st, (const ModelK<T> *)b->dModels, (const EnsK<T> *)b->dEns, b->dTiles, ns,
-              step0 + done, b->chunk, b->nVmax, b->dObs, b->dWords, b->dOff, b->dErr);
+          bulkStepKernel<T, true, 1><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
+              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dWords,
+              b->dOff, b->dErr);
+      } else if (b->minBlocks >= 4 && b->blockThreads <= 256) {
+        bulkStepKernel<T, false, 4><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
+            st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, nullptr,
+            nullptr, b->dErr);
+      } else if (b->minBlocks == 3 && b->blockThreads <= 256) {
+        bulkStepKernel<T, false, 3><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
+            st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, nullptr,
+            nullptr, b->dErr);
       } else {
-        bulkStepKernel<T, false><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
-            st, (const ModelK<T> *)b->dModels, (const EnsK<T> *)b->dEns, b->dTiles, ns,
-            step0 + done, b->chunk, b->nVmax, b->dObs, nullptr, nullptr, b->dErr);
+        bulkStepKernel<T, false, 1><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
+            st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, nullptr,
+            nullptr, b->dErr);
       }
       EMCG_CUDA(cudaGetLastError());
     }
@@ -601,6 +614,8 @@ extern "C" int32_t emcg_destroy(emcg_handle *h) {
 }
 
 extern "C" int64_t emcg_num_particles(emcg_handle *h, int32_t e) {
+  if (h && h->kind == 2)
+    return e == 0 ? emcg::deviceNumParticles(h) : -1;
   BulkImpl *b = nullptr;
   if (bulkOf(h, &b) || e < 0 || e >= b->nEns)
     return -1;
@@ -637,6 +652,10 @@ static int32_t setStateTyped(BulkImpl *b, int e, const emcg_state *s) {
 }
 
 extern "C" int32_t emcg_set_state(emcg_handle *h, int32_t e, const emcg_state *s) {
+  if (h && h->kind == 2) {
+    EMCG_CHECK_ARG(e == 0, "a device engine has one ensemble");
+    return emcg::deviceSetState(h, s);
+  }
   BulkImpl *b;
   EMCG_TRY(bulkOf(h, &b));
   EMCG_CHECK_ARG(s && e >= 0 && e < b->nEns, "bad ensemble or state");
@@ -681,6 +700,10 @@ template <class T> static int32_t getStateTyped(BulkImpl *b, int e, emcg_state *
 }
 
 extern "C" int32_t emcg_get_state(emcg_handle *h, int32_t e, emcg_state *s) {
+  if (h && h->kind == 2) {
+    EMCG_CHECK_ARG(e == 0, "a device engine has one ensemble");
+    return emcg::deviceGetState(h, s);
+  }
   BulkImpl *b;
   EMCG_TRY(bulkOf(h, &b));
   EMCG_CHECK_ARG(s && e >= 0 && e < b->nEns, "bad ensemble or state");
@@ -792,6 +815,15 @@ extern "C" int32_t emcg_last_kernel_ms(emcg_handle *h, double *ms) {
   EMCG_TRY(bulkOf(h, &b));
   EMCG_CHECK_ARG(ms, "ms is NULL");
   *ms = b->lastMs;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_set_occupancy(emcg_handle *h, int32_t min_blocks_per_sm) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(min_blocks_per_sm == 1 || min_blocks_per_sm == 3 || min_blocks_per_sm == 4,
+                 "min_blocks_per_sm must be 1, 3 or 4");
+  b->minBlocks = min_blocks_per_sm;
   return EMCG_OK;
 }
 

@@ -18,6 +18,7 @@ constexpr double kQ = 1.60219e-19;
 constexpr double kKB = 1.38066e-23;
 constexpr double kHBAR = 1.05459e-34;
 constexpr double kPI = 3.14159265358979323846;
+constexpr double kEPS0 = 8.85419e-12;
 
 // ---------------------------------------------------------------------------
 // kernel-side model (built on the host from emcg_model_desc)

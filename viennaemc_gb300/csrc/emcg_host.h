@@ -49,7 +49,11 @@ struct DeviceImpl;
 
 struct emcg_handle;
 namespace emcg {
-int32_t destroyDevice(emcg_handle *h); // emcg_device.cu
+// emcg_device.cu
+int32_t destroyDevice(emcg_handle *h);
+int32_t deviceSetState(emcg_handle *h, const emcg_state *s);
+int32_t deviceGetState(emcg_handle *h, emcg_state *s);
+int64_t deviceNumParticles(emcg_handle *h);
 }
 
 struct emcg_handle {

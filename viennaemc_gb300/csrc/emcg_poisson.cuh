@@ -1,0 +1,78 @@
+// Grid Poisson solver of the device engine.
+//
+// Discrete equation (include/PoissonSolver/emcSORSolver.hpp:131-197,
+// 330-412), Debye-normalised, at every node that is not a reservoir contact:
+//   F_i(phi) = sum_d hF_d (phi_{i-d} + phi_{i+d} - 2 phi_i)      (mirror at
+//              artificial boundaries)
+//            + hP (p_i - n_i + C_i) + G_i (Vg_i - phi_i) = 0
+// with p = exp(-phi), n = the carrier concentration (non-equilibrium) or
+// exp(phi) (equilibrium), G the gate Robin coefficient.  The reference's
+// lexicographic SOR reaches the fixed point of this equation; here it is
+// solved by Newton / defect correction in double precision whose correction
+// equation J d = -F is solved approximately by one multigrid V-cycle per
+// iteration (red-black Gauss-Seidel, bilinear transfer, finite-volume
+// coarse operators), in float or double.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+namespace emcg {
+
+// static per-node data of the fine grid (host arrays)
+struct PoissonSetup {
+  int nx = 0, ny = 0;
+  double h[2] = {0, 0};       // normalised spacing
+  std::vector<uint8_t> fixed; // Dirichlet (reservoir) nodes
+  std::vector<double> C;      // normalised doping
+  std::vector<double> gSum;   // sum of gate coefficients G at the node
+  std::vector<double> gVeq;   // sum of G * barrier
+  std::vector<double> gVne;   // sum of G * (barrier + applied)
+  std::vector<double> gDensX; // FV Robin density of an x-side gate (gF / 2)
+  std::vector<double> gDensY; // FV Robin density of a y-side gate
+  std::vector<uint8_t> resetMask; // nodes whose value resetBC sets
+  std::vector<double> resetEq, resetNe; // and the values it sets
+};
+
+struct MGLevel {
+  int nx, ny;
+  // FV coefficients (w, e, s, n), area and static diagonal (couplings + Robin)
+  float *cw, *ce, *cs, *cn, *area, *diag0;
+  double *dcw, *dce, *dcs, *dcn, *darea, *ddiag0;
+  uint8_t *fixed;
+  float *d, *r, *rho;    // correction, right-hand side, reaction density (float MG)
+  double *dd, *dr, *drho; // the same in double (double MG)
+  // transfer to the next coarser level
+  int *rxIdx, *ryIdx;      // restriction: 3 fine indices per coarse index
+  float *rxW, *ryW;
+  int *pxIdx, *pyIdx;      // prolongation: lower coarse index per fine index
+  float *pxW, *pyW;        // weight of the lower coarse node
+  int *mapX, *mapY;        // coarse index -> fine index (injection)
+};
+
+struct PoissonMG {
+  PoissonSetup S;
+  std::vector<MGLevel> L;
+  // fine-grid device data (double)
+  double *C = nullptr, *gSum = nullptr, *gVeq = nullptr, *gVne = nullptr;
+  uint8_t *resetMask = nullptr;
+  double *resetEq = nullptr, *resetNe = nullptr;
+  double *stats = nullptr; // [max|F|, scale, max|d|] as ordered bits
+  int pre = 2, post = 2, coarseSweeps = 40;
+  bool fp32 = true;
+  double hF[2], hP;
+};
+
+int32_t poissonCreate(PoissonMG &P, const PoissonSetup &S, bool fp32, int smooth,
+                      cudaStream_t st);
+void poissonFree(PoissonMG &P);
+// Solve for pot (device, normalised).  conc == nullptr: equilibrium.
+// Returns EMCG_OK / EMCG_ERR_NONCONVERGED / EMCG_ERR_CUDA; outputs the final
+// relative residual and the number of V-cycles.
+int32_t poissonSolve(PoissonMG &P, double *pot, const double *conc, bool resetBC,
+                     double rtol, int maxCycles, cudaStream_t st, double *relRes,
+                     int *cycles);
+
+} // namespace emcg
