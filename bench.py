@@ -215,8 +215,8 @@ def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units,
             value64, vd32, vd64, win, k64, wall, clocks):
     peak, peak_src = _peaks()
     bpp = BYTES_PER_PARTICLE_STEP["fp32"]
-    achieved = bpp * value / 1e9
-    traffic = _profiled_traffic()
+    achieved = bpp * value / 1e9  # algorithmic GB/s (72 B per particle-step)
+    traffic = _profiled_traffic(N)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -232,7 +232,9 @@ def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_src,
-                     "bytes_per_unit": bpp, "unit_of_work": "particle-step"},
+                     "bytes_per_unit": bpp, "unit_of_work": "particle-step",
+                     "algorithmic_bytes_per_launch": bpp * N * per,
+                     "traffic_per": "launch of steps_per_launch steps"},
         "wall_s": wall,
     }
     if value64:
@@ -268,12 +270,13 @@ def _host_state(v, N):
     return st
 
 
-def _profiled_traffic():
-    """DRAM bytes per launch of the bulk kernel from the committed ncu summary."""
+def _profiled_traffic(n_electrons):
+    """DRAM bytes of one bench launch of the bulk kernel, from the committed
+    ncu capture (bytes per electron per launch, scaled to this launch)."""
     p = os.path.join(ROOT, "profiles", "bulk_step_fp32_traffic.json")
     try:
         with open(p) as f:
-            return float(json.load(f)["dram_bytes_per_launch"])
+            return float(json.load(f)["dram_bytes_per_electron_per_launch"]) * n_electrons
     except Exception:
         return None
 

@@ -224,6 +224,15 @@ int32_t emcg_last_kernel_ms(emcg_handle *h, double *ms);
 int32_t emcg_set_launch(emcg_handle *h, int32_t block_threads,
                         int32_t steps_per_launch);
 
+/* Tuning: 1 (default) runs the block-queued step kernel (scatter events of a
+   thread block processed together by its first warps), 0 the lockstep
+   kernel (each warp handles its own events).  Both follow the same
+   per-particle algorithm; replay always uses the lockstep kernel.  In the
+   queued kernel the grain free-flight redraw takes its own Philox calls, so
+   its double-precision stream differs from the lockstep kernel and the oracle
+   in that (rare) event only. */
+int32_t emcg_set_scatter_mode(emcg_handle *h, int32_t queued);
+
 /* Tuning: register cap of the step kernel, as the minimum number of resident
    256-thread blocks per SM (1 = uncapped, 3 or 4); capped variants apply to
    blocks of at most 256 threads. */

@@ -1,0 +1,52 @@
+// Builds the bulk benchmark model through emcgpu::ModelBuilder on the
+// reference's own classes and prints the engine descriptor (hex floats), so
+// that tests/test_adapter.py can compare it with the Python host builder.
+// GpuBulkParticleHandler is instantiated to check that it compiles and links.
+#include <cstdio>
+#include <memory>
+
+#include <ParticleType/emcElectron.hpp>
+#include <emcDevice.hpp>
+
+#include "emcgpu_reference.hpp"
+
+using T = double;
+using Dev3 = emcDevice<T, 3>;
+template class emcgpu::GpuBulkParticleHandler<T, Dev3>;
+
+int main() {
+  Dev3 device{emcMaterial<T>{11.8, 2329., 1.45e16, 9040., 1.15}, {5e-7, 5e-7, 5e-7},
+              {1e-7, 1e-7, 1e-7}, 300.};
+  device.addConstantDopingRegion({0, 0, 0}, {5e-7, 5e-7, 5e-7}, 1e21);
+  emcElectron<T, Dev3> el(1000, 1., false);
+  std::unique_ptr<emcNonParabolicAnisotropValley<T>> v(
+      new emcNonParabolicAnisotropValley<T>({0.916, 0.19, 0.19}, el.getMass(), 3, 0.5));
+  v->setSubValleyEllipseCoordSystem(0, {1, 0, 0}, {0, 1, 0}, {0, 0, 1});
+  v->setSubValleyEllipseCoordSystem(1, {0, 1, 0}, {1, 0, 0}, {0, 0, 1});
+  v->setSubValleyEllipseCoordSystem(2, {0, 0, 1}, {0, 1, 0}, {1, 0, 0});
+  el.addValley(std::move(v));
+  emcgpu::ModelBuilder<T, Dev3> mb(el, 1000, 1.);
+  std::map<SizeType, std::vector<SizeType>> G = {{0, {0}}, {1, {1}}, {2, {2}}};
+  std::map<SizeType, std::vector<SizeType>> F = {{0, {1, 1, 2, 2}}, {1, {0, 0, 2, 2}},
+                                                 {2, {0, 0, 1, 1}}};
+  mb.addAcoustic(0, 9., device, {0});
+  const double th[6] = {140., 215., 720., 220., 550., 685.};
+  const double D[6] = {0.5e10, 0.8e10, 11.e10, 0.3e10, 2.0e10, 2.0e10};
+  const char *nm[6] = {"G1", "G2", "G3", "F1", "F2", "F3"};
+  for (int i = 0; i < 6; i++) {
+    double e = constants::kB * th[i] / constants::q;
+    mb.addZeroOrderAbsorption(nm[i], 0, i < 3 ? G : F, D[i], e, device, {0});
+    mb.addZeroOrderEmission(nm[i], 0, i < 3 ? G : F, D[i], e, device, {0});
+  }
+  const emcg_model_desc &d = mb.desc();
+  std::printf("counts %d %d %d %d\n", d.n_valleys, d.n_mechs, d.n_tablesets, d.n_levels);
+  std::printf("tau %a\n", d.tablesets[0].tau_max);
+  for (int i = 0; i < 3; i++)
+    std::printf("relmass %a\n", d.valleys[0].rel_mass[i]);
+  for (int m = 0; m < d.n_mechs; m++)
+    std::printf("mech %d %d %a %d\n", d.mechs[m].kind, d.mechs[m].n_final, d.mechs[m].shift,
+                d.mechs[m].final_sub[1][0]);
+  for (int i = 0; i < d.n_mechs * d.n_levels; i += 97)
+    std::printf("table %d %a\n", i, d.tables[i]);
+  return 0;
+}

@@ -170,10 +170,12 @@ class BulkBatch:
         self._earr[ens] = d
 
     # ---- dynamics ------------------------------------------------------------
-    def set_launch(self, block_threads=0, steps_per_launch=0, min_blocks=0):
+    def set_launch(self, block_threads=0, steps_per_launch=0, min_blocks=0, queued=None):
         L.check(self._lib.emcg_set_launch(self.h, block_threads, steps_per_launch))
         if min_blocks:
             L.check(self._lib.emcg_set_occupancy(self.h, min_blocks))
+        if queued is not None:
+            L.check(self._lib.emcg_set_scatter_mode(self.h, int(queued)))
 
     def step(self, n_steps: int = 1, observables: bool = True, step0: int | None = None):
         """Advance all ensembles; returns sums [ens, step, valley, {E, v.dir, count}]."""

@@ -183,6 +183,226 @@ __global__ void __launch_bounds__(256, MINB) bulkStepKernel(StateK<T> st, const 
   recordError(err, myErr);
 }
 
+
+// ---------------------------------------------------------------------------
+// Queued variant (Philox only).  The block's particles live in shared memory
+// for the whole launch.  Each step:
+//   A (owner)  free flight to min(tau, dt); a particle with an event inside
+//              the step appends its index to the block's queue;
+//   B (block)  the first warps process every queued event (selection, final
+//              state, new free flight, remaining drift) for the whole block;
+//   C (owner)  tau -= dt, grain timer, observables (merged with the next A).
+// The scatter path thus runs once per 32 queued particles instead of once
+// per warp holding one, and no particle state stays in registers across the
+// barriers.  Random numbers: the event of particle pid in step s uses counter
+// (pid, s, call, stream) as in the lockstep kernel; the grain free-flight
+// redraw uses calls from 0x40000000 so that it does not depend on how many
+// words the event consumed.
+template <class T> struct BlockState {
+  T *k0, *k1, *k2, *p0, *p1, *p2, *E, *tau, *gtau, *n0, *n1, *n2;
+  uint32_t *meta;
+  int32_t *queue;
+};
+
+template <class T>
+__device__ __forceinline__ BlockState<T> blockState(unsigned char *base, int cap) {
+  BlockState<T> b;
+  T *t = reinterpret_cast<T *>(base);
+  T **f[12] = {&b.k0, &b.k1, &b.k2, &b.p0, &b.p1, &b.p2, &b.E, &b.tau, &b.gtau, &b.n0, &b.n1, &b.n2};
+  for (int i = 0; i < 12; i++)
+    *f[i] = t + (size_t)i * cap;
+  b.meta = reinterpret_cast<uint32_t *>(t + (size_t)12 * cap);
+  b.queue = reinterpret_cast<int32_t *>(b.meta + cap);
+  return b;
+}
+
+template <class T>
+__host__ __device__ constexpr size_t blockStateBytes(int cap) {
+  return (size_t)cap * (12 * sizeof(T) + sizeof(uint32_t) + sizeof(int32_t));
+}
+
+template <class T, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+    bulkStepQueuedKernel(StateK<T> st, const ModelK<T> *__restrict__ models,
+                         const EnsK<T> *__restrict__ ens, const Tile *__restrict__ tiles,
+                         int nSteps, uint32_t step0, int chunk, int nVmax,
+                         double *__restrict__ obs, int *__restrict__ err) {
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  const int nWarps = blockDim.x >> 5;
+  const int Q = nVmax * 3;
+  T *sbuf = reinterpret_cast<T *>(smemRaw); // [chunk][nWarps][Q]
+  unsigned char *base = smemRaw + (((size_t)chunk * nWarps * Q * sizeof(T) + 15) & ~size_t(15));
+  const BlockState<T> B = blockState<T>(base, blockDim.x);
+  __shared__ int qCount[2];
+  const Tile tl = tiles[blockIdx.x];
+  const EnsK<T> &EK = ens[tl.ens];
+  const ModelK<T> &M = models[EK.model];
+  const int nV = EK.nV;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, me = threadIdx.x;
+  const int64_t gi = tl.begin + me;
+  const bool active = gi < tl.end;
+  const T dt = EK.dt;
+  if (me < 2)
+    qCount[me] = 0;
+  if (active) {
+    B.k0[me] = st.kx[gi];
+    B.k1[me] = st.ky[gi];
+    B.k2[me] = st.kz[gi];
+    B.p0[me] = st.px[gi];
+    B.p1[me] = st.py[gi];
+    B.p2[me] = st.pz[gi];
+    B.E[me] = st.E[gi];
+    B.tau[me] = st.tau[gi];
+    B.gtau[me] = st.gtau[gi];
+    B.meta[me] = st.meta[gi];
+  }
+  __syncthreads();
+  // phase A of the first step
+  if (active) {
+    T k[3] = {B.k0[me], B.k1[me], B.k2[me]}, pos[3] = {B.p0[me], B.p1[me], B.p2[me]};
+    T E = B.E[me], tau = B.tau[me], kN[3];
+    uint32_t mt = B.meta[me];
+    int valley = mt & 0xff, sub = (mt >> 8) & 0xff;
+    driftBulk(M.v[valley], sub, EK.fv[valley][sub], dt < tau ? dt : tau, k, E, pos, kN, EK.box);
+    B.k0[me] = k[0];
+    B.k1[me] = k[1];
+    B.k2[me] = k[2];
+    B.p0[me] = pos[0];
+    B.p1[me] = pos[1];
+    B.p2[me] = pos[2];
+    B.E[me] = E;
+    B.n0[me] = kN[0];
+    B.n1[me] = kN[1];
+    B.n2[me] = kN[2];
+    if (dt - tau > T(0))
+      B.queue[atomicAdd(&qCount[0], 1)] = me;
+  }
+  __syncthreads();
+  double *obsE = obs + (size_t)tl.ens * nSteps * Q;
+  for (int s = 0; s < nSteps; s++) {
+    const uint32_t step = step0 + (uint32_t)s;
+    // phase B: queued events of step s
+    const int nq = qCount[s & 1];
+    if (me == 0)
+      qCount[(s + 1) & 1] = 0;
+    for (int j = me; j < nq; j += blockDim.x) {
+      const int p = B.queue[j];
+      T k[3] = {B.k0[p], B.k1[p], B.k2[p]}, pos[3] = {B.p0[p], B.p1[p], B.p2[p]};
+      T E = B.E[p], tau = B.tau[p], kN[3];
+      uint32_t mt = B.meta[p];
+      int valley = mt & 0xff, sub = (mt >> 8) & 0xff, region = mt >> 16;
+      T tRem = dt - tau;
+      PhiloxSrc<T> rng;
+      rng.init((uint32_t)(tl.begin + p - EK.begin), step, EK.stream, EK.key0, EK.key1);
+      int guard = 0, e = 0;
+      while (tRem > T(0)) {
+        if (++guard > kMaxScatterPerStep) {
+          e = EMCG_ERR_TIMEOUT;
+          break;
+        }
+        e = scatterParticle(M, k, E, valley, sub, region, rng);
+        if (e)
+          break;
+        T nt = -m_log(rng.ulog()) * tauOf(M, valley, region);
+        tau += nt;
+        driftBulk(M.v[valley], sub, EK.fv[valley][sub], nt < tRem ? nt : tRem, k, E, pos, kN,
+                  EK.box);
+        tRem -= nt;
+      }
+      recordError(err, e);
+      B.k0[p] = k[0];
+      B.k1[p] = k[1];
+      B.k2[p] = k[2];
+      B.p0[p] = pos[0];
+      B.p1[p] = pos[1];
+      B.p2[p] = pos[2];
+      B.E[p] = E;
+      B.tau[p] = tau;
+      B.n0[p] = kN[0];
+      B.n1[p] = kN[1];
+      B.n2[p] = kN[2];
+      B.meta[p] = packMeta(valley, sub, region);
+    }
+    __syncthreads();
+    // phase C of step s (+ phase A of step s + 1)
+    T E = T(0), vd = T(0);
+    int valley = 0;
+    if (active) {
+      T tau = B.tau[me] - dt, gtau = B.gtau[me] - dt;
+      E = B.E[me];
+      uint32_t mt = B.meta[me];
+      valley = mt & 0xff;
+      int sub = (mt >> 8) & 0xff;
+      if (gtau <= T(0)) {
+        PhiloxSrc<T> rng;
+        rng.init((uint32_t)(gi - EK.begin), step, EK.stream, EK.key0, EK.key1);
+        rng.c2 = 0x40000000u;
+        gtau = -m_log(rng.ulog()) * M.grainTau;
+      }
+      B.gtau[me] = gtau;
+      const ValleyK<T> &V = M.v[valley];
+      const T *g = EK.g[valley][sub];
+      T npf = m_sqrt(T(1) + T(4) * V.alpha * gammaOf(V, E));
+      vd = m_div(V.cX * (g[0] * B.n0[me] + g[1] * B.n1[me] + g[2] * B.n2[me]), npf);
+      if (s + 1 < nSteps) { // phase A of the next step
+        T k[3] = {B.k0[me], B.k1[me], B.k2[me]}, pos[3] = {B.p0[me], B.p1[me], B.p2[me]};
+        T E2 = E, kN[3];
+        driftBulk(V, sub, EK.fv[valley][sub], dt < tau ? dt : tau, k, E2, pos, kN, EK.box);
+        B.k0[me] = k[0];
+        B.k1[me] = k[1];
+        B.k2[me] = k[2];
+        B.p0[me] = pos[0];
+        B.p1[me] = pos[1];
+        B.p2[me] = pos[2];
+        B.E[me] = E2;
+        B.n0[me] = kN[0];
+        B.n1[me] = kN[1];
+        B.n2[me] = kN[2];
+        if (dt - tau > T(0))
+          B.queue[atomicAdd(&qCount[(s + 1) & 1], 1)] = me;
+      }
+      B.tau[me] = tau;
+    }
+    T *row = sbuf + ((s % chunk) * nWarps + warp) * Q;
+    for (int v = 0; v < nV; v++) {
+      bool in = active && valley == v;
+      T e = warpSum(in ? E : T(0));
+      T d = warpSum(in ? vd : T(0));
+      unsigned c = __popc(__ballot_sync(0xffffffffu, in));
+      if (lane == 0) {
+        row[v * 3 + 0] = e;
+        row[v * 3 + 1] = d;
+        row[v * 3 + 2] = (T)c;
+      }
+    }
+    __syncthreads();
+    if ((s + 1) % chunk == 0 || s == nSteps - 1) {
+      const int inChunk = s % chunk + 1, sBase = s - s % chunk;
+      const int nQ = nV * 3;
+      for (int idx = me; idx < inChunk * nQ; idx += blockDim.x) {
+        int cs = idx / nQ, qq = idx - cs * nQ;
+        double acc = 0.;
+        for (int w = 0; w < nWarps; w++)
+          acc += (double)sbuf[(cs * nWarps + w) * Q + qq];
+        atomicAdd(&obsE[(size_t)(sBase + cs) * Q + qq], acc);
+      }
+      __syncthreads();
+    }
+  }
+  if (active) {
+    st.kx[gi] = B.k0[me];
+    st.ky[gi] = B.k1[me];
+    st.kz[gi] = B.k2[me];
+    st.px[gi] = B.p0[me];
+    st.py[gi] = B.p1[me];
+    st.pz[gi] = B.p2[me];
+    st.E[gi] = B.E[me];
+    st.tau[gi] = B.tau[me];
+    st.gtau[gi] = B.gtau[me];
+    st.meta[gi] = B.meta[me];
+  }
+}
+
 // Initial particles (include/ParticleType/emcElectron.hpp:75-90,
 // include/emcParticleInitialization.hpp:14-51), Philox counter
 // (i, 0xFFFFFFFF, call, stream).  coords == nullptr: uniform in the box.
@@ -301,6 +521,7 @@ struct BulkImpl {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int blockThreads = 256;
   int minBlocks = 1; // register cap variant of the step kernel (1, 3 or 4)
+  int queued = 1;    // 1: block-queued scatter kernel (Philox), 0: lockstep kernel
   int stepsPerLaunch = 0;
   int chunk = 16;
   uint64_t *dWords = nullptr;
@@ -454,6 +675,17 @@ static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHos
           bulkStepKernel<T, true, 1><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
               st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dWords,
               b->dOff, b->dErr);
+      } else if (b->queued) {
+        const size_t qsmem = ((smem + 15) & ~size_t(15)) + blockStateBytes<T>(b->blockThreads);
+        if (b->minBlocks >= 4 && b->blockThreads <= 256)
+          bulkStepQueuedKernel<T, 4><<<b->nTiles, b->blockThreads, qsmem, b->stream>>>(
+              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
+        else if (b->minBlocks == 3 && b->blockThreads <= 256)
+          bulkStepQueuedKernel<T, 3><<<b->nTiles, b->blockThreads, qsmem, b->stream>>>(
+              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
+        else
+          bulkStepQueuedKernel<T, 1><<<b->nTiles, b->blockThreads, qsmem, b->stream>>>(
+              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
       } else if (b->minBlocks >= 4 && b->blockThreads <= 256) {
         bulkStepKernel<T, false, 4><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
             st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, nullptr,
@@ -545,6 +777,10 @@ extern "C" int32_t emcg_bulk_create(const emcg_model_desc *models, int32_t n_mod
   }
   BulkImpl *b = new BulkImpl();
   b->precision = precision;
+  // defaults measured on GB300: the float engine runs the block-queued kernel
+  // with a 3-blocks-per-SM register cap, the double engine the lockstep one
+  b->queued = precision == EMCG_FP32 ? 1 : 0;
+  b->minBlocks = precision == EMCG_FP32 ? 3 : 1;
   b->tsz = precision == EMCG_FP64 ? 8 : 4;
   b->nModels = n_models;
   b->nEns = n_ens;
@@ -815,6 +1051,14 @@ extern "C" int32_t emcg_last_kernel_ms(emcg_handle *h, double *ms) {
   EMCG_TRY(bulkOf(h, &b));
   EMCG_CHECK_ARG(ms, "ms is NULL");
   *ms = b->lastMs;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_set_scatter_mode(emcg_handle *h, int32_t queued) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(queued == 0 || queued == 1, "queued must be 0 or 1");
+  b->queued = queued;
   return EMCG_OK;
 }
 
