@@ -336,6 +336,33 @@ int32_t emcg_device_set_replay(emcg_handle *h, int32_t phase, const uint64_t *wo
 /* Device-side time of the last emcg_device_step / poisson call (ms). */
 int32_t emcg_device_timing(emcg_handle *h, double *step_ms, double *poisson_ms);
 
+/* Poisson solve that allocates nothing.  No counterpart in the reference: it
+   is the solve of emcg_device_poisson (float multigrid V-cycles inside double
+   Newton / defect correction) for callers that must not allocate device
+   memory when they solve -- a host whose memory pool owns the GPU, or an
+   embedder that fixes its device footprint at start-up.
+   Works on caller-owned device arrays of nx * ny doubles: d_pot (in/out) is
+   the potential in thermal voltages and d_conc the electron concentration
+   normalised to ni (the units of EMCG_GRID_POTENTIAL / EMCG_GRID_CONC), or
+   NULL for the equilibrium equation.  reset_bc, the smoothing sweeps (0 = 2),
+   rtol and max_cycles mean what they mean for emcg_device_create's
+   configuration and emcg_device_poisson.  cuda_stream may be NULL (default
+   stream); the call returns after the solve has finished on that stream.
+   Working memory is one fixed device array of about 21 MB in this library,
+   reserved when its device code is loaded: grids of up to 131072 nodes and
+   8192 nodes per dimension, at most 64 contacts (ohmic or gate); larger
+   inputs return EMCG_ERR_ARG and touch nothing.  Every call rebuilds the
+   array's contents, including the statistics that must start at zero.
+   The first call on each device looks the array's address up
+   (cudaGetSymbolAddress, with that device current); make it before any
+   stream capture begins on that device.  All calls share the array: calls whose work can overlap on a device, from
+   several host threads or on several streams, race and corrupt each other's
+   results; serialise them. */
+int32_t emcg_poisson_solve_noalloc(const emcg_device_desc *dev, double *d_pot,
+                                   const double *d_conc, int32_t reset_bc, int32_t smooth,
+                                   double rtol, int32_t max_cycles, void *cuda_stream,
+                                   double *rel_residual, int32_t *cycles);
+
 #ifdef __cplusplus
 }
 #endif

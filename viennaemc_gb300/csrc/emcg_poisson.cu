@@ -1,10 +1,12 @@
 // Grid Poisson solver of the device engine: double-precision Newton / defect
 // correction around geometric multigrid V-cycles (see emcg_poisson.cuh).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
+#include "emcg_common.cuh"
 #include "emcg_host.h"
 #include "emcg_poisson.cuh"
 
@@ -509,3 +511,468 @@ int32_t poissonSolve(PoissonMG &P, double *pot, const double *conc, bool resetBC
 }
 
 } // namespace emcg
+
+// ===========================================================================
+// Poisson solve that allocates nothing (emcg_poisson_solve_noalloc).
+//
+// Some callers cannot allocate device memory at the moment they solve: a host
+// whose memory pool owns the whole GPU, a caller inside a region where the CUDA
+// allocator must not be entered, or an embedder that must not grow the
+// process's device footprint after start-up.  For them the solver's working set
+// -- fine-grid inputs, the multigrid hierarchy, transfer tables and residual
+// statistics -- lives in one file-scope device array of fixed size, reserved
+// when this library's device code is loaded.  It is rebuilt from the caller's
+// description by kernels on every call; the host side uses only stack memory.
+// Host code cannot pass the array's name to a kernel as an address: the first
+// call on each device asks the runtime for the address (cudaGetSymbolAddress,
+// with that device current) and keeps it.  The array is shared by all calls,
+// so calls whose work can overlap on a device race with one another.
+// ===========================================================================
+namespace emcg {
+namespace {
+
+constexpr int kNAMaxNodes = 1 << 17;           // fine-grid nodes, e.g. 401 x 201 or 362 x 362
+constexpr int kNAMaxDim = 8192;                // nodes per dimension
+constexpr int kNAMaxLevels = 16;               // as the allocating hierarchy
+constexpr int kNAMaxContacts = 64;
+constexpr int kNAMaxDevices = 64;
+constexpr int kNALevelNodes = 2 * kNAMaxNodes; // nodes of all levels together
+constexpr int kNA1D = 16 * kNAMaxDim;          // 1-D transfer entries of all levels
+
+// byte offsets inside the scratch array
+constexpr size_t kOffDoping = 0;                       // double [N]  doping (upload)
+constexpr size_t kOffC = kOffDoping + 8ull * kNAMaxNodes;   // double [N]  C = doping / ni
+constexpr size_t kOffGSum = kOffC + 8ull * kNAMaxNodes;     // double [N]  gate sums
+constexpr size_t kOffGVeq = kOffGSum + 8ull * kNAMaxNodes;
+constexpr size_t kOffGVne = kOffGVeq + 8ull * kNAMaxNodes;
+constexpr size_t kOffGDx = kOffGVne + 8ull * kNAMaxNodes;   // double [N]  Robin densities
+constexpr size_t kOffGDy = kOffGDx + 8ull * kNAMaxNodes;
+constexpr size_t kOffResEq = kOffGDy + 8ull * kNAMaxNodes;  // double [N]  resetBC values
+constexpr size_t kOffResNe = kOffResEq + 8ull * kNAMaxNodes;
+constexpr size_t kOffStats = kOffResNe + 8ull * kNAMaxNodes; // double [4] residual maxima
+constexpr size_t kOffLevelF = kOffStats + 256;               // float [9 x all levels]
+constexpr size_t kOffTransF = kOffLevelF + 4ull * 9 * kNALevelNodes; // float [1-D]
+constexpr size_t kOffTransI = kOffTransF + 4ull * kNA1D;             // int   [1-D]
+constexpr size_t kOffBnd = kOffTransI + 4ull * kNA1D;                // int   [2 (ny + nx)]
+constexpr size_t kOffCtype = kOffBnd + 4ull * 4 * kNAMaxDim;         // int   [contacts]
+constexpr size_t kOffResMask = kOffCtype + 4ull * kNAMaxContacts;    // u8    [N]
+constexpr size_t kOffFixed = kOffResMask + kNAMaxNodes;              // u8    [all levels]
+constexpr size_t kNABytes = (kOffFixed + kNALevelNodes + 255) & ~size_t(255); // about 21 MB
+
+struct NALevels {
+  int n;
+  int nx[kNAMaxLevels], ny[kNAMaxLevels];
+  double h0, h1; // normalised fine spacing
+};
+
+struct NAContacts {
+  double gF[kNAMaxContacts], barrier[kNAMaxContacts], volt[kNAMaxContacts];
+};
+
+// fine index of node I of level l along one dimension (coarse node I sits on
+// node min(2I, n - 1) of the level below while that level has more than 3)
+__device__ __forceinline__ int naFineIndex(const NALevels &lv, int l, int I, bool ydim) {
+  for (int k = l; k > 0; k--) {
+    int nf = ydim ? lv.ny[k - 1] : lv.nx[k - 1];
+    if (nf > 3)
+      I = min(2 * I, nf - 1);
+  }
+  return I;
+}
+__device__ __forceinline__ double naCoord(const NALevels &lv, int l, int I, bool ydim) {
+  return naFineIndex(lv, l, I, ydim) * (ydim ? lv.h1 : lv.h0);
+}
+
+// Fine-grid data of the reference equation
+// (include/PoissonSolver/emcSORSolver.hpp:25-36, 330-368): the same values
+// emcg_device_create prepares on the host for the allocating solver.
+__global__ void naFineSetupKernel(int nx, int ny, double Ni, double hF0, double hF1, double h0,
+                                  double h1, NAContacts ct, const double *doping,
+                                  const int32_t *bnd, const int32_t *ctype, double *C,
+                                  double *gSum, double *gVeq, double *gVne, double *gDx,
+                                  double *gDy, uint8_t *resMask, double *resEq, double *resNe,
+                                  uint8_t *fixed) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nx * ny)
+    return;
+  const int x = i % nx, y = i / nx;
+  // boundary b's contact at a node: XMIN/XMAX indexed by y, YMIN/YMAX by x
+  auto contact = [&](int b) { return b == 0 ? bnd[y] : b == 1 ? bnd[ny + y]
+                                     : b == 2 ? bnd[2 * ny + x] : bnd[2 * ny + nx + x]; };
+  const double c = doping[i] / Ni;
+  C[i] = c;
+  // reservoir nodes: the first boundary holding the node decides
+  // (emcSurface::getBoundaryPos, include/emcSurface.hpp)
+  int fb = x == 0 ? 0 : (x == nx - 1 ? 1 : (y == 0 ? 2 : (y == ny - 1 ? 3 : -1)));
+  int fc = fb < 0 ? -1 : contact(fb);
+  fixed[i] = fc >= 0 && ctype[fc] == EMCG_CONTACT_OHMIC;
+  // gate Robin terms of every side the node lies on
+  const double hF[2] = {hF0, hF1}, h[2] = {h0, h1};
+  double gs = 0, ge = 0, gn = 0, dx = 0, dy = 0;
+  for (int k = 0; k < 2; k++) {
+    int co = k == 0 ? x : y, mx = k == 0 ? nx - 1 : ny - 1;
+    for (int side = 0; side < 2; side++) {
+      if (co != (side == 0 ? 0 : mx))
+        continue;
+      int cc = contact(2 * k + side);
+      if (cc < 0 || ctype[cc] != EMCG_CONTACT_GATE)
+        continue;
+      double G = __dmul_rn(__dmul_rn(ct.gF[cc], hF[k]), h[k]);
+      gs = __dadd_rn(gs, G);
+      ge = __dadd_rn(ge, __dmul_rn(G, ct.barrier[cc]));
+      gn = __dadd_rn(gn, __dmul_rn(G, __dadd_rn(ct.barrier[cc], ct.volt[cc])));
+      if (k == 0)
+        dx = __dadd_rn(dx, 0.5 * ct.gF[cc]);
+      else
+        dy = __dadd_rn(dy, 0.5 * ct.gF[cc]);
+    }
+  }
+  gSum[i] = gs;
+  gVeq[i] = ge;
+  gVne[i] = gn;
+  gDx[i] = dx;
+  gDy[i] = dy;
+  // resetBC: every boundary coordinate of an ohmic contact, later boundaries
+  // (XMIN, XMAX, YMIN, YMAX order) overriding earlier ones at corners
+  uint8_t m = 0;
+  double re = 0, rn = 0;
+  for (int b = 0; b < 4; b++) {
+    bool on = b == 0 ? x == 0 : b == 1 ? x == nx - 1 : b == 2 ? y == 0 : y == ny - 1;
+    int cc = on ? contact(b) : -1;
+    if (cc < 0 || ctype[cc] != EMCG_CONTACT_OHMIC)
+      continue;
+    double bi = asinh(0.5 * c);
+    m = 1;
+    re = bi;
+    rn = __dadd_rn(ct.volt[cc], bi);
+  }
+  resMask[i] = m;
+  resEq[i] = re;
+  resNe[i] = rn;
+}
+
+// finite-volume coefficients and Dirichlet mask of level l, by injection of
+// the fine data (the construction poissonCreate runs on the host)
+__global__ void naLevelSetupKernel(NALevels lv, int l, const double *gDx, const double *gDy,
+                                   const uint8_t *fixed0, int nx0, float *cw, float *ce, float *cs,
+                                   float *cn, float *area, float *diag0, uint8_t *fixed) {
+  const int lx = lv.nx[l], ly = lv.ny[l];
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= lx * ly)
+    return;
+  const int i = k % lx, j = k / lx;
+  const double Xi = naCoord(lv, l, i, false), Yj = naCoord(lv, l, j, true);
+  const double dxw = i > 0 ? Xi - naCoord(lv, l, i - 1, false) : 0;
+  const double dxe = i < lx - 1 ? naCoord(lv, l, i + 1, false) - Xi : 0;
+  const double dys = j > 0 ? Yj - naCoord(lv, l, j - 1, true) : 0;
+  const double dyn = j < ly - 1 ? naCoord(lv, l, j + 1, true) - Yj : 0;
+  const double lxd = 0.5 * (dxw + dxe), lyd = 0.5 * (dys + dyn);
+  const double w = i > 0 ? lyd / dxw : 0, e = i < lx - 1 ? lyd / dxe : 0;
+  const double s = j > 0 ? lxd / dys : 0, n = j < ly - 1 ? lxd / dyn : 0;
+  const int f = naFineIndex(lv, l, j, true) * nx0 + naFineIndex(lv, l, i, false);
+  double d = __dadd_rn(__dadd_rn(__dadd_rn(w, e), s), n);
+  d = __dadd_rn(__dadd_rn(d, __dmul_rn(gDx[f], lyd)), __dmul_rn(gDy[f], lxd));
+  cw[k] = (float)w;
+  ce[k] = (float)e;
+  cs[k] = (float)s;
+  cn[k] = (float)n;
+  area[k] = (float)(lxd * lyd);
+  diag0[k] = (float)d;
+  if (l > 0)
+    fixed[k] = fixed0[f];
+}
+
+// 1-D transfer between level l (nf nodes) and level l + 1 (nc nodes) along one
+// dimension: prolongation's lower coarse node and weight per fine node,
+// restriction's (up to 3) fine nodes and weights per coarse node in ascending
+// fine order, and the coarse -> fine injection map
+__global__ void naTransferKernel(NALevels lv, int l, bool ydim, int *pIdx, float *pW, int *rIdx,
+                                 float *rW, int *map) {
+  const int nf = ydim ? lv.ny[l] : lv.nx[l];
+  const int nc = ydim ? lv.ny[l + 1] : lv.nx[l + 1];
+  auto cmap = [&](int J) { return nf > 3 ? min(2 * J, nf - 1) : J; };
+  auto X = [&](int i) { return naCoord(lv, l, i, ydim); };
+  auto lower = [&](int i, int &I, float &w) {
+    I = min(nf > 3 ? i / 2 : i, nc - 1);
+    while (I + 1 < nc && cmap(I + 1) <= i)
+      I++;
+    while (I > 0 && cmap(I) > i)
+      I--;
+    if (cmap(I) == i || I + 1 >= nc)
+      w = 1.f;
+    else
+      w = (float)((X(cmap(I + 1)) - X(i)) / (X(cmap(I + 1)) - X(cmap(I))));
+  };
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nf) {
+    int I;
+    float w;
+    lower(t, I, w);
+    pIdx[t] = I;
+    pW[t] = w;
+  }
+  if (t < nc) {
+    map[t] = cmap(t);
+    for (int q = 0; q < 3; q++) {
+      rIdx[3 * t + q] = 0;
+      rW[3 * t + q] = 0.f;
+    }
+    int cnt = 0;
+    const int lo = t > 0 ? cmap(t - 1) : 0, hi = t + 1 < nc ? cmap(t + 1) : nf - 1;
+    for (int i = lo; i <= hi && cnt < 3; i++) {
+      int I;
+      float w;
+      lower(i, I, w);
+      if (I == t && w > 0.f) {
+        rIdx[3 * t + cnt] = i;
+        rW[3 * t + cnt] = w;
+        cnt++;
+      } else if (I + 1 == t && w < 1.f) {
+        rIdx[3 * t + cnt] = i;
+        rW[3 * t + cnt] = 1.f - w;
+        cnt++;
+      }
+    }
+  }
+}
+
+// the allocating solver's V-cycle (float multigrid), over a fixed level array
+void naVcycle(const MGLevel *lev, int nLev, int l, int pre, int post, int coarseSweeps,
+              cudaStream_t st) {
+  const MGLevel &lv = lev[l];
+  LevelK<float> K = levelK<float>(lv);
+  const int n = lv.nx * lv.ny;
+  if (l + 1 == nLev) {
+    coarseSolveKernel<float><<<1, 256, 0, st>>>(K, coarseSweeps);
+    return;
+  }
+  const int half = ((lv.nx + 1) / 2) * lv.ny;
+  const int gs = (half + kBlock - 1) / kBlock;
+  for (int s = 0; s < pre; s++) {
+    smoothKernel<float><<<gs, kBlock, 0, st>>>(K, 0);
+    smoothKernel<float><<<gs, kBlock, 0, st>>>(K, 1);
+  }
+  const MGLevel &cl = lev[l + 1];
+  LevelK<float> Kc = levelK<float>(cl);
+  const int nc = cl.nx * cl.ny;
+  restrictKernel<float><<<(nc + kBlock - 1) / kBlock, kBlock, 0, st>>>(
+      K, Kc, lv.rxIdx, lv.rxW, lv.ryIdx, lv.ryW, lv.mapX, lv.mapY);
+  naVcycle(lev, nLev, l + 1, pre, post, coarseSweeps, st);
+  prolongKernel<float><<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(K, Kc, lv.pxIdx, lv.pxW,
+                                                                     lv.pyIdx, lv.pyW);
+  for (int s = 0; s < post; s++) {
+    smoothKernel<float><<<gs, kBlock, 0, st>>>(K, 1);
+    smoothKernel<float><<<gs, kBlock, 0, st>>>(K, 0);
+  }
+}
+
+} // namespace
+
+// the array and its per-device address
+static __device__ __align__(256) unsigned char g_poissonScratch[kNABytes];
+static std::atomic<void *> g_poissonScratchAddr[kNAMaxDevices];
+
+static int32_t poissonScratchAddress(unsigned char **out) {
+  int dev = -1;
+  EMCG_CUDA(cudaGetDevice(&dev));
+  EMCG_CHECK_ARG(dev >= 0 && dev < kNAMaxDevices, "device %d is beyond the %d devices supported",
+                 dev, kNAMaxDevices);
+  void *p = g_poissonScratchAddr[dev].load(std::memory_order_acquire);
+  if (!p) {
+    cudaError_t e = cudaGetSymbolAddress(&p, g_poissonScratch);
+    if (e != cudaSuccess || !p) {
+      setError("cudaGetSymbolAddress of the Poisson scratch array failed on device %d: %s", dev,
+               cudaGetErrorString(e));
+      return EMCG_ERR_CUDA;
+    }
+    g_poissonScratchAddr[dev].store(p, std::memory_order_release);
+  }
+  *out = static_cast<unsigned char *>(p);
+  return EMCG_OK;
+}
+
+} // namespace emcg
+
+extern "C" int32_t emcg_poisson_solve_noalloc(const emcg_device_desc *dv, double *d_pot,
+                                              const double *d_conc, int32_t reset_bc,
+                                              int32_t smooth, double rtol, int32_t max_cycles,
+                                              void *cuda_stream, double *rel_residual,
+                                              int32_t *cycles) {
+  using namespace emcg;
+  EMCG_CHECK_ARG(dv && d_pot, "device description and potential are required");
+  const int nx = dv->nx, ny = dv->ny;
+  EMCG_CHECK_ARG(nx >= 3 && ny >= 3, "grid must have at least 3 x 3 nodes (got %d x %d)", nx, ny);
+  EMCG_CHECK_ARG(nx <= kNAMaxDim && ny <= kNAMaxDim && (int64_t)nx * ny <= kNAMaxNodes,
+                 "grid %d x %d exceeds the no-allocation Poisson limit of %d nodes and %d per "
+                 "dimension",
+                 nx, ny, kNAMaxNodes, kNAMaxDim);
+  EMCG_CHECK_ARG(dv->n_contacts >= 0 && dv->n_contacts <= kNAMaxContacts,
+                 "%d contacts exceed the no-allocation Poisson limit of %d", dv->n_contacts,
+                 kNAMaxContacts);
+  EMCG_CHECK_ARG(dv->doping && dv->boundary_contact[0] && dv->boundary_contact[1] &&
+                     dv->boundary_contact[2] && dv->boundary_contact[3],
+                 "doping and boundary contact arrays are required");
+  EMCG_CHECK_ARG(dv->n_contacts == 0 ||
+                     (dv->contact_type && dv->contact_voltage && dv->contact_param),
+                 "contact arrays are required");
+  EMCG_CHECK_ARG(dv->hx > 0 && dv->hy > 0 && dv->temperature > 0 && dv->ni > 0 && dv->eps_r > 0,
+                 "spacing, temperature, ni and eps_r must be positive");
+  EMCG_CHECK_ARG(rtol > 0 && max_cycles >= 0 && smooth >= 0, "bad Poisson settings");
+  for (int c = 0; c < dv->n_contacts; c++)
+    EMCG_CHECK_ARG(dv->contact_type[c] == EMCG_CONTACT_OHMIC ||
+                       dv->contact_type[c] == EMCG_CONTACT_GATE,
+                   "contact %d: only ohmic and gate contacts are supported", c);
+  for (int b = 0; b < 4; b++)
+    for (int k = 0; k < (b < 2 ? ny : nx); k++)
+      EMCG_CHECK_ARG(dv->boundary_contact[b][k] >= -1 &&
+                         dv->boundary_contact[b][k] < dv->n_contacts,
+                     "boundary %d, node %d: contact index %d out of range", b, k,
+                     dv->boundary_contact[b][k]);
+  // level shapes and their scratch footprint, checked before anything is written
+  NALevels lv;
+  lv.n = 0;
+  size_t nodes = 0, oneD = 0;
+  for (int l = 0, lx = nx, ly = ny; l < kNAMaxLevels; l++) {
+    lv.nx[l] = lx;
+    lv.ny[l] = ly;
+    lv.n = l + 1;
+    nodes += (size_t)lx * ly;
+    const int cx = lx > 3 ? lx / 2 + 1 : lx, cy = ly > 3 ? ly / 2 + 1 : ly;
+    if (cx == lx && cy == ly)
+      break;
+    oneD += (size_t)lx + ly + 4 * (size_t)cx + 4 * (size_t)cy;
+    lx = cx;
+    ly = cy;
+  }
+  EMCG_CHECK_ARG(nodes <= (size_t)kNALevelNodes && oneD <= (size_t)kNA1D,
+                 "grid %d x %d: multigrid hierarchy exceeds the no-allocation scratch", nx, ny);
+  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  unsigned char *S = nullptr;
+  EMCG_TRY(poissonScratchAddress(&S));
+  const int n = nx * ny;
+  // normalisation (include/emcDevice.hpp:87, emcSORSolver.hpp:330-368)
+  const double Vt = kKB / kQ * dv->temperature;
+  const double Ld = std::sqrt(kEPS0 * dv->eps_r * Vt / kQ / dv->ni);
+  lv.h0 = dv->hx / Ld;
+  lv.h1 = dv->hy / Ld;
+  NAContacts ct;
+  for (int c = 0; c < dv->n_contacts; c++) {
+    ct.volt[c] = dv->contact_voltage[c] / Vt;
+    ct.gF[c] = ct.barrier[c] = 0;
+    if (dv->contact_type[c] == EMCG_CONTACT_GATE) {
+      const double gamma = dv->contact_param[3 * c + 0] / dv->eps_r;
+      const double tox = dv->contact_param[3 * c + 1] / Ld;
+      ct.gF[c] = 2 * gamma / tox;
+      ct.barrier[c] = dv->contact_param[3 * c + 2] / Vt;
+    }
+  }
+  double *doping = (double *)(S + kOffDoping), *C = (double *)(S + kOffC);
+  double *gSum = (double *)(S + kOffGSum), *gVeq = (double *)(S + kOffGVeq);
+  double *gVne = (double *)(S + kOffGVne), *gDx = (double *)(S + kOffGDx);
+  double *gDy = (double *)(S + kOffGDy), *resEq = (double *)(S + kOffResEq);
+  double *resNe = (double *)(S + kOffResNe), *stats = (double *)(S + kOffStats);
+  float *levF = (float *)(S + kOffLevelF), *trF = (float *)(S + kOffTransF);
+  int *trI = (int *)(S + kOffTransI);
+  int32_t *bnd = (int32_t *)(S + kOffBnd), *ctype = (int32_t *)(S + kOffCtype);
+  uint8_t *resMask = S + kOffResMask, *fixedAll = S + kOffFixed;
+  EMCG_CUDA(cudaMemcpyAsync(doping, dv->doping, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  const int32_t *bsrc[4] = {dv->boundary_contact[0], dv->boundary_contact[1],
+                            dv->boundary_contact[2], dv->boundary_contact[3]};
+  const size_t boff[4] = {0, (size_t)ny, 2 * (size_t)ny, 2 * (size_t)ny + nx};
+  for (int b = 0; b < 4; b++)
+    EMCG_CUDA(cudaMemcpyAsync(bnd + boff[b], bsrc[b], sizeof(int32_t) * (b < 2 ? ny : nx),
+                              cudaMemcpyHostToDevice, st));
+  if (dv->n_contacts)
+    EMCG_CUDA(cudaMemcpyAsync(ctype, dv->contact_type, sizeof(int32_t) * dv->n_contacts,
+                              cudaMemcpyHostToDevice, st));
+  const double hF0 = lv.h1 / lv.h0, hF1 = lv.h0 / lv.h1;
+  double hP = 1.;
+  hP = hP * lv.h0;
+  hP = hP * lv.h1;
+  naFineSetupKernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(
+      nx, ny, dv->ni, hF0, hF1, lv.h0, lv.h1, ct, doping, bnd, ctype, C, gSum, gVeq, gVne, gDx,
+      gDy, resMask, resEq, resNe, fixedAll);
+  EMCG_CUDA(cudaGetLastError());
+  // carve the levels out of the scratch and build them
+  MGLevel lev[kNAMaxLevels];
+  size_t fo = 0, uo = 0, to = 0;
+  for (int l = 0; l < lv.n; l++) {
+    MGLevel &M = lev[l];
+    std::memset(&M, 0, sizeof(M));
+    M.nx = lv.nx[l];
+    M.ny = lv.ny[l];
+    const size_t m = (size_t)M.nx * M.ny;
+    float **arr[9] = {&M.cw, &M.ce, &M.cs, &M.cn, &M.area, &M.diag0, &M.d, &M.r, &M.rho};
+    for (int a = 0; a < 9; a++) {
+      *arr[a] = levF + fo;
+      fo += m;
+    }
+    M.fixed = fixedAll + uo;
+    uo += m;
+    naLevelSetupKernel<<<(int)((m + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+        lv, l, gDx, gDy, fixedAll, nx, M.cw, M.ce, M.cs, M.cn, M.area, M.diag0, M.fixed);
+    EMCG_CUDA(cudaGetLastError());
+    if (l + 1 < lv.n) {
+      const int nfx = M.nx, nfy = M.ny, ncx = lv.nx[l + 1], ncy = lv.ny[l + 1];
+      M.pxIdx = trI + to;
+      M.pxW = trF + to;
+      to += nfx;
+      M.pyIdx = trI + to;
+      M.pyW = trF + to;
+      to += nfy;
+      M.rxIdx = trI + to;
+      M.rxW = trF + to;
+      to += 3 * (size_t)ncx;
+      M.ryIdx = trI + to;
+      M.ryW = trF + to;
+      to += 3 * (size_t)ncy;
+      M.mapX = trI + to;
+      to += ncx;
+      M.mapY = trI + to;
+      to += ncy;
+      naTransferKernel<<<(nfx + kBlock - 1) / kBlock, kBlock, 0, st>>>(lv, l, false, M.pxIdx,
+                                                                       M.pxW, M.rxIdx, M.rxW,
+                                                                       M.mapX);
+      naTransferKernel<<<(nfy + kBlock - 1) / kBlock, kBlock, 0, st>>>(lv, l, true, M.pyIdx,
+                                                                       M.pyW, M.ryIdx, M.ryW,
+                                                                       M.mapY);
+      EMCG_CUDA(cudaGetLastError());
+    }
+  }
+  // Newton / defect correction: the loop of the allocating solver (float MG)
+  const int grid = (n + kBlock - 1) / kBlock;
+  if (reset_bc) {
+    resetBCKernel<<<grid, kBlock, 0, st>>>(d_pot, resMask, d_conc ? resNe : resEq, n);
+    EMCG_CUDA(cudaGetLastError());
+  }
+  const int pre = smooth > 0 ? smooth : 2, post = pre, coarseSweeps = 40;
+  LevelK<float> K0 = levelK<float>(lev[0]);
+  double h_stats[2] = {0, 0};
+  double rel = INFINITY;
+  int it = 0;
+  for (; it <= max_cycles; it++) {
+    // the residual maxima accumulate by atomic max and must start at zero
+    EMCG_CUDA(cudaMemsetAsync(stats, 0, 4 * sizeof(double), st));
+    nonlinResidualKernel<float><<<grid, kBlock, 0, st>>>(
+        d_pot, d_conc, C, lev[0].fixed, gSum, d_conc ? gVne : gVeq, nx, ny, hF0, hF1, hP, K0.r,
+        K0.rho, K0.d, stats);
+    EMCG_CUDA(cudaGetLastError());
+    EMCG_CUDA(cudaMemcpyAsync(h_stats, stats, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    EMCG_CUDA(cudaStreamSynchronize(st));
+    rel = h_stats[1] > 0 ? h_stats[0] / h_stats[1] : h_stats[0];
+    if (rel <= rtol || it == max_cycles)
+      break;
+    naVcycle(lev, lv.n, 0, pre, post, coarseSweeps, st);
+    updatePotKernel<float><<<grid, kBlock, 0, st>>>(d_pot, K0.d, lev[0].fixed, n, stats);
+    EMCG_CUDA(cudaGetLastError());
+  }
+  if (rel_residual)
+    *rel_residual = rel;
+  if (cycles)
+    *cycles = it;
+  if (!(rel <= rtol)) {
+    setError("Poisson: relative residual %.3e after %d V-cycles (target %.1e)", rel, it, rtol);
+    return EMCG_ERR_NONCONVERGED;
+  }
+  return EMCG_OK;
+}
