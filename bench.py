@@ -163,8 +163,9 @@ def run_engine(args):
     else:
         value64 = vd32 = vd64 = k64 = None
         win = slice(0, 0)
+    device = _device_bench(args, rank) if args.device_steps > 0 else None
     _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units, h2d, d2h,
-            value64, vd32, vd64, win, k64, wall, clocks)
+            value64, vd32, vd64, win, k64, wall, clocks, device)
     if ws > 1:
         torch.distributed.destroy_process_group()
 
@@ -212,7 +213,7 @@ def _fp64(v, pt, args, N, K, W, per, rank, avg):
 
 
 def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units, h2d, d2h,
-            value64, vd32, vd64, win, k64, wall, clocks):
+            value64, vd32, vd64, win, k64, wall, clocks, device=None):
     peak, peak_src = _peaks()
     bpp = BYTES_PER_PARTICLE_STEP["fp32"]
     achieved = bpp * value / 1e9  # algorithmic GB/s (72 B per particle-step)
@@ -223,7 +224,7 @@ def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units,
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": "bulk Si, 2^20 electrons, 1e6 V/m <100>, dt 1 fs, 5000 steps",
                    "particles": N, "steps_per_launch": per, "block_threads": args.block,
-                   "min_blocks_per_sm": args.min_blocks,
+                   "min_blocks_per_sm": args.min_blocks, "scatter_kernel": "lockstep",
                    "l2": "flushed (256 MB write) between timed launches",
                    "observables": "per-step FP64 sums of E, v.dir, count"},
         "e2e": {"value": e2e_units / e2e_s if e2e_units else None, "unit": UNIT,
@@ -245,10 +246,85 @@ def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units,
                             "window_steps": [win.start, win.stop]}
     if clocks:
         line["clocks"] = clocks
+    if device:
+        line["device"] = device
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(N, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def resistor_device(D, P):
+    """2-D n+ Si resistor: 100 nm x 50 nm, 0.5 nm spacing (201 x 101 nodes),
+    Nd = 1e24 m^-3, ohmic contacts at both ends with 0.5 V across, width
+    1e-4 m so that about 5e5 electrons fill it."""
+    dev = D.Device(P.silicon_material(), (100e-9, 50e-9), (0.5e-9, 0.5e-9))
+    dev.setDeviceWidth(1e-4)
+    dev.addConstantDopingRegion((0, 0), (100e-9, 50e-9), 1e24)
+    dev.addOhmicContact(D.XMAX, 0.0, (0,), (50e-9,))
+    dev.addOhmicContact(D.XMIN, 0.5, (0,), (50e-9,))
+    return dev
+
+
+def _device_bench(args, rank):
+    """The device path on the resistor: performEMCStep (Poisson -> E -> move ->
+    contacts -> CIC assignment) every 0.1 fs in FP32 with the float-multigrid /
+    double-Newton Poisson solve to 1e-8 relative residual; the reference's SOR
+    (omega 1.8, 1e-4 V) is timed on the host on the same potential and
+    concentration."""
+    from viennaemc_gb300 import device as D
+    from viennaemc_gb300 import physics as P
+    dev = resistor_device(D, P)
+    pt = P.silicon_electron("refbulk", n_levels=1000, max_energy=4.0, regions=[0], coulomb=True,
+                            region_doping=dev.getDopingRegionDoping)
+    sim = D.DeviceSimulation(dev, pt, scheme=D.CIC, dt=1e-16, seed=11 + rank, precision="fp32",
+                             poisson_rtol=1e-8, poisson_max_cycles=60, poisson_fp32=True)
+    sim.calcEquilibriumCharacteristics()
+    sim.performEMCStep(args.device_warmup)
+    n0 = sim.num_particles()
+    K = args.device_steps
+    t0 = time.perf_counter()
+    sim.performEMCStep(K)
+    wall = time.perf_counter() - t0
+    n1 = sim.num_particles()
+    step_ms, pois_ms = sim.timing()
+    cycles, solves = sim.poisson_counts()
+    cur = sim.current()
+    out = {"workload": "2-D Si resistor 100 x 50 nm, 201 x 101 nodes, Nd 1e24, 0.5 V, CIC, "
+                       "dt 0.1 fs, acoustic + zero/first-order IV + Coulomb",
+           "particles": [n0, n1], "steps": K, "warmup": args.device_warmup,
+           "value": 0.5 * (n0 + n1) * K / (step_ms / 1e3), "unit": UNIT,
+           "ms_per_step": step_ms / K, "poisson_ms_per_solve": pois_ms / K,
+           "poisson_cycles_per_solve": cycles / max(solves, 1),
+           "poisson": "float V-cycles in double Newton, stop at 1e-8 relative residual",
+           "wall_s": wall, "current_A": [float(c) for c in cur]}
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_reference_sor"] = _cpu_sor(dev, sim.potential, sim.concentration)
+    sim.close()
+    return out
+
+
+def _cpu_sor(dev, pot, conc, repeats=3):
+    """The reference's SOR solve (oracle port, one thread like the reference)
+    from the engine's potential with its latest concentration."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    po.build()
+    ct = np.array([c[0] for c in dev.contacts], np.int32)
+    cv = np.array([c[1] for c in dev.contacts], np.float64)
+    cp = np.array([p for c in dev.contacts for p in c[2]], np.float64).reshape(-1, 3)
+    od = po.Device(dev.nx, dev.ny, dev.spacing[0], dev.spacing[1], dev.width, dev.doping,
+                   dev.region, dev.bnd, ct, cv, cp)
+    od.set_max(*dev.max_pos)
+    times, sweeps = [], []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        _, n = od.sor(pot, conc, 1.8, 1e-4, False)
+        times.append(time.perf_counter() - t0)
+        sweeps.append(int(n))
+    return {"ms_per_solve": 1e3 * statistics.median(times), "sweeps": sweeps, "cores": 1,
+            "kind": "port", "sample": f"{repeats} solves on the engine's last potential and "
+                                      "concentration, omega 1.8, accuracy 1e-4 V"}
 
 
 def _host_state(v, N):
@@ -366,7 +442,10 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=1 << 20)
     ap.add_argument("--steps-per-launch", type=int, default=500)
     ap.add_argument("--block", type=int, default=256)
-    ap.add_argument("--min-blocks", type=int, default=1, help="register cap variant (1, 3, 4)")
+    ap.add_argument("--min-blocks", type=int, default=4, help="register cap variant (1, 3, 4)")
+    ap.add_argument("--device-steps", type=int, default=1000,
+                    help="timed resistor device steps (0: skip the device path)")
+    ap.add_argument("--device-warmup", type=int, default=20)
     ap.add_argument("--fp64-steps", type=int, default=1500)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

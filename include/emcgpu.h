@@ -335,6 +335,13 @@ int32_t emcg_device_set_replay(emcg_handle *h, int32_t phase, const uint64_t *wo
                                int64_t nwords, const int64_t *offsets, int64_t n_offsets);
 /* Device-side time of the last emcg_device_step / poisson call (ms). */
 int32_t emcg_device_timing(emcg_handle *h, double *step_ms, double *poisson_ms);
+/* Poisson execution: mode 1 = the whole solve in one launch of a thread-block
+   cluster (default where the grid fits), 0 = one launch per multigrid phase,
+   -1 = leave as is.  *cluster_size (may be NULL) receives the CTAs per
+   cluster of the solve in use, 0 for the multi-launch path. */
+int32_t emcg_device_poisson_mode(emcg_handle *h, int32_t mode, int32_t *cluster_size);
+/* Newton / V-cycles and Poisson solves of the last emcg_device_step call. */
+int32_t emcg_device_poisson_counts(emcg_handle *h, int64_t *cycles, int64_t *solves);
 
 /* Poisson solve that allocates nothing.  No counterpart in the reference: it
    is the solve of emcg_device_poisson (float multigrid V-cycles inside double

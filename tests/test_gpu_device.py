@@ -194,3 +194,56 @@ def test_full_device_steps_run_and_conserve_count(engine):
         assert n1 == n0 - int(netto.sum())
         assert np.all(np.isfinite(sim.potential))
         sim.close()
+
+
+def _resistor_201x101():
+    from viennaemc_gb300 import device as D
+    from viennaemc_gb300.physics import silicon_material
+    dev = D.Device(silicon_material(), (100e-9, 50e-9), (0.5e-9, 0.5e-9))
+    dev.setDeviceWidth(1e-4)
+    dev.addConstantDopingRegion((0, 0), (100e-9, 50e-9), 1e24)
+    dev.addOhmicContact(D.XMAX, 0.0, (0,), (50e-9,))
+    dev.addOhmicContact(D.XMIN, 0.5, (0,), (50e-9,))
+    return dev
+
+
+@pytest.mark.parametrize("case", DEVICE_CASES + ["resistor_201x101"])
+def test_poisson_cluster_equals_multilaunch(engine, case):
+    """The single-launch cluster solve and the one-launch-per-phase solve
+    evaluate the same expressions on the same values: same cycles, same
+    potential (1e-13 thermal voltages)."""
+    from viennaemc_gb300 import _lib as L
+    from viennaemc_gb300 import device as D
+    if case == "resistor_201x101":
+        from viennaemc_gb300 import physics as P
+        dev = _resistor_201x101()
+        pt = P.silicon_electron("refbulk", n_levels=1000, max_energy=4.0, regions=[0],
+                                coulomb=True, region_doping=dev.getDopingRegionDoping)
+        sim = D.DeviceSimulation(dev, pt, scheme=D.CIC, dt=1e-16, seed=5, precision="fp32",
+                                 poisson_rtol=1e-10, poisson_max_cycles=200)
+        pot0 = np.arcsinh(0.5 * dev.doping / dev.material.Ni)
+        rs = np.random.default_rng(1)
+        conc = np.exp(pot0) * (1 + 0.05 * rs.standard_normal(pot0.size))
+    else:
+        g = golden(case)
+        sim, dev, pt = _sim(engine, g, case, precision="fp32", poisson_rtol=1e-10,
+                            poisson_max_cycles=200)
+        pot0, conc = g["pot_init"], g["conc0"]
+    assert sim.poisson_mode() >= 1
+    if case == "resistor_201x101":
+        assert sim.poisson_mode() > 1  # distributed over several CTAs
+    out = {}
+    for mode in (1, 0):
+        sim.poisson_mode(mode)
+        sim.set_grid(L.GRID_POTENTIAL, pot0)
+        r1 = sim.poisson(equilibrium=True, reset_bc=True)
+        eq = sim.potential
+        sim.set_grid(L.GRID_CONC, conc)
+        r2 = sim.poisson(equilibrium=False, reset_bc=True)
+        out[mode] = (r1, r2, eq, sim.potential)
+    sim.close()
+    a, b = out[1], out[0]
+    assert a[0][1] == b[0][1] and a[1][1] == b[1][1], (a[0], b[0], a[1], b[1])
+    assert max(a[0][0], a[1][0]) <= 1e-10
+    assert np.max(np.abs(a[2] - b[2])) <= 1e-13 * max(1.0, np.abs(b[2]).max())
+    assert np.max(np.abs(a[3] - b[3])) <= 1e-13 * max(1.0, np.abs(b[3]).max())

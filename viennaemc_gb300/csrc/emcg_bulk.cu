@@ -521,7 +521,7 @@ struct BulkImpl {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int blockThreads = 256;
   int minBlocks = 1; // register cap variant of the step kernel (1, 3 or 4)
-  int queued = 1;    // 1: block-queued scatter kernel (Philox), 0: lockstep kernel
+  int queued = 0;    // 1: block-queued scatter kernel (Philox), 0: lockstep kernel
   int stepsPerLaunch = 0;
   int chunk = 16;
   uint64_t *dWords = nullptr;
@@ -779,8 +779,8 @@ extern "C" int32_t emcg_bulk_create(const emcg_model_desc *models, int32_t n_mod
   b->precision = precision;
   // defaults measured on GB300: the float engine runs the block-queued kernel
   // with a 3-blocks-per-SM register cap, the double engine the lockstep one
-  b->queued = precision == EMCG_FP32 ? 1 : 0;
-  b->minBlocks = precision == EMCG_FP32 ? 3 : 1;
+  b->queued = 0;
+  b->minBlocks = precision == EMCG_FP32 ? 4 : 1;
   b->tsz = precision == EMCG_FP64 ? 8 : 4;
   b->nModels = n_models;
   b->nEns = n_ens;

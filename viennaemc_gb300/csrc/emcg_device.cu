@@ -633,6 +633,7 @@ struct DeviceImpl {
   int64_t wordsCap[2] = {0, 0}, offCap[2] = {0, 0};
   bool replay[2] = {false, false};
   double stepMs = 0, poissonMs = 0;
+  int64_t poissonCycles = 0, poissonSolves = 0; // V-cycles and solves of the last step call
   int nBlocks() const { return (int)((capacity + kCB - 1) / kCB); }
 };
 
@@ -1237,6 +1238,7 @@ extern "C" int32_t emcg_device_step(emcg_handle *h, int32_t n_steps, uint32_t st
   const int nc = d->nContacts;
   std::vector<int32_t> hn(2 * (nc + 1));
   double stepMs = 0, poisMs = 0;
+  d->poissonCycles = d->poissonSolves = 0;
   for (int s = 0; s < n_steps; s++) {
     EMCG_CUDA(cudaEventRecord(d->ev[0], d->stream));
     double rel;
@@ -1246,6 +1248,8 @@ extern "C" int32_t emcg_device_step(emcg_handle *h, int32_t n_steps, uint32_t st
     if (ps)
       return ps;
     poisMs += d->poissonMs;
+    d->poissonCycles += cyc;
+    d->poissonSolves++;
     EMCG_TRY(d->precision == EMCG_FP64 ? efieldT<double>(d) : efieldT<float>(d));
     EMCG_CUDA(cudaMemsetAsync(d->dNetto, 0, (nc + 1) * sizeof(int32_t), d->stream));
     EMCG_CUDA(cudaMemsetAsync(d->dRemInj, 0, (nc + 1) * sizeof(int32_t), d->stream));
@@ -1271,6 +1275,27 @@ extern "C" int32_t emcg_device_step(emcg_handle *h, int32_t n_steps, uint32_t st
   }
   d->stepMs = stepMs;
   d->poissonMs = poisMs;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_device_poisson_mode(emcg_handle *h, int32_t mode, int32_t *cluster_size) {
+  DeviceImpl *d;
+  EMCG_TRY(devOf(h, &d));
+  EMCG_CHECK_ARG(mode >= -1 && mode <= 1, "mode must be -1 (query), 0 or 1");
+  if (mode >= 0)
+    d->mg.useCluster = mode == 1;
+  if (cluster_size)
+    *cluster_size = d->mg.useCluster ? d->mg.clusterSize : 0;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_device_poisson_counts(emcg_handle *h, int64_t *cycles, int64_t *solves) {
+  DeviceImpl *d;
+  EMCG_TRY(devOf(h, &d));
+  if (cycles)
+    *cycles = d->poissonCycles;
+  if (solves)
+    *solves = d->poissonSolves;
   return EMCG_OK;
 }
 

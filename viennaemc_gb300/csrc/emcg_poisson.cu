@@ -1,16 +1,22 @@
 // Grid Poisson solver of the device engine: double-precision Newton / defect
 // correction around geometric multigrid V-cycles (see emcg_poisson.cuh).
 #include <algorithm>
+#include <array>
 #include <atomic>
+#include <map>
 #include <cmath>
 #include <cstring>
 #include <vector>
+
+#include <cooperative_groups.h>
 
 #include "emcg_common.cuh"
 #include "emcg_host.h"
 #include "emcg_poisson.cuh"
 
 namespace emcg {
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -240,6 +246,671 @@ template <> LevelK<double> levelK<double>(const MGLevel &l) {
   return {l.nx, l.ny, l.dcw, l.dce, l.dcs, l.dcn, l.darea, l.ddiag0, l.fixed, l.dd, l.dr, l.drho};
 }
 
+// ---------------------------------------------------------------------------
+// The whole solve in one launch of one thread-block cluster.
+//
+// Device-engine grids hold at most a few 1e5 nodes and stay on chip, so the
+// multi-launch solve is bound by launch and host-synchronisation latency (one
+// V-cycle is ~90 dependent phases), not by bandwidth.  Here one cluster of up to
+// 16 CTAs runs the Newton / defect-correction loop, every V-cycle and the
+// convergence test, with everything a phase touches in shared memory:
+//  - rows of each level are split over the CTAs in bands, aligned between
+//    levels where the sizes allow (a CTA's coarse rows lie under its fine
+//    rows); the correction d, right-hand side r, reaction rho and residual of
+//    every level live in the owning CTA, neighbours' rows are read through
+//    distributed shared memory; the double potential stays in global memory,
+//    read and written only by the residual and update phases;
+//  - the static coefficients are a per-node class index into a small table of
+//    the level's distinct coefficient tuples; they and the transfer tables are
+//    staged once per launch;
+//  - levels with at most kSmallNodes nodes live whole in CTA 0, which runs the
+//    coarse part of every V-cycle alone with block barriers, the coarsest grid
+//    in the registers of one warp;
+//  - phases over distributed levels are separated by cluster barriers
+//    (release / acquire).
+// Every phase evaluates the expressions of the corresponding multi-launch
+// kernel on the same values, so both paths give the same potential.
+// ---------------------------------------------------------------------------
+constexpr int kClusterThreads = 512;
+constexpr int kMaxCluster = 16;
+constexpr int kSmallNodes = 4096;
+constexpr size_t kClusterSmemMax = 227 * 1024;
+
+// q = t / d for 0 <= t and t * d < 2^32, by one wide multiply (m = ceil(2^32 / d))
+struct FastDiv {
+  unsigned long long m;
+  __host__ void set(unsigned d) { m = ((1ull << 32) + d - 1) / d; }
+  __device__ __forceinline__ int div(int t) const {
+    return (int)(((unsigned long long)(unsigned)t * m) >> 32);
+  }
+};
+
+template <class MT> struct CLevel {
+  int nx, ny, small, rowsPer; // small: all rows in CTA 0; else rowsPer rows per CTA
+  int nCls, ncx, ncy, pad_;   // ncx, ncy: next level's size (0 on the coarsest)
+  FastDiv byNx, byHalf, byRows; // nx, (nx + 1) / 2 and rowsPer
+  // byte offsets in dynamic shared memory: this CTA's rows of d, r, rho, the
+  // residual and the class index, the class table (8 MT per class) and the
+  // transfer tables to the next level (prolongation index / weight per fine x
+  // and y, restriction 3 per coarse index, injection map)
+  unsigned offD, offR, offRho, offRes, offCls, offTab;
+  unsigned offPxI, offPxW, offPyI, offPyW, offRxI, offRxW, offRyI, offRyW, offMapX, offMapY;
+  const uint8_t *cls; // global sources staged at launch
+  const MT *tab;
+  const int *rxIdx, *ryIdx, *pxIdx, *pyIdx, *mapX, *mapY;
+  const float *rxW, *ryW, *pxW, *pyW;
+};
+
+template <class MT> struct CMG {
+  int nLev, pre, post, coarseSweeps, firstSmall;
+  unsigned offRed;
+  CLevel<MT> L[16];
+};
+
+struct CCtx {
+  char *const *base; // generic address of each rank's dynamic shared memory
+  char *smem;        // this CTA's dynamic shared memory
+  int rank;
+};
+
+template <class MT> struct Coef {
+  MT cw, ce, cs, cn, area, diag0, fixed, pad;
+};
+
+template <class MT> __device__ __forceinline__ Coef<MT> loadCoef(const MT *K);
+template <> __device__ __forceinline__ Coef<float> loadCoef<float>(const float *K) {
+  const float4 a = reinterpret_cast<const float4 *>(K)[0];
+  const float4 b = reinterpret_cast<const float4 *>(K)[1];
+  return {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+}
+template <> __device__ __forceinline__ Coef<double> loadCoef<double>(const double *K) {
+  const double2 a = reinterpret_cast<const double2 *>(K)[0];
+  const double2 b = reinterpret_cast<const double2 *>(K)[1];
+  const double2 e = reinterpret_cast<const double2 *>(K)[2];
+  const double2 f = reinterpret_cast<const double2 *>(K)[3];
+  return {a.x, a.y, b.x, b.y, e.x, e.y, f.x, f.y};
+}
+
+// rows [r0, r1) of level L held by this CTA
+template <class MT>
+__device__ __forceinline__ void cOwnRows(const CCtx &c, const CLevel<MT> &L, int &r0, int &r1) {
+  if (L.small) {
+    r0 = 0;
+    r1 = c.rank == 0 ? L.ny : 0;
+  } else {
+    r0 = min(L.ny, c.rank * L.rowsPer);
+    r1 = min(L.ny, r0 + L.rowsPer);
+  }
+}
+
+// row y of an array of level L, wherever it lives
+template <class T, class MT>
+__device__ __forceinline__ T *cRow(const CCtx &c, const CLevel<MT> &L, unsigned off, int y) {
+  if (L.small)
+    return reinterpret_cast<T *>((c.rank == 0 ? c.smem : c.base[0]) + off) + (size_t)y * L.nx;
+  const int owner = L.byRows.div(y);
+  return reinterpret_cast<T *>((owner == c.rank ? c.smem : c.base[owner]) + off) +
+         (size_t)(y - owner * L.rowsPer) * L.nx;
+}
+
+// row r0 + ly of level L, for this CTA's rows and their neighbours
+template <class T, class MT>
+__device__ __forceinline__ T *cRowNear(const CCtx &c, const CLevel<MT> &L, unsigned off, int ly) {
+  if (L.small || (ly >= 0 && ly < L.rowsPer))
+    return reinterpret_cast<T *>(c.smem + off) + (size_t)ly * L.nx;
+  if (ly < 0)
+    return reinterpret_cast<T *>(c.base[c.rank - 1] + off) + (size_t)(L.rowsPer - 1) * L.nx;
+  return reinterpret_cast<T *>(c.base[c.rank + 1] + off);
+}
+
+template <class T> __device__ __forceinline__ const T *cTab(const CCtx &c, unsigned off) {
+  return reinterpret_cast<const T *>(c.smem + off);
+}
+
+template <class MT>
+__device__ __forceinline__ Coef<MT> cCoef(const CCtx &c, const CLevel<MT> &L, uint8_t k) {
+  return loadCoef<MT>(reinterpret_cast<const MT *>(c.smem + L.offTab) + 8 * k);
+}
+
+__device__ __forceinline__ void cSync(bool small) {
+  if (small)
+    __syncthreads();
+  else
+    cg::this_cluster().sync();
+}
+
+template <class MT> __device__ void cSmooth(const CCtx &c, const CLevel<MT> &L, int color) {
+  int r0, r1;
+  cOwnRows(c, L, r0, r1);
+  const int half = (L.nx + 1) / 2, cnt = half * (r1 - r0);
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const int ly = L.byHalf.div(t), y = r0 + ly;
+    const int x = 2 * (t - ly * half) + ((y + color) & 1);
+    if (x >= L.nx)
+      continue;
+    const Coef<MT> K = cCoef(c, L, cRowNear<uint8_t>(c, L, L.offCls, ly)[x]);
+    if (K.fixed != MT(0))
+      continue;
+    MT *d = cRowNear<MT>(c, L, L.offD, ly);
+    MT s = cRowNear<MT>(c, L, L.offR, ly)[x];
+    if (x > 0)
+      s += K.cw * d[x - 1];
+    if (x < L.nx - 1)
+      s += K.ce * d[x + 1];
+    if (y > 0)
+      s += K.cs * cRowNear<MT>(c, L, L.offD, ly - 1)[x];
+    if (y < L.ny - 1)
+      s += K.cn * cRowNear<MT>(c, L, L.offD, ly + 1)[x];
+    d[x] = s / (K.diag0 + K.area * cRowNear<MT>(c, L, L.offRho, ly)[x]);
+  }
+  cSync(L.small);
+}
+
+// residual r - A d of the correction equation at this CTA's nodes of level F
+// (0 at Dirichlet nodes), as restrictKernel evaluates it
+template <class MT> __device__ void cResidual(const CCtx &c, const CLevel<MT> &F) {
+  int r0, r1;
+  cOwnRows(c, F, r0, r1);
+  const int cnt = F.nx * (r1 - r0);
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const int ly = F.byNx.div(t), y = r0 + ly, x = t - ly * F.nx;
+    const Coef<MT> K = cCoef(c, F, cRowNear<uint8_t>(c, F, F.offCls, ly)[x]);
+    MT res = MT(0);
+    if (K.fixed == MT(0)) {
+      const MT *d = cRowNear<MT>(c, F, F.offD, ly);
+      MT a = (K.diag0 + K.area * cRowNear<MT>(c, F, F.offRho, ly)[x]) * d[x];
+      if (x > 0)
+        a -= K.cw * d[x - 1];
+      if (x < F.nx - 1)
+        a -= K.ce * d[x + 1];
+      if (y > 0)
+        a -= K.cs * cRowNear<MT>(c, F, F.offD, ly - 1)[x];
+      if (y < F.ny - 1)
+        a -= K.cn * cRowNear<MT>(c, F, F.offD, ly + 1)[x];
+      res = cRowNear<MT>(c, F, F.offR, ly)[x] - a;
+    }
+    cRowNear<MT>(c, F, F.offRes, ly)[x] = res;
+  }
+  cSync(F.small);
+}
+
+// coarse rows whose injection row mapY[Y] this CTA holds: [Y0, Y1)
+template <class MT>
+__device__ __forceinline__ void cRestrictRows(const CCtx &c, const CLevel<MT> &F,
+                                              const CLevel<MT> &Cc, int &Y0, int &Y1) {
+  int r0, r1;
+  cOwnRows(c, F, r0, r1);
+  if (r0 >= r1) {
+    Y0 = Y1 = 0;
+    return;
+  }
+  if (F.ny <= 3) { // not coarsened along y: identity map
+    Y0 = r0;
+    Y1 = r1;
+    return;
+  }
+  Y0 = (r0 + 1) / 2;
+  Y1 = r1 == F.ny ? Cc.ny : min(Cc.ny, (r1 + 1) / 2);
+}
+
+// coarse right-hand side P^T (fine residual), reaction by injection, d = 0
+template <class MT>
+__device__ void cRestrict(const CCtx &c, const CLevel<MT> &F, const CLevel<MT> &Cc) {
+  int Y0, Y1;
+  cRestrictRows(c, F, Cc, Y0, Y1);
+  const int cnt = Cc.nx * (Y1 - Y0);
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const int q = Cc.byNx.div(t), Y = Y0 + q, X = t - q * Cc.nx;
+    cRow<MT>(c, Cc, Cc.offD, Y)[X] = MT(0);
+    cRow<MT>(c, Cc, Cc.offRho, Y)[X] =
+        cRow<MT>(c, F, F.offRho, cTab<int>(c, F.offMapY)[Y])[cTab<int>(c, F.offMapX)[X]];
+    const Coef<MT> KC = cCoef(c, Cc, cRow<uint8_t>(c, Cc, Cc.offCls, Y)[X]);
+    MT acc = MT(0);
+    if (KC.fixed == MT(0)) {
+      MT wxs[3];
+      int xs[3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        wxs[k] = (MT)cTab<float>(c, F.offRxW)[3 * X + k];
+        xs[k] = cTab<int>(c, F.offRxI)[3 * X + k];
+      }
+#pragma unroll
+      for (int b = 0; b < 3; b++) {
+        const MT wy = (MT)cTab<float>(c, F.offRyW)[3 * Y + b];
+        if (wy == MT(0))
+          continue;
+        const MT *res = cRow<MT>(c, F, F.offRes, cTab<int>(c, F.offRyI)[3 * Y + b]);
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+          if (wxs[a] == MT(0))
+            continue;
+          acc += wxs[a] * wy * res[xs[a]];
+        }
+      }
+    }
+    cRow<MT>(c, Cc, Cc.offR, Y)[X] = acc;
+  }
+  cSync(F.small);
+}
+
+template <class MT>
+__device__ void cProlong(const CCtx &c, const CLevel<MT> &F, const CLevel<MT> &Cc) {
+  int r0, r1;
+  cOwnRows(c, F, r0, r1);
+  const int cnt = F.nx * (r1 - r0);
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const int ly = F.byNx.div(t), y = r0 + ly, x = t - ly * F.nx;
+    if (cCoef(c, F, cRowNear<uint8_t>(c, F, F.offCls, ly)[x]).fixed != MT(0))
+      continue;
+    const int X0 = cTab<int>(c, F.offPxI)[x], Y0 = cTab<int>(c, F.offPyI)[y];
+    const MT wx = (MT)cTab<float>(c, F.offPxW)[x], wy = (MT)cTab<float>(c, F.offPyW)[y];
+    const MT *c0 = cRow<MT>(c, Cc, Cc.offD, Y0);
+    MT v = wx * wy * c0[X0];
+    if (wx < MT(1))
+      v += (MT(1) - wx) * wy * c0[X0 + 1];
+    if (wy < MT(1)) {
+      const MT *c1 = cRow<MT>(c, Cc, Cc.offD, Y0 + 1);
+      v += wx * (MT(1) - wy) * c1[X0];
+      if (wx < MT(1))
+        v += (MT(1) - wx) * (MT(1) - wy) * c1[X0 + 1];
+    }
+    cRowNear<MT>(c, F, F.offD, ly)[x] += v;
+  }
+  cSync(F.small);
+}
+
+// coarsest level (held by CTA 0): red-black sweeps, in the registers of warp 0
+// when it has at most 32 nodes, else by the block with block barriers
+template <class MT> __device__ void cCoarse(const CCtx &c, const CLevel<MT> &L, int sweeps) {
+  const int n = L.nx * L.ny;
+  if (n <= 32) {
+    if (threadIdx.x < 32) {
+      const int i = threadIdx.x, x = i % L.nx, y = i / L.nx;
+      const bool live = i < n;
+      const Coef<MT> K = cCoef(c, L, live ? cRow<uint8_t>(c, L, L.offCls, y)[x] : 0);
+      MT *dp = live ? cRow<MT>(c, L, L.offD, y) + x : nullptr;
+      const MT r = live ? cRow<MT>(c, L, L.offR, y)[x] : MT(0);
+      const MT den = live ? K.diag0 + K.area * cRow<MT>(c, L, L.offRho, y)[x] : MT(1);
+      const bool upd = live && K.fixed == MT(0);
+      MT d = live ? *dp : MT(0);
+      for (int it = 0; it < sweeps; it++) {
+        for (int color = 0; color < 2; color++) {
+          const MT dw = __shfl_sync(0xffffffffu, d, (i + 31) & 31);
+          const MT de = __shfl_sync(0xffffffffu, d, (i + 1) & 31);
+          const MT ds = __shfl_sync(0xffffffffu, d, (i - L.nx + 32) & 31);
+          const MT dn = __shfl_sync(0xffffffffu, d, (i + L.nx) & 31);
+          if (upd && ((x + y) & 1) == color) {
+            MT s = r;
+            if (x > 0)
+              s += K.cw * dw;
+            if (x < L.nx - 1)
+              s += K.ce * de;
+            if (y > 0)
+              s += K.cs * ds;
+            if (y < L.ny - 1)
+              s += K.cn * dn;
+            d = s / den;
+          }
+        }
+      }
+      if (live)
+        *dp = d;
+    }
+    __syncthreads();
+    return;
+  }
+  for (int it = 0; it < sweeps; it++) {
+    for (int color = 0; color < 2; color++) {
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int x = i % L.nx, y = i / L.nx;
+        const Coef<MT> K = cCoef(c, L, cRow<uint8_t>(c, L, L.offCls, y)[x]);
+        if (((x + y) & 1) != color || K.fixed != MT(0))
+          continue;
+        MT *d = cRow<MT>(c, L, L.offD, y);
+        MT s = cRow<MT>(c, L, L.offR, y)[x];
+        if (x > 0)
+          s += K.cw * d[x - 1];
+        if (x < L.nx - 1)
+          s += K.ce * d[x + 1];
+        if (y > 0)
+          s += K.cs * cRow<MT>(c, L, L.offD, y - 1)[x];
+        if (y < L.ny - 1)
+          s += K.cn * cRow<MT>(c, L, L.offD, y + 1)[x];
+        d[x] = s / (K.diag0 + K.area * cRow<MT>(c, L, L.offRho, y)[x]);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// max over the block, then over the cluster (every thread of every CTA gets it);
+// each CTA's two block maxima sit at byte offset offRed of its shared memory
+__device__ __forceinline__ void cClusterMax2(const CCtx &c, unsigned offRed, double &a,
+                                             double &b, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    sh[2 * w] = a;
+    sh[2 * w + 1] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ma = 0., mb = 0.;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+      ma = fmax(ma, sh[2 * k]);
+      mb = fmax(mb, sh[2 * k + 1]);
+    }
+    double *red = reinterpret_cast<double *>(c.smem + offRed);
+    red[0] = ma;
+    red[1] = mb;
+  }
+  cg::this_cluster().sync();
+  const int ranks = (int)cg::this_cluster().num_blocks();
+  a = 0.;
+  b = 0.;
+  for (int r = 0; r < ranks; r++) {
+    const double *o = reinterpret_cast<const double *>(c.base[r] + offRed);
+    a = fmax(a, o[0]);
+    b = fmax(b, o[1]);
+  }
+}
+
+// out[0] = final relative residual, out[1] = V-cycles done
+template <class MT>
+__global__ void __launch_bounds__(kClusterThreads, 1)
+    poissonClusterKernel(CMG<MT> M, double *__restrict__ pot, const double *__restrict__ conc,
+                         const double *__restrict__ C, const double *__restrict__ gSum,
+                         const double *__restrict__ gV, double hF0, double hF1, double hP,
+                         double rtol, int maxCycles, double *__restrict__ out) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ char *sBase[kMaxCluster];
+  __shared__ double sh[2 * (kClusterThreads / 32)];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank(), ranks = (int)cluster.num_blocks();
+  if (threadIdx.x < ranks)
+    sBase[threadIdx.x] = static_cast<char *>(cluster.map_shared_rank((void *)smem, threadIdx.x));
+  // stage the class and transfer tables (every CTA) and this CTA's rows of
+  // class indices
+  for (int l = 0; l < M.nLev; l++) {
+    const CLevel<MT> &L = M.L[l];
+    auto stage = [&](unsigned off, const void *src, int n) {
+      const int *sp = static_cast<const int *>(src);
+      int *dp = reinterpret_cast<int *>(smem + off);
+      for (int k = threadIdx.x; k < n; k += blockDim.x)
+        dp[k] = sp[k];
+    };
+    stage(L.offTab, L.tab, 8 * L.nCls * (int)(sizeof(MT) / 4));
+    int r0, r1;
+    cOwnRows(CCtx{sBase, smem, rank}, L, r0, r1);
+    uint8_t *cl = reinterpret_cast<uint8_t *>(smem + L.offCls);
+    for (int k = threadIdx.x; k < L.nx * (r1 - r0); k += blockDim.x)
+      cl[k] = L.cls[(size_t)r0 * L.nx + k];
+    if (L.ncx > 0) {
+      stage(L.offPxI, L.pxIdx, L.nx);
+      stage(L.offPxW, L.pxW, L.nx);
+      stage(L.offPyI, L.pyIdx, L.ny);
+      stage(L.offPyW, L.pyW, L.ny);
+      stage(L.offRxI, L.rxIdx, 3 * L.ncx);
+      stage(L.offRxW, L.rxW, 3 * L.ncx);
+      stage(L.offRyI, L.ryIdx, 3 * L.ncy);
+      stage(L.offRyW, L.ryW, 3 * L.ncy);
+      stage(L.offMapX, L.mapX, L.ncx);
+      stage(L.offMapY, L.mapY, L.ncy);
+    }
+  }
+  __syncthreads();
+  CCtx c{sBase, smem, rank};
+  const CLevel<MT> &L0 = M.L[0];
+  const int nx = L0.nx, ny = L0.ny;
+  int p0, p1;
+  cOwnRows(c, L0, p0, p1);
+  const int nOwn = nx * (p1 - p0);
+  cluster.sync();
+  double rel = INFINITY;
+  int it = 0;
+  for (;; it++) {
+    // F(phi), Jacobian reaction and FV-scaled right-hand side (nonlinResidualKernel)
+    double aF = 0., sc = 0.;
+    for (int t = threadIdx.x; t < nOwn; t += blockDim.x) {
+      const int ly = L0.byNx.div(t), y = p0 + ly, x = t - ly * nx, i = y * nx + x;
+      MT *d0 = cRowNear<MT>(c, L0, L0.offD, ly), *r0 = cRowNear<MT>(c, L0, L0.offR, ly);
+      MT *rho0 = cRowNear<MT>(c, L0, L0.offRho, ly);
+      d0[x] = MT(0);
+      if (cCoef(c, L0, cRowNear<uint8_t>(c, L0, L0.offCls, ly)[x]).fixed != MT(0)) {
+        r0[x] = MT(0);
+        rho0[x] = MT(0);
+        continue;
+      }
+      const double phi = pot[i];
+      const double p = exp(-phi);
+      const double n = conc ? conc[i] : exp(phi);
+      const double w = x > 0 ? pot[i - 1] : pot[i + 1];
+      const double e = x < nx - 1 ? pot[i + 1] : pot[i - 1];
+      const double s = y > 0 ? pot[i - nx] : pot[i + nx];
+      const double nn = y < ny - 1 ? pot[i + nx] : pot[i - nx];
+      const double F = hF0 * (w + e - 2 * phi) + hF1 * (s + nn - 2 * phi) + hP * (p - n + C[i]) +
+                       (gV[i] - gSum[i] * phi);
+      const int bd = (x == 0 || x == nx - 1) + (y == 0 || y == ny - 1);
+      const double scale = bd == 0 ? 1.0 : (bd == 1 ? 0.5 : 0.25);
+      r0[x] = (MT)(F * scale);
+      rho0[x] = (MT)(conc ? p : p + n);
+      aF = fmax(aF, fabs(F));
+      sc = fmax(sc, hP * (fabs(C[i]) + n + p));
+    }
+    // its cluster barrier also orders the writes above; the maxima are next
+    // written after the V-cycle's barriers, when every CTA has read them
+    cClusterMax2(c, M.offRed, aF, sc, sh);
+    rel = sc > 0 ? aF / sc : aF;
+    if (rel <= rtol || it == maxCycles)
+      break;
+    // one V-cycle: the distributed levels down ...
+    const int Ls = M.firstSmall;
+    for (int l = 0; l < Ls; l++) {
+      for (int s = 0; s < M.pre; s++) {
+        cSmooth(c, M.L[l], 0);
+        cSmooth(c, M.L[l], 1);
+      }
+      cResidual(c, M.L[l]);
+      cRestrict(c, M.L[l], M.L[l + 1]);
+    }
+    // ... the levels held by CTA 0 ...
+    if (rank == 0) {
+      for (int l = Ls; l + 1 < M.nLev; l++) {
+        for (int s = 0; s < M.pre; s++) {
+          cSmooth(c, M.L[l], 0);
+          cSmooth(c, M.L[l], 1);
+        }
+        cResidual(c, M.L[l]);
+        cRestrict(c, M.L[l], M.L[l + 1]);
+      }
+      cCoarse(c, M.L[M.nLev - 1], M.coarseSweeps);
+      for (int l = M.nLev - 2; l >= Ls; l--) {
+        cProlong(c, M.L[l], M.L[l + 1]);
+        for (int s = 0; s < M.post; s++) {
+          cSmooth(c, M.L[l], 1);
+          cSmooth(c, M.L[l], 0);
+        }
+      }
+    }
+    cluster.sync();
+    // ... and the distributed levels up
+    for (int l = Ls - 1; l >= 0; l--) {
+      cProlong(c, M.L[l], M.L[l + 1]);
+      for (int s = 0; s < M.post; s++) {
+        cSmooth(c, M.L[l], 1);
+        cSmooth(c, M.L[l], 0);
+      }
+    }
+    // clamped Newton update of this CTA's rows (updatePotKernel); the cluster
+    // barrier makes the new values visible to the neighbours' next residual
+    for (int t = threadIdx.x; t < nOwn; t += blockDim.x) {
+      const int ly = L0.byNx.div(t), x = t - ly * nx;
+      if (cCoef(c, L0, cRowNear<uint8_t>(c, L0, L0.offCls, ly)[x]).fixed != MT(0))
+        continue;
+      const double v = (double)cRowNear<MT>(c, L0, L0.offD, ly)[x];
+      pot[(size_t)(p0 + ly) * nx + x] += fmin(kMaxNewtonStep, fmax(-kMaxNewtonStep, v));
+    }
+    cluster.sync();
+  }
+  if (rank == 0 && threadIdx.x == 0) {
+    out[0] = rel;
+    out[1] = (double)it;
+  }
+  cluster.sync(); // no CTA leaves while another may still read its shared memory
+}
+
+// Level layout of the cluster solve for CL CTAs; *bytes = dynamic shared memory,
+// 0 if some level has too many coefficient classes.
+template <class MT> CMG<MT> clusterDesc(const PoissonMG &P, int CL, size_t *bytes) {
+  CMG<MT> M;
+  std::memset(&M, 0, sizeof(M));
+  M.nLev = (int)P.L.size();
+  M.pre = P.pre;
+  M.post = P.post;
+  M.coarseSweeps = P.coarseSweeps;
+  M.firstSmall = M.nLev - 1;
+  *bytes = 0;
+  for (int l = 0; l < M.nLev; l++) {
+    if (P.L[l].nCls <= 0)
+      return M;
+    const bool small = CL == 1 || P.L[l].nx * P.L[l].ny <= kSmallNodes || l == M.nLev - 1;
+    if (small && l < M.firstSmall)
+      M.firstSmall = l;
+  }
+  for (int l = 0; l < M.nLev; l++) {
+    CLevel<MT> &c = M.L[l];
+    c.nx = P.L[l].nx;
+    c.ny = P.L[l].ny;
+    c.small = l >= M.firstSmall ? 1 : 0;
+  }
+  // bands: level 0 split evenly (rounded to even rows when a distributed
+  // level follows), each next distributed level on half the rows of the level
+  // above where that covers it, else split evenly
+  const int B = M.firstSmall - 1;
+  for (int l = 0; l <= B; l++) {
+    CLevel<MT> &c = M.L[l];
+    const int even = (c.ny + CL - 1) / CL;
+    int rows = even;
+    if (l > 0 && M.L[l - 1].ny > 3 && M.L[l - 1].rowsPer / 2 * CL >= c.ny)
+      rows = M.L[l - 1].rowsPer / 2;
+    if (l < B && (rows & 1))
+      rows++;
+    c.rowsPer = rows;
+  }
+  size_t off = 0;
+  auto take = [&](size_t b) {
+    const size_t o = off;
+    off += (b + 15) & ~size_t(15);
+    return (unsigned)o;
+  };
+  for (int l = 0; l < M.nLev; l++) {
+    const MGLevel &v = P.L[l];
+    CLevel<MT> &c = M.L[l];
+    if (c.small)
+      c.rowsPer = c.ny;
+    c.byNx.set(c.nx);
+    c.byHalf.set((c.nx + 1) / 2);
+    c.byRows.set(c.rowsPer);
+    const size_t cells = (size_t)c.rowsPer * c.nx;
+    c.offD = take(cells * sizeof(MT));
+    c.offR = take(cells * sizeof(MT));
+    c.offRho = take(cells * sizeof(MT));
+    c.offRes = l + 1 < M.nLev ? take(cells * sizeof(MT)) : 0;
+    c.offCls = take(cells);
+    c.nCls = v.nCls;
+    c.offTab = take((size_t)8 * v.nCls * sizeof(MT));
+    c.cls = v.cls;
+    c.tab = static_cast<const MT *>(v.clsTab);
+    if (l + 1 < M.nLev) {
+      c.ncx = P.L[l + 1].nx;
+      c.ncy = P.L[l + 1].ny;
+      c.offPxI = take(4 * (size_t)c.nx);
+      c.offPxW = take(4 * (size_t)c.nx);
+      c.offPyI = take(4 * (size_t)c.ny);
+      c.offPyW = take(4 * (size_t)c.ny);
+      c.offRxI = take(12 * (size_t)c.ncx);
+      c.offRxW = take(12 * (size_t)c.ncx);
+      c.offRyI = take(12 * (size_t)c.ncy);
+      c.offRyW = take(12 * (size_t)c.ncy);
+      c.offMapX = take(4 * (size_t)c.ncx);
+      c.offMapY = take(4 * (size_t)c.ncy);
+    }
+    c.rxIdx = v.rxIdx;
+    c.ryIdx = v.ryIdx;
+    c.pxIdx = v.pxIdx;
+    c.pyIdx = v.pyIdx;
+    c.mapX = v.mapX;
+    c.mapY = v.mapY;
+    c.rxW = v.rxW;
+    c.ryW = v.ryW;
+    c.pxW = v.pxW;
+    c.pyW = v.pyW;
+  }
+  M.offRed = take(2 * sizeof(double));
+  *bytes = off;
+  return M;
+}
+
+template <class MT> cudaLaunchConfig_t clusterConfig(int CL, size_t bytes, cudaStream_t st,
+                                                     cudaLaunchAttribute *at) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CL, 1, 1);
+  cfg.blockDim = dim3(kClusterThreads, 1, 1);
+  cfg.dynamicSmemBytes = bytes;
+  cfg.stream = st;
+  at->id = cudaLaunchAttributeClusterDimension;
+  at->val.clusterDim.x = CL;
+  at->val.clusterDim.y = 1;
+  at->val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
+// Largest cluster (16, 8, 4, 2 or 1 CTAs) whose layout fits in shared memory
+// and that the device can place; none: the multi-launch path serves the grid.
+template <class MT> void clusterPlan(PoissonMG &P) {
+  P.clusterSize = 0;
+  P.clusterSmem = 0;
+  const int n = P.S.nx * P.S.ny;
+  const int cands[] = {16, 8, 4, 2, 1};
+  for (int CL : cands) {
+    if (CL > 1 && n <= kSmallNodes)
+      continue;
+    size_t bytes = 0;
+    clusterDesc<MT>(P, CL, &bytes);
+    if (bytes == 0 || bytes + 1024 > kClusterSmemMax)
+      continue;
+    auto k = poissonClusterKernel<MT>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (CL > 8 &&
+        cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    cudaLaunchAttribute at;
+    cudaLaunchConfig_t cfg = clusterConfig<MT>(CL, bytes, nullptr, &at);
+    int nc = 0;
+    if (cudaOccupancyMaxActiveClusters(&nc, k, &cfg) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (nc < 1)
+      continue;
+    P.clusterSize = CL;
+    P.clusterSmem = bytes;
+    return;
+  }
+}
+
 template <class MT> void vcycle(PoissonMG &P, int l, cudaStream_t st) {
   MGLevel &lv = P.L[l];
   LevelK<MT> K = levelK<MT>(lv);
@@ -324,6 +995,45 @@ template <class V> int32_t upload(V **dst, const std::vector<V> &src, cudaStream
   return EMCG_OK;
 }
 
+// Distinct coefficient tuples of a level (a uniform grid has a handful:
+// interior, edges, corners, contacts, gates) and each node's class.
+template <class MT>
+int32_t coefficientClasses(MGLevel &L, const std::vector<double> &cw,
+                           const std::vector<double> &ce, const std::vector<double> &cs,
+                           const std::vector<double> &cn, const std::vector<double> &ar,
+                           const std::vector<double> &dg, const std::vector<uint8_t> &fixed,
+                           cudaStream_t st) {
+  const size_t m = cw.size();
+  std::vector<uint8_t> cls(m);
+  std::vector<MT> tab;
+  std::map<std::array<MT, 7>, int> ids;
+  for (size_t k = 0; k < m && L.nCls >= 0; k++) {
+    std::array<MT, 7> t = {(MT)cw[k], (MT)ce[k], (MT)cs[k], (MT)cn[k],
+                           (MT)ar[k], (MT)dg[k], (MT)(fixed[k] ? 1 : 0)};
+    auto it = ids.find(t);
+    if (it == ids.end()) {
+      if (ids.size() == 255) {
+        L.nCls = -1;
+        break;
+      }
+      it = ids.emplace(t, (int)ids.size()).first;
+      tab.insert(tab.end(), t.begin(), t.end());
+      tab.push_back(MT(0));
+    }
+    cls[k] = (uint8_t)it->second;
+  }
+  if (L.nCls < 0) {
+    L.nCls = 0;
+    return EMCG_OK;
+  }
+  L.nCls = (int)ids.size();
+  EMCG_TRY(upload(&L.cls, cls, st));
+  MT *t = nullptr;
+  EMCG_TRY(upload(&t, tab, st));
+  L.clsTab = t;
+  return EMCG_OK;
+}
+
 } // namespace
 
 int32_t poissonCreate(PoissonMG &P, const PoissonSetup &S, bool fp32, int smooth,
@@ -398,6 +1108,8 @@ int32_t poissonCreate(PoissonMG &P, const PoissonSetup &S, bool fp32, int smooth
       EMCG_CUDA(cudaMalloc(&L.drho, sizeof(double) * m));
     }
     EMCG_TRY(upload(&L.fixed, fixed, st));
+    EMCG_TRY(fp32 ? coefficientClasses<float>(L, cw, ce, cs, cn, ar, dg, fixed, st)
+                  : coefficientClasses<double>(L, cw, ce, cs, cn, ar, dg, fixed, st));
     std::vector<int> mx, my;
     coarsen1d(lx, mx);
     coarsen1d(ly, my);
@@ -446,6 +1158,10 @@ int32_t poissonCreate(PoissonMG &P, const PoissonSetup &S, bool fp32, int smooth
     ly = ncy;
   }
   EMCG_CUDA(cudaStreamSynchronize(st));
+  if (fp32)
+    clusterPlan<float>(P);
+  else
+    clusterPlan<double>(P);
   return EMCG_OK;
 }
 
@@ -454,7 +1170,7 @@ void poissonFree(PoissonMG &P) {
     void *ps[] = {L.cw,  L.ce,    L.cs,    L.cn,    L.area,  L.diag0, L.dcw,   L.dce,
                   L.dcs, L.dcn,   L.darea, L.ddiag0, L.fixed, L.d,     L.r,     L.rho,
                   L.dd,  L.dr,    L.drho,  L.rxIdx, L.ryIdx, L.rxW,   L.ryW,   L.pxIdx,
-                  L.pyIdx, L.pxW, L.pyW,   L.mapX,  L.mapY};
+                  L.pyIdx, L.pxW, L.pyW,   L.mapX,  L.mapY, L.cls, L.clsTab};
     for (void *p : ps)
       cudaFree(p);
   }
@@ -478,7 +1194,21 @@ static int32_t solveT(PoissonMG &P, double *pot, const double *conc, bool resetB
   double stats[3] = {0, 0, 0};
   double rel = INFINITY;
   int it = 0;
-  for (; it <= maxCycles; it++) {
+  const bool cluster = P.useCluster && P.clusterSize > 0;
+  if (cluster) {
+    size_t bytes = 0;
+    const CMG<MT> M = clusterDesc<MT>(P, P.clusterSize, &bytes);
+    cudaLaunchAttribute at;
+    cudaLaunchConfig_t cfg = clusterConfig<MT>(P.clusterSize, bytes, st, &at);
+    EMCG_CUDA(cudaLaunchKernelEx(&cfg, poissonClusterKernel<MT>, M, pot, conc, P.C, P.gSum,
+                                 conc ? P.gVne : P.gVeq, P.hF[0], P.hF[1], P.hP, rtol, maxCycles,
+                                 P.stats));
+    EMCG_CUDA(cudaMemcpyAsync(stats, P.stats, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    EMCG_CUDA(cudaStreamSynchronize(st));
+    rel = stats[0];
+    it = (int)stats[1];
+  }
+  for (; !cluster && it <= maxCycles; it++) {
     EMCG_CUDA(cudaMemsetAsync(P.stats, 0, 3 * sizeof(double), st));
     nonlinResidualKernel<MT><<<grid, kBlock, 0, st>>>(
         pot, conc, P.C, L0.fixed, P.gSum, conc ? P.gVne : P.gVeq, nx, ny, P.hF[0], P.hF[1], P.hP,

@@ -50,6 +50,12 @@ struct MGLevel {
   int *pxIdx, *pyIdx;      // prolongation: lower coarse index per fine index
   float *pxW, *pyW;        // weight of the lower coarse node
   int *mapX, *mapY;        // coarse index -> fine index (injection)
+  // coefficient classes of the cluster solve: per node an index into a table
+  // of the distinct (cw, ce, cs, cn, area, diag0, fixed) tuples of the level,
+  // 8 entries of the multigrid type per class; nCls = 0: more than 255 classes
+  uint8_t *cls;
+  void *clsTab;
+  int nCls;
 };
 
 struct PoissonMG {
@@ -63,6 +69,12 @@ struct PoissonMG {
   int pre = 2, post = 2, coarseSweeps = 40;
   bool fp32 = true;
   double hF[2], hP;
+  // single-launch cluster solve: CTAs per cluster (0 = not available for this
+  // grid) and its dynamic shared memory; useCluster = 0 forces the
+  // multi-launch path
+  int clusterSize = 0;
+  size_t clusterSmem = 0;
+  bool useCluster = true;
 };
 
 int32_t poissonCreate(PoissonMG &P, const PoissonSetup &S, bool fp32, int smooth,

@@ -306,6 +306,19 @@ class DeviceSimulation:
         L.check(self._lib.emcg_device_timing(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def poisson_mode(self, mode=-1):
+        """Select (1 cluster, 0 multi-launch) or query (-1) the Poisson execution;
+        returns the CTAs per cluster in use (0: multi-launch)."""
+        cs = C.c_int32()
+        L.check(self._lib.emcg_device_poisson_mode(self.h, int(mode), C.byref(cs)))
+        return cs.value
+
+    def poisson_counts(self):
+        """(V-cycles, solves) of the last performEMCStep call."""
+        a, b = C.c_int64(), C.c_int64()
+        L.check(self._lib.emcg_device_poisson_counts(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def current(self, transient_steps=0):
         """Average current per contact [A]: netto particles per step times
         carriers * charge / dt (emcSimulationResults::updateCurrent, :125-150)."""
