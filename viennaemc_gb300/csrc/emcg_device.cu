@@ -335,44 +335,66 @@ __global__ void reservoirListKernel(StateK<T> st, DevK G, const int64_t *__restr
     listCount[blockIdx.x] = tot;
 }
 
-// rank the reservoir particles per node in index order; mark the excess
-// (rank * carriers >= expected) for removal
-__global__ void contactRankKernel(const int32_t *__restrict__ list,
-                                  const int32_t *__restrict__ listNode,
-                                  const int32_t *__restrict__ listCount, int nb,
+// the per-block reservoir lists, concatenated in block order: all reservoir
+// particles in index order (off = exclusive scan of the block counts)
+__global__ void gatherListKernel(const int32_t *__restrict__ list,
+                                 const int32_t *__restrict__ listNode,
+                                 const int32_t *__restrict__ off, int nb,
+                                 const int64_t *__restrict__ total, int32_t *__restrict__ gList,
+                                 int32_t *__restrict__ gNode) {
+  const int b = blockIdx.x;
+  const int o = off[b];
+  const int cnt = (b + 1 < nb ? off[b + 1] : (int)*total) - o;
+  for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+    gList[o + j] = list[(int64_t)b * kCB + j];
+    gNode[o + j] = listNode[(int64_t)b * kCB + j];
+  }
+}
+
+// One warp per reservoir node walks the reservoir particles in index order:
+// the r-th particle at the node (r from 0) stays while r * carriers is below
+// the expected number there, the rest are marked for removal
+// (emcBasicParticleHandler::handleOhmicContacts, :158-192).
+__global__ void contactRankKernel(const int32_t *__restrict__ gList,
+                                  const int32_t *__restrict__ gNode,
+                                  const int64_t *__restrict__ total,
+                                  const int32_t *__restrict__ resNodes, int nRes,
                                   const double *__restrict__ expNr, double nrC,
                                   const int32_t *__restrict__ nodeContact,
-                                  int32_t *__restrict__ seen, uint8_t *__restrict__ drop,
-                                  int32_t *__restrict__ kept, int32_t *__restrict__ remInj) {
-  __shared__ int nodes[kCB];
-  for (int b = 0; b < nb; b++) {
-    const int cnt = listCount[b];
-    for (int base = 0; base < cnt; base += blockDim.x) {
-      int j = base + threadIdx.x;
-      int node = -1, idx = -1;
-      if (j < cnt) {
-        node = listNode[(int64_t)b * kCB + j];
-        idx = list[(int64_t)b * kCB + j];
+                                  uint8_t *__restrict__ drop, int32_t *__restrict__ kept,
+                                  int32_t *__restrict__ remInj) {
+  const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= nRes)
+    return;
+  const int g = resNodes[w];
+  const double e = expNr[g];
+  const int R = (int)*total;
+  int seen = 0, nKept = 0, nDrop = 0;
+  for (int base = 0; base < R; base += 32) {
+    const int j = base + lane;
+    const bool mine = j < R && gNode[j] == g;
+    const unsigned m = __ballot_sync(0xffffffffu, mine);
+    if (mine) {
+      const int r = seen + __popc(m & ((1u << lane) - 1u));
+      if ((double)r * nrC < e)
+        nKept++;
+      else {
+        drop[gList[j]] = 1;
+        nDrop++;
       }
-      nodes[threadIdx.x] = node;
-      __syncthreads();
-      if (node >= 0) {
-        int rank = 0;
-        for (int q = 0; q < (int)threadIdx.x; q++)
-          rank += nodes[q] == node;
-        int r = seen[node] + rank;
-        if ((double)r * nrC < expNr[node]) {
-          atomicAdd(&kept[node], 1);
-        } else {
-          drop[idx] = 1;
-          atomicAdd(&remInj[nodeContact[node]], -1);
-        }
-      }
-      __syncthreads();
-      if (node >= 0)
-        atomicAdd(&seen[node], 1);
-      __syncthreads();
     }
+    seen += __popc(m);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    nKept += __shfl_xor_sync(0xffffffffu, nKept, o);
+    nDrop += __shfl_xor_sync(0xffffffffu, nDrop, o);
+  }
+  if (lane == 0) {
+    kept[g] = nKept;
+    if (nDrop)
+      atomicAdd(&remInj[nodeContact[g]], -nDrop);
   }
 }
 
@@ -614,11 +636,13 @@ struct DeviceImpl {
   uint32_t *dMeta[2] = {};
   int cur = 0;
   int64_t capacity = 0;
-  int64_t *dN = nullptr;      // [0] particle count, [1] scratch count, [2] injection total
+  int64_t *dN = nullptr; // [0] particle count, [1] scratch count, [2] injection total,
+                         // [3] reservoir particles
   uint8_t *dDrop = nullptr;
   int32_t *dBlock = nullptr;  // per compaction block counts / offsets
   int32_t *dList = nullptr, *dListNode = nullptr, *dListCount = nullptr;
-  int32_t *dSeen = nullptr, *dKept = nullptr;
+  int32_t *dKept = nullptr;
+  int32_t *dGList = nullptr, *dGNode = nullptr; // reservoir particles in index order
   int32_t *dResNodes = nullptr, *dInjCount = nullptr;
   int32_t *dNetto = nullptr, *dRemInj = nullptr;
   int *dErr = nullptr;
@@ -695,7 +719,7 @@ int32_t destroyDevice(emcg_handle *h) {
   poissonFree(d->mg);
   void *ps[] = {d->dModel, d->dTables, d->dRegion, d->dNodeContact, d->dNodeRes, d->dNodeOhmic,
                 d->dPot, d->dNr, d->dConc, d->dExp, d->dEx, d->dEy, d->dN, d->dDrop, d->dBlock,
-                d->dList, d->dListNode, d->dListCount, d->dSeen, d->dKept, d->dResNodes,
+                d->dList, d->dListNode, d->dListCount, d->dGList, d->dGNode, d->dKept, d->dResNodes,
                 d->dInjCount, d->dNetto, d->dRemInj, d->dErr};
   for (void *p : ps)
     cudaFree(p);
@@ -901,7 +925,8 @@ extern "C" int32_t emcg_device_create(const emcg_model_desc *model, const emcg_d
        cudaMalloc(&d->dList, cap * sizeof(int32_t)) == cudaSuccess &&
        cudaMalloc(&d->dListNode, cap * sizeof(int32_t)) == cudaSuccess &&
        cudaMalloc(&d->dListCount, (nb + 1) * sizeof(int32_t)) == cudaSuccess &&
-       cudaMalloc(&d->dSeen, n * sizeof(int32_t)) == cudaSuccess &&
+       cudaMalloc(&d->dGList, cap * sizeof(int32_t)) == cudaSuccess &&
+       cudaMalloc(&d->dGNode, cap * sizeof(int32_t)) == cudaSuccess &&
        cudaMalloc(&d->dKept, n * sizeof(int32_t)) == cudaSuccess &&
        cudaMalloc(&d->dInjCount, (d->resNodesH.size() + 1) * sizeof(int32_t)) == cudaSuccess &&
        cudaMalloc(&d->dNetto, (d->nContacts + 1) * sizeof(int32_t)) == cudaSuccess &&
@@ -1059,17 +1084,20 @@ template <class T> static int32_t contactsT(DeviceImpl *d, uint32_t step) {
   const int n = d->nx * d->ny;
   cudaStream_t st = d->stream;
   DevK G = devK(d);
+  const int nRes = (int)d->resNodesH.size();
   EMCG_CUDA(cudaMemsetAsync(d->dDrop, 0, d->capacity, st));
-  EMCG_CUDA(cudaMemsetAsync(d->dSeen, 0, n * sizeof(int32_t), st));
   EMCG_CUDA(cudaMemsetAsync(d->dKept, 0, n * sizeof(int32_t), st));
   reservoirListKernel<T><<<nb, kCB, 0, st>>>(devState<T>(d, d->cur), G, d->dN, d->dList,
                                              d->dListNode, d->dListCount);
-  contactRankKernel<<<1, kCB, 0, st>>>(d->dList, d->dListNode, d->dListCount, nb, d->dExp,
-                                       d->cfg.carriers_per_particle, d->dNodeContact, d->dSeen,
-                                       d->dDrop, d->dKept, d->dRemInj);
+  scanBlocksKernel<<<1, 1024, 0, st>>>(d->dListCount, nb, d->dN + 3);
+  gatherListKernel<<<nb, 256, 0, st>>>(d->dList, d->dListNode, d->dListCount, nb, d->dN + 3,
+                                       d->dGList, d->dGNode);
+  if (nRes > 0)
+    contactRankKernel<<<(nRes * 32 + 255) / 256, 256, 0, st>>>(
+        d->dGList, d->dGNode, d->dN + 3, d->dResNodes, nRes, d->dExp,
+        d->cfg.carriers_per_particle, d->dNodeContact, d->dDrop, d->dKept, d->dRemInj);
   EMCG_CUDA(cudaGetLastError());
   EMCG_TRY(compact(d));
-  const int nRes = (int)d->resNodesH.size();
   if (nRes == 0)
     return EMCG_OK;
   injectCountKernel<<<(nRes + 255) / 256, 256, 0, st>>>(d->dResNodes, nRes, d->dExp, d->dKept,

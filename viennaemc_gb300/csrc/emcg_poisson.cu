@@ -46,6 +46,12 @@ __device__ __forceinline__ double blockMax(double v) {
   return v; // valid in thread 0
 }
 
+// Gauss-Seidel update s / (diagonal): the float smoother divides with the
+// fast approximate division (its error is far below the float multigrid's own
+// 1e-7), the double one exactly
+__device__ __forceinline__ float mgDiv(float s, float den) { return __fdividef(s, den); }
+__device__ __forceinline__ double mgDiv(double s, double den) { return s / den; }
+
 __global__ void resetBCKernel(double *pot, const uint8_t *mask, const double *val, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n && mask[i])
@@ -60,7 +66,7 @@ __global__ void nonlinResidualKernel(const double *__restrict__ pot, const doubl
                                      const double *__restrict__ gSum, const double *__restrict__ gV,
                                      int nx, int ny, double hF0, double hF1, double hP,
                                      MT *__restrict__ rhs, MT *__restrict__ rho, MT *__restrict__ d,
-                                     double *__restrict__ stats) {
+                                     double *__restrict__ stats, int withScale) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   double aF = 0., sc = 0.;
   if (i < nx * ny) {
@@ -84,15 +90,17 @@ __global__ void nonlinResidualKernel(const double *__restrict__ pot, const doubl
       rhs[i] = (MT)(F * scale);
       rho[i] = (MT)(conc ? p : p + n);
       aF = fabs(F);
-      sc = hP * (fabs(C[i]) + n + p);
+      if (withScale)
+        sc = hP * (fabs(C[i]) + n + p);
     }
   }
   double m1 = blockMax(aF);
   __syncthreads();
-  double m2 = blockMax(sc);
+  double m2 = withScale ? blockMax(sc) : 0.;
   if (threadIdx.x == 0) {
     atomicMaxPos(&stats[0], m1);
-    atomicMaxPos(&stats[1], m2);
+    if (withScale)
+      atomicMaxPos(&stats[1], m2);
   }
 }
 
@@ -155,7 +163,7 @@ template <class MT> __global__ void smoothKernel(LevelK<MT> L, int color) {
     s += L.cs[i] * L.d[i - L.nx];
   if (y < L.ny - 1)
     s += L.cn[i] * L.d[i + L.nx];
-  L.d[i] = s / (L.diag0[i] + L.area[i] * L.rho[i]);
+  L.d[i] = mgDiv(s, L.diag0[i] + L.area[i] * L.rho[i]);
 }
 
 // coarse rhs = P^T (fine residual); coarse reaction by injection; coarse d = 0
@@ -231,7 +239,7 @@ template <class MT> __global__ void coarseSolveKernel(LevelK<MT> L, int sweeps) 
           s += L.cs[i] * L.d[i - L.nx];
         if (y < L.ny - 1)
           s += L.cn[i] * L.d[i + L.nx];
-        L.d[i] = s / (L.diag0[i] + L.area[i] * L.rho[i]);
+        L.d[i] = mgDiv(s, L.diag0[i] + L.area[i] * L.rho[i]);
       }
       __syncthreads();
     }
@@ -302,7 +310,8 @@ template <class MT> struct CLevel {
 };
 
 template <class MT> struct CMG {
-  int nLev, pre, post, coarseSweeps, firstSmall;
+  int nLev, pre, post, coarseSweeps, firstSmall, vcycles;
+  double twoCycleRel;
   unsigned offRed;
   CLevel<MT> L[16];
 };
@@ -372,8 +381,10 @@ __device__ __forceinline__ Coef<MT> cCoef(const CCtx &c, const CLevel<MT> &L, ui
   return loadCoef<MT>(reinterpret_cast<const MT *>(c.smem + L.offTab) + 8 * k);
 }
 
-__device__ __forceinline__ void cSync(bool small) {
-  if (small)
+// end of a phase over level L: cluster barrier for a distributed level, block
+// barrier for one held by CTA 0
+template <class MT> __device__ __forceinline__ void cSync(const CLevel<MT> &L) {
+  if (L.small)
     __syncthreads();
   else
     cg::this_cluster().sync();
@@ -401,9 +412,9 @@ template <class MT> __device__ void cSmooth(const CCtx &c, const CLevel<MT> &L, 
       s += K.cs * cRowNear<MT>(c, L, L.offD, ly - 1)[x];
     if (y < L.ny - 1)
       s += K.cn * cRowNear<MT>(c, L, L.offD, ly + 1)[x];
-    d[x] = s / (K.diag0 + K.area * cRowNear<MT>(c, L, L.offRho, ly)[x]);
+    d[x] = mgDiv(s, K.diag0 + K.area * cRowNear<MT>(c, L, L.offRho, ly)[x]);
   }
-  cSync(L.small);
+  cSync(L);
 }
 
 // residual r - A d of the correction equation at this CTA's nodes of level F
@@ -431,7 +442,7 @@ template <class MT> __device__ void cResidual(const CCtx &c, const CLevel<MT> &F
     }
     cRowNear<MT>(c, F, F.offRes, ly)[x] = res;
   }
-  cSync(F.small);
+  cSync(F);
 }
 
 // coarse rows whose injection row mapY[Y] this CTA holds: [Y0, Y1)
@@ -490,7 +501,7 @@ __device__ void cRestrict(const CCtx &c, const CLevel<MT> &F, const CLevel<MT> &
     }
     cRow<MT>(c, Cc, Cc.offR, Y)[X] = acc;
   }
-  cSync(F.small);
+  cSync(F);
 }
 
 template <class MT>
@@ -516,7 +527,7 @@ __device__ void cProlong(const CCtx &c, const CLevel<MT> &F, const CLevel<MT> &C
     }
     cRowNear<MT>(c, F, F.offD, ly)[x] += v;
   }
-  cSync(F.small);
+  cSync(F);
 }
 
 // coarsest level (held by CTA 0): red-black sweeps, in the registers of warp 0
@@ -549,7 +560,7 @@ template <class MT> __device__ void cCoarse(const CCtx &c, const CLevel<MT> &L, 
               s += K.cs * ds;
             if (y < L.ny - 1)
               s += K.cn * dn;
-            d = s / den;
+            d = mgDiv(s, den);
           }
         }
       }
@@ -576,7 +587,7 @@ template <class MT> __device__ void cCoarse(const CCtx &c, const CLevel<MT> &L, 
           s += K.cs * cRow<MT>(c, L, L.offD, y - 1)[x];
         if (y < L.ny - 1)
           s += K.cn * cRow<MT>(c, L, L.offD, y + 1)[x];
-        d[x] = s / (K.diag0 + K.area * cRow<MT>(c, L, L.offRho, y)[x]);
+        d[x] = mgDiv(s, K.diag0 + K.area * cRow<MT>(c, L, L.offRho, y)[x]);
       }
       __syncthreads();
     }
@@ -622,13 +633,20 @@ __device__ __forceinline__ void cClusterMax2(const CCtx &c, unsigned offRed, dou
 // out[0] = final relative residual, out[1] = V-cycles done
 template <class MT>
 __global__ void __launch_bounds__(kClusterThreads, 1)
-    poissonClusterKernel(CMG<MT> M, double *__restrict__ pot, const double *__restrict__ conc,
+    poissonClusterKernel(CMG<MT> Mp, double *__restrict__ pot, const double *__restrict__ conc,
                          const double *__restrict__ C, const double *__restrict__ gSum,
                          const double *__restrict__ gV, double hF0, double hF1, double hP,
                          double rtol, int maxCycles, double *__restrict__ out) {
   extern __shared__ __align__(16) char smem[];
   __shared__ char *sBase[kMaxCluster];
   __shared__ double sh[2 * (kClusterThreads / 32)];
+  // the level descriptors, read by every phase, from shared memory rather than
+  // the parameter bank
+  __shared__ __align__(16) int sM[sizeof(CMG<MT>) / sizeof(int)];
+  for (int k = threadIdx.x; k < (int)(sizeof(CMG<MT>) / sizeof(int)); k += blockDim.x)
+    sM[k] = reinterpret_cast<const int *>(&Mp)[k];
+  __syncthreads();
+  const CMG<MT> &M = *reinterpret_cast<const CMG<MT> *>(sM);
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank(), ranks = (int)cluster.num_blocks();
   if (threadIdx.x < ranks)
@@ -670,10 +688,11 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
   cOwnRows(c, L0, p0, p1);
   const int nOwn = nx * (p1 - p0);
   cluster.sync();
-  double rel = INFINITY;
+  double rel = INFINITY, scale = 0.;
   int it = 0;
   for (;; it++) {
-    // F(phi), Jacobian reaction and FV-scaled right-hand side (nonlinResidualKernel)
+    // F(phi), Jacobian reaction and FV-scaled right-hand side (nonlinResidualKernel);
+    // the scale of the relative residual from the first iteration's state
     double aF = 0., sc = 0.;
     for (int t = threadIdx.x; t < nOwn; t += blockDim.x) {
       const int ly = L0.byNx.div(t), y = p0 + ly, x = t - ly * nx, i = y * nx + x;
@@ -699,27 +718,22 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
       r0[x] = (MT)(F * scale);
       rho0[x] = (MT)(conc ? p : p + n);
       aF = fmax(aF, fabs(F));
-      sc = fmax(sc, hP * (fabs(C[i]) + n + p));
+      if (it == 0)
+        sc = fmax(sc, hP * (fabs(C[i]) + n + p));
     }
     // its cluster barrier also orders the writes above; the maxima are next
     // written after the V-cycle's barriers, when every CTA has read them
     cClusterMax2(c, M.offRed, aF, sc, sh);
-    rel = sc > 0 ? aF / sc : aF;
+    if (it == 0)
+      scale = sc;
+    rel = scale > 0 ? aF / scale : aF;
     if (rel <= rtol || it == maxCycles)
       break;
-    // one V-cycle: the distributed levels down ...
-    const int Ls = M.firstSmall;
-    for (int l = 0; l < Ls; l++) {
-      for (int s = 0; s < M.pre; s++) {
-        cSmooth(c, M.L[l], 0);
-        cSmooth(c, M.L[l], 1);
-      }
-      cResidual(c, M.L[l]);
-      cRestrict(c, M.L[l], M.L[l + 1]);
-    }
-    // ... the levels held by CTA 0 ...
-    if (rank == 0) {
-      for (int l = Ls; l + 1 < M.nLev; l++) {
+    const int nv = rel < M.twoCycleRel ? M.vcycles : 1;
+    for (int vc = 0; vc < nv; vc++) {
+      // one V-cycle: the distributed levels down ...
+      const int Ls = M.firstSmall;
+      for (int l = 0; l < Ls; l++) {
         for (int s = 0; s < M.pre; s++) {
           cSmooth(c, M.L[l], 0);
           cSmooth(c, M.L[l], 1);
@@ -727,22 +741,33 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
         cResidual(c, M.L[l]);
         cRestrict(c, M.L[l], M.L[l + 1]);
       }
-      cCoarse(c, M.L[M.nLev - 1], M.coarseSweeps);
-      for (int l = M.nLev - 2; l >= Ls; l--) {
+      // ... the levels held by CTA 0 ...
+      if (rank == 0) {
+        for (int l = Ls; l + 1 < M.nLev; l++) {
+          for (int s = 0; s < M.pre; s++) {
+            cSmooth(c, M.L[l], 0);
+            cSmooth(c, M.L[l], 1);
+          }
+          cResidual(c, M.L[l]);
+          cRestrict(c, M.L[l], M.L[l + 1]);
+        }
+        cCoarse(c, M.L[M.nLev - 1], M.coarseSweeps);
+        for (int l = M.nLev - 2; l >= Ls; l--) {
+          cProlong(c, M.L[l], M.L[l + 1]);
+          for (int s = 0; s < M.post; s++) {
+            cSmooth(c, M.L[l], 1);
+            cSmooth(c, M.L[l], 0);
+          }
+        }
+      }
+      cluster.sync();
+      // ... and the distributed levels up
+      for (int l = Ls - 1; l >= 0; l--) {
         cProlong(c, M.L[l], M.L[l + 1]);
         for (int s = 0; s < M.post; s++) {
           cSmooth(c, M.L[l], 1);
           cSmooth(c, M.L[l], 0);
         }
-      }
-    }
-    cluster.sync();
-    // ... and the distributed levels up
-    for (int l = Ls - 1; l >= 0; l--) {
-      cProlong(c, M.L[l], M.L[l + 1]);
-      for (int s = 0; s < M.post; s++) {
-        cSmooth(c, M.L[l], 1);
-        cSmooth(c, M.L[l], 0);
       }
     }
     // clamped Newton update of this CTA's rows (updatePotKernel); the cluster
@@ -772,6 +797,8 @@ template <class MT> CMG<MT> clusterDesc(const PoissonMG &P, int CL, size_t *byte
   M.pre = P.pre;
   M.post = P.post;
   M.coarseSweeps = P.coarseSweeps;
+  M.vcycles = P.vcyclesPerNewton;
+  M.twoCycleRel = P.twoCycleRel;
   M.firstSmall = M.nLev - 1;
   *bytes = 0;
   for (int l = 0; l < M.nLev; l++) {
@@ -883,7 +910,7 @@ template <class MT> void clusterPlan(PoissonMG &P) {
       continue;
     size_t bytes = 0;
     clusterDesc<MT>(P, CL, &bytes);
-    if (bytes == 0 || bytes + 1024 > kClusterSmemMax)
+    if (bytes == 0 || bytes + sizeof(CMG<MT>) + 1024 > kClusterSmemMax)
       continue;
     auto k = poissonClusterKernel<MT>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
@@ -1208,18 +1235,23 @@ static int32_t solveT(PoissonMG &P, double *pot, const double *conc, bool resetB
     rel = stats[0];
     it = (int)stats[1];
   }
+  double scale = 0.;
   for (; !cluster && it <= maxCycles; it++) {
     EMCG_CUDA(cudaMemsetAsync(P.stats, 0, 3 * sizeof(double), st));
     nonlinResidualKernel<MT><<<grid, kBlock, 0, st>>>(
         pot, conc, P.C, L0.fixed, P.gSum, conc ? P.gVne : P.gVeq, nx, ny, P.hF[0], P.hF[1], P.hP,
-        K0.r, K0.rho, K0.d, P.stats);
+        K0.r, K0.rho, K0.d, P.stats, it == 0);
     EMCG_CUDA(cudaGetLastError());
     EMCG_CUDA(cudaMemcpyAsync(stats, P.stats, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
     EMCG_CUDA(cudaStreamSynchronize(st));
-    rel = stats[1] > 0 ? stats[0] / stats[1] : stats[0];
+    if (it == 0)
+      scale = stats[1];
+    rel = scale > 0 ? stats[0] / scale : stats[0];
     if (rel <= rtol || it == maxCycles)
       break;
-    vcycle<MT>(P, 0, st);
+    const int nv = rel < P.twoCycleRel ? P.vcyclesPerNewton : 1;
+    for (int k = 0; k < nv; k++)
+      vcycle<MT>(P, 0, st);
     updatePotKernel<MT><<<grid, kBlock, 0, st>>>(pot, K0.d, L0.fixed, n, P.stats);
     EMCG_CUDA(cudaGetLastError());
   }
@@ -1266,6 +1298,8 @@ constexpr int kNAMaxDim = 8192;                // nodes per dimension
 constexpr int kNAMaxLevels = 16;               // as the allocating hierarchy
 constexpr int kNAMaxContacts = 64;
 constexpr int kNAMaxDevices = 64;
+constexpr int kNAVcyclesPerNewton = 2; // as PoissonMG's defaults
+constexpr double kNATwoCycleRel = 1e-2;
 constexpr int kNALevelNodes = 2 * kNAMaxNodes; // nodes of all levels together
 constexpr int kNA1D = 16 * kNAMaxDim;          // 1-D transfer entries of all levels
 
@@ -1680,19 +1714,24 @@ extern "C" int32_t emcg_poisson_solve_noalloc(const emcg_device_desc *dv, double
   double h_stats[2] = {0, 0};
   double rel = INFINITY;
   int it = 0;
+  double scale = 0.;
   for (; it <= max_cycles; it++) {
     // the residual maxima accumulate by atomic max and must start at zero
     EMCG_CUDA(cudaMemsetAsync(stats, 0, 4 * sizeof(double), st));
     nonlinResidualKernel<float><<<grid, kBlock, 0, st>>>(
         d_pot, d_conc, C, lev[0].fixed, gSum, d_conc ? gVne : gVeq, nx, ny, hF0, hF1, hP, K0.r,
-        K0.rho, K0.d, stats);
+        K0.rho, K0.d, stats, it == 0);
     EMCG_CUDA(cudaGetLastError());
     EMCG_CUDA(cudaMemcpyAsync(h_stats, stats, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
     EMCG_CUDA(cudaStreamSynchronize(st));
-    rel = h_stats[1] > 0 ? h_stats[0] / h_stats[1] : h_stats[0];
+    if (it == 0)
+      scale = h_stats[1];
+    rel = scale > 0 ? h_stats[0] / scale : h_stats[0];
     if (rel <= rtol || it == max_cycles)
       break;
-    naVcycle(lev, lv.n, 0, pre, post, coarseSweeps, st);
+    const int nv = rel < kNATwoCycleRel ? kNAVcyclesPerNewton : 1;
+    for (int k = 0; k < nv; k++)
+      naVcycle(lev, lv.n, 0, pre, post, coarseSweeps, st);
     updatePotKernel<float><<<grid, kBlock, 0, st>>>(d_pot, K0.d, lev[0].fixed, n, stats);
     EMCG_CUDA(cudaGetLastError());
   }

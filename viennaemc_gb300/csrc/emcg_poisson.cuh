@@ -9,9 +9,11 @@
 // exp(phi) (equilibrium), G the gate Robin coefficient.  The reference's
 // lexicographic SOR reaches the fixed point of this equation; here it is
 // solved by Newton / defect correction in double precision whose correction
-// equation J d = -F is solved approximately by one multigrid V-cycle per
-// iteration (red-black Gauss-Seidel, bilinear transfer, finite-volume
-// coarse operators), in float or double.
+// equation J d = -F is solved approximately by one or two multigrid V-cycles
+// per iteration (red-black Gauss-Seidel, bilinear transfer, finite-volume
+// coarse operators), in float or double.  The solve stops when
+// max|F| <= rtol * max(hP (|C| + n + p)), the scale taken at the first
+// iteration.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -67,6 +69,11 @@ struct PoissonMG {
   double *resetEq = nullptr, *resetNe = nullptr;
   double *stats = nullptr; // [max|F|, scale, max|d|] as ordered bits
   int pre = 2, post = 2, coarseSweeps = 40;
+  // V-cycles on the correction equation per Newton step once the relative
+  // residual is below twoCycleRel; above it one (while Newton steps are clamped
+  // a more exact linear solve gains nothing)
+  int vcyclesPerNewton = 2;
+  double twoCycleRel = 1e-2;
   bool fp32 = true;
   double hF[2], hP;
   // single-launch cluster solve: CTAs per cluster (0 = not available for this
