@@ -237,6 +237,18 @@ int32_t emcg_set_scatter_mode(emcg_handle *h, int32_t queued);
    256-thread blocks per SM (1 = uncapped, 3 or 4); capped variants apply to
    blocks of at most 256 threads. */
 int32_t emcg_set_occupancy(emcg_handle *h, int32_t min_blocks_per_sm);
+/* Graph replay (enable != 0): each launch of steps is an instantiated CUDA
+   graph (observable reset -> step kernel) replayed with its step offset
+   updated; results equal the direct launches.  No reference counterpart. */
+int32_t emcg_bulk_set_graph(emcg_handle *h, int32_t enable);
+/* Autotuner: runs trial_steps steps (from step0, advancing the ensembles --
+   use it as warm-up) with each candidate launch shape (block threads 128 /
+   256, register cap 1 / 3 / 4 resident blocks per SM, lockstep or
+   block-queued scatter) and keeps the fastest.  *steps_used = steps run;
+   outputs may be NULL.  No reference counterpart. */
+int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint32_t step0,
+                           int32_t *steps_used, int32_t *block_threads, int32_t *min_blocks,
+                           int32_t *queued);
 
 /* ---- single-particle kernels (known-answer tests of the reference) ----- */
 /* drift() of include/emcParticleDrift.hpp:11-36 for n independent

@@ -340,3 +340,63 @@ def test_queued_kernel_equals_lockstep_kernel(engine, precision):
     assert bad.sum() <= a.n // 200, bad.sum()
     assert np.allclose(oa[..., 2], oq[..., 2])
     assert np.allclose(oa[..., 0], oq[..., 0], rtol=1e-3)
+
+
+def _sweep_batch(engine, precision="fp32", seed=41):
+    """Uneven ensembles on two temperature models, two directions, a few fields."""
+    from viennaemc_gb300 import physics as P
+    from viennaemc_gb300.bulk import BulkBatch, EnsembleSpec
+    models = [P.silicon_electron("jacoboni", temperature=T, max_energy=2.0) for T in (77.0, 300.0)]
+    specs, k = [], 0
+    for m in range(2):
+        for d in ((1, 0, 0), (1, 1, 1)):
+            for f in (1e4, 1e6, 1e7):
+                n = (700, 2500, 300, 1300, 4000, 900)[k % 6] + 37 * k
+                specs.append(EnsembleSpec(m, n, f, d, (1e-6,) * 3, 1e-15, seed + k, 0,
+                                          (77.0, 300.0)[m]))
+                k += 1
+    b = BulkBatch(models, specs, precision)
+    for e in range(len(specs)):
+        b.init_particles(e)
+    return b
+
+
+def test_graph_replay_equals_direct_launches(engine):
+    """Graph replay of the step launches gives the same bits as direct launches."""
+    out = []
+    for graph in (False, True):
+        b = _sweep_batch(engine)
+        b.set_launch(256, 7)
+        b.set_graph(graph)
+        o = b.step(30)
+        st = [b.get_state(e) for e in range(len(b.specs))]
+        b.close()
+        out.append((o, st))
+    assert np.array_equal(out[0][0], out[1][0])
+    for a, c in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a.kx, c.kx) and np.array_equal(a.energy, c.energy)
+        assert np.array_equal(a.sub, c.sub)
+
+
+def test_autotune_picks_a_valid_shape_and_keeps_results(engine):
+    """The autotuner tries every candidate shape on the trial steps, returns one
+    of them, and the run continues with it: the same trajectories as a run with
+    the default shape up to float branch flips of the queued scheme, so
+    per-ensemble mean energies agree closely and particle totals exactly."""
+    b = _sweep_batch(engine)
+    b.set_launch(256, 20)
+    cfg = b.autotune(10)
+    assert cfg["steps_used"] == 80
+    assert cfg["block_threads"] in (128, 256) and cfg["min_blocks"] in (1, 3, 4)
+    assert cfg["queued"] in (0, 1)
+    o = b.step(20)
+    b.close()
+    b2 = _sweep_batch(engine)
+    b2.set_launch(256, 20)
+    b2.step(80)
+    o2 = b2.step(20)
+    b2.close()
+    cnt, cnt2 = o[..., 2].sum(axis=-1), o2[..., 2].sum(axis=-1)
+    assert np.array_equal(cnt, cnt2)
+    e, e2 = o[..., 0].sum(axis=(1, 2)), o2[..., 0].sum(axis=(1, 2))
+    assert np.all(np.isfinite(e)) and np.allclose(e, e2, rtol=2e-2)

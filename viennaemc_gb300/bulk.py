@@ -177,6 +177,21 @@ class BulkBatch:
         if queued is not None:
             L.check(self._lib.emcg_set_scatter_mode(self.h, int(queued)))
 
+    def set_graph(self, enable: bool = True):
+        """Replay each launch of steps from an instantiated CUDA graph."""
+        L.check(self._lib.emcg_bulk_set_graph(self.h, int(enable)))
+
+    def autotune(self, trial_steps: int = 50, step0: int | None = None) -> dict:
+        """Time each candidate launch shape on trial_steps steps (they advance
+        the ensembles, like warm-up steps) and keep the fastest."""
+        s0 = self.step_index if step0 is None else int(step0)
+        used, blk, mb, q = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        L.check(self._lib.emcg_bulk_autotune(self.h, int(trial_steps), s0, C.byref(used),
+                                             C.byref(blk), C.byref(mb), C.byref(q)))
+        self.step_index = s0 + used.value
+        return {"block_threads": blk.value, "min_blocks": mb.value, "queued": q.value,
+                "steps_used": used.value}
+
     def step(self, n_steps: int = 1, observables: bool = True, step0: int | None = None):
         """Advance all ensembles; returns sums [ens, step, valley, {E, v.dir, count}]."""
         s0 = self.step_index if step0 is None else int(step0)

@@ -532,6 +532,32 @@ struct BulkImpl {
   double lastMs = 0;
   // host staging for state transfer
   std::vector<unsigned char> stage;
+  // graph replay of one launch of steps: [observable reset] -> [step kernel],
+  // instantiated per launch shape, the step offset updated before each replay
+  bool useGraph = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  cudaGraphNode_t gKernel = nullptr;
+  cudaKernelNodeParams gKp = {};
+  int gNs = -1, gBlock = 0, gMinb = 0, gQueued = -1, gTiles = -1;
+  alignas(16) unsigned char gArgs[256] = {};
+  void *gParams[12] = {};
+};
+
+// arguments of the step kernels, in parameter order
+template <class T> struct StepArgs {
+  StateK<T> st;
+  const ModelK<T> *mp;
+  const EnsK<T> *ep;
+  const Tile *tiles;
+  int ns;
+  uint32_t step0;
+  int chunk;
+  int nVmax;
+  double *obs;
+  const uint64_t *words;
+  const int64_t *off;
+  int *err;
 };
 
 template <class T> static StateK<T> stateOf(BulkImpl *b) {
@@ -645,6 +671,93 @@ static int32_t readError(BulkImpl *b) {
   return EMCG_OK;
 }
 
+static void dropGraph(BulkImpl *b) {
+  if (b->gexec)
+    cudaGraphExecDestroy(b->gexec);
+  if (b->graph)
+    cudaGraphDestroy(b->graph);
+  b->gexec = nullptr;
+  b->graph = nullptr;
+  b->gKernel = nullptr;
+  b->gNs = -1;
+}
+
+// the step kernel of the current launch configuration (Philox streams)
+template <class T> static void *stepKernelFn(const BulkImpl *b, bool *queued) {
+  *queued = b->queued != 0;
+  if (b->queued) {
+    if (b->minBlocks >= 4 && b->blockThreads <= 256)
+      return (void *)bulkStepQueuedKernel<T, 4>;
+    if (b->minBlocks == 3 && b->blockThreads <= 256)
+      return (void *)bulkStepQueuedKernel<T, 3>;
+    return (void *)bulkStepQueuedKernel<T, 1>;
+  }
+  if (b->minBlocks >= 4 && b->blockThreads <= 256)
+    return (void *)bulkStepKernel<T, false, 4>;
+  if (b->minBlocks == 3 && b->blockThreads <= 256)
+    return (void *)bulkStepKernel<T, false, 3>;
+  return (void *)bulkStepKernel<T, false, 1>;
+}
+
+// (Re)build the graph of one launch of ns steps for the current configuration.
+template <class T> static int32_t graphFor(BulkImpl *b, int ns, size_t smem, size_t qsmem) {
+  if (b->gexec && b->gNs == ns && b->gBlock == b->blockThreads && b->gMinb == b->minBlocks &&
+      b->gQueued == b->queued && b->gTiles == b->nTiles)
+    return EMCG_OK;
+  dropGraph(b);
+  static_assert(sizeof(StepArgs<T>) <= sizeof(b->gArgs), "step arguments exceed the buffer");
+  StepArgs<T> &a = *reinterpret_cast<StepArgs<T> *>(b->gArgs);
+  a.st = stateOf<T>(b);
+  a.mp = (const ModelK<T> *)b->dModels;
+  a.ep = (const EnsK<T> *)b->dEns;
+  a.tiles = b->dTiles;
+  a.ns = ns;
+  a.step0 = 0;
+  a.chunk = b->chunk;
+  a.nVmax = b->nVmax;
+  a.obs = b->dObs;
+  a.words = nullptr;
+  a.off = nullptr;
+  a.err = b->dErr;
+  bool queued = false;
+  void *fn = stepKernelFn<T>(b, &queued);
+  void *lock[12] = {&a.st,    &a.mp,   &a.ep,  &a.tiles, &a.ns,    &a.step0,
+                    &a.chunk, &a.nVmax, &a.obs, &a.words, &a.off, &a.err};
+  void *que[10] = {&a.st, &a.mp, &a.ep, &a.tiles, &a.ns, &a.step0, &a.chunk, &a.nVmax, &a.obs,
+                   &a.err};
+  if (queued)
+    std::memcpy(b->gParams, que, sizeof(que));
+  else
+    std::memcpy(b->gParams, lock, sizeof(lock));
+  const int Q = b->nVmax * 3;
+  const size_t obsBytes = (size_t)b->nEns * ns * Q * sizeof(double);
+  EMCG_CUDA(cudaGraphCreate(&b->graph, 0));
+  cudaMemsetParams mp = {};
+  mp.dst = b->dObs;
+  mp.value = 0;
+  mp.elementSize = 4;
+  mp.width = obsBytes / 4;
+  mp.height = 1;
+  mp.pitch = 0;
+  cudaGraphNode_t mn;
+  EMCG_CUDA(cudaGraphAddMemsetNode(&mn, b->graph, nullptr, 0, &mp));
+  cudaKernelNodeParams &kp = b->gKp;
+  kp = {};
+  kp.func = fn;
+  kp.gridDim = dim3(b->nTiles, 1, 1);
+  kp.blockDim = dim3(b->blockThreads, 1, 1);
+  kp.sharedMemBytes = (unsigned)(queued ? qsmem : smem);
+  kp.kernelParams = b->gParams;
+  EMCG_CUDA(cudaGraphAddKernelNode(&b->gKernel, b->graph, &mn, 1, &kp));
+  EMCG_CUDA(cudaGraphInstantiate(&b->gexec, b->graph, 0));
+  b->gNs = ns;
+  b->gBlock = b->blockThreads;
+  b->gMinb = b->minBlocks;
+  b->gQueued = b->queued;
+  b->gTiles = b->nTiles;
+  return EMCG_OK;
+}
+
 template <class T>
 static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHost) {
   EMCG_TRY(ensureTiles(b));
@@ -654,6 +767,7 @@ static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHos
     per = 1;
   size_t need = (size_t)b->nEns * per * Q;
   if (need > b->obsCap) {
+    dropGraph(b); // it holds the old buffer
     cudaFree(b->dObs);
     b->dObs = nullptr;
     EMCG_CUDA(cudaMalloc(&b->dObs, need * sizeof(double)));
@@ -663,43 +777,53 @@ static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHos
   const size_t smem = (size_t)b->chunk * nWarps * Q * sizeof(T);
   StateK<T> st = stateOf<T>(b);
   double totalMs = 0;
+  const bool graph = b->useGraph && !b->replay && b->nTiles > 0;
   for (int done = 0; done < nSteps; done += per) {
     int ns = std::min(per, nSteps - done);
-    EMCG_CUDA(cudaMemsetAsync(b->dObs, 0, (size_t)b->nEns * ns * Q * sizeof(double), b->stream));
-    EMCG_CUDA(cudaEventRecord(b->ev0, b->stream));
-    if (b->nTiles > 0) {
-      const ModelK<T> *mp = (const ModelK<T> *)b->dModels;
-      const EnsK<T> *ep = (const EnsK<T> *)b->dEns;
-      if (b->replay) {
-        if constexpr (sizeof(T) == 8)
-          bulkStepKernel<T, true, 1><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
-              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dWords,
-              b->dOff, b->dErr);
-      } else if (b->queued) {
-        const size_t qsmem = ((smem + 15) & ~size_t(15)) + blockStateBytes<T>(b->blockThreads);
-        if (b->minBlocks >= 4 && b->blockThreads <= 256)
-          bulkStepQueuedKernel<T, 4><<<b->nTiles, b->blockThreads, qsmem, b->stream>>>(
-              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
-        else if (b->minBlocks == 3 && b->blockThreads <= 256)
-          bulkStepQueuedKernel<T, 3><<<b->nTiles, b->blockThreads, qsmem, b->stream>>>(
-              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
-        else
-          bulkStepQueuedKernel<T, 1><<<b->nTiles, b->blockThreads, qsmem, b->stream>>>(
-              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
-      } else if (b->minBlocks >= 4 && b->blockThreads <= 256) {
-        bulkStepKernel<T, false, 4><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
-            st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, nullptr,
-            nullptr, b->dErr);
-      } else if (b->minBlocks == 3 && b->blockThreads <= 256) {
-        bulkStepKernel<T, false, 3><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
-            st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, nullptr,
-            nullptr, b->dErr);
-      } else {
-        bulkStepKernel<T, false, 1><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
-            st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, nullptr,
-            nullptr, b->dErr);
+    if (graph) {
+      const size_t qsmem = ((smem + 15) & ~size_t(15)) + blockStateBytes<T>(b->blockThreads);
+      EMCG_TRY(graphFor<T>(b, ns, smem, qsmem));
+      reinterpret_cast<StepArgs<T> *>(b->gArgs)->step0 = step0 + done;
+      EMCG_CUDA(cudaGraphExecKernelNodeSetParams(b->gexec, b->gKernel, &b->gKp));
+      EMCG_CUDA(cudaEventRecord(b->ev0, b->stream));
+      EMCG_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+    } else {
+      EMCG_CUDA(cudaMemsetAsync(b->dObs, 0, (size_t)b->nEns * ns * Q * sizeof(double), b->stream));
+      EMCG_CUDA(cudaEventRecord(b->ev0, b->stream));
+      if (b->nTiles > 0) {
+        const ModelK<T> *mp = (const ModelK<T> *)b->dModels;
+        const EnsK<T> *ep = (const EnsK<T> *)b->dEns;
+        if (b->replay) {
+          if constexpr (sizeof(T) == 8)
+            bulkStepKernel<T, true, 1><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
+                st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dWords,
+                b->dOff, b->dErr);
+        } else if (b->queued) {
+          const size_t qsmem = ((smem + 15) & ~size_t(15)) + blockStateBytes<T>(b->blockThreads);
+          if (b->minBlocks >= 4 && b->blockThreads <= 256)
+            bulkStepQueuedKernel<T, 4><<<b->nTiles, b->blockThreads, qsmem, b->stream>>>(
+                st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
+          else if (b->minBlocks == 3 && b->blockThreads <= 256)
+            bulkStepQueuedKernel<T, 3><<<b->nTiles, b->blockThreads, qsmem, b->stream>>>(
+                st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
+          else
+            bulkStepQueuedKernel<T, 1><<<b->nTiles, b->blockThreads, qsmem, b->stream>>>(
+                st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
+        } else if (b->minBlocks >= 4 && b->blockThreads <= 256) {
+          bulkStepKernel<T, false, 4><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
+              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, nullptr,
+              nullptr, b->dErr);
+        } else if (b->minBlocks == 3 && b->blockThreads <= 256) {
+          bulkStepKernel<T, false, 3><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
+              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, nullptr,
+              nullptr, b->dErr);
+        } else {
+          bulkStepKernel<T, false, 1><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
+              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, nullptr,
+              nullptr, b->dErr);
+        }
+        EMCG_CUDA(cudaGetLastError());
       }
-      EMCG_CUDA(cudaGetLastError());
     }
     EMCG_CUDA(cudaEventRecord(b->ev1, b->stream));
     if (obsHost) {
@@ -738,6 +862,7 @@ static void freeBulk(BulkImpl *b) {
   cudaFree(b->dErr);
   cudaFree(b->dWords);
   cudaFree(b->dOff);
+  dropGraph(b);
   if (b->ev0)
     cudaEventDestroy(b->ev0);
   if (b->ev1)
@@ -1086,6 +1211,70 @@ extern "C" int32_t emcg_set_launch(emcg_handle *h, int32_t block_threads,
     EMCG_CHECK_ARG(steps_per_launch > 0, "steps_per_launch must be positive");
     b->stepsPerLaunch = steps_per_launch;
   }
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_bulk_set_graph(emcg_handle *h, int32_t enable) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  b->useGraph = enable != 0;
+  if (!b->useGraph)
+    dropGraph(b);
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint32_t step0,
+                                      int32_t *steps_used, int32_t *block_threads,
+                                      int32_t *min_blocks, int32_t *queued) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(trial_steps > 0, "trial_steps must be positive");
+  EMCG_CHECK_ARG(!b->replay, "autotuning runs Philox steps; clear replay first");
+  // launch shapes: block threads x register cap (resident blocks per SM) x
+  // scatter scheme; each runs trial_steps steps (advancing the ensembles) and
+  // the fastest device time wins
+  struct Cand {
+    int block, minb, queued;
+  };
+  const Cand cands[] = {{256, 4, 0}, {256, 3, 0}, {256, 1, 0}, {128, 4, 0},
+                        {128, 1, 0}, {256, 4, 1}, {256, 3, 1}, {128, 4, 1}};
+  const int keepPer = b->stepsPerLaunch;
+  b->stepsPerLaunch = trial_steps;
+  double best = INFINITY;
+  Cand bestC = {b->blockThreads, b->minBlocks, b->queued};
+  uint32_t s = step0;
+  for (const Cand &c : cands) {
+    if (c.block != b->blockThreads)
+      b->tilesDirty = true;
+    b->blockThreads = c.block;
+    b->minBlocks = c.minb;
+    b->queued = c.queued;
+    int32_t st = b->precision == EMCG_FP64 ? stepTyped<double>(b, trial_steps, s, nullptr)
+                                           : stepTyped<float>(b, trial_steps, s, nullptr);
+    s += trial_steps;
+    if (st != EMCG_OK) {
+      b->stepsPerLaunch = keepPer;
+      return st;
+    }
+    if (b->lastMs < best) {
+      best = b->lastMs;
+      bestC = c;
+    }
+  }
+  if (bestC.block != b->blockThreads)
+    b->tilesDirty = true;
+  b->blockThreads = bestC.block;
+  b->minBlocks = bestC.minb;
+  b->queued = bestC.queued;
+  b->stepsPerLaunch = keepPer;
+  if (steps_used)
+    *steps_used = (int32_t)(s - step0);
+  if (block_threads)
+    *block_threads = bestC.block;
+  if (min_blocks)
+    *min_blocks = bestC.minb;
+  if (queued)
+    *queued = bestC.queued;
   return EMCG_OK;
 }
 
