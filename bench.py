@@ -165,6 +165,8 @@ def run_engine(args):
         win = slice(0, 0)
     batched = _batched_bench(args, rank) if args.batch_steps > 0 else None
     device = _device_bench(args, rank) if args.device_steps > 0 else None
+    if device is not None and args.mosfet_steps > 0:
+        device["mosfet_sweep"] = _mosfet_bench(args, rank)
     _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units, h2d, d2h,
             value64, vd32, vd64, win, k64, wall, clocks, device, batched)
     if ws > 1:
@@ -391,6 +393,65 @@ def _device_bench(args, rank):
     return out
 
 
+def mosfet_device(D, P, vds, vgs=1.0):
+    """2-D Si n-MOSFET: 200 nm x 100 nm at 0.5 nm (401 x 201 nodes), gate
+    length 50 nm over 1 nm SiO2 (eps_r 3.9, barrier Eg/2), source and drain
+    Nd = 1e26 m^-3 to 20 nm depth, channel and bulk Na = 1e24 m^-3, substrate
+    contact at the back; the contact layout of the reference mosfet2D."""
+    mat = P.silicon_material()
+    dev = D.Device(mat, (200e-9, 100e-9), (0.5e-9, 0.5e-9))
+    dev.setDeviceWidth(1.3e-6)
+    dev.addConstantDopingRegion((0, 20e-9), (200e-9, 100e-9), -1e24)
+    dev.addConstantDopingRegion((0, 0), (75e-9, 20e-9), 1e26)
+    dev.addConstantDopingRegion((75e-9, 0), (125e-9, 20e-9), -1e24)
+    dev.addConstantDopingRegion((125e-9, 0), (200e-9, 20e-9), 1e26)
+    dev.addOhmicContact(D.YMAX, 0.0, (0,), (200e-9,))
+    dev.addOhmicContact(D.YMIN, 0.0, (0,), (75e-9,))
+    dev.addGateContact(D.YMIN, vgs, (75e-9,), (125e-9,), 3.9, 1e-9, 1.12 / 2)
+    dev.addOhmicContact(D.YMIN, vds, (125e-9,), (200e-9,))
+    return dev
+
+
+def _mosfet_bench(args, rank):
+    """Eight drain biases 0..1 V at Vgs = 1 V stepped together (one engine per
+    bias, each on its own stream), FP32 particles, per-step Poisson to 1e-8."""
+    from viennaemc_gb300 import device as D
+    from viennaemc_gb300 import physics as P
+    sims = []
+    for k, vds in enumerate(np.linspace(0.0, 1.0, 8)):
+        dev = mosfet_device(D, P, float(vds))
+        regs = list(range(dev.n_regions))
+        pt = P.silicon_electron("refbulk", n_levels=1000, max_energy=4.0, regions=regs,
+                                coulomb=True, region_doping=dev.getDopingRegionDoping,
+                                first_order=False)
+        sim = D.DeviceSimulation(dev, pt, scheme=D.CIC, dt=1e-16, seed=100 + k + 8 * rank,
+                                 precision="fp32", poisson_rtol=1e-8, poisson_max_cycles=200,
+                                 tau_region_is_valley=True)
+        sim.calcEquilibriumCharacteristics()
+        sims.append(sim)
+    D.DeviceSimulation.performEMCStepMany(sims, args.device_warmup)
+    n0 = [s.num_particles() for s in sims]
+    K = args.mosfet_steps
+    t0 = time.perf_counter()
+    D.DeviceSimulation.performEMCStepMany(sims, K)
+    wall = time.perf_counter() - t0
+    n1 = [s.num_particles() for s in sims]
+    pois = [s.timing()[1] / K for s in sims]
+    step = [s.timing()[0] / K for s in sims]
+    drain = [float(s.current(args.device_warmup)[3]) for s in sims]
+    for s in sims:
+        s.close()
+    tot = sum(0.5 * (a + b) for a, b in zip(n0, n1))
+    return {"workload": "Si n-MOSFET 401 x 201 nodes (0.5 nm), Lg 50 nm, 1 nm SiO2, S/D 1e26, "
+                        "channel 1e24, Vgs 1 V, Vds = 0..1 V in 8 steps, one engine per bias",
+            "steps": K, "particles": n1, "wall_ms_per_step": 1e3 * wall / K,
+            "value": tot * K / wall, "unit": UNIT,
+            "device_ms_per_step_each": step, "poisson_ms_per_solve_each": pois,
+            "drain_current_A": drain,
+            "note": "value = particles of all 8 engines x steps / wall time of the batch "
+                    "(host-timed, the engines overlap on the GPU)"}
+
+
 def _cpu_sor(dev, pot, conc, repeats=3):
     """The reference's SOR solve (oracle port, one thread like the reference)
     from the engine's potential with its latest concentration."""
@@ -584,6 +645,8 @@ def main(argv=None):
     ap.add_argument("--device-steps", type=int, default=1000,
                     help="timed resistor device steps (0: skip the device path)")
     ap.add_argument("--device-warmup", type=int, default=20)
+    ap.add_argument("--mosfet-steps", type=int, default=200,
+                    help="timed steps of the 8-bias MOSFET batch (0: skip it)")
     ap.add_argument("--fp64-steps", type=int, default=1500)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -347,6 +347,13 @@ int32_t emcg_device_set_replay(emcg_handle *h, int32_t phase, const uint64_t *wo
                                int64_t nwords, const int64_t *offsets, int64_t n_offsets);
 /* Device-side time of the last emcg_device_step / poisson call (ms). */
 int32_t emcg_device_timing(emcg_handle *h, double *step_ms, double *poisson_ms);
+/* emcg_device_step on n engines at once (a bias sweep, several devices): one
+   host thread per engine, each on its engine's stream, so their kernels run
+   concurrently.  netto (may be NULL) holds one n_steps x n_contacts array per
+   engine.  Returns the first failing engine's status.  No reference
+   counterpart (the reference runs one emcSimulation per process). */
+int32_t emcg_device_step_many(emcg_handle **h, int32_t n, int32_t n_steps, uint32_t step0,
+                              int32_t **netto);
 /* Poisson execution: mode 1 = the whole solve in one launch of a thread-block
    cluster (default where the grid fits), 0 = one launch per multigrid phase,
    -1 = leave as is.  *cluster_size (may be NULL) receives the CTAs per

@@ -247,3 +247,27 @@ def test_poisson_cluster_equals_multilaunch(engine, case):
     assert max(a[0][0], a[1][0]) <= 1e-10
     assert np.max(np.abs(a[2] - b[2])) <= 1e-13 * max(1.0, np.abs(b[2]).max())
     assert np.max(np.abs(a[3] - b[3])) <= 1e-13 * max(1.0, np.abs(b[3]).max())
+
+
+def test_step_many_equals_separate_steps(engine):
+    """Stepping two engines concurrently gives what stepping each alone gives."""
+    from viennaemc_gb300 import _lib as L
+    from viennaemc_gb300 import device as D
+    g = golden(DEVICE_CASES[1])
+    runs = []
+    for batch in (False, True):
+        sims = []
+        for seed in (5, 6):
+            sim, dev, pt = _sim(engine, g, DEVICE_CASES[1], precision="fp32", seed=seed)
+            sim.calcEquilibriumCharacteristics()
+            sims.append(sim)
+        if batch:
+            nets = D.DeviceSimulation.performEMCStepMany(sims, 4)
+        else:
+            nets = [s.performEMCStep(4) for s in sims]
+        runs.append([(n, s.potential, s.num_particles()) for n, s in zip(nets, sims)])
+        for s in sims:
+            s.close()
+    for (na, pa, ca), (nb, pb, cb) in zip(*runs):
+        assert np.array_equal(na, nb) and ca == cb
+        assert np.allclose(pa, pb, rtol=1e-9, atol=1e-9)

@@ -228,6 +228,8 @@ _EXTRA_DECLS.extend([
     ("emcg_device_timing", [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("emcg_device_poisson_counts", [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("emcg_device_poisson_mode", [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
+    ("emcg_device_step_many", [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_uint32,
+                               C.POINTER(C.POINTER(C.c_int32))]),
     ("emcg_bulk_set_graph", [C.c_void_p, C.c_int32]),
     ("emcg_bulk_autotune", [C.c_void_p, C.c_int32, C.c_uint32, C.POINTER(C.c_int32),
                             C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),

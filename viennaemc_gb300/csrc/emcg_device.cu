@@ -7,6 +7,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "emcg_common.cuh"
@@ -1303,6 +1305,44 @@ extern "C" int32_t emcg_device_step(emcg_handle *h, int32_t n_steps, uint32_t st
   }
   d->stepMs = stepMs;
   d->poissonMs = poisMs;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_device_step_many(emcg_handle **hs, int32_t n, int32_t n_steps,
+                                         uint32_t step0, int32_t **netto) {
+  EMCG_CHECK_ARG(hs && n >= 0 && n_steps >= 0, "bad batch arguments");
+  for (int i = 0; i < n; i++) {
+    DeviceImpl *d;
+    EMCG_TRY(devOf(hs[i], &d));
+    for (int j = 0; j < i; j++)
+      EMCG_CHECK_ARG(hs[j] != hs[i], "handle %d appears twice in the batch", i);
+  }
+  int dev = 0;
+  EMCG_CUDA(cudaGetDevice(&dev));
+  // one host thread per engine: each drives its own stream, so the engines'
+  // kernels (one Poisson cluster each, the particle kernels) run side by side
+  std::vector<int32_t> status(n, EMCG_OK);
+  std::vector<std::string> message(n);
+  std::vector<std::thread> workers;
+  workers.reserve(n);
+  for (int i = 0; i < n; i++)
+    workers.emplace_back([&, i]() {
+      if (cudaSetDevice(dev) != cudaSuccess) {
+        status[i] = EMCG_ERR_CUDA;
+        message[i] = "cudaSetDevice failed in a batch worker";
+        return;
+      }
+      status[i] = emcg_device_step(hs[i], n_steps, step0, netto ? netto[i] : nullptr);
+      if (status[i] != EMCG_OK)
+        message[i] = emcg_last_error();
+    });
+  for (auto &w : workers)
+    w.join();
+  for (int i = 0; i < n; i++)
+    if (status[i] != EMCG_OK) {
+      setError("engine %d of the batch: %s", i, message[i].c_str());
+      return status[i];
+    }
   return EMCG_OK;
 }
 

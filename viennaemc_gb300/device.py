@@ -297,6 +297,29 @@ class DeviceSimulation:
         self.netto.extend(list(netto[:, :self.nc]))
         return netto[:, :self.nc]
 
+    @staticmethod
+    def performEMCStepMany(sims, n_steps=1):
+        """performEMCStep on several simulations at once (e.g. a bias sweep):
+        the library steps each on its own stream from its own host thread.
+        Every simulation must be at the same step index."""
+        sims = list(sims)
+        if not sims:
+            return []
+        s0 = sims[0].step_index
+        if any(x.step_index != s0 for x in sims):
+            raise ValueError("simulations of a batch must be at the same step")
+        lib = sims[0]._lib
+        outs = [np.zeros((n_steps, max(x.nc, 1)), np.int32) for x in sims]
+        hs = (C.c_void_p * len(sims))(*[x.h.value for x in sims])
+        ptrs = (C.POINTER(C.c_int32) * len(sims))(*[_ip(o) for o in outs])
+        L.check(lib.emcg_device_step_many(hs, len(sims), n_steps, s0, ptrs))
+        res = []
+        for x, o in zip(sims, outs):
+            x.step_index += n_steps
+            x.netto.extend(list(o[:, :x.nc]))
+            res.append(o[:, :x.nc])
+        return res
+
     def execute(self, n_steps):
         self.calcEquilibriumCharacteristics()
         return self.performEMCStep(n_steps)
