@@ -309,7 +309,7 @@ def _batched_bench(args, rank):
            "ensembles": len(specs), "particles_total": ntot, "steps": K, "value": value,
            "unit": UNIT, "ms_per_step": ms / K, "autotune": tuned, "graph_replay": True,
            "steps_per_launch": args.steps_per_launch,
-           "l2": "working set larger than L2 (%.0f MB of particle state)" % (ntot * 36 / 1e6)}
+           "l2": "working set larger than L2 (%.0f MB of particle state)" % (ntot * 40 / 1e6)}
     if args.batch_fp64_steps > 0:
         # plain FP64 engine on the same batch from the same seeds: speed and v_d
         k64 = args.batch_fp64_steps

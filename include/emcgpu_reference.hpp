@@ -15,6 +15,10 @@
 //                            the API of basicBulkParticleHandler
 //                            (examples/bulkSimulation/basicBulkParticleHandler.hpp)
 //                            with the particles resident on the GPU.
+//   emcgpu::DeviceDesc, emcgpu::GpuDeviceSimulation
+//                            a 2-D reference emcDevice as the engine's device
+//                            description, and emcSimulation's equilibrium /
+//                            performEMCStep on the GPU.
 //
 // Every status returned by the C ABI other than EMCG_OK is turned into the
 // reference's own error path (emcMessage::addError, which aborts).
@@ -28,6 +32,7 @@
 #include <memory>
 #include <string>
 #include <utility>
+#include <tuple>
 #include <vector>
 
 #include <ParticleType/emcParticleType.hpp>
@@ -36,6 +41,8 @@
 #include <ScatterMechanisms/emcFirstOrderInterValleyScatterMechanism.hpp>
 #include <ScatterMechanisms/emcZeroOrderInterValleyScatterMechanism.hpp>
 #include <ValleyTypes/emcNonParabolicAnistropValley.hpp>
+#include <emcBoundaryPos.hpp>
+#include <emcContact.hpp>
 #include <emcMessage.hpp>
 
 #include "emcgpu.h"
@@ -323,6 +330,135 @@ private:
   int64_t n_ = 0;
   uint32_t step_ = 0;
   std::vector<double> obs_, last_;
+};
+
+// emcg_device_desc of a 2-D reference device (emcDevice<T, 2>), read through
+// its public accessors: grid extent and spacing, material, doping and doping
+// region per node (emcDopingProfile), the contact index of every boundary
+// coordinate and the contacts' types, voltages and gate parameters
+// (emcSurface).  emcDevice keeps its width private; it is recovered from the
+// cell volume (getCellVolume = hx * hy * width).
+template <class T, class DeviceType> class DeviceDesc {
+public:
+  using SizeVec = typename DeviceType::SizeVec;
+  static_assert(std::tuple_size<SizeVec>::value == 2, "the device engine is 2-D");
+
+  explicit DeviceDesc(const DeviceType &dev) {
+    const SizeVec ext = dev.getGridExtent();
+    const SizeType nx = ext[0], ny = ext[1];
+    const auto h = dev.getSpacing();
+    const auto mx = dev.getMaxPos();
+    d_ = emcg_device_desc{};
+    d_.nx = (int32_t)nx;
+    d_.ny = (int32_t)ny;
+    d_.hx = h[0];
+    d_.hy = h[1];
+    d_.max_x = mx[0];
+    d_.max_y = mx[1];
+    d_.width = dev.getCellVolume() / (h[0] * h[1]);
+    d_.temperature = dev.getTemperature();
+    d_.ni = dev.getMaterial().getNi();
+    d_.eps_r = dev.getMaterial().getEpsR();
+    doping_.resize(nx * ny);
+    region_.resize(nx * ny);
+    const auto &dp = dev.getDopingProfile();
+    for (SizeType y = 0; y < ny; y++)
+      for (SizeType x = 0; x < nx; x++) {
+        const SizeVec c = {x, y};
+        doping_[y * nx + x] = dp.getDoping(c);
+        region_[y * nx + x] = dp.getDopingRegionIdx(c);
+      }
+    const auto &sf = dev.getSurface();
+    for (int b = 0; b < 4; b++) {
+      const SizeType len = b < 2 ? ny : nx;
+      bnd_[b].resize(len);
+      for (SizeType c = 0; c < len; c++)
+        bnd_[b][c] = sf.getContactIdx(std::array<SizeType, 1>{c}, (emcBoundaryPos)b);
+      d_.boundary_contact[b] = bnd_[b].data();
+    }
+    const SizeType nc = sf.getNrContacts();
+    for (SizeType k = 0; k < nc; k++) {
+      const emcContactType t = sf.getContactType(k);
+      type_.push_back(t == emcContactType::OHMIC      ? EMCG_CONTACT_OHMIC
+                      : t == emcContactType::SCHOTTKY ? EMCG_CONTACT_SCHOTTKY
+                                                      : EMCG_CONTACT_GATE);
+      volt_.push_back(sf.getContactVoltage(k));
+      for (SizeType q = 0; q < 3; q++)
+        param_.push_back(t == emcContactType::GATE ? sf.getContactFurtherParameter(k, q) : 0.);
+    }
+    d_.doping = doping_.data();
+    d_.region = region_.data();
+    d_.n_contacts = (int32_t)nc;
+    d_.contact_type = type_.empty() ? nullptr : type_.data();
+    d_.contact_voltage = volt_.empty() ? nullptr : volt_.data();
+    d_.contact_param = param_.empty() ? nullptr : param_.data();
+  }
+  DeviceDesc(const DeviceDesc &) = delete;
+  DeviceDesc &operator=(const DeviceDesc &) = delete;
+
+  const emcg_device_desc &desc() const { return d_; }
+
+private:
+  emcg_device_desc d_;
+  std::vector<double> doping_, volt_, param_;
+  std::vector<int32_t> region_, type_;
+  std::vector<int32_t> bnd_[4];
+};
+
+// emcSimulation (include/emcSimulation.hpp) with particle handler, PM scheme
+// and Poisson solver on the GPU, for one particle type on a 2-D device.
+template <class T, class DeviceType> class GpuDeviceSimulation {
+public:
+  // cfg: PM scheme, dt, seed, capacity and the Poisson settings; its charge is
+  // taken from the particle type
+  GpuDeviceSimulation(const DeviceType &device, ModelBuilder<T, DeviceType> &model,
+                      emcg_device_config cfg, int precision = EMCG_FP32)
+      : dd_(device) {
+    cfg.charge = model.particleType().getCharge();
+    const emcg_model_desc &md = model.desc();
+    check(emcg_device_create(&md, &dd_.desc(), &cfg, precision, &h_));
+    nc_ = dd_.desc().n_contacts;
+  }
+  ~GpuDeviceSimulation() { emcg_destroy(h_); }
+  GpuDeviceSimulation(const GpuDeviceSimulation &) = delete;
+  GpuDeviceSimulation &operator=(const GpuDeviceSimulation &) = delete;
+
+  // calcEquilibriumCharacteristics (emcSimulation.hpp:139-146): equilibrium
+  // potential, field, initial particles (from the doping, or from the
+  // potential), charge assignment
+  void calcEquilibriumCharacteristics(bool potentialBased = false) {
+    double rel = 0;
+    int32_t cycles = 0;
+    check(emcg_device_poisson(h_, 1, 1, &rel, &cycles));
+    check(emcg_device_efield(h_));
+    check(emcg_device_init(h_, potentialBased ? 1 : 0, 0));
+    check(emcg_device_assign(h_));
+  }
+
+  // performEMCStep (emcSimulation.hpp:164-193) nSteps times; per step and
+  // contact the netto particle count that emcSimulationResults::updateCurrent
+  // takes (removed - (injected - deleted)), step-major
+  std::vector<int32_t> performEMCStep(int nSteps = 1) {
+    std::vector<int32_t> netto((size_t)nSteps * (nc_ > 0 ? nc_ : 1), 0);
+    check(emcg_device_step(h_, nSteps, step_, netto.data()));
+    step_ += (uint32_t)nSteps;
+    return netto;
+  }
+
+  // EMCG_GRID_POTENTIAL (phi / Vt), EMCG_GRID_CONC (n / Ni), ...
+  std::vector<double> grid(int which) const {
+    std::vector<double> v((size_t)dd_.desc().nx * dd_.desc().ny);
+    check(emcg_device_get_grid(h_, which, v.data()));
+    return v;
+  }
+
+  SizeType getNrParticles() const { return (SizeType)emcg_num_particles(h_, 0); }
+
+private:
+  DeviceDesc<T, DeviceType> dd_;
+  emcg_handle *h_ = nullptr;
+  int nc_ = 0;
+  uint32_t step_ = 0;
 };
 
 } // namespace emcgpu

@@ -12,7 +12,9 @@
 
 using T = double;
 using Dev3 = emcDevice<T, 3>;
+using Dev2 = emcDevice<T, 2>;
 template class emcgpu::GpuBulkParticleHandler<T, Dev3>;
+template class emcgpu::GpuDeviceSimulation<T, Dev2>;
 
 int main() {
   Dev3 device{emcMaterial<T>{11.8, 2329., 1.45e16, 9040., 1.15}, {5e-7, 5e-7, 5e-7},
@@ -48,5 +50,29 @@ int main() {
                 d.mechs[m].final_sub[1][0]);
   for (int i = 0; i < d.n_mechs * d.n_levels; i += 97)
     std::printf("table %d %a\n", i, d.tables[i]);
+  // a gated 2-D device described through DeviceDesc
+  Dev2 dev2{emcMaterial<T>{11.8, 2329., 1.45e16, 9040., 1.15}, {30e-9, 20e-9}, {1e-9, 1e-9},
+            300.};
+  dev2.setDeviceWidth(3e-8);
+  dev2.addConstantDopingRegion({0, 8e-9}, {30e-9, 20e-9}, -1e24);
+  dev2.addConstantDopingRegion({0, 0}, {10e-9, 8e-9}, 1e26);
+  dev2.addConstantDopingRegion({10e-9, 0}, {20e-9, 8e-9}, -1e24);
+  dev2.addConstantDopingRegion({20e-9, 0}, {30e-9, 8e-9}, 1e26);
+  dev2.addOhmicContact(emcBoundaryPos::YMAX, 0, {0}, {30e-9});
+  dev2.addOhmicContact(emcBoundaryPos::YMIN, 0, {0}, {10e-9});
+  dev2.addGateContact(emcBoundaryPos::YMIN, 1.0, {10e-9}, {20e-9}, 3.9, 1.2e-9, 1.15 / 2.0);
+  dev2.addOhmicContact(emcBoundaryPos::YMIN, 0.5, {20e-9}, {30e-9});
+  emcgpu::DeviceDesc<T, Dev2> dd(dev2);
+  const emcg_device_desc &g = dd.desc();
+  std::printf("dev %d %d %a %a %a %a %a %a %a %a\n", g.nx, g.ny, g.hx, g.hy, g.max_x, g.max_y,
+              g.width, g.temperature, g.ni, g.eps_r);
+  for (int i = 0; i < g.nx * g.ny; i++)
+    std::printf("node %d %a %d\n", i, g.doping[i], g.region[i]);
+  for (int b = 0; b < 4; b++)
+    for (int c = 0; c < (b < 2 ? g.ny : g.nx); c++)
+      std::printf("bnd %d %d %d\n", b, c, g.boundary_contact[b][c]);
+  for (int k = 0; k < g.n_contacts; k++)
+    std::printf("contact %d %d %a %a %a %a\n", k, g.contact_type[k], g.contact_voltage[k],
+                g.contact_param[3 * k], g.contact_param[3 * k + 1], g.contact_param[3 * k + 2]);
   return 0;
 }
