@@ -260,8 +260,10 @@ int32_t emcg_drift_kat(emcg_handle *h, int32_t valley, int64_t n,
                        double *energy);
 
 /* ---- device engine (include/emcSimulation.hpp:164-193) ------------------ */
-#define EMCG_PM_NGP 0 /* include/PMSchemes/emcNGPScheme.hpp */
-#define EMCG_PM_CIC 1 /* include/PMSchemes/emcCICScheme.hpp */
+#define EMCG_PM_NGP 0     /* include/PMSchemes/emcNGPScheme.hpp */
+#define EMCG_PM_CIC 1     /* include/PMSchemes/emcCICScheme.hpp */
+#define EMCG_PM_NEC 2     /* include/PMSchemes/emcNECScheme.hpp */
+#define EMCG_PM_NEC_VWD 3 /* examples/mosfet2D/NECSchemeVWD.hpp */
 #define EMCG_CONTACT_OHMIC 0
 #define EMCG_CONTACT_SCHOTTKY 1
 #define EMCG_CONTACT_GATE 2
@@ -297,7 +299,7 @@ typedef struct {
 
 /* emcSimulationParameter + particle handler + solver settings. */
 typedef struct {
-  int32_t pm_scheme;            /* EMCG_PM_NGP | EMCG_PM_CIC */
+  int32_t pm_scheme;            /* EMCG_PM_NGP | _CIC | _NEC | _NEC_VWD */
   int32_t tau_region_is_valley; /* injection draws tau with the valley as the
                                    region (examples/mosfet2D/electronVWD.hpp:87) */
   int64_t capacity;             /* particle slots */
@@ -310,6 +312,10 @@ typedef struct {
   double poisson_rtol;          /* relative residual target */
   int32_t poisson_smooth;       /* red-black sweeps before and after */
   int32_t poisson_fp32;         /* 1: float V-cycles in double refinement */
+  int32_t round_expected;       /* 1: expected particles at the contacts rounded to
+                                   whole particles, as electronVWD
+                                   (examples/mosfet2D/electronVWD.hpp:46-56) */
+  int32_t pad_;
 } emcg_device_config;
 
 /* Create a device engine (emcSimulation constructor: particle handler with

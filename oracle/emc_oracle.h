@@ -159,7 +159,7 @@ void oc_init_particle(const oc_model *m, const int64_t coord[3],
                       int32_t tauRegionIsValley);
 
 /* ---- device (2-D) path ------------------------------------------------- */
-enum { OC_NGP = 0, OC_CIC = 1 };
+enum { OC_NGP = 0, OC_CIC = 1, OC_NEC = 2, OC_NEC_VWD = 3 };
 enum { OC_OHMIC = 0, OC_SCHOTTKY = 1, OC_GATE = 2 };
 enum { OC_XMIN = 0, OC_XMAX = 1, OC_YMIN = 2, OC_YMAX = 3 };
 
@@ -187,6 +187,9 @@ double oc_dev_cell_volume(const oc_dev *d);
 int32_t oc_dev_contact_idx(const oc_dev *d, int32_t x, int32_t y);
 int32_t oc_dev_is_reservoir(const oc_dev *d, int32_t x, int32_t y);
 void oc_dev_efield(const oc_dev *d, const double *pot, double *Ex, double *Ey);
+/* the E field of PM scheme `scheme` (NGP and CIC: oc_dev_efield) */
+void oc_dev_efield_pm(const oc_dev *d, int32_t scheme, const double *pot, double *Ex,
+                      double *Ey);
 void oc_dev_assign(const oc_dev *d, int32_t scheme, const double *px,
                    const double *py, int64_t n, double nrCarriers,
                    double *grid);

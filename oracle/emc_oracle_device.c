@@ -79,6 +79,8 @@ static void pos_to_coord(const oc_dev *d, const double *pos, int64_t *c) {
 }
 
 /* ---- E field (include/PMSchemes/emcEFieldCalculation.hpp:13-30, 58-81) --- */
+static void efield_boundary(const oc_dev *d, double *Ex, double *Ey);
+
 void oc_dev_efield(const oc_dev *d, const double *pot, double *Ex, double *Ey) {
   const int nx = d->nx, ny = d->ny;
   const double Vt = vt_of(d);
@@ -90,7 +92,43 @@ void oc_dev_efield(const oc_dev *d, const double *pot, double *Ex, double *Ey) {
       if (y != 0 && y != ny - 1)
         Ey[i] = (pot[i - nx] - pot[i + nx]) * Vt / (2 * d->hy);
     }
-  /* boundary values: 0 normal to an artificial boundary, else the neighbour */
+  efield_boundary(d, Ex, Ey);
+}
+
+/* The field of a PM scheme.  NGP, CIC: at the grid points (above).  NEC
+   (include/PMSchemes/emcNECScheme.hpp:115-119 with calcEFieldAtEdgeMidPts,
+   emcEFieldCalculation.hpp:35-52): forward differences on the edges, the
+   boundary values as for the grid-point field.  NEC-VWD
+   (examples/mosfet2D/NECSchemeVWD.hpp, calcEField): forward differences, 0 on
+   the last edge of each direction, no boundary pass. */
+void oc_dev_efield_pm(const oc_dev *d, int32_t scheme, const double *pot, double *Ex,
+                      double *Ey) {
+  const int nx = d->nx, ny = d->ny;
+  const double Vt = vt_of(d);
+  if (scheme == OC_NGP || scheme == OC_CIC) {
+    oc_dev_efield(d, pot, Ex, Ey);
+    return;
+  }
+  for (int y = 0; y < ny; y++)
+    for (int x = 0; x < nx; x++) {
+      int i = y * nx + x;
+      if (scheme == OC_NEC) {
+        if (x != 0 && x != nx - 1)
+          Ex[i] = (pot[i] - pot[i + 1]) * Vt / d->hx;
+        if (y != 0 && y != ny - 1)
+          Ey[i] = (pot[i] - pot[i + nx]) * Vt / d->hy;
+      } else {
+        Ex[i] = x != nx - 1 ? (pot[i] - pot[i + 1]) * Vt / d->hx : 0.;
+        Ey[i] = y != ny - 1 ? (pot[i] - pot[i + nx]) * Vt / d->hy : 0.;
+      }
+    }
+  if (scheme == OC_NEC)
+    efield_boundary(d, Ex, Ey);
+}
+
+/* boundary values: 0 normal to an artificial boundary, else the neighbour */
+static void efield_boundary(const oc_dev *d, double *Ex, double *Ey) {
+  const int nx = d->nx, ny = d->ny;
   for (int b = 0; b < 4; b++) {
     int n = b < 2 ? ny : nx;
     for (int c = 0; c < n; c++) {
@@ -122,7 +160,16 @@ static void grid_add(const oc_dev *d, double *g, int64_t x, int64_t y, double v)
 void oc_dev_assign(const oc_dev *d, int32_t scheme, const double *px,
                    const double *py, int64_t n, double nrC, double *grid) {
   for (int64_t i = 0; i < n; i++) {
-    if (scheme == OC_NGP) {
+    if (scheme == OC_NEC || scheme == OC_NEC_VWD) {
+      /* a quarter to each corner of the element (emcNECScheme.hpp:24-33,
+         NECSchemeVWD.hpp assignToMesh) */
+      int64_t mx = (int64_t)floor(px[i] / d->hx), my = (int64_t)floor(py[i] / d->hy);
+      double w = 0.25 * nrC;
+      grid_add(d, grid, mx, my, w);
+      grid_add(d, grid, mx + 1, my, w);
+      grid_add(d, grid, mx, my + 1, w);
+      grid_add(d, grid, mx + 1, my + 1, w);
+    } else if (scheme == OC_NGP) {
       int64_t x = (int64_t)round(px[i] / d->hx), y = (int64_t)round(py[i] / d->hy);
       grid_add(d, grid, x, y, nrC);
     } else {
@@ -149,7 +196,18 @@ void oc_dev_force(const oc_dev *d, int32_t scheme, const double *Ex,
                   const double *Ey, double x, double y, double charge,
                   double F[3]) {
   const double *E[2] = {Ex, Ey};
-  if (scheme == OC_NGP) {
+  if (scheme == OC_NEC || scheme == OC_NEC_VWD) {
+    /* NEC (emcNECScheme.hpp:102-113): the two edges of the element along each
+       direction; NEC-VWD (NECSchemeVWD.hpp interpolateForce) takes the nearest
+       column and only the edge below on the last one */
+    int64_t mx = scheme == OC_NEC ? (int64_t)floor(x / d->hx) : (int64_t)round(x / d->hx);
+    int64_t my = (int64_t)floor(y / d->hy);
+    F[0] = charge * (grid_get(d, Ex, mx, my) + grid_get(d, Ex, mx, my + 1)) / 2;
+    if (scheme == OC_NEC_VWD && mx == d->nx - 1)
+      F[1] = charge * grid_get(d, Ey, mx, my);
+    else
+      F[1] = charge * (grid_get(d, Ey, mx, my) + grid_get(d, Ey, mx + 1, my)) / 2;
+  } else if (scheme == OC_NGP) {
     int64_t cx = (int64_t)round(x / d->hx), cy = (int64_t)round(y / d->hy);
     for (int k = 0; k < 2; k++)
       F[k] = charge * grid_get(d, E[k], cx, cy);

@@ -388,7 +388,7 @@ def state_from_ref(d: dict, tag: str) -> State:
 
 
 # ---- device (2-D) path ----------------------------------------------------------
-NGP, CIC = 0, 1
+NGP, CIC, NEC, NEC_VWD = 0, 1, 2, 3
 
 
 class DevDesc(C.Structure):
@@ -413,6 +413,7 @@ def _declare_dev(L):
     L.oc_dev_is_reservoir.restype = i32
     L.oc_dev_is_reservoir.argtypes = [P(DevDesc), i32, i32]
     L.oc_dev_efield.argtypes = [P(DevDesc), P(d), P(d), P(d)]
+    L.oc_dev_efield_pm.argtypes = [P(DevDesc), C.c_int32, P(d), P(d), P(d)]
     L.oc_dev_assign.argtypes = [P(DevDesc), i32, P(d), P(d), i64, d, P(d)]
     L.oc_dev_force.argtypes = [P(DevDesc), i32, P(d), P(d), d, d, d, P(d)]
     L.oc_dev_move.restype = i32
@@ -464,10 +465,10 @@ class Device:
     def L(self):
         return lib()
 
-    def efield(self, pot):
+    def efield(self, pot, scheme=NGP):
         Ex = np.zeros(self.nx * self.ny)
         Ey = np.zeros(self.nx * self.ny)
-        self.L.oc_dev_efield(C.byref(self.d), dptr(darr(pot)), dptr(Ex), dptr(Ey))
+        self.L.oc_dev_efield_pm(C.byref(self.d), scheme, dptr(darr(pot)), dptr(Ex), dptr(Ey))
         return Ex, Ey
 
     def sor(self, pot, conc=None, omega=1.8, acc=1e-4, reset=True, max_sweeps=10 ** 7):

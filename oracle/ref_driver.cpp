@@ -39,6 +39,7 @@
 #include <ScatterMechanisms/emcZeroOrderInterValleyScatterMechanism.hpp>
 #include <ValleyTypes/emcNonParabolicAnistropValley.hpp>
 #include <PMSchemes/emcCICScheme.hpp>
+#include <PMSchemes/emcNECScheme.hpp>
 #include <PMSchemes/emcNGPScheme.hpp>
 #include <ParticleHandler/emcBasicParticleHandler.hpp>
 #include <PoissonSolver/emcSORSolver.hpp>
@@ -46,6 +47,8 @@
 #include <emcParticleDrift.hpp>
 #include <emcSimulation.hpp>
 #include "../examples/bulkSimulation/basicBulkParticleHandler.hpp"
+#include "../examples/mosfet2D/NECSchemeVWD.hpp"
+#include "../examples/mosfet2D/electronVWD.hpp"
 
 using T = double;
 using Dev3 = emcDevice<T, 3>;
@@ -344,13 +347,17 @@ template <class PH> static void dumpDevState(const char *tag, PH &ph) {
   reci((t + "_region").c_str(), reg);
 }
 
-// usage: ref_driver device <resistor|mosfet> <seed> <dt> <nSteps> <accV> <width>
-template <class PM> static int runDeviceT(const std::string &kind, unsigned long seed, double dt,
-                                          int nSteps, double acc, double width) {
+// usage: ref_driver device <resistor|mosfet|resistor_nec|mosfet_vwd> <seed> <dt> <nSteps>
+//                          <accV> <width>
+// resistor: NGP, mosfet: CIC, resistor_nec: emcNECScheme, all with emcElectron;
+// mosfet_vwd: the mosfet2D example's NEC-VWD scheme with its electronVWD
+template <class PM, class PT>
+static int runDeviceT(const std::string &kind, unsigned long seed, double dt, int nSteps,
+                      double acc, double width) {
   using PH = emcBasicParticleHandler<T, Dev2, PM>;
   using Solver = emcSORSolver<T, Dev2, PH>;
   using Sim = emcSimulation<T, Dev2, Solver, PH, PM>;
-  const bool mos = kind == "mosfet";
+  const bool mos = kind.rfind("mosfet", 0) == 0;
   std::array<T, 2> maxPos = mos ? std::array<T, 2>{30e-9, 20e-9} : std::array<T, 2>{20e-9, 10e-9};
   std::array<T, 2> spacing = {1e-9, 1e-9};
   Dev2 device{silicon(), maxPos, spacing, 300.};
@@ -380,7 +387,11 @@ template <class PM> static int runDeviceT(const std::string &kind, unsigned long
   param.setSeed(seed);
   param.setNrStepsBetweenShowProgress(1000000);
   param.setNrStepsForFinalAvg(1);
-  auto el = std::make_unique<emcElectron<T, Dev2>>(1000, 4., mos);
+  std::unique_ptr<PT> el;
+  if constexpr (std::is_same<PT, emcElectron<T, Dev2>>::value)
+    el = std::make_unique<PT>(1000, 4., mos);
+  else
+    el = std::make_unique<PT>(1000, 4.);
   addValley(el, 0.196);
   ModelSpec spec;
   spec.name = "refbulk";
@@ -479,9 +490,15 @@ static int runDevice(int argc, char **argv) {
   int n = std::atoi(argv[5]);
   double acc = std::atof(argv[6]);
   double width = std::atof(argv[7]);
+  using El = emcElectron<T, Dev2>;
   if (kind == "mosfet")
-    return runDeviceT<emcCICScheme<T, Dev2>>(kind, seed, dt, n, acc, width);
-  return runDeviceT<emcNGPScheme<T, Dev2>>(kind, seed, dt, n, acc, width);
+    return runDeviceT<emcCICScheme<T, Dev2>, El>(kind, seed, dt, n, acc, width);
+  if (kind == "resistor_nec")
+    return runDeviceT<emcNECScheme<T, Dev2>, El>(kind, seed, dt, n, acc, width);
+  if (kind == "mosfet_vwd")
+    return runDeviceT<emcNECSchemeVWD<T, Dev2>, electronVWD<T, Dev2>>(kind, seed, dt, n, acc,
+                                                                      width);
+  return runDeviceT<emcNGPScheme<T, Dev2>, El>(kind, seed, dt, n, acc, width);
 }
 
 int main(int argc, char **argv) {

@@ -85,7 +85,17 @@ def make_bulk(case):
 
 # (name, kind, seed, dt, steps, SOR accuracy [V], device width [m])
 DEVICE_CASES = [("resistor_ngp", "resistor", 42, 1e-15, 3, 1e-4, 3e-7),
-                ("mosfet_cic", "mosfet", 7, 1e-15, 3, 1e-4, 3e-8)]
+                ("mosfet_cic", "mosfet", 7, 1e-15, 3, 1e-4, 3e-8),
+                ("resistor_nec", "resistor_nec", 42, 1e-15, 3, 1e-4, 3e-7),
+                ("mosfet_necvwd", "mosfet_vwd", 7, 1e-15, 3, 1e-4, 3e-8)]
+
+
+def device_flavour(kind):
+    """PM scheme, potential-based initial counts, electronVWD (rounded counts,
+    tau drawn with the valley as the region) of a harness device kind."""
+    scheme = {"resistor": po.NGP, "mosfet": po.CIC, "resistor_nec": po.NEC,
+              "mosfet_vwd": po.NEC_VWD}[kind]
+    return scheme, kind.startswith("mosfet"), kind == "mosfet_vwd"
 
 
 def device_of(d):
@@ -130,24 +140,30 @@ def make_device(case):
     out["raw_r0"] = np.stack([d[f"raw_v0_r0_t{t}"] for t in range(6)])
     out["raw_coulomb"] = np.stack([d[f"raw_v0_r{r}_t1"] for r in regs])
     out["params"] = np.array([seed, dt, steps, acc, width])
-    scheme = po.CIC if kind == "mosfet" else po.NGP
+    out["kind"] = np.array(kind)
+    scheme, pot_init, vwd = device_flavour(kind)
     pot, _ = dev.sor(d["pot_init"], None, 1.8, acc, True)
     assert np.array_equal(pot, d["pot_eq"])
+    Ex, Ey = dev.efield(pot, scheme)
+    assert np.array_equal(Ex, d["ex_eq"]) and np.array_equal(Ey, d["ey_eq"])
     rng = po.RngState(po.RNG_MT, 0)
     rng.load_mt(d["mt_pre"])
-    st = dev.init_particles(m, rng, pot if kind == "mosfet" else None)
+    st = dev.init_particles(m, rng, pot if pot_init else None, round_counts=vwd,
+                            tau_region_is_valley=vwd)
     for f in po.STATE_F + po.STATE_I:
         assert np.array_equal(getattr(st, f), d[f"s0_{f}"])
         out[f"s0_{f}"] = d[f"s0_{f}"]
-    expnr = dev.exp_nr(False)
+    expnr = dev.exp_nr(vwd)
+    assert np.array_equal(expnr, d["expnr"])
     conc = dev.concentration(dev.assign(scheme, st))
     cap = 1 << 16
     cur = st.resize(cap)
     cur.n = st.n
     for s in range(1, steps + 1):
         pot, _ = dev.sor(pot, conc, 1.8, acc, s == 1)
-        Ex, Ey = dev.efield(pot)
+        Ex, Ey = dev.efield(pot, scheme)
         assert np.array_equal(pot, d[f"pot{s}"]) and np.array_equal(Ex, d[f"ex{s}"])
+        assert np.array_equal(Ey, d[f"ey{s}"])
         n_before = cur.n
         rng.start_record(1 << 20)
         rc, netto, off = dev.move(m, scheme, cur, Ex, Ey, dt, rng, s, offsets=True)
@@ -156,7 +172,7 @@ def make_device(case):
         out[f"move_offsets{s}"] = off
         out[f"move_n{s}"] = np.array([n_before, cur.n])
         rng.start_record(1 << 20)
-        rem_inj = dev.contacts(m, cur, cap, expnr, rng, s)
+        rem_inj = dev.contacts(m, cur, cap, expnr, rng, s, tau_region_is_valley=vwd)
         out[f"inject_words{s}"] = rng.recorded()
         out[f"netto{s}"] = d[f"netto{s}"]
         assert np.array_equal(netto - rem_inj, d[f"netto{s}"])

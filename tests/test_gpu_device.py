@@ -12,7 +12,8 @@ import numpy as np
 import pytest
 
 from conftest import golden
-from test_oracle_device_golden import DEVICE_CASES, _host_device, _oracle_device, _oracle_model
+from test_oracle_device_golden import (DEVICE_CASES, _host_device, _oracle_device, _oracle_model,
+                                       flavour)
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-12
@@ -42,12 +43,13 @@ def _electron(engine, dev):
 
 def _sim(engine, g, case, precision="fp64", seed=1, **kw):
     from viennaemc_gb300 import device as D
-    mos = "mosfet" in case
-    dev = _host_device(g, mos)
+    scheme, pot_init, vwd = flavour(g)
+    dev = _host_device(g, pot_init)
     pt = _electron(engine, dev)
-    return D.DeviceSimulation(dev, pt, scheme=D.CIC if mos else D.NGP, dt=float(g["params"][1]),
+    return D.DeviceSimulation(dev, pt, scheme=scheme, dt=float(g["params"][1]),
                               seed=seed, capacity=1 << 15, precision=precision,
-                              potential_init=mos, **kw), dev, pt
+                              potential_init=pot_init, round_counts=vwd,
+                              tau_region_is_valley=vwd, **kw), dev, pt
 
 
 def _engine_state(engine, g, s):
@@ -153,22 +155,22 @@ def test_philox_step_matches_oracle(engine, oracle, case):
     sim, dev, pt = _sim(engine, g, case, seed=seed)
     odev = _oracle_device(oracle, g)
     m, regs = _oracle_model(oracle, g)
-    scheme = oracle.CIC if "mosfet" in case else oracle.NGP
+    scheme, _, vwd = flavour(g)
     dt = float(g["params"][1])
     cur = oracle.State.from_dict({f: g[f"s0_{f}"] for f in oracle.STATE_F + oracle.STATE_I})
     cur = cur.resize(1 << 15)
     cur.n = len(g["s0_E"])
     sim.set_state(_engine_state(engine, g, 0))
     rng = oracle.RngState(oracle.RNG_PHILOX, seed, stream)
-    expnr = odev.exp_nr(False)
+    expnr = odev.exp_nr(vwd)
     for s in range(1, 4):
         sim.set_grid(L.GRID_POTENTIAL, g[f"pot{s}"])
         sim.efield()
-        Ex, Ey = odev.efield(g[f"pot{s}"])
+        Ex, Ey = odev.efield(g[f"pot{s}"], scheme)
         netto = sim.move(step=s)
         rem_inj = sim.contacts(step=s)
         rc, onet, _ = odev.move(m, scheme, cur, Ex, Ey, dt, rng, s)
-        ori = odev.contacts(m, cur, 1 << 15, expnr, rng, s)
+        ori = odev.contacts(m, cur, 1 << 15, expnr, rng, s, tau_region_is_valley=vwd)
         assert np.array_equal(netto, onet) and np.array_equal(rem_inj, ori)
         st = sim.get_state()
         assert st.n == cur.n

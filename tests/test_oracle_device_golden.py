@@ -6,7 +6,19 @@ import pytest
 
 from conftest import golden
 
-DEVICE_CASES = ["device_resistor_ngp.npz", "device_mosfet_cic.npz"]
+DEVICE_CASES = ["device_resistor_ngp.npz", "device_mosfet_cic.npz", "device_resistor_nec.npz",
+                "device_mosfet_necvwd.npz"]
+
+
+def flavour(g):
+    """(PM scheme, potential-based initial counts, electronVWD) of a fixture:
+    resistor NGP, MOSFET CIC, resistor with the NEC scheme, and the mosfet2D
+    example's NEC-VWD scheme with its electronVWD particle type (rounded counts,
+    tau drawn with the valley as the region).  Scheme numbers are shared by the
+    oracle and the engine."""
+    kind = str(g["kind"])
+    scheme = {"resistor": 0, "mosfet": 1, "resistor_nec": 2, "mosfet_vwd": 3}[kind]
+    return scheme, kind.startswith("mosfet"), kind == "mosfet_vwd"
 
 
 def _oracle_device(oracle, g):
@@ -48,20 +60,20 @@ def test_device_pipeline_matches_reference(oracle, case):
         assert np.array_equal(m.raw_table(0, r, 1), g["raw_coulomb"][r])
     for t in range(6):
         assert np.array_equal(m.raw_table(0, 0, t), g["raw_r0"][t])
-    mos = "mosfet" in case
-    scheme = oracle.CIC if mos else oracle.NGP
+    scheme, pot_init, vwd = flavour(g)
     seed, dt, steps, acc, width = g["params"]
     pot, _ = dev.sor(g["pot_init"], None, 1.8, acc, True)
     assert np.array_equal(pot, g["pot_eq"])
-    Ex, Ey = dev.efield(pot)
+    Ex, Ey = dev.efield(pot, scheme)
     assert np.array_equal(Ex, g["ex_eq"]) and np.array_equal(Ey, g["ey_eq"])
     rng = oracle.RngState(oracle.RNG_MT, 0)
     rng.load_mt(g["mt_pre"])
-    st = dev.init_particles(m, rng, pot if mos else None)
+    st = dev.init_particles(m, rng, pot if pot_init else None, round_counts=vwd,
+                            tau_region_is_valley=vwd)
     s0 = _state(oracle, g, 0)
     for f in oracle.STATE_F + oracle.STATE_I:
         assert np.array_equal(getattr(st, f), getattr(s0, f)), f
-    assert np.array_equal(dev.exp_nr(False), g["expnr"])
+    assert np.array_equal(dev.exp_nr(vwd), g["expnr"])
     nr = dev.assign(scheme, st)
     assert np.array_equal(nr, g["nr0"])
     conc = dev.concentration(nr)
@@ -71,11 +83,12 @@ def test_device_pipeline_matches_reference(oracle, case):
     for s in range(1, int(steps) + 1):
         pot, _ = dev.sor(pot, conc, 1.8, acc, s == 1)
         assert np.array_equal(pot, g[f"pot{s}"])
-        Ex, Ey = dev.efield(pot)
+        Ex, Ey = dev.efield(pot, scheme)
         assert np.array_equal(Ex, g[f"ex{s}"]) and np.array_equal(Ey, g[f"ey{s}"])
         rc, netto, _ = dev.move(m, scheme, cur, Ex, Ey, dt, rng, s)
         assert rc == 0
-        rem_inj = dev.contacts(m, cur, 1 << 16, dev.exp_nr(False), rng, s)
+        rem_inj = dev.contacts(m, cur, 1 << 16, dev.exp_nr(vwd), rng, s,
+                               tau_region_is_valley=vwd)
         assert np.array_equal(netto - rem_inj, g[f"netto{s}"])
         ref = _state(oracle, g, s)
         assert cur.n == ref.n
@@ -111,7 +124,7 @@ def _host_device(g, mos):
 @pytest.mark.parametrize("case", DEVICE_CASES)
 def test_host_device_builder_matches_reference(case):
     g = golden(case)
-    dev = _host_device(g, "mosfet" in case)
+    dev = _host_device(g, flavour(g)[1])
     assert np.array_equal(dev.doping, g["doping"])
     assert np.array_equal(dev.region, g["region"])
     for b in range(4):
@@ -127,7 +140,7 @@ def test_host_device_builder_matches_reference(case):
 def test_host_coulomb_tables_match_reference(case):
     from viennaemc_gb300 import physics
     g = golden(case)
-    dev = _host_device(g, "mosfet" in case)
+    dev = _host_device(g, flavour(g)[1])
     regs = list(range(dev.n_regions))
     pt = physics.silicon_electron("refbulk", n_levels=1000, max_energy=4.0, regions=regs,
                                   coulomb=True, region_doping=dev.getDopingRegionDoping,

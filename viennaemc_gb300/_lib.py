@@ -181,7 +181,7 @@ def check(status: int) -> None:
 
 
 # ---- device engine ---------------------------------------------------------------
-PM_NGP, PM_CIC = 0, 1
+PM_NGP, PM_CIC, PM_NEC, PM_NEC_VWD = 0, 1, 2, 3
 CONTACT_OHMIC, CONTACT_SCHOTTKY, CONTACT_GATE = 0, 1, 2
 GRID_POTENTIAL, GRID_EX, GRID_EY, GRID_NRPART, GRID_CONC = range(5)
 
@@ -203,7 +203,8 @@ class DeviceConfig(C.Structure):
                 ("carriers_per_particle", C.c_double), ("seed", C.c_uint64),
                 ("stream", C.c_uint32), ("poisson_max_cycles", C.c_int32),
                 ("poisson_rtol", C.c_double), ("poisson_smooth", C.c_int32),
-                ("poisson_fp32", C.c_int32)]
+                ("poisson_fp32", C.c_int32), ("round_expected", C.c_int32),
+                ("pad_", C.c_int32)]
 
 
 def _i32p():

@@ -63,12 +63,28 @@ __device__ __forceinline__ T gridAt(const DevK &G, const T *E, int x, int y) {
   return (x < 0 || y < 0 || x >= G.nx || y >= G.ny) ? T(0) : E[y * G.nx + x];
 }
 
-// NGP (include/PMSchemes/emcNGPScheme.hpp:46-57) or CIC with the reference's
-// weights (include/PMSchemes/emcCICScheme.hpp:126-143)
+// NGP (include/PMSchemes/emcNGPScheme.hpp:46-57), CIC with the reference's
+// weights (include/PMSchemes/emcCICScheme.hpp:126-143), NEC
+// (include/PMSchemes/emcNECScheme.hpp:102-113: the element's two edges along
+// each direction) or NEC-VWD (examples/mosfet2D/NECSchemeVWD.hpp,
+// interpolateForce: nearest column, the edge below only on the last column).
+// Corners outside the grid read 0 (a particle exactly on the far boundary).
 template <class T, int SCHEME>
 __device__ __forceinline__ void interpForce(const DevK &G, const T *Ex, const T *Ey, T x, T y,
                                             T charge, T F[2]) {
-  if (SCHEME == EMCG_PM_NGP) {
+  if (SCHEME == EMCG_PM_NEC || SCHEME == EMCG_PM_NEC_VWD) {
+    int mx, my;
+    if (SCHEME == EMCG_PM_NEC)
+      floorDiv<T>(x, G.hx, G.invhx, mx);
+    else
+      mx = roundIdx<T>(x, G.hx, G.invhx);
+    floorDiv<T>(y, G.hy, G.invhy, my);
+    F[0] = charge * (gridAt(G, Ex, mx, my) + gridAt(G, Ex, mx, my + 1)) / T(2);
+    if (SCHEME == EMCG_PM_NEC_VWD && mx == G.nx - 1)
+      F[1] = charge * gridAt(G, Ey, mx, my);
+    else
+      F[1] = charge * (gridAt(G, Ey, mx, my) + gridAt(G, Ey, mx + 1, my)) / T(2);
+  } else if (SCHEME == EMCG_PM_NGP) {
     int cx = clampi(roundIdx<T>(x, G.hx, G.invhx), 0, G.nx - 1);
     int cy = clampi(roundIdx<T>(y, G.hy, G.invhy), 0, G.ny - 1);
     F[0] = charge * Ex[cy * G.nx + cx];
@@ -551,7 +567,17 @@ __global__ void assignKernel(StateK<T> st, DevK G, const int64_t *__restrict__ n
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n)
     return;
-  if (SCHEME == EMCG_PM_NGP) {
+  if (SCHEME == EMCG_PM_NEC || SCHEME == EMCG_PM_NEC_VWD) {
+    // a quarter to each corner of the element (emcNECScheme.hpp:24-33)
+    int mx, my;
+    floorDiv<T>(st.px[i], G.hx, G.invhx, mx);
+    floorDiv<T>(st.py[i], G.hy, G.invhy, my);
+    const double w = 0.25 * nrC;
+    gridAdd(G, nr, mx, my, w);
+    gridAdd(G, nr, mx + 1, my, w);
+    gridAdd(G, nr, mx, my + 1, w);
+    gridAdd(G, nr, mx + 1, my + 1, w);
+  } else if (SCHEME == EMCG_PM_NGP) {
     int cx = roundIdx<T>(st.px[i], G.hx, G.invhx), cy = roundIdx<T>(st.py[i], G.hy, G.invhy);
     gridAdd(G, nr, cx, cy, nrC);
   } else {
@@ -579,22 +605,35 @@ __global__ void concKernel(DevK G, const double *__restrict__ nr, double *__rest
   conc[i] = c;
 }
 
-// include/PMSchemes/emcEFieldCalculation.hpp:13-30, 58-81
+// The E field of the PM scheme.  NGP, CIC: at the grid points
+// (include/PMSchemes/emcEFieldCalculation.hpp:13-30).  NEC: forward differences
+// on the edges (calcEFieldAtEdgeMidPts, :35-52).  Both then take the boundary
+// values of :58-81 (0 normal to an artificial boundary, else the neighbour).
+// NEC-VWD (examples/mosfet2D/NECSchemeVWD.hpp, calcEField): forward
+// differences, 0 on the last edge, no boundary pass.
 template <class T>
 __global__ void efieldKernel(DevK G, const double *__restrict__ pot, T *__restrict__ Ex,
-                             T *__restrict__ Ey) {
+                             T *__restrict__ Ey, int scheme) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= G.nx * G.ny)
     return;
   const int nx = G.nx, ny = G.ny, x = i % nx, y = i / nx;
+  const bool edges = scheme == EMCG_PM_NEC || scheme == EMCG_PM_NEC_VWD;
   auto ex = [&](int xi) {
     int j = y * nx + xi;
-    return (pot[j - 1] - pot[j + 1]) * G.Vt / (2 * G.hx);
+    return edges ? (pot[j] - pot[j + 1]) * G.Vt / G.hx
+                 : (pot[j - 1] - pot[j + 1]) * G.Vt / (2 * G.hx);
   };
   auto ey = [&](int yi) {
     int j = yi * nx + x;
-    return (pot[j - nx] - pot[j + nx]) * G.Vt / (2 * G.hy);
+    return edges ? (pot[j] - pot[j + nx]) * G.Vt / G.hy
+                 : (pot[j - nx] - pot[j + nx]) * G.Vt / (2 * G.hy);
   };
+  if (scheme == EMCG_PM_NEC_VWD) {
+    Ex[i] = (T)(x != nx - 1 ? ex(x) : 0.);
+    Ey[i] = (T)(y != ny - 1 ? ey(y) : 0.);
+    return;
+  }
   double vx, vy;
   if (x != 0 && x != nx - 1)
     vx = ex(x);
@@ -805,7 +844,8 @@ extern "C" int32_t emcg_device_create(const emcg_model_desc *model, const emcg_d
                  "contact arrays are NULL");
   for (int b = 0; b < 4; b++)
     EMCG_CHECK_ARG(dv->boundary_contact[b], "boundary_contact[%d] is NULL", b);
-  EMCG_CHECK_ARG(cfg->pm_scheme == EMCG_PM_NGP || cfg->pm_scheme == EMCG_PM_CIC, "bad PM scheme");
+  EMCG_CHECK_ARG(cfg->pm_scheme >= EMCG_PM_NGP && cfg->pm_scheme <= EMCG_PM_NEC_VWD,
+                 "bad PM scheme %d", cfg->pm_scheme);
   EMCG_CHECK_ARG(cfg->capacity > 0 && cfg->capacity < (int64_t(1) << 31), "bad capacity");
   EMCG_CHECK_ARG(cfg->dt > 0 && cfg->carriers_per_particle > 0, "bad dt / carriers");
   EMCG_CHECK_ARG(cfg->poisson_max_cycles >= 1 && cfg->poisson_rtol > 0, "bad Poisson settings");
@@ -885,6 +925,8 @@ extern "C" int32_t emcg_device_create(const emcg_model_desc *model, const emcg_d
           e *= 0.5;
         if (y == 0 || y == ny - 1)
           e *= 0.5;
+        if (cfg->round_expected) // examples/mosfet2D/electronVWD.hpp:46-56
+          e = std::round(e);
         d->expNrH[g] = e;
         d->injBound += (int64_t)std::ceil(std::max(e, 0.) / cfg->carriers_per_particle) + 1;
       }
@@ -1025,7 +1067,7 @@ namespace emcg {
 template <class T> static int32_t efieldT(DeviceImpl *d) {
   const int n = d->nx * d->ny;
   efieldKernel<T><<<(n + 255) / 256, 256, 0, d->stream>>>(devK(d), d->dPot, (T *)d->dEx,
-                                                          (T *)d->dEy);
+                                                          (T *)d->dEy, d->cfg.pm_scheme);
   EMCG_CUDA(cudaGetLastError());
   return EMCG_OK;
 }
@@ -1067,13 +1109,21 @@ template <class T> static int32_t moveT(DeviceImpl *d, uint32_t step) {
     if constexpr (sizeof(T) == 8) {
       if (c.pm_scheme == EMCG_PM_NGP)
         EMCG_MOVE(EMCG_PM_NGP, true);
-      else
+      else if (c.pm_scheme == EMCG_PM_CIC)
         EMCG_MOVE(EMCG_PM_CIC, true);
+      else if (c.pm_scheme == EMCG_PM_NEC)
+        EMCG_MOVE(EMCG_PM_NEC, true);
+      else
+        EMCG_MOVE(EMCG_PM_NEC_VWD, true);
     }
   } else if (c.pm_scheme == EMCG_PM_NGP) {
     EMCG_MOVE(EMCG_PM_NGP, false);
-  } else {
+  } else if (c.pm_scheme == EMCG_PM_CIC) {
     EMCG_MOVE(EMCG_PM_CIC, false);
+  } else if (c.pm_scheme == EMCG_PM_NEC) {
+    EMCG_MOVE(EMCG_PM_NEC, false);
+  } else {
+    EMCG_MOVE(EMCG_PM_NEC_VWD, false);
   }
 #undef EMCG_MOVE
   EMCG_CUDA(cudaGetLastError());
@@ -1131,12 +1181,16 @@ template <class T> static int32_t assignT(DeviceImpl *d) {
   const int n = d->nx * d->ny;
   const int nb = (int)((d->capacity + 255) / 256);
   EMCG_CUDA(cudaMemsetAsync(d->dNr, 0, n * sizeof(double), d->stream));
+  const double nrC = d->cfg.carriers_per_particle;
   if (d->cfg.pm_scheme == EMCG_PM_NGP)
     assignKernel<T, EMCG_PM_NGP><<<nb, 256, 0, d->stream>>>(devState<T>(d, d->cur), devK(d), d->dN,
-                                                           d->cfg.carriers_per_particle, d->dNr);
-  else
+                                                           nrC, d->dNr);
+  else if (d->cfg.pm_scheme == EMCG_PM_CIC)
     assignKernel<T, EMCG_PM_CIC><<<nb, 256, 0, d->stream>>>(devState<T>(d, d->cur), devK(d), d->dN,
-                                                           d->cfg.carriers_per_particle, d->dNr);
+                                                           nrC, d->dNr);
+  else
+    assignKernel<T, EMCG_PM_NEC><<<nb, 256, 0, d->stream>>>(devState<T>(d, d->cur), devK(d), d->dN,
+                                                           nrC, d->dNr);
   concKernel<<<(n + 255) / 256, 256, 0, d->stream>>>(devK(d), d->dNr, d->dConc);
   EMCG_CUDA(cudaGetLastError());
   return EMCG_OK;

@@ -21,7 +21,7 @@ from .physics import Material, thermal_voltage
 
 XMIN, XMAX, YMIN, YMAX = range(4)  # emcBoundaryPos (include/emcBoundaryPos.hpp:13-20)
 OHMIC, SCHOTTKY, GATE = L.CONTACT_OHMIC, L.CONTACT_SCHOTTKY, L.CONTACT_GATE
-NGP, CIC = L.PM_NGP, L.PM_CIC
+NGP, CIC, NEC, NEC_VWD = L.PM_NGP, L.PM_CIC, L.PM_NEC, L.PM_NEC_VWD
 
 
 def _dp(a):
@@ -194,6 +194,8 @@ class DeviceSimulation:
         cfg.poisson_rtol = poisson_rtol
         cfg.poisson_smooth = poisson_smooth
         cfg.poisson_fp32 = int(poisson_fp32)
+        # electronVWD rounds both the initial and the expected contact counts
+        cfg.round_expected = int(round_counts)
         self.cfg = cfg
         self.precision = L.FP64 if precision in ("fp64", L.FP64) else L.FP32
         h = C.c_void_p()
