@@ -348,12 +348,15 @@ template <class PH> static void dumpDevState(const char *tag, PH &ph) {
 }
 
 // usage: ref_driver device <resistor|mosfet|resistor_nec|mosfet_vwd> <seed> <dt> <nSteps>
-//                          <accV> <width>
+//                          <accV> <width> [outDir]
 // resistor: NGP, mosfet: CIC, resistor_nec: emcNECScheme, all with emcElectron;
 // mosfet_vwd: the mosfet2D example's NEC-VWD scheme with its electronVWD
+// With outDir, the reference's own writers put their files there after the
+// last step (emcSimulationResults::writeCurrentResults with suffix "Step",
+// emcBasicParticleHandler::print, and writeFinalResults averaged over all steps).
 template <class PM, class PT>
 static int runDeviceT(const std::string &kind, unsigned long seed, double dt, int nSteps,
-                      double acc, double width) {
+                      double acc, double width, const std::string &outDir) {
   using PH = emcBasicParticleHandler<T, Dev2, PM>;
   using Solver = emcSORSolver<T, Dev2, PH>;
   using Sim = emcSimulation<T, Dev2, Solver, PH, PM>;
@@ -387,6 +390,8 @@ static int runDeviceT(const std::string &kind, unsigned long seed, double dt, in
   param.setSeed(seed);
   param.setNrStepsBetweenShowProgress(1000000);
   param.setNrStepsForFinalAvg(1);
+  if (!outDir.empty())
+    param.setNamePrefix(outDir + "/");
   std::unique_ptr<PT> el;
   if constexpr (std::is_same<PT, emcElectron<T, Dev2>>::value)
     el = std::make_unique<PT>(1000, 4., mos);
@@ -459,6 +464,8 @@ static int runDeviceT(const std::string &kind, unsigned long seed, double dt, in
   }
   for (int s = 1; s <= nSteps; s++) {
     sim.performEMCStep(s == 1, false, true);
+    if (!outDir.empty())
+      res.updateAverageCharacteristics();
     char k[48];
     std::snprintf(k, sizeof k, "s%d", s);
     dumpDevState(k, sim.particleHandler);
@@ -478,6 +485,11 @@ static int runDeviceT(const std::string &kind, unsigned long seed, double dt, in
     std::snprintf(k, sizeof k, "cur%d", s);
     rec(k, std::vector<double>(res.current[s - 1][0].begin(), res.current[s - 1][0].end()));
   }
+  if (!outDir.empty()) {
+    res.writeCurrentResults("Step", device);
+    sim.particleHandler.print(param.namePrefix, "Step");
+    res.writeFinalResults(device);
+  }
   return 0;
 }
 
@@ -490,15 +502,16 @@ static int runDevice(int argc, char **argv) {
   int n = std::atoi(argv[5]);
   double acc = std::atof(argv[6]);
   double width = std::atof(argv[7]);
+  std::string out = argc > 8 ? argv[8] : "";
   using El = emcElectron<T, Dev2>;
   if (kind == "mosfet")
-    return runDeviceT<emcCICScheme<T, Dev2>, El>(kind, seed, dt, n, acc, width);
+    return runDeviceT<emcCICScheme<T, Dev2>, El>(kind, seed, dt, n, acc, width, out);
   if (kind == "resistor_nec")
-    return runDeviceT<emcNECScheme<T, Dev2>, El>(kind, seed, dt, n, acc, width);
+    return runDeviceT<emcNECScheme<T, Dev2>, El>(kind, seed, dt, n, acc, width, out);
   if (kind == "mosfet_vwd")
     return runDeviceT<emcNECSchemeVWD<T, Dev2>, electronVWD<T, Dev2>>(kind, seed, dt, n, acc,
-                                                                      width);
-  return runDeviceT<emcNGPScheme<T, Dev2>, El>(kind, seed, dt, n, acc, width);
+                                                                      width, out);
+  return runDeviceT<emcNGPScheme<T, Dev2>, El>(kind, seed, dt, n, acc, width, out);
 }
 
 int main(int argc, char **argv) {

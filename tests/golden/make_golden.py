@@ -188,6 +188,23 @@ def make_device(case):
     print(f"device_{name}: {dev.nx}x{dev.ny} n0={st.n} steps={steps}")
 
 
+def make_output(case, outdir_name):
+    """The reference's own output files after the device case's last step
+    (potential, concentration and E field with suffix "Step", the particle dump,
+    the step-averaged potential and concentration, the current table)."""
+    import shutil
+    import tempfile
+    name, kind, seed, dt, steps, acc, width = case
+    dst = os.path.join(HERE, outdir_name)
+    tmp = tempfile.mkdtemp(prefix="emc_out_")
+    po.run_ref("device", kind, seed, dt, steps, acc, width, tmp)
+    os.makedirs(dst, exist_ok=True)
+    for f in sorted(os.listdir(tmp)):
+        shutil.copy(os.path.join(tmp, f), os.path.join(dst, f))
+    shutil.rmtree(tmp)
+    print(f"{outdir_name}: {sorted(os.listdir(dst))}")
+
+
 def make_mt():
     d = po.run_ref("mt", 5489, 2000)
     np.savez_compressed(os.path.join(HERE, "mt19937_64.npz"), words=d["mt"], canon=d["canon"])
@@ -201,3 +218,5 @@ if __name__ == "__main__":
         make_bulk(c)
     for c in DEVICE_CASES:
         make_device(c)
+    make_output(DEVICE_CASES[0], "output_resistor_ngp")
+    make_output(DEVICE_CASES[3], "output_mosfet_necvwd")

@@ -7,6 +7,7 @@ with the same netto contact counts.  Poisson: the multigrid / defect-correction
 solver against the reference's SOR iteration run to 1e-12 V.
 """
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -273,3 +274,33 @@ def test_step_many_equals_separate_steps(engine):
     for (na, pa, ca), (nb, pb, cb) in zip(*runs):
         assert np.array_equal(na, nb) and ca == cb
         assert np.allclose(pa, pb, rtol=1e-9, atol=1e-9)
+
+
+def test_execute_writes_reference_output_files(engine, tmp_path):
+    """execute() with an output prefix writes the reference's file set: grids
+    with their extent, the particle dump, the current table over the
+    non-transient steps (the same writers are byte-checked against the
+    reference's files in test_results_output.py)."""
+    g = golden(DEVICE_CASES[0])
+    sim, dev, pt = _sim(engine, g, DEVICE_CASES[0], precision="fp32", seed=9)
+    prefix = str(tmp_path / "out") + "/"
+    netto = sim.execute(12, transient_steps=2, steps_for_avg=4, output_prefix=prefix)
+    n = sim.num_particles()
+    sim.close()
+    names = sorted(os.listdir(tmp_path / "out"))
+    assert names == sorted(["PotentialEq.txt", "ElectronsConcEq.txt", "EFieldXEq.txt",
+                            "EFieldYEq.txt", "ElectronsEq.txt", "ElectronsCurrent.txt",
+                            "ElectronsConcAvg.txt", "PotentialAvg.txt", "ElectronsFinal.txt"])
+    for f in ("PotentialEq.txt", "ElectronsConcAvg.txt", "PotentialAvg.txt"):
+        lines = open(tmp_path / "out" / f).read().splitlines()
+        assert lines[0] == f"{dev.nx} {dev.ny}" and len(lines) == dev.ny + 1
+        assert all(len(l.split()) == dev.nx for l in lines[1:])
+    parts = open(tmp_path / "out" / "ElectronsFinal.txt").read().split("\n")
+    assert len(parts) == n + 1 and all(len(p.split()) == 10 for p in parts[1:])
+    cur = np.loadtxt(tmp_path / "out" / "ElectronsCurrent.txt")
+    assert cur.shape == (10, 1 + 2 * len(dev.contacts))
+    nt = netto[2:].astype(np.float64)
+    factor = -1.60219e-19 / float(g["params"][1])
+    expect = np.cumsum(nt, axis=0) / np.arange(1, 11)[:, None] * factor
+    assert np.allclose(cur[:, 1:1 + len(dev.contacts)], nt)
+    assert np.allclose(cur[:, 1 + len(dev.contacts):], expect, rtol=1e-5)

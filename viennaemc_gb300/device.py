@@ -16,6 +16,7 @@ import math
 import numpy as np
 
 from . import _lib as L
+from . import results as R
 from .bulk import ParticleState
 from .physics import Material, thermal_voltage
 
@@ -204,6 +205,12 @@ class DeviceSimulation:
         self.h = h
         self.step_index = 0
         self.netto = []
+        self.transient_steps = 0
+        # emcSimulationResults: averages, netto counts and current per step
+        self.results = R.SimulationResults(
+            device.nx, device.ny, device.getThermalVoltage(), device.material.Ni,
+            self.carriers * particle_type.getCharge() / self.dt,
+            getattr(particle_type, "getName", lambda: "Electrons")())
         self.poisson_info = None
 
     def close(self):
@@ -295,9 +302,15 @@ class DeviceSimulation:
         """include/emcSimulation.hpp:164-193 (non-FMM branch), n_steps times."""
         netto = np.zeros((n_steps, max(self.nc, 1)), np.int32)
         L.check(self._lib.emcg_device_step(self.h, n_steps, self.step_index, _ip(netto)))
-        self.step_index += n_steps
-        self.netto.extend(list(netto[:, :self.nc]))
+        self._record(netto[:, :self.nc])
         return netto[:, :self.nc]
+
+    def _record(self, rows):
+        for r in rows:
+            if self.step_index >= self.transient_steps:  # updateCurrent: non-transient steps
+                self.results.update_current(r)
+            self.netto.append(r)
+            self.step_index += 1
 
     @staticmethod
     def performEMCStepMany(sims, n_steps=1):
@@ -317,14 +330,49 @@ class DeviceSimulation:
         L.check(lib.emcg_device_step_many(hs, len(sims), n_steps, s0, ptrs))
         res = []
         for x, o in zip(sims, outs):
-            x.step_index += n_steps
-            x.netto.extend(list(o[:, :x.nc]))
+            x._record(o[:, :x.nc])
             res.append(o[:, :x.nc])
         return res
 
-    def execute(self, n_steps):
+    def execute(self, n_steps, transient_steps=0, steps_for_avg=0, output_prefix=None):
+        """emcSimulation::execute (include/emcSimulation.hpp:106-127): equilibrium,
+        n_steps steps, the potential and concentration averaged over the last
+        steps_for_avg steps, the current over the steps after transient_steps.
+        With output_prefix the reference's files are written: the "Eq"
+        results, then the current table, averages and the "Final" particles."""
+        self.transient_steps = int(transient_steps)
         self.calcEquilibriumCharacteristics()
-        return self.performEMCStep(n_steps)
+        if output_prefix is not None:
+            R.ensure_dir(output_prefix)
+            self.writeCurrentResultsToFiles(output_prefix, "Eq")
+        steps_for_avg = min(int(steps_for_avg), n_steps)
+        first = n_steps - steps_for_avg
+        if first > 0:
+            self.performEMCStep(first)
+        for _ in range(steps_for_avg):
+            self.performEMCStep(1)
+            self.results.update_average(self.potential, self.concentration)
+        if output_prefix is not None:
+            self.writeFinalResults(output_prefix)
+        return np.array(self.netto[-n_steps:]) if n_steps else np.zeros((0, self.nc), np.int32)
+
+    # ---- output (emcSimulation.hpp:222-230) ---------------------------------------
+    def writeCurrentResultsToFiles(self, prefix, suffix):
+        """Potential, concentration, E field and particles now, as the reference
+        writes them."""
+        self.results.write_current_results(prefix, suffix, self.potential, self.concentration,
+                                           self.get_grid(L.GRID_EX), self.get_grid(L.GRID_EY))
+        self.print(prefix, suffix)
+
+    def writeFinalResults(self, prefix):
+        """Current table, averaged concentration and potential, final particles."""
+        self.results.write_final_results(prefix, self.dt, self.transient_steps * self.dt)
+        self.print(prefix, "Final")
+
+    def print(self, prefix, suffix):
+        """emcBasicParticleHandler::print: the particle dump."""
+        R.write_particles(f"{prefix}{self.results.name}{suffix}.txt", self.device.max_pos,
+                          self.get_state())
 
     def timing(self):
         a, b = C.c_double(), C.c_double()
