@@ -389,6 +389,17 @@ def _device_bench(args, rank):
            "wall_s": wall, "current_A": [float(c) for c in cur]}
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_reference_sor"] = _cpu_sor(dev, sim.potential, sim.concentration)
+    # the same steps with the reference SOR's stopping rule (no update above 1e-4 V)
+    sim.set_poisson(update_tol=1e-4)
+    K2 = max(K // 4, 1)
+    sim.performEMCStep(K2)
+    step2, pois2 = sim.timing()
+    cyc2, sol2 = sim.poisson_counts()
+    out["reference_rule"] = {"steps": K2, "ms_per_step": step2 / K2,
+                             "poisson_ms_per_solve": pois2 / K2,
+                             "poisson_newton_per_solve": cyc2 / max(sol2, 1),
+                             "rule": "stop once a Newton update moves no node by more than "
+                                     "1e-4 V (the reference SOR's rule at its accuracy)"}
     sim.close()
     return out
 

@@ -316,6 +316,10 @@ typedef struct {
                                    whole particles, as electronVWD
                                    (examples/mosfet2D/electronVWD.hpp:46-56) */
   int32_t pad_;
+  double poisson_update_tol;    /* V; > 0: also stop once a Newton update changes
+                                   no node's potential by more than this, the
+                                   reference SOR's rule (emcSORSolver.hpp:25-27,
+                                   190-196); 0: the residual rule only */
 } emcg_device_config;
 
 /* Create a device engine (emcSimulation constructor: particle handler with
@@ -365,6 +369,10 @@ int32_t emcg_device_step_many(emcg_handle **h, int32_t n, int32_t n_steps, uint3
    -1 = leave as is.  *cluster_size (may be NULL) receives the CTAs per
    cluster of the solve in use, 0 for the multi-launch path. */
 int32_t emcg_device_poisson_mode(emcg_handle *h, int32_t mode, int32_t *cluster_size);
+/* Change the Poisson settings of a device engine (negative: keep):
+   relative-residual target, Newton-step limit, update tolerance [V]. */
+int32_t emcg_device_set_poisson(emcg_handle *h, double rtol, int32_t max_cycles,
+                                double update_tol);
 /* Newton / V-cycles and Poisson solves of the last emcg_device_step call. */
 int32_t emcg_device_poisson_counts(emcg_handle *h, int64_t *cycles, int64_t *solves);
 

@@ -304,3 +304,28 @@ def test_execute_writes_reference_output_files(engine, tmp_path):
     expect = np.cumsum(nt, axis=0) / np.arange(1, 11)[:, None] * factor
     assert np.allclose(cur[:, 1:1 + len(dev.contacts)], nt)
     assert np.allclose(cur[:, 1 + len(dev.contacts):], expect, rtol=1e-5)
+
+
+def test_poisson_update_rule_matches_between_paths(engine):
+    """The reference SOR's rule (stop once an update moves no potential by more
+    than 1e-4 V) stops both executions at the same Newton step with the same
+    potential, earlier than the residual rule."""
+    from viennaemc_gb300 import _lib as L
+    g = golden(DEVICE_CASES[1])
+    sim, dev, pt = _sim(engine, g, DEVICE_CASES[1], precision="fp32", poisson_rtol=1e-12,
+                        poisson_max_cycles=200)
+    out = {}
+    for mode in (1, 0):
+        sim.poisson_mode(mode)
+        sim.set_poisson(update_tol=1e-4)
+        sim.set_grid(L.GRID_POTENTIAL, g["pot_eq"])
+        sim.set_grid(L.GRID_CONC, g["conc0"])
+        rel, cyc = sim.poisson(equilibrium=False, reset_bc=True)
+        out[mode] = (cyc, sim.potential)
+        sim.set_poisson(update_tol=0.0)
+        sim.set_grid(L.GRID_POTENTIAL, g["pot_eq"])
+        rel2, cyc2 = sim.poisson(equilibrium=False, reset_bc=True)
+        assert cyc2 > cyc and rel2 <= 1e-12
+    sim.close()
+    assert out[1][0] == out[0][0]
+    assert np.max(np.abs(out[1][1] - out[0][1])) <= 1e-12 * np.abs(out[0][1]).max()

@@ -204,7 +204,7 @@ class DeviceConfig(C.Structure):
                 ("stream", C.c_uint32), ("poisson_max_cycles", C.c_int32),
                 ("poisson_rtol", C.c_double), ("poisson_smooth", C.c_int32),
                 ("poisson_fp32", C.c_int32), ("round_expected", C.c_int32),
-                ("pad_", C.c_int32)]
+                ("pad_", C.c_int32), ("poisson_update_tol", C.c_double)]
 
 
 def _i32p():
@@ -229,6 +229,7 @@ _EXTRA_DECLS.extend([
     ("emcg_device_timing", [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("emcg_device_poisson_counts", [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("emcg_device_poisson_mode", [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
+    ("emcg_device_set_poisson", [C.c_void_p, C.c_double, C.c_int32, C.c_double]),
     ("emcg_device_step_many", [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_uint32,
                                C.POINTER(C.POINTER(C.c_int32))]),
     ("emcg_bulk_set_graph", [C.c_void_p, C.c_int32]),

@@ -1055,6 +1055,7 @@ extern "C" int32_t emcg_device_create(const emcg_model_desc *model, const emcg_d
   }
   if ((s = poissonCreate(d->mg, S, cfg->poisson_fp32 != 0, cfg->poisson_smooth, st)))
     return fail(s);
+  d->mg.updTol = cfg->poisson_update_tol > 0 ? cfg->poisson_update_tol / d->Vt : 0.;
   emcg_handle *h = new emcg_handle();
   h->kind = 2;
   h->dev = d;
@@ -1408,6 +1409,23 @@ extern "C" int32_t emcg_device_poisson_mode(emcg_handle *h, int32_t mode, int32_
     d->mg.useCluster = mode == 1;
   if (cluster_size)
     *cluster_size = d->mg.useCluster ? d->mg.clusterSize : 0;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_device_set_poisson(emcg_handle *h, double rtol, int32_t max_cycles,
+                                           double update_tol) {
+  DeviceImpl *d;
+  EMCG_TRY(devOf(h, &d));
+  if (rtol >= 0) {
+    EMCG_CHECK_ARG(rtol > 0, "rtol must be positive");
+    d->cfg.poisson_rtol = rtol;
+  }
+  if (max_cycles >= 0)
+    d->cfg.poisson_max_cycles = max_cycles;
+  if (update_tol >= 0) {
+    d->cfg.poisson_update_tol = update_tol;
+    d->mg.updTol = update_tol > 0 ? update_tol / d->Vt : 0.;
+  }
   return EMCG_OK;
 }
 

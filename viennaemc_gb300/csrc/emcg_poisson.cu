@@ -630,13 +630,15 @@ __device__ __forceinline__ void cClusterMax2(const CCtx &c, unsigned offRed, dou
   }
 }
 
-// out[0] = final relative residual, out[1] = V-cycles done
+// out[0] = final relative residual, out[1] = Newton steps done, out[2] = 1 if the
+// update rule stopped the solve
 template <class MT>
 __global__ void __launch_bounds__(kClusterThreads, 1)
     poissonClusterKernel(CMG<MT> Mp, double *__restrict__ pot, const double *__restrict__ conc,
                          const double *__restrict__ C, const double *__restrict__ gSum,
                          const double *__restrict__ gV, double hF0, double hF1, double hP,
-                         double rtol, int maxCycles, double *__restrict__ out) {
+                         double rtol, int maxCycles, double updTol,
+                         double *__restrict__ out) {
   extern __shared__ __align__(16) char smem[];
   __shared__ char *sBase[kMaxCluster];
   __shared__ double sh[2 * (kClusterThreads / 32)];
@@ -690,6 +692,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
   cluster.sync();
   double rel = INFINITY, scale = 0.;
   int it = 0;
+  bool stopped = false;
   for (;; it++) {
     // F(phi), Jacobian reaction and FV-scaled right-hand side (nonlinResidualKernel);
     // the scale of the relative residual from the first iteration's state
@@ -772,18 +775,32 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     }
     // clamped Newton update of this CTA's rows (updatePotKernel); the cluster
     // barrier makes the new values visible to the neighbours' next residual
+    double upd = 0.;
     for (int t = threadIdx.x; t < nOwn; t += blockDim.x) {
       const int ly = L0.byNx.div(t), x = t - ly * nx;
       if (cCoef(c, L0, cRowNear<uint8_t>(c, L0, L0.offCls, ly)[x]).fixed != MT(0))
         continue;
-      const double v = (double)cRowNear<MT>(c, L0, L0.offD, ly)[x];
-      pot[(size_t)(p0 + ly) * nx + x] += fmin(kMaxNewtonStep, fmax(-kMaxNewtonStep, v));
+      const double v =
+          fmin(kMaxNewtonStep, fmax(-kMaxNewtonStep, (double)cRowNear<MT>(c, L0, L0.offD, ly)[x]));
+      pot[(size_t)(p0 + ly) * nx + x] += v;
+      upd = fmax(upd, fabs(v));
+    }
+    if (updTol > 0.) {
+      // the maxima of this rule use their own slot (offRed + 16)
+      double none = 0.;
+      cClusterMax2(c, M.offRed + 16, upd, none, sh);
+      if (upd < updTol) {
+        it++;
+        stopped = true;
+        break;
+      }
     }
     cluster.sync();
   }
   if (rank == 0 && threadIdx.x == 0) {
     out[0] = rel;
     out[1] = (double)it;
+    out[2] = stopped ? 1. : 0.;
   }
   cluster.sync(); // no CTA leaves while another may still read its shared memory
 }
@@ -877,7 +894,7 @@ template <class MT> CMG<MT> clusterDesc(const PoissonMG &P, int CL, size_t *byte
     c.pxW = v.pxW;
     c.pyW = v.pyW;
   }
-  M.offRed = take(2 * sizeof(double));
+  M.offRed = take(4 * sizeof(double)); // two slots of two maxima
   *bytes = off;
   return M;
 }
@@ -1221,6 +1238,7 @@ static int32_t solveT(PoissonMG &P, double *pot, const double *conc, bool resetB
   double stats[3] = {0, 0, 0};
   double rel = INFINITY;
   int it = 0;
+  bool updStop = false;
   const bool cluster = P.useCluster && P.clusterSize > 0;
   if (cluster) {
     size_t bytes = 0;
@@ -1229,11 +1247,12 @@ static int32_t solveT(PoissonMG &P, double *pot, const double *conc, bool resetB
     cudaLaunchConfig_t cfg = clusterConfig<MT>(P.clusterSize, bytes, st, &at);
     EMCG_CUDA(cudaLaunchKernelEx(&cfg, poissonClusterKernel<MT>, M, pot, conc, P.C, P.gSum,
                                  conc ? P.gVne : P.gVeq, P.hF[0], P.hF[1], P.hP, rtol, maxCycles,
-                                 P.stats));
-    EMCG_CUDA(cudaMemcpyAsync(stats, P.stats, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+                                 P.updTol, P.stats));
+    EMCG_CUDA(cudaMemcpyAsync(stats, P.stats, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     EMCG_CUDA(cudaStreamSynchronize(st));
     rel = stats[0];
     it = (int)stats[1];
+    updStop = stats[2] != 0.;
   }
   double scale = 0.;
   for (; !cluster && it <= maxCycles; it++) {
@@ -1254,12 +1273,22 @@ static int32_t solveT(PoissonMG &P, double *pot, const double *conc, bool resetB
       vcycle<MT>(P, 0, st);
     updatePotKernel<MT><<<grid, kBlock, 0, st>>>(pot, K0.d, L0.fixed, n, P.stats);
     EMCG_CUDA(cudaGetLastError());
+    if (P.updTol > 0.) {
+      EMCG_CUDA(cudaMemcpyAsync(&stats[2], P.stats + 2, sizeof(double), cudaMemcpyDeviceToHost,
+                                st));
+      EMCG_CUDA(cudaStreamSynchronize(st));
+      if (stats[2] < P.updTol) {
+        it++;
+        updStop = true;
+        break;
+      }
+    }
   }
   if (relRes)
     *relRes = rel;
   if (cycles)
     *cycles = it;
-  if (!(rel <= rtol)) {
+  if (!updStop && !(rel <= rtol)) {
     setError("Poisson: relative residual %.3e after %d V-cycles (target %.1e)", rel, it, rtol);
     return EMCG_ERR_NONCONVERGED;
   }

@@ -74,6 +74,9 @@ struct PoissonMG {
   // a more exact linear solve gains nothing)
   int vcyclesPerNewton = 2;
   double twoCycleRel = 1e-2;
+  // the reference's SOR stopping rule as an alternative: stop once a Newton
+  // update changes no potential by more than updTol (thermal voltages; 0 = off)
+  double updTol = 0.;
   bool fp32 = true;
   double hF[2], hP;
   // single-launch cluster solve: CTAs per cluster (0 = not available for this

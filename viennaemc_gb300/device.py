@@ -168,7 +168,7 @@ class DeviceSimulation:
                  capacity=None, precision="fp64", carriers_per_particle=1.0,
                  potential_init=False, round_counts=False, tau_region_is_valley=False,
                  poisson_rtol=1e-8, poisson_max_cycles=60, poisson_fp32=True, poisson_smooth=2,
-                 stream=0):
+                 stream=0, poisson_update_tol=0.0):
         self._lib = L.lib()
         self.device = device
         self.type = particle_type
@@ -197,6 +197,7 @@ class DeviceSimulation:
         cfg.poisson_fp32 = int(poisson_fp32)
         # electronVWD rounds both the initial and the expected contact counts
         cfg.round_expected = int(round_counts)
+        cfg.poisson_update_tol = float(poisson_update_tol)
         self.cfg = cfg
         self.precision = L.FP64 if precision in ("fp64", L.FP64) else L.FP32
         h = C.c_void_p()
@@ -385,6 +386,14 @@ class DeviceSimulation:
         cs = C.c_int32()
         L.check(self._lib.emcg_device_poisson_mode(self.h, int(mode), C.byref(cs)))
         return cs.value
+
+    def set_poisson(self, rtol=None, max_cycles=None, update_tol=None):
+        """Poisson settings: relative-residual target, Newton-step limit, and the
+        reference SOR's update tolerance in volts (0: off)."""
+        L.check(self._lib.emcg_device_set_poisson(
+            self.h, -1.0 if rtol is None else float(rtol),
+            -1 if max_cycles is None else int(max_cycles),
+            -1.0 if update_tol is None else float(update_tol)))
 
     def poisson_counts(self):
         """(V-cycles, solves) of the last performEMCStep call."""
