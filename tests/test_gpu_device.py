@@ -329,3 +329,19 @@ def test_poisson_update_rule_matches_between_paths(engine):
     sim.close()
     assert out[1][0] == out[0][0]
     assert np.max(np.abs(out[1][1] - out[0][1])) <= 1e-12 * np.abs(out[0][1]).max()
+
+
+def test_initial_particles_beyond_capacity_are_rejected(engine):
+    """A capacity below the device's initial particle count is an argument
+    error with a message, not a silent truncation."""
+    g = golden(DEVICE_CASES[0])
+    sim, dev, pt = _sim(engine, g, DEVICE_CASES[0], precision="fp32")
+    sim.close()
+    from viennaemc_gb300 import device as D
+    small = D.DeviceSimulation(dev, pt, scheme=D.NGP, dt=1e-15, seed=1, capacity=100,
+                               precision="fp32")
+    small.poisson(equilibrium=True, reset_bc=True)
+    with pytest.raises(engine._lib.EmcgError) as ei:
+        small.init_particles()
+    assert ei.value.status == -1 and "capacity" in str(ei.value)
+    small.close()
