@@ -123,7 +123,8 @@ def run_engine(args):
     pt = silicon_model(v, "fp32")
     spec = EnsembleSpec(0, N, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 1234 + rank, 0, 300.0)
     b = BulkBatch([pt], [spec], "fp32")
-    b.set_launch(args.block, per, args.min_blocks)
+    b.set_launch(args.block, per, args.min_blocks,
+                 queued=args.scatter_mode)
     b.init_particles(0)
     # warm-up (untimed)
     b.step(W)
@@ -220,14 +221,16 @@ def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units,
     peak, peak_src = _peaks()
     bpp = BYTES_PER_PARTICLE_STEP["fp32"]
     achieved = bpp * value / 1e9  # algorithmic GB/s (72 B per particle-step)
-    traffic = _profiled_traffic(N)
+    kernel = {0: "lockstep", 1: "block-queued", 2: "warp-asynchronous"}[args.scatter_mode]
+    traffic = _profiled_traffic(N, kernel)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": "bulk Si, 2^20 electrons, 1e6 V/m <100>, dt 1 fs, 5000 steps",
                    "particles": N, "steps_per_launch": per, "block_threads": args.block,
-                   "min_blocks_per_sm": args.min_blocks, "scatter_kernel": "lockstep",
+                   "min_blocks_per_sm": args.min_blocks,
+                   "scatter_kernel": kernel,
                    "l2": "flushed (256 MB write) between timed launches",
                    "observables": "per-step FP64 sums of E, v.dir, count"},
         "e2e": {"value": e2e_units / e2e_s if e2e_units else None, "unit": UNIT,
@@ -552,14 +555,16 @@ def _host_state(v, N):
     return st
 
 
-def _profiled_traffic(n_electrons):
+def _profiled_traffic(n_electrons, kernel):
     """DRAM bytes of one bench launch of the bulk kernel, from the committed
-    ncu capture (bytes per electron per launch, scaled to this launch)."""
+    ncu capture of that kernel (bytes per electron per launch, scaled to this
+    launch); None when no capture of the kernel is committed."""
     p = os.path.join(ROOT, "profiles", "bulk_step_fp32_traffic.json")
     try:
         with open(p) as f:
-            return float(json.load(f)["dram_bytes_per_electron_per_launch"]) * n_electrons
-    except Exception:
+            k = json.load(f)["kernels"][kernel]
+        return float(k["dram_bytes_per_electron_per_launch"]) * n_electrons
+    except (OSError, KeyError, ValueError):
         return None
 
 
@@ -649,9 +654,12 @@ def main(argv=None):
     ap.add_argument("--steps-per-launch", type=int, default=500)
     ap.add_argument("--block", type=int, default=256)
     ap.add_argument("--min-blocks", type=int, default=4, help="register cap variant (1, 3, 4)")
+    ap.add_argument("--scatter-mode", type=int, default=2, choices=(0, 1, 2),
+                    help="step kernel: 0 lockstep, 1 block-queued, 2 warp-asynchronous")
     ap.add_argument("--batch-steps", type=int, default=4000,
                     help="timed steps of the 64-ensemble sweep (0: skip it)")
-    ap.add_argument("--batch-trial", type=int, default=20, help="autotuner steps per shape")
+    ap.add_argument("--batch-trial", type=int, default=50,
+                    help="autotuner steps per shape and pass")
     ap.add_argument("--batch-fp64-steps", type=int, default=400)
     ap.add_argument("--device-steps", type=int, default=1000,
                     help="timed resistor device steps (0: skip the device path)")

@@ -224,13 +224,19 @@ int32_t emcg_last_kernel_ms(emcg_handle *h, double *ms);
 int32_t emcg_set_launch(emcg_handle *h, int32_t block_threads,
                         int32_t steps_per_launch);
 
-/* Tuning: 1 (default) runs the block-queued step kernel (scatter events of a
-   thread block processed together by its first warps), 0 the lockstep
-   kernel (each warp handles its own events).  Both follow the same
+/* Tuning, the step kernel: 0 lockstep (each warp advances its particles
+   step by step and handles their events; the default of the double engine);
+   1 block-queued (the events of a thread block are processed together by its
+   first warps); 2 warp-asynchronous, float only and the float engine's
+   default (each lane runs its particle from event to event across step
+   boundaries, so a warp's lanes process their events together; per-step
+   observables go through a per-warp window).  All follow the same
    per-particle algorithm; replay always uses the lockstep kernel.  In the
    queued kernel the grain free-flight redraw takes its own Philox calls, so
-   its double-precision stream differs from the lockstep kernel and the oracle
-   in that (rare) event only. */
+   its double-precision stream differs from the lockstep kernel and the
+   oracle in that (rare) event only.  The warp-asynchronous kernel adds its
+   per-step sums in float in an order that varies from run to run: particle
+   states are reproducible bit for bit, observables to float rounding. */
 int32_t emcg_set_scatter_mode(emcg_handle *h, int32_t queued);
 
 /* Tuning: register cap of the step kernel, as the minimum number of resident
@@ -243,9 +249,11 @@ int32_t emcg_set_occupancy(emcg_handle *h, int32_t min_blocks_per_sm);
 int32_t emcg_bulk_set_graph(emcg_handle *h, int32_t enable);
 /* Autotuner: runs trial_steps steps (from step0, advancing the ensembles --
    use it as warm-up) with each candidate launch shape (block threads 128 /
-   256, register cap 1 / 3 / 4 resident blocks per SM, lockstep or
-   block-queued scatter) and keeps the fastest.  *steps_used = steps run;
-   outputs may be NULL.  No reference counterpart. */
+   256, register cap 1 / 3 / 4 resident blocks per SM, lockstep,
+   block-queued or, for float, warp-asynchronous scatter), twice: in a
+   forward and then a backward pass over the shapes.  It keeps the shape of
+   least total device time.  *steps_used = steps run (2 x shapes x
+   trial_steps); outputs may be NULL.  No reference counterpart. */
 int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint32_t step0,
                            int32_t *steps_used, int32_t *block_threads, int32_t *min_blocks,
                            int32_t *queued);

@@ -182,8 +182,9 @@ class BulkBatch:
         L.check(self._lib.emcg_bulk_set_graph(self.h, int(enable)))
 
     def autotune(self, trial_steps: int = 50, step0: int | None = None) -> dict:
-        """Time each candidate launch shape on trial_steps steps (they advance
-        the ensembles, like warm-up steps) and keep the fastest."""
+        """Time each candidate launch shape on trial_steps steps, in a forward
+        and a backward pass over the shapes (the steps advance the ensembles,
+        like warm-up steps), and keep the fastest."""
         s0 = self.step_index if step0 is None else int(step0)
         used, blk, mb, q = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
         L.check(self._lib.emcg_bulk_autotune(self.h, int(trial_steps), s0, C.byref(used),

@@ -467,6 +467,178 @@ __global__ void bulkInitKernel(StateK<T> st, const ModelK<T> *__restrict__ model
   st.meta[g] = packMeta(valley, sub, 0);
 }
 
+// ---------------------------------------------------------------------------
+// Warp-asynchronous variant (float, Philox).  In the lockstep kernel nearly
+// every warp holds a particle with an event in a given step, so the warp runs
+// the scatter path with a few lanes active.  Here each lane runs its own
+// particle from event to event: in one iteration it crosses the step
+// boundaries up to its next event (free flight to the end of the step, the
+// end-of-step bookkeeping, its observables), then the lanes process their
+// events together.  The physics and the random numbers are those of the
+// lockstep kernel: the same free flights, the Philox counter (pid, step, call)
+// restarted at each step, the grain timer at each step end.
+// Observables: a lane writes its per-step values into its own column of a
+// small per-warp window; once every lane of the warp has passed a step, the
+// warp folds that row into the block's float step sums (shared memory), which
+// go to the device's double sums at the end of the launch.  A lane runs at
+// most kAsyncWindow steps ahead of the slowest lane of its warp.
+// ---------------------------------------------------------------------------
+constexpr int kAsyncWindow = 8;
+
+__host__ __device__ constexpr size_t asyncSmemBytes(int nWarps, int nSteps, int Q) {
+  return (size_t)nSteps * Q * sizeof(float) +
+         (size_t)nWarps * kAsyncWindow * 32 * (2 * sizeof(float) + 1);
+}
+// steps per launch whose block sums fit beside the windows in 64 KB
+inline int asyncMaxSteps(int nWarps, int Q) {
+  const long rest = 65536 - (long)nWarps * kAsyncWindow * 32 * (2 * (long)sizeof(float) + 1);
+  return (int)std::max(1L, rest / (long)(Q * sizeof(float)));
+}
+
+
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB)
+    bulkStepAsyncKernel(StateK<float> st, const ModelK<float> *__restrict__ models,
+                        const EnsK<float> *__restrict__ ens, const Tile *__restrict__ tiles,
+                        int nSteps, uint32_t step0, int chunk, int nVmax,
+                        double *__restrict__ obs, int *__restrict__ err) {
+  using T = float;
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  const int Q = nVmax * 3;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nWarps = blockDim.x >> 5;
+  float *bins = reinterpret_cast<float *>(smemRaw); // [nSteps][Q] block sums
+  float *winE = bins + (size_t)nSteps * Q + (size_t)warp * kAsyncWindow * 64; // [W][32]
+  float *winD = winE + kAsyncWindow * 32;                                    // [W][32]
+  uint8_t *winVal = reinterpret_cast<uint8_t *>(bins + (size_t)nSteps * Q +
+                                                (size_t)nWarps * kAsyncWindow * 64) +
+                    warp * kAsyncWindow * 32; // [W][32]
+  for (int i = threadIdx.x; i < nSteps * Q; i += blockDim.x)
+    bins[i] = 0.f;
+  __syncthreads();
+  const Tile tl = tiles[blockIdx.x];
+  const EnsK<T> &EK = ens[tl.ens];
+  const ModelK<T> &M = models[EK.model];
+  const int nV = EK.nV;
+  const int64_t gi = tl.begin + threadIdx.x;
+  const bool active = gi < tl.end;
+  const uint32_t pid = (uint32_t)(gi - EK.begin);
+  const T dt = EK.dt;
+
+  T k[3] = {0, 0, 0}, pos[3] = {0, 0, 0}, kN[3] = {0, 0, 0}, E = 0, tau = 0, gtau = 0;
+  int valley = 0, sub = 0, region = 0;
+  if (active) {
+    k[0] = st.kx[gi];
+    k[1] = st.ky[gi];
+    k[2] = st.kz[gi];
+    pos[0] = st.px[gi];
+    pos[1] = st.py[gi];
+    pos[2] = st.pz[gi];
+    E = st.E[gi];
+    tau = st.tau[gi];
+    gtau = st.gtau[gi];
+    uint32_t mt = st.meta[gi];
+    valley = mt & 0xff;
+    sub = (mt >> 8) & 0xff;
+    region = mt >> 16;
+  }
+  bool live = active;    // false once the particle has failed
+  int s = live ? 0 : nSteps; // the step the particle is in
+  T tIn = 0;             // time already spent inside step s
+  int nEv = 0;           // events in step s (bounded)
+  int myErr = 0;
+  PhiloxSrc<T> rng;
+  rng.init(pid, step0, EK.stream, EK.key0, EK.key1);
+  int flushed = 0; // steps folded into the block sums
+  while (true) {
+    const int sMin = __reduce_min_sync(0xffffffffu, s);
+    for (; flushed < sMin; flushed++) {
+      const int slot = (flushed % kAsyncWindow) * 32 + lane;
+      for (int v = 0; v < nV; v++) {
+        const bool in = live && winVal[slot] == v;
+        const T e = warpSum(in ? winE[slot] : T(0));
+        const T d = warpSum(in ? winD[slot] : T(0));
+        const unsigned c = __popc(__ballot_sync(0xffffffffu, in));
+        if (lane == 0) {
+          float *b = bins + (size_t)flushed * Q + v * 3;
+          atomicAdd(b + 0, e);
+          atomicAdd(b + 1, d);
+          atomicAdd(b + 2, (float)c);
+        }
+      }
+    }
+    if (sMin >= nSteps)
+      break;
+    const int limit = min(nSteps, flushed + kAsyncWindow);
+    if (s < limit) {
+      // step ends before the next event (bulkParticleStep without an event)
+      while (s < limit && !(tau < dt - tIn)) {
+        const T rem = dt - tIn;
+        driftBulk(M.v[valley], sub, EK.fv[valley][sub], rem, k, E, pos, kN, EK.box);
+        tau -= rem;
+        gtau -= dt;
+        if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
+          gtau = -m_log(rng.ulog()) * M.grainTau;
+        const ValleyK<T> &V = M.v[valley];
+        const T *g = EK.g[valley][sub];
+        const T npf = m_sqrt(T(1) + T(4) * V.alpha * gammaOf(V, E));
+        const int slot = (s % kAsyncWindow) * 32 + lane;
+        winE[slot] = E;
+        winD[slot] = m_div(V.cX * (g[0] * kN[0] + g[1] * kN[1] + g[2] * kN[2]), npf);
+        winVal[slot] = (uint8_t)valley;
+        s++;
+        tIn = T(0);
+        nEv = 0;
+        rng.init(pid, step0 + (uint32_t)s, EK.stream, EK.key0, EK.key1);
+      }
+      // the event inside step s: free flight to it, scattering, new free flight
+      if (s < limit) {
+        int e = 0;
+        if (++nEv > kMaxScatterPerStep) {
+          e = EMCG_ERR_TIMEOUT;
+        } else {
+          driftBulk(M.v[valley], sub, EK.fv[valley][sub], tau, k, E, pos, kN, EK.box);
+          tIn += tau;
+          e = scatterParticle(M, k, E, valley, sub, region, rng);
+          if (!e)
+            tau = -m_log(rng.ulog()) * tauOf(M, valley, region);
+        }
+        if (e) {
+          myErr = e;
+          live = false;
+          s = nSteps;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  double *obsE = obs + (size_t)tl.ens * nSteps * Q;
+  for (int i = threadIdx.x; i < nSteps * Q; i += blockDim.x)
+    if (bins[i] != 0.f)
+      atomicAdd(&obsE[i], (double)bins[i]);
+  if (active) {
+    st.kx[gi] = k[0];
+    st.ky[gi] = k[1];
+    st.kz[gi] = k[2];
+    st.px[gi] = pos[0];
+    st.py[gi] = pos[1];
+    st.pz[gi] = pos[2];
+    st.E[gi] = E;
+    st.tau[gi] = tau;
+    st.gtau[gi] = gtau;
+    st.meta[gi] = packMeta(valley, sub, region);
+  }
+  recordError(err, myErr);
+}
+
+// dynamic shared memory above the default 48 KB needs the kernel's opt-in
+template <int MINB> int32_t asyncSmemOptIn(size_t bytes) {
+  if (bytes <= 48 * 1024)
+    return EMCG_OK;
+  EMCG_CUDA(cudaFuncSetAttribute(bulkStepAsyncKernel<MINB>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return EMCG_OK;
+}
+
 // drift() known-answer kernel: independent particles, per-particle force/dt
 template <class T>
 __global__ void driftKatKernel(const ModelK<T> *__restrict__ models, int valley, int64_t n,
@@ -685,6 +857,15 @@ static void dropGraph(BulkImpl *b) {
 // the step kernel of the current launch configuration (Philox streams)
 template <class T> static void *stepKernelFn(const BulkImpl *b, bool *queued) {
   *queued = b->queued != 0;
+  if constexpr (sizeof(T) == 4) {
+    if (b->queued == 2) {
+      if (b->minBlocks >= 4 && b->blockThreads <= 256)
+        return (void *)bulkStepAsyncKernel<4>;
+      if (b->minBlocks == 3 && b->blockThreads <= 256)
+        return (void *)bulkStepAsyncKernel<3>;
+      return (void *)bulkStepAsyncKernel<1>;
+    }
+  }
   if (b->queued) {
     if (b->minBlocks >= 4 && b->blockThreads <= 256)
       return (void *)bulkStepQueuedKernel<T, 4>;
@@ -746,8 +927,13 @@ template <class T> static int32_t graphFor(BulkImpl *b, int ns, size_t smem, siz
   kp.func = fn;
   kp.gridDim = dim3(b->nTiles, 1, 1);
   kp.blockDim = dim3(b->blockThreads, 1, 1);
-  kp.sharedMemBytes = (unsigned)(queued ? qsmem : smem);
+  kp.sharedMemBytes = (unsigned)(b->queued == 2 && sizeof(T) == 4
+                                      ? asyncSmemBytes(b->blockThreads / 32, ns, b->nVmax * 3)
+                                      : (queued ? qsmem : smem));
   kp.kernelParams = b->gParams;
+  if (kp.sharedMemBytes > 48 * 1024) // above the default needs the kernel's opt-in
+    EMCG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kp.sharedMemBytes));
   EMCG_CUDA(cudaGraphAddKernelNode(&b->gKernel, b->graph, &mn, 1, &kp));
   EMCG_CUDA(cudaGraphInstantiate(&b->gexec, b->graph, 0));
   b->gNs = ns;
@@ -765,6 +951,9 @@ static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHos
   int per = b->stepsPerLaunch > 0 ? b->stepsPerLaunch : nSteps;
   if (b->replay)
     per = 1;
+  const bool async = b->queued == 2 && sizeof(T) == 4 && !b->replay;
+  if (async) // the block's step sums live in shared memory
+    per = std::min(per, asyncMaxSteps(b->blockThreads / 32, Q));
   size_t need = (size_t)b->nEns * per * Q;
   if (need > b->obsCap) {
     dropGraph(b); // it holds the old buffer
@@ -798,6 +987,23 @@ static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHos
             bulkStepKernel<T, true, 1><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
                 st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dWords,
                 b->dOff, b->dErr);
+        } else if (async) {
+          if constexpr (sizeof(T) == 4) {
+            const size_t asmem = asyncSmemBytes(b->blockThreads / 32, ns, Q);
+            if (b->minBlocks >= 4 && b->blockThreads <= 256) {
+              EMCG_TRY(asyncSmemOptIn<4>(asmem));
+              bulkStepAsyncKernel<4><<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
+                  st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
+            } else if (b->minBlocks == 3 && b->blockThreads <= 256) {
+              EMCG_TRY(asyncSmemOptIn<3>(asmem));
+              bulkStepAsyncKernel<3><<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
+                  st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
+            } else {
+              EMCG_TRY(asyncSmemOptIn<1>(asmem));
+              bulkStepAsyncKernel<1><<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
+                  st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
+            }
+          }
         } else if (b->queued) {
           const size_t qsmem = ((smem + 15) & ~size_t(15)) + blockStateBytes<T>(b->blockThreads);
           if (b->minBlocks >= 4 && b->blockThreads <= 256)
@@ -902,9 +1108,10 @@ extern "C" int32_t emcg_bulk_create(const emcg_model_desc *models, int32_t n_mod
   }
   BulkImpl *b = new BulkImpl();
   b->precision = precision;
-  // defaults measured on GB300: the float engine runs the block-queued kernel
-  // with a 3-blocks-per-SM register cap, the double engine the lockstep one
-  b->queued = 0;
+  // defaults measured on GB300: the float engine runs the warp-asynchronous
+  // kernel with a 4-blocks-per-SM register cap, the double engine the
+  // lockstep kernel without a cap
+  b->queued = precision == EMCG_FP32 ? 2 : 0;
   b->minBlocks = precision == EMCG_FP32 ? 4 : 1;
   b->tsz = precision == EMCG_FP64 ? 8 : 4;
   b->nModels = n_models;
@@ -1182,7 +1389,9 @@ extern "C" int32_t emcg_last_kernel_ms(emcg_handle *h, double *ms) {
 extern "C" int32_t emcg_set_scatter_mode(emcg_handle *h, int32_t queued) {
   BulkImpl *b;
   EMCG_TRY(bulkOf(h, &b));
-  EMCG_CHECK_ARG(queued == 0 || queued == 1, "queued must be 0 or 1");
+  EMCG_CHECK_ARG(queued >= 0 && queued <= 2, "scatter mode must be 0, 1 or 2");
+  EMCG_CHECK_ARG(queued != 2 || b->precision == EMCG_FP32,
+                 "the warp-asynchronous kernel (mode 2) is float only");
   b->queued = queued;
   return EMCG_OK;
 }
@@ -1231,19 +1440,25 @@ extern "C" int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint3
   EMCG_CHECK_ARG(trial_steps > 0, "trial_steps must be positive");
   EMCG_CHECK_ARG(!b->replay, "autotuning runs Philox steps; clear replay first");
   // launch shapes: block threads x register cap (resident blocks per SM) x
-  // scatter scheme; each runs trial_steps steps (advancing the ensembles) and
-  // the fastest device time wins
+  // scatter scheme.  Each runs trial_steps steps (advancing the ensembles)
+  // twice, once in a forward and once in a backward pass over the shapes, so
+  // that the ensembles' warming up from the initial distribution (events get
+  // more frequent) weighs on every shape alike; the least total device time
+  // wins
   struct Cand {
     int block, minb, queued;
   };
-  const Cand cands[] = {{256, 4, 0}, {256, 3, 0}, {256, 1, 0}, {128, 4, 0},
-                        {128, 1, 0}, {256, 4, 1}, {256, 3, 1}, {128, 4, 1}};
+  const Cand cands[] = {{256, 4, 0}, {256, 3, 0}, {256, 1, 0}, {128, 4, 0}, {128, 1, 0},
+                        {256, 4, 1}, {256, 3, 1}, {128, 4, 1}, {256, 4, 2}, {256, 3, 2},
+                        {128, 4, 2}};
+  const int nCands = b->precision == EMCG_FP32 ? 11 : 8; // mode 2 is float only
   const int keepPer = b->stepsPerLaunch;
   b->stepsPerLaunch = trial_steps;
-  double best = INFINITY;
-  Cand bestC = {b->blockThreads, b->minBlocks, b->queued};
+  double ms[11] = {};
   uint32_t s = step0;
-  for (const Cand &c : cands) {
+  for (int pass = 0; pass < 2 * nCands; pass++) {
+    const int ci = pass < nCands ? pass : 2 * nCands - 1 - pass;
+    const Cand &c = cands[ci];
     if (c.block != b->blockThreads)
       b->tilesDirty = true;
     b->blockThreads = c.block;
@@ -1256,11 +1471,13 @@ extern "C" int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint3
       b->stepsPerLaunch = keepPer;
       return st;
     }
-    if (b->lastMs < best) {
-      best = b->lastMs;
-      bestC = c;
-    }
+    ms[ci] += b->lastMs;
   }
+  int bi = 0;
+  for (int ci = 1; ci < nCands; ci++)
+    if (ms[ci] < ms[bi])
+      bi = ci;
+  const Cand bestC = cands[bi];
   if (bestC.block != b->blockThreads)
     b->tilesDirty = true;
   b->blockThreads = bestC.block;
