@@ -279,6 +279,26 @@ def sweep_specs(seed=2024):
     return temps, specs
 
 
+def _rate_rebuild_timing(b, models, reps=50):
+    """reinitScatterTables on the GPU from rates already in device memory:
+    host wall time per model rebuild (the call, the stream-ordered kernel),
+    averaged over reps rebuilds of every model, the stream drained at the end."""
+    import torch
+    raws = [torch.tensor(m.raw_rates(), dtype=torch.float64, device="cuda") for m in models]
+    b.get_rates(0)  # drains the handle's stream
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        for mi, r in enumerate(raws):
+            b.reinit_scatter_tables(mi, r)
+    b.get_rates(0)
+    us = (time.perf_counter() - t0) / (reps * len(raws)) * 1e6
+    h = models[0].scatterHandler
+    return {"us_per_model": us, "tables": sum(len(v) for v in h.table_mechs.values()),
+            "levels": h.n_levels, "source": "device rates (CUDA tensor)",
+            "timing": "host wall clock, call + kernel, %d rebuilds of %d models" %
+                      (reps, len(raws))}
+
+
 def _batched_bench(args, rank):
     """The velocity-field sweep in one launch per chunk of steps: FP32 state,
     autotuned launch shape, CUDA-graph replay; the plain FP64 engine on the same
@@ -305,6 +325,7 @@ def _batched_bench(args, rank):
         obs.append(b.step(ns))
         ms += b.last_kernel_ms()
         done += ns
+    rebuild = _rate_rebuild_timing(b, models)
     b.close()
     value = ntot * K / (ms / 1e3)
     out = {"workload": "64 bulk Si ensembles: <100>,<111> x 77/200/300/400 K x 8 fields "
@@ -312,7 +333,8 @@ def _batched_bench(args, rank):
            "ensembles": len(specs), "particles_total": ntot, "steps": K, "value": value,
            "unit": UNIT, "ms_per_step": ms / K, "autotune": tuned, "graph_replay": True,
            "steps_per_launch": args.steps_per_launch,
-           "l2": "working set larger than L2 (%.0f MB of particle state)" % (ntot * 40 / 1e6)}
+           "l2": "working set larger than L2 (%.0f MB of particle state)" % (ntot * 40 / 1e6),
+           "rate_rebuild": rebuild}
     if args.batch_fp64_steps > 0:
         # plain FP64 engine on the same batch from the same seeds: speed and v_d
         k64 = args.batch_fp64_steps

@@ -258,6 +258,31 @@ int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint32_t step0,
                            int32_t *steps_used, int32_t *block_threads, int32_t *min_blocks,
                            int32_t *queued);
 
+/* ---- rate-table rebuild (include/emcScatterHandler.hpp:100-108) -------- */
+/* emcScatterHandler::reinitScatterTables for model `model` of a bulk
+   handle, or of a device handle (model 0): the caller refills the rates --
+   getScatterRate at (level + 1) dE of every table (fillScatterTables,
+   :220-235), for instance after a phonon bath changed them -- and the GPU
+   renormalises them (renormalizeTables, :248-273): cumulative sums in table
+   order, their maximum Gmax over levels, tables / Gmax and tau = 1 / Gmax,
+   in double, stored in the handle's precision in place of the old tables.
+   raw: per table set in the model's order, n_tables x n_levels doubles,
+   table-major (the layout of emcg_model_desc.tables before
+   normalisation); the table sets, their mechanisms and the level grid stay
+   those of the model.  raw_on_device == 0: host memory, checked (finite
+   rates, positive Gmax) before anything is launched.  raw_on_device != 0:
+   device memory of the handle's device, complete when the call is made and
+   unchanged until the next step call returns; a set with a non-finite rate
+   or Gmax <= 0 is left as it was and the next step call returns
+   EMCG_ERR_ARG.  The rebuild is ordered on the handle's stream before the
+   next step (graph replay included); the call does not wait for it. */
+int32_t emcg_update_rates(emcg_handle *h, int32_t model, const double *raw,
+                          int32_t raw_on_device);
+/* The handle's current tables of model `model`, converted to double, in the
+   layout of emcg_update_rates' raw (NULL to skip), and tau_max per table set
+   (n_tablesets doubles, NULL to skip).  Waits for the handle's stream. */
+int32_t emcg_get_rates(emcg_handle *h, int32_t model, double *tables, double *tau);
+
 /* ---- single-particle kernels (known-answer tests of the reference) ----- */
 /* drift() of include/emcParticleDrift.hpp:11-36 for n independent
    particles of valley v of model 0: k, pos (3 x n, SoA) and energy in/out,

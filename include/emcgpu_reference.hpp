@@ -174,6 +174,20 @@ public:
     return d_;
   }
 
+  // The rates of every table refilled now from the reference mechanisms
+  // (fillScatterTables, include/emcScatterHandler.hpp:220-235), in the table
+  // sets' order of desc(), table-major: what emcg_update_rates takes after a
+  // dynamic mechanism (e.g. one reading an emcPhononBath) changed.
+  std::vector<double> rawRates() const {
+    const T dE = maxE_ / nL_;
+    std::vector<double> raw;
+    for (auto &[key, idx] : sets_of_)
+      for (size_t j = 0; j < idx.size(); j++)
+        for (SizeType l = 0; l < nL_; l++)
+          raw.push_back((double)ptrs_[idx[j]]->getScatterRate((l + 1) * dE, key.second));
+    return raw;
+  }
+
   ParticleType &particleType() { return pt_; }
 
 private:
@@ -275,6 +289,14 @@ public:
   ~GpuBulkParticleHandler() { emcg_destroy(h_); }
   GpuBulkParticleHandler(const GpuBulkParticleHandler &) = delete;
   GpuBulkParticleHandler &operator=(const GpuBulkParticleHandler &) = delete;
+
+  // particleType.reinitScatterTables() (include/emcScatterHandler.hpp:100-108)
+  // on the GPU: rates refilled from the reference mechanisms, renormalised by
+  // the engine before the next move
+  void reinitScatterTables() {
+    const std::vector<double> raw = model_.rawRates();
+    check(emcg_update_rates(h_, 0, raw.data(), 0));
+  }
 
   void resetAppliedFieldStrength(T f) { // :135-137
     for (int i = 0; i < 3; i++)
@@ -418,6 +440,14 @@ public:
     const emcg_model_desc &md = model.desc();
     check(emcg_device_create(&md, &dd_.desc(), &cfg, precision, &h_));
     nc_ = dd_.desc().n_contacts;
+    model_ = &model;
+  }
+
+  // the particle type's reinitScatterTables() (include/emcScatterHandler.hpp:
+  // 100-108) on the GPU, before the next performEMCStep
+  void reinitScatterTables() {
+    const std::vector<double> raw = model_->rawRates();
+    check(emcg_update_rates(h_, 0, raw.data(), 0));
   }
   ~GpuDeviceSimulation() { emcg_destroy(h_); }
   GpuDeviceSimulation(const GpuDeviceSimulation &) = delete;
@@ -456,6 +486,7 @@ public:
 
 private:
   DeviceDesc<T, DeviceType> dd_;
+  ModelBuilder<T, DeviceType> *model_ = nullptr;
   emcg_handle *h_ = nullptr;
   int nc_ = 0;
   uint32_t step_ = 0;

@@ -435,6 +435,39 @@ static double scatter_rate(const oc_model *m, const oc_mech *me, double E,
   return 0;
 }
 
+/* include/emcScatterHandler.hpp:248-273: cumulative sums in table order
+   (std::transform with std::plus, :256-261), the maximum of the last row
+   (:264-265), every table divided by it (:267-270), tau = 1 / maximum (:271). */
+static void renormalize_set(oc_model *m, int v, int r) {
+  int L = m->nLevels, nT = m->tsN[v][r];
+  if (nT == 0) {
+    m->tau[v][r] = 2e-15;
+    return;
+  }
+  double *nt = m->norm[v][r];
+  memcpy(nt, m->raw[v][r], sizeof(double) * (size_t)nT * L);
+  for (int t = 1; t < nT; t++)
+    for (int l = 0; l < L; l++)
+      nt[t * L + l] = nt[t * L + l] + nt[(t - 1) * L + l];
+  double mx = nt[(nT - 1) * L];
+  for (int l = 1; l < L; l++)
+    if (mx < nt[(nT - 1) * L + l])
+      mx = nt[(nT - 1) * L + l];
+  for (int i = 0; i < nT * L; i++)
+    nt[i] /= mx;
+  m->tau[v][r] = 1. / mx;
+}
+
+/* include/emcScatterHandler.hpp:100-108 (reinitScatterTables) with the
+   refilled rates supplied by the caller: nT x nLevels doubles, table-major. */
+int32_t oc_set_raw_tables(oc_model *m, int32_t v, int32_t r, const double *raw) {
+  if (oc_n_tables(m, v, r) < 0 || !m->built)
+    return -1;
+  memcpy(m->raw[v][r], raw, sizeof(double) * (size_t)m->tsN[v][r] * m->nLevels);
+  renormalize_set(m, v, r);
+  return 0;
+}
+
 /* include/emcScatterHandler.hpp:220-235 (fill) and :248-273 (renormalize) */
 int32_t oc_build_tables(oc_model *m) {
   int L = m->nLevels;
@@ -452,22 +485,7 @@ int32_t oc_build_tables(oc_model *m) {
         for (int l = 0; l < L; l++)
           m->raw[v][r][t * L + l] = scatter_rate(m, me, (l + 1) * m->dE, r);
       }
-      if (nT == 0) {
-        m->tau[v][r] = 2e-15;
-        continue;
-      }
-      double *nt = m->norm[v][r];
-      memcpy(nt, m->raw[v][r], sizeof(double) * (size_t)nT * L);
-      for (int t = 1; t < nT; t++)
-        for (int l = 0; l < L; l++)
-          nt[t * L + l] = nt[t * L + l] + nt[(t - 1) * L + l];
-      double mx = nt[(nT - 1) * L];
-      for (int l = 1; l < L; l++)
-        if (mx < nt[(nT - 1) * L + l])
-          mx = nt[(nT - 1) * L + l];
-      for (int i = 0; i < nT * L; i++)
-        nt[i] /= mx;
-      m->tau[v][r] = 1. / mx;
+      renormalize_set(m, v, r);
     }
   m->built = 1;
   return 0;

@@ -107,6 +107,9 @@ int32_t oc_add_mech(oc_model *m, int32_t kind, int32_t valley,
                     int32_t nRegions);
 int32_t oc_set_region_doping(oc_model *m, int32_t region, double doping);
 int32_t oc_build_tables(oc_model *m);
+/* replace the rates of one built (valley, region) table set and
+   renormalise it (reinitScatterTables with caller-filled rates) */
+int32_t oc_set_raw_tables(oc_model *m, int32_t valley, int32_t region, const double *raw);
 int32_t oc_get_raw_table(const oc_model *m, int32_t valley, int32_t region,
                          int32_t idxTable, double *out);
 int32_t oc_get_norm_table(const oc_model *m, int32_t valley, int32_t region,

@@ -70,6 +70,8 @@ def _declare(L):
     for fn in ("oc_get_raw_table", "oc_get_norm_table"):
         getattr(L, fn).restype = i32
         getattr(L, fn).argtypes = [vp, i32, i32, i32, P(d)]
+    L.oc_set_raw_tables.restype = i32
+    L.oc_set_raw_tables.argtypes = [vp, i32, i32, P(d)]
     L.oc_n_tables.restype = i32
     L.oc_n_tables.argtypes = [vp, i32, i32]
     L.oc_table_mech.restype = i32
@@ -266,6 +268,12 @@ class Model:
         assert lib().oc_get_norm_table(self.h, valley, region, t, dptr(out)) == 0
         return out
 
+    def set_raw_tables(self, valley, region, raw):
+        """reinitScatterTables with the rates raw (n_tables x n_levels)."""
+        a = np.ascontiguousarray(np.asarray(raw, np.float64).reshape(-1))
+        assert a.size == self.n_tables(valley, region) * self.n_levels
+        assert lib().oc_set_raw_tables(self.h, valley, region, dptr(a)) == 0
+
     def tau(self, valley, region):
         return lib().oc_get_tau(self.h, valley, region)
 
@@ -364,7 +372,7 @@ def parse_ref(text: str) -> dict:
             continue
         key, n = parts[0], int(parts[1])
         vals = parts[2:2 + n]
-        if key.startswith("name_"):
+        if key.startswith("name_") or "_name_v" in key:
             out[key] = vals[0] if vals else ""
         elif vals and (vals[0].startswith("0x") or vals[0].startswith("-0x")
                        or "p" in vals[0] or vals[0] in ("inf", "-inf", "nan")):

@@ -38,6 +38,8 @@
 #include <ScatterMechanisms/emcFirstOrderInterValleyScatterMechanism.hpp>
 #include <ScatterMechanisms/emcZeroOrderInterValleyScatterMechanism.hpp>
 #include <ValleyTypes/emcNonParabolicAnistropValley.hpp>
+#include <ScatterMechanisms/emcHotPhononFroehlichMechanism.hpp>
+#include <emcPhononBath.hpp>
 #include <PMSchemes/emcCICScheme.hpp>
 #include <PMSchemes/emcNECScheme.hpp>
 #include <PMSchemes/emcNGPScheme.hpp>
@@ -150,7 +152,7 @@ static emcMaterial<T> silicon() {
   return emcMaterial<T>{11.8, 2329., 1.45e16, 9040., 1.15};
 }
 
-template <class PT> static void dumpTablesOf(PT &pt) {
+template <class PT> static void dumpTablesOf(PT &pt, const char *prefix = "") {
   auto &h = pt.scatterHandler;
   for (auto &[key, tables] : h.scatterTables) {
     auto v = std::get<0>(key), r = std::get<1>(key);
@@ -161,15 +163,16 @@ template <class PT> static void dumpTablesOf(PT &pt) {
       for (SizeType l = 0; l < h.nrEnergyLevels; l++)
         raw[l] = mech->getScatterRate((l + 1) * h.dE, r);
       char key1[96], key2[96];
-      std::snprintf(key1, sizeof key1, "raw_v%zu_r%zu_t%zu", (size_t)v, (size_t)r, t);
-      std::snprintf(key2, sizeof key2, "norm_v%zu_r%zu_t%zu", (size_t)v, (size_t)r, t);
+      std::snprintf(key1, sizeof key1, "%sraw_v%zu_r%zu_t%zu", prefix, (size_t)v, (size_t)r, t);
+      std::snprintf(key2, sizeof key2, "%snorm_v%zu_r%zu_t%zu", prefix, (size_t)v, (size_t)r,
+                    t);
       rec(key1, raw);
       rec(key2, tables[t]);
-      std::printf("name_v%zu_r%zu_t%zu 1 %s\n", (size_t)v, (size_t)r, t,
+      std::printf("%sname_v%zu_r%zu_t%zu 1 %s\n", prefix, (size_t)v, (size_t)r, t,
                   mech->getName().c_str());
     }
     char kt[64];
-    std::snprintf(kt, sizeof kt, "tau_v%zu_r%zu", (size_t)v, (size_t)r);
+    std::snprintf(kt, sizeof kt, "%stau_v%zu_r%zu", prefix, (size_t)v, (size_t)r);
     rec(kt, {h.getTau(r, v)});
   }
 }
@@ -514,6 +517,46 @@ static int runDevice(int argc, char **argv) {
   return runDeviceT<emcNGPScheme<T, Dev2>, El>(kind, seed, dt, n, acc, width, out);
 }
 
+// reinitScatterTables with rates that change: acoustic scattering and the
+// hot-phonon Froehlich absorption / emission pair sharing one emcPhononBath
+// (include/ScatterMechanisms/emcHotPhononFroehlichMechanism.hpp,
+// include/emcPhononBath.hpp).  The tables are dumped after initScatterTables
+// ("init_"), then the bath records emissions over its q range and is advanced
+// by dt, the tables are rebuilt, and dumped again ("re_").
+// args: nLevels maxE nEmissions dt
+static int runReinit(int argc, char **argv) {
+  if (argc < 6)
+    return 2;
+  const int nLevels = std::atoi(argv[2]);
+  const double maxE = std::atof(argv[3]);
+  const int nEm = std::atoi(argv[4]);
+  const double dtBath = std::atof(argv[5]);
+  const double temp = 300.;
+  std::array<T, 3> maxPos = {1e-7, 1e-7, 1e-7}, spacing = {1e-8, 1e-8, 1e-8};
+  Dev3 device{silicon(), maxPos, spacing, temp};
+  auto el = std::make_unique<emcElectron<T, Dev3>>(nLevels, maxE, false);
+  addValley(el, 0.19);
+  // LO phonon of 36 meV, 200 q bins of 1e7 1/m, 3 ps lifetime, 1e-21 m^3
+  auto bath = std::make_shared<emcPhononBath<T>>(200, 1e7, 3e-12, 0.036, temp, 1e-21);
+  el->addScatterMechanism({0}, std::make_unique<emcAcousticScatterMechanism<T>>(0, 9., device));
+  el->addScatterMechanism(
+      {0}, std::make_unique<emcHotPhononFroehlichAbsorption3D<T>>(0, 0.036, 0.26, 10.9, 12.9,
+                                                                   bath));
+  el->addScatterMechanism(
+      {0}, std::make_unique<emcHotPhononFroehlichEmission3D<T>>(0, 0.036, 0.26, 10.9, 12.9,
+                                                                 bath));
+  el->initScatterTables();
+  dumpTablesOf(*el, "init_");
+  rec("init_meanNq", {bath->getMeanNq()});
+  for (int i = 0; i < nEm; i++) // q over the bath's range, denser at small q
+    bath->recordEmission(1e7 * 200. * std::pow((i + 0.5) / nEm, 2.));
+  bath->update(dtBath);
+  el->reinitScatterTables();
+  dumpTablesOf(*el, "re_");
+  rec("re_meanNq", {bath->getMeanNq()});
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc < 2) {
     std::fprintf(stderr, "usage: ref_driver {bulk|mt} ...\n");
@@ -535,6 +578,8 @@ int main(int argc, char **argv) {
     rc = runMt(argc, argv);
   else if (mode == "device")
     rc = runDevice(argc, argv);
+  else if (mode == "reinit")
+    rc = runReinit(argc, argv);
   std::cout.rdbuf(orig);
   return rc;
 }

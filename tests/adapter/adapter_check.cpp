@@ -4,6 +4,7 @@
 // GpuBulkParticleHandler is instantiated to check that it compiles and links.
 #include <cstdio>
 #include <memory>
+#include <vector>
 
 #include <ParticleType/emcElectron.hpp>
 #include <emcDevice.hpp>
@@ -50,6 +51,11 @@ int main() {
                 d.mechs[m].final_sub[1][0]);
   for (int i = 0; i < d.n_mechs * d.n_levels; i += 97)
     std::printf("table %d %a\n", i, d.tables[i]);
+  // the refilled rates that reinitScatterTables hands to emcg_update_rates
+  const std::vector<double> raw = mb.rawRates();
+  std::printf("rawcount %zu\n", raw.size());
+  for (size_t i = 0; i < raw.size(); i += 89)
+    std::printf("raw %zu %a\n", i, raw[i]);
   // a gated 2-D device described through DeviceDesc
   Dev2 dev2{emcMaterial<T>{11.8, 2329., 1.45e16, 9040., 1.15}, {30e-9, 20e-9}, {1e-9, 1e-9},
             300.};

@@ -11,8 +11,14 @@ headers by `make -C oracle ref`, which needs the reference tree) and stores:
                     (offsets into `words`, recorded by the oracle while it
                     reproduced the reference bit for bit).
   mt19937_64.npz    first words of std::mt19937_64(5489) and canonical maps.
+  reinit_hot_phonon.npz
+                    rates, normalised tables and tau of an acoustic + hot-phonon
+                    Froehlich absorption/emission set before and after the
+                    reference's reinitScatterTables, with the phonon bath
+                    advanced in between (the rates change).
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [part ...]
+(parts: mt bulk device output reinit; default all).
 """
 from __future__ import annotations
 
@@ -205,6 +211,27 @@ def make_output(case, outdir_name):
     print(f"{outdir_name}: {sorted(os.listdir(dst))}")
 
 
+REINIT_CASE = (1000, 1.0, 20000, 1e-13)  # levels, max energy [eV], emissions, bath dt [s]
+
+
+def make_reinit():
+    nL, maxE, nEm, dtb = REINIT_CASE
+    d = po.run_ref("reinit", nL, maxE, nEm, dtb)
+    out = {"params": np.array(REINIT_CASE, dtype=np.float64)}
+    for tag in ("init", "re"):
+        nT = len([k for k in d if k.startswith(f"{tag}_raw_v0_r0_t")])
+        raw = np.stack([d[f"{tag}_raw_v0_r0_t{t}"] for t in range(nT)])
+        norm = np.stack([d[f"{tag}_norm_v0_r0_t{t}"] for t in range(nT)])
+        out[f"{tag}_raw"], out[f"{tag}_norm"] = raw, norm
+        out[f"{tag}_tau"] = d[f"{tag}_tau_v0_r0"]
+        out[f"{tag}_meanNq"] = d[f"{tag}_meanNq"]
+        out["names"] = np.array([d[f"{tag}_name_v0_r0_t{t}"] for t in range(nT)])
+    assert not np.array_equal(out["init_raw"], out["re_raw"]), "the rates did not change"
+    np.savez_compressed(os.path.join(HERE, "reinit_hot_phonon.npz"), **out)
+    print(f"reinit_hot_phonon: {out['init_raw'].shape} tables, tau "
+          f"{out['init_tau'][0]:.4e} -> {out['re_tau'][0]:.4e}")
+
+
 def make_mt():
     d = po.run_ref("mt", 5489, 2000)
     np.savez_compressed(os.path.join(HERE, "mt19937_64.npz"), words=d["mt"], canon=d["canon"])
@@ -213,10 +240,17 @@ def make_mt():
 
 if __name__ == "__main__":
     po.build(force=True)
-    make_mt()
-    for c in CASES:
-        make_bulk(c)
-    for c in DEVICE_CASES:
-        make_device(c)
-    make_output(DEVICE_CASES[0], "output_resistor_ngp")
-    make_output(DEVICE_CASES[3], "output_mosfet_necvwd")
+    parts = set(sys.argv[1:]) or {"mt", "bulk", "device", "output", "reinit"}
+    if "mt" in parts:
+        make_mt()
+    if "bulk" in parts:
+        for c in CASES:
+            make_bulk(c)
+    if "device" in parts:
+        for c in DEVICE_CASES:
+            make_device(c)
+    if "output" in parts:
+        make_output(DEVICE_CASES[0], "output_resistor_ngp")
+        make_output(DEVICE_CASES[3], "output_mosfet_necvwd")
+    if "reinit" in parts:
+        make_reinit()

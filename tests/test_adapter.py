@@ -91,3 +91,26 @@ def test_adapter_device_desc_matches_host_device(tmp_path):
         k = int(k)
         assert int(t) == d.contact_type[k] and float.fromhex(v) == d.contact_voltage[k]
         assert [float.fromhex(p) for p in (p0, p1, p2)] == list(d.contact_param[3 * k:3 * k + 3])
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include")),
+                    reason="reference headers not available")
+def test_adapter_raw_rates_match_host_refill(tmp_path):
+    """ModelBuilder::rawRates (the reference mechanisms refilled, as the C++
+    reinitScatterTables passes them to emcg_update_rates) equals the host
+    model's refill bit for bit, in the same layout."""
+    from viennaemc_gb300 import _lib, physics
+    lib = _lib.build()
+    exe = tmp_path / "adapter_check"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-w", f"-I{REF}/include", f"-I{ROOT}/include",
+                    os.path.join(ROOT, "tests", "adapter", "adapter_check.cpp"), "-o", str(exe),
+                    f"-L{os.path.dirname(lib)}", "-lemcgpu",
+                    f"-Wl,-rpath,{os.path.dirname(lib)}"], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    raw = physics.silicon_electron("jacoboni").raw_rates()
+    n = int([l for l in out if l.startswith("rawcount")][0].split()[1])
+    assert n == raw.size
+    lines = [l.split() for l in out if l.startswith("raw ")]
+    assert len(lines) == (n + 88) // 89
+    for _, i, v in lines:
+        assert float.fromhex(v) == raw[int(i)], i

@@ -16,7 +16,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 LIB_PATH = os.path.join(PKG, "libemcgpu.so")
 SOURCES = ["emcg_core.cu", "emcg_bulk.cu", "emcg_device.cu", "emcg_poisson.cu"]
-HEADERS = ["emcg_common.cuh", "emcg_host.h", "emcg_model.h", "emcg_poisson.cuh"]
+HEADERS = ["emcg_common.cuh", "emcg_host.h", "emcg_model.h", "emcg_poisson.cuh", "emcg_rates.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 MAX_VALLEYS, MAX_DEG, MAX_MECH, MAX_NF, MAX_REGIONS = 4, 8, 32, 8, 16
@@ -238,4 +238,6 @@ _EXTRA_DECLS.extend([
     ("emcg_poisson_solve_noalloc", [C.POINTER(DeviceDesc), C.c_void_p, C.c_void_p, C.c_int32,
                                     C.c_int32, C.c_double, C.c_int32, C.c_void_p,
                                     C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
+    ("emcg_update_rates", [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32]),
+    ("emcg_get_rates", [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
 ])

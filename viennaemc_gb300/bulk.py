@@ -58,6 +58,37 @@ class ParticleState:
         return d
 
 
+def update_rates(lib, h, model: int, raw, particle_type) -> object:
+    """emcg_update_rates: raw is a host array, a CUDA float64 tensor (device
+    rates), or None (refill from the particle type's mechanisms).  Returns
+    what must stay alive until the next step call (a device tensor)."""
+    if raw is None:
+        raw = particle_type.raw_rates()
+    if hasattr(raw, "is_cuda") and raw.is_cuda:
+        import torch
+        if raw.dtype != torch.float64 or not raw.is_contiguous():
+            raise ValueError("device rates must be a contiguous float64 tensor")
+        torch.cuda.current_stream(raw.device).synchronize()  # complete before the call
+        L.check(lib.emcg_update_rates(h, model, C.c_void_p(raw.data_ptr()), 1))
+        return raw
+    a = np.ascontiguousarray(np.asarray(raw, np.float64).reshape(-1))
+    want = particle_type.scatterHandler.fill_size()
+    if a.size != want:
+        raise ValueError(f"rates: {a.size} values, the model's tables hold {want}")
+    L.check(lib.emcg_update_rates(h, model, a.ctypes.data_as(C.c_void_p), 0))
+    return None
+
+
+def get_rates(lib, h, model: int, particle_type):
+    """emcg_get_rates: (tables in the raw layout, tau per table set)."""
+    n = particle_type.scatterHandler.fill_size()
+    nts = len(particle_type.scatterHandler.table_mechs)
+    tables, tau = np.zeros(max(n, 1)), np.zeros(max(nts, 1))
+    L.check(lib.emcg_get_rates(h, model, tables.ctypes.data_as(C.c_void_p),
+                               tau.ctypes.data_as(C.c_void_p)))
+    return tables[:n], tau[:nts]
+
+
 def _normalize(v):
     s = 0.0
     for x in v:
@@ -201,6 +232,17 @@ class BulkBatch:
         self.step_index = s0 + n_steps
         return obs
 
+    def reinit_scatter_tables(self, model: int = 0, raw=None):
+        """emcScatterHandler::reinitScatterTables (include/emcScatterHandler.hpp:
+        100-108) of model `model` on the GPU, before the next step: raw are the
+        refilled rates (host array, or CUDA float64 tensor), None refills them
+        from the model's mechanisms now."""
+        self._rates_keep = update_rates(self._lib, self.h, model, raw, self.models[model])
+
+    def get_rates(self, model: int = 0):
+        """The engine's normalised tables (raw layout) and tau per table set."""
+        return get_rates(self._lib, self.h, model, self.models[model])
+
     def set_replay(self, words, offsets):
         w = np.ascontiguousarray(np.asarray(words, np.uint64))
         o = np.ascontiguousarray(np.asarray(offsets, np.int64))
@@ -320,6 +362,18 @@ class BulkParticleHandler:
         obs = b.step(n_steps)
         self._last = BulkBatch.averages(obs, [self.n])
         return self._last
+
+    def reinitScatterTables(self, raw=None):
+        """The particle type's scatterHandler.reinitScatterTables() on the GPU
+        (before any particle exists: on the host model the engine is built
+        from)."""
+        if raw is None:  # refill on the host model too, so a rebuilt engine agrees
+            h = self.type.scatterHandler
+            h.reinitScatterTables()
+            raw = np.concatenate([h.raw[k].reshape(-1) for k in sorted(h.table_mechs)]) \
+                if h.table_mechs else np.zeros(0)
+        if self._batch is not None:
+            self._batch.reinit_scatter_tables(0, raw)
 
     def getAvgEnergy(self, idx_type=0):
         return self._current()["energy"]

@@ -11,6 +11,7 @@
 #include "emcg_common.cuh"
 #include "emcg_host.h"
 #include "emcg_model.h"
+#include "emcg_rates.cuh"
 
 namespace emcg {
 
@@ -680,6 +681,9 @@ struct BulkImpl {
   int64_t totalCap = 0;
   void *dModels = nullptr;
   std::vector<void *> dTables;
+  std::vector<RateLayout> rates; // table layout per model (rate-table rebuild)
+  double *dRawStage = nullptr;   // host rates staged for a rebuild
+  int64_t rawStageCap = 0;
   void *dEns = nullptr;
   Tile *dTiles = nullptr;
   int nTiles = 0, tilesCap = 0;
@@ -693,7 +697,7 @@ struct BulkImpl {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int blockThreads = 256;
   int minBlocks = 1; // register cap variant of the step kernel (1, 3 or 4)
-  int queued = 0;    // 1: block-queued scatter kernel (Philox), 0: lockstep kernel
+  int queued = 0; // step kernel: 0 lockstep, 1 block-queued, 2 warp-asynchronous (float)
   int stepsPerLaunch = 0;
   int chunk = 16;
   uint64_t *dWords = nullptr;
@@ -783,9 +787,11 @@ static int32_t createTyped(BulkImpl *b, const emcg_model_desc *models, int nMode
                            const emcg_ensemble_desc *ens, int nEns) {
   std::vector<ModelK<T>> mk(nModels);
   b->dTables.assign(nModels, nullptr);
+  b->rates.resize(nModels);
   for (int i = 0; i < nModels; i++) {
     std::vector<T> tab;
     EMCG_TRY(buildModelK<T>(models[i], mk[i], tab));
+    b->rates[i] = rateLayoutOf(models[i]);
     EMCG_CUDA(cudaMalloc(&b->dTables[i], tab.size() * sizeof(T)));
     EMCG_CUDA(cudaMemcpy(b->dTables[i], tab.data(), tab.size() * sizeof(T),
                          cudaMemcpyHostToDevice));
@@ -1068,6 +1074,7 @@ static void freeBulk(BulkImpl *b) {
   cudaFree(b->dErr);
   cudaFree(b->dWords);
   cudaFree(b->dOff);
+  cudaFree(b->dRawStage);
   dropGraph(b);
   if (b->ev0)
     cudaEventDestroy(b->ev0);
@@ -1082,6 +1089,33 @@ static int32_t bulkOf(emcg_handle *h, BulkImpl **out) {
   EMCG_CHECK_ARG(h && h->kind == 1 && h->bulk, "handle is not a bulk engine");
   *out = h->bulk;
   return EMCG_OK;
+}
+
+int32_t bulkUpdateRates(emcg_handle *h, int model, const double *raw, bool onDevice) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(model >= 0 && model < b->nModels, "model %d out of range", model);
+  const size_t mb = b->precision == EMCG_FP64 ? sizeof(ModelK<double>) : sizeof(ModelK<float>);
+  void *dm = (char *)b->dModels + (size_t)model * mb;
+  if (b->precision == EMCG_FP64)
+    return launchRateUpdate<double>(dm, b->dTables[model], b->rates[model], raw, onDevice,
+                                    &b->dRawStage, &b->rawStageCap, b->dErr, b->stream);
+  return launchRateUpdate<float>(dm, b->dTables[model], b->rates[model], raw, onDevice,
+                                 &b->dRawStage, &b->rawStageCap, b->dErr, b->stream);
+}
+
+int32_t bulkGetRates(emcg_handle *h, int model, double *tables, double *tau) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(model >= 0 && model < b->nModels, "model %d out of range", model);
+  const size_t mb = b->precision == EMCG_FP64 ? sizeof(ModelK<double>) : sizeof(ModelK<float>);
+  const void *dm = (const char *)b->dModels + (size_t)model * mb;
+  EMCG_TRY(b->precision == EMCG_FP64
+               ? readRateTables<double>(dm, b->dTables[model], b->rates[model], tables, tau,
+                                        b->stream)
+               : readRateTables<float>(dm, b->dTables[model], b->rates[model], tables, tau,
+                                       b->stream));
+  return readError(b);
 }
 
 } // namespace emcg

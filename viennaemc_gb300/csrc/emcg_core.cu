@@ -35,3 +35,22 @@ extern "C" const char *emcg_last_error(void) {
 }
 
 extern "C" int32_t emcg_version(void) { return 100; }
+
+extern "C" int32_t emcg_update_rates(emcg_handle *h, int32_t model, const double *raw,
+                                     int32_t raw_on_device) {
+  EMCG_CHECK_ARG(h, "handle is NULL");
+  if (h->kind == 2) {
+    EMCG_CHECK_ARG(model == 0, "a device engine has one model (index 0)");
+    return emcg::deviceUpdateRates(h, raw, raw_on_device != 0);
+  }
+  return emcg::bulkUpdateRates(h, model, raw, raw_on_device != 0);
+}
+
+extern "C" int32_t emcg_get_rates(emcg_handle *h, int32_t model, double *tables, double *tau) {
+  EMCG_CHECK_ARG(h, "handle is NULL");
+  if (h->kind == 2) {
+    EMCG_CHECK_ARG(model == 0, "a device engine has one model (index 0)");
+    return emcg::deviceGetRates(h, tables, tau);
+  }
+  return emcg::bulkGetRates(h, model, tables, tau);
+}

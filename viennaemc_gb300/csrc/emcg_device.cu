@@ -15,6 +15,7 @@
 #include "emcg_host.h"
 #include "emcg_model.h"
 #include "emcg_poisson.cuh"
+#include "emcg_rates.cuh"
 
 namespace emcg {
 
@@ -669,6 +670,9 @@ struct DeviceImpl {
   std::vector<double> expNrH;
   // device
   void *dModel = nullptr, *dTables = nullptr;
+  RateLayout rates;            // table layout (rate-table rebuild)
+  double *dRawStage = nullptr; // host rates staged for a rebuild
+  int64_t rawStageCap = 0;
   int32_t *dRegion = nullptr, *dNodeContact = nullptr, *dNodeRes = nullptr, *dBnd[4] = {};
   uint8_t *dNodeOhmic = nullptr;
   double *dPot = nullptr, *dNr = nullptr, *dConc = nullptr, *dExp = nullptr;
@@ -751,6 +755,25 @@ static int32_t devOf(emcg_handle *h, DeviceImpl **out) {
   return EMCG_OK;
 }
 
+int32_t deviceUpdateRates(emcg_handle *h, const double *raw, bool onDevice) {
+  DeviceImpl *d;
+  EMCG_TRY(devOf(h, &d));
+  if (d->precision == EMCG_FP64)
+    return launchRateUpdate<double>(d->dModel, d->dTables, d->rates, raw, onDevice,
+                                    &d->dRawStage, &d->rawStageCap, d->dErr, d->stream);
+  return launchRateUpdate<float>(d->dModel, d->dTables, d->rates, raw, onDevice, &d->dRawStage,
+                                 &d->rawStageCap, d->dErr, d->stream);
+}
+
+int32_t deviceGetRates(emcg_handle *h, double *tables, double *tau) {
+  DeviceImpl *d;
+  EMCG_TRY(devOf(h, &d));
+  EMCG_TRY(d->precision == EMCG_FP64
+               ? readRateTables<double>(d->dModel, d->dTables, d->rates, tables, tau, d->stream)
+               : readRateTables<float>(d->dModel, d->dTables, d->rates, tables, tau, d->stream));
+  return readErr(d);
+}
+
 int32_t destroyDevice(emcg_handle *h) {
   DeviceImpl *d = h ? h->dev : nullptr;
   if (!d)
@@ -761,7 +784,7 @@ int32_t destroyDevice(emcg_handle *h) {
   void *ps[] = {d->dModel, d->dTables, d->dRegion, d->dNodeContact, d->dNodeRes, d->dNodeOhmic,
                 d->dPot, d->dNr, d->dConc, d->dExp, d->dEx, d->dEy, d->dN, d->dDrop, d->dBlock,
                 d->dList, d->dListNode, d->dListCount, d->dGList, d->dGNode, d->dKept, d->dResNodes,
-                d->dInjCount, d->dNetto, d->dRemInj, d->dErr};
+                d->dInjCount, d->dNetto, d->dRemInj, d->dErr, d->dRawStage};
   for (void *p : ps)
     cudaFree(p);
   for (int b = 0; b < 4; b++)
@@ -810,6 +833,7 @@ template <class T> static int32_t createModel(DeviceImpl *d, const emcg_model_de
   ModelK<T> K;
   std::vector<T> tab;
   EMCG_TRY(buildModelK<T>(m, K, tab));
+  d->rates = rateLayoutOf(m);
   EMCG_TRY(up((T **)&d->dTables, tab.data(), tab.size(), d->stream));
   K.tables = (const T *)d->dTables;
   EMCG_TRY(up((ModelK<T> **)&d->dModel, &K, 1, d->stream));

@@ -49,6 +49,11 @@ struct DeviceImpl;
 
 struct emcg_handle;
 namespace emcg {
+// rate-table rebuild (emcg_bulk.cu, emcg_device.cu)
+int32_t bulkUpdateRates(emcg_handle *h, int model, const double *raw, bool onDevice);
+int32_t bulkGetRates(emcg_handle *h, int model, double *tables, double *tau);
+int32_t deviceUpdateRates(emcg_handle *h, const double *raw, bool onDevice);
+int32_t deviceGetRates(emcg_handle *h, double *tables, double *tau);
 // emcg_device.cu
 int32_t destroyDevice(emcg_handle *h);
 int32_t deviceSetState(emcg_handle *h, const emcg_state *s);

@@ -17,7 +17,7 @@ import numpy as np
 
 from . import _lib as L
 from . import results as R
-from .bulk import ParticleState
+from .bulk import ParticleState, get_rates, update_rates
 from .physics import Material, thermal_voltage
 
 XMIN, XMAX, YMIN, YMAX = range(4)  # emcBoundaryPos (include/emcBoundaryPos.hpp:13-20)
@@ -224,6 +224,18 @@ class DeviceSimulation:
             self.close()
         except Exception:
             pass
+
+    # ---- scatter tables --------------------------------------------------------
+    def reinitScatterTables(self, raw=None):
+        """The particle type's scatterHandler.reinitScatterTables()
+        (include/emcScatterHandler.hpp:100-108) on the GPU, before the next
+        step: raw are the refilled rates (host array or CUDA float64 tensor);
+        None refills them from the mechanisms now."""
+        self._rates_keep = update_rates(self._lib, self.h, 0, raw, self.type)
+
+    def get_rates(self):
+        """The engine's normalised tables (raw layout) and tau per table set."""
+        return get_rates(self._lib, self.h, 0, self.type)
 
     # ---- grids -----------------------------------------------------------------
     def get_grid(self, which):

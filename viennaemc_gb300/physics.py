@@ -296,16 +296,39 @@ class ScatterHandler:
         for r in regions:
             self.table_mechs.setdefault((mech.idx_valley, int(r)), []).append(idx)
 
+    def _fill(self, key):
+        """fillScatterTables (:220-235) for one (valley, region) table set: the
+        rate of each of its mechanisms at (level + 1) dE."""
+        v, r = key
+        dE, L_ = self.dE, self.n_levels
+        rows = []
+        for mi in self.table_mechs[key]:
+            m = self.mechanisms[mi]
+            rows.append([m.getScatterRate((l + 1) * dE, r) for l in range(L_)])
+        return np.array(rows, dtype=np.float64).reshape(len(rows), L_)
+
+    def fill_rates(self) -> np.ndarray:
+        """The refilled rates of every table set in key order, table-major and
+        concatenated: the raw layout the engine's rate-table rebuild takes."""
+        chunks = [self._fill(key).reshape(-1) for key in sorted(self.table_mechs)]
+        return np.concatenate(chunks) if chunks else np.zeros(0)
+
+    def fill_size(self) -> int:
+        """Number of rates in the concatenated raw layout."""
+        return sum(len(m) for m in self.table_mechs.values()) * self.n_levels
+
+    def reinitScatterTables(self):
+        """reinitScatterTables (:100-108): refill and renormalise, no files."""
+        self.raw.clear()
+        self.norm.clear()
+        self.tau.clear()
+        self.initScatterTables()
+
     def initScatterTables(self):
         """fillScatterTables + renormalizeTables (:220-235, :248-273)"""
-        dE, L_ = self.dE, self.n_levels
         for key in sorted(self.table_mechs):
-            v, r = key
-            rows = []
-            for mi in self.table_mechs[key]:
-                m = self.mechanisms[mi]
-                rows.append([m.getScatterRate((l + 1) * dE, r) for l in range(L_)])
-            raw = np.array(rows, dtype=np.float64).reshape(len(rows), L_)
+            rows = self.table_mechs[key]
+            raw = self._fill(key)
             self.raw[key] = raw
             if len(rows) == 0:
                 self.tau[key] = 2e-15
@@ -356,6 +379,12 @@ class Electron:
 
     def getTau(self, valley, region):
         return self.scatterHandler.getTau(region, valley)
+
+    def raw_rates(self) -> np.ndarray:
+        """The rates of the scatter tables refilled now from the mechanisms
+        (fillScatterTables without renormalisation), in the layout of the
+        engine's rate-table rebuild."""
+        return self.scatterHandler.fill_rates()
 
     # ---- engine descriptor -------------------------------------------------
     def model_desc(self, region_doping=None):
