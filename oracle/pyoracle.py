@@ -386,8 +386,18 @@ def parse_ref(text: str) -> dict:
 def run_ref(*args) -> dict:
     if not os.path.exists(REF_DRIVER):
         raise FileNotFoundError("reference harness not built (make -C oracle ref)")
-    r = subprocess.run([REF_DRIVER] + [str(a) for a in args], check=True,
-                       capture_output=True, text=True)
+    # the reference writes its table files into the working directory: run it
+    # in a scratch directory under oracle/_ref/ and remove that afterwards
+    import shutil
+    import tempfile
+    base = os.path.join(HERE, "_ref", "scratch")
+    os.makedirs(base, exist_ok=True)
+    work = tempfile.mkdtemp(dir=base)
+    try:
+        r = subprocess.run([REF_DRIVER] + [str(a) for a in args], check=True,
+                           capture_output=True, text=True, cwd=work)
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
     return parse_ref(r.stdout)
 
 

@@ -563,11 +563,8 @@ int main(int argc, char **argv) {
     return 2;
   }
   std::string mode = argv[1];
-  // initScatterTables writes one file per table into the working directory
-  char tmpl[] = "/tmp/emcrefXXXXXX";
-  if (char *d = mkdtemp(tmpl))
-    if (chdir(d) != 0)
-      return 3;
+  // initScatterTables writes one file per table into the working directory:
+  // the caller runs the harness in a scratch directory (oracle/pyoracle.py)
   std::cout.setf(std::ios::unitbuf);
   // the reference prints progress to stdout; route it to stderr
   std::streambuf *orig = std::cout.rdbuf(std::cerr.rdbuf());

@@ -13,6 +13,8 @@ for p in (ROOT, os.path.join(ROOT, "oracle")):
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a) and libemcgpu")
+    if not config.option.basetemp:  # keep test scratch files inside the repository
+        config.option.basetemp = os.path.join(ROOT, ".pytest_tmp")
 
 
 def golden(name: str) -> dict:

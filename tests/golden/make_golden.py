@@ -202,7 +202,9 @@ def make_output(case, outdir_name):
     import tempfile
     name, kind, seed, dt, steps, acc, width = case
     dst = os.path.join(HERE, outdir_name)
-    tmp = tempfile.mkdtemp(prefix="emc_out_")
+    scratch = os.path.join(ROOT, "oracle", "_ref", "scratch")
+    os.makedirs(scratch, exist_ok=True)
+    tmp = tempfile.mkdtemp(prefix="emc_out_", dir=scratch)
     po.run_ref("device", kind, seed, dt, steps, acc, width, tmp)
     os.makedirs(dst, exist_ok=True)
     for f in sorted(os.listdir(tmp)):

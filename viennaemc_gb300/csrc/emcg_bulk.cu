@@ -682,8 +682,7 @@ struct BulkImpl {
   void *dModels = nullptr;
   std::vector<void *> dTables;
   std::vector<RateLayout> rates; // table layout per model (rate-table rebuild)
-  double *dRawStage = nullptr;   // host rates staged for a rebuild
-  int64_t rawStageCap = 0;
+  RateScratch rateScratch;        // device scratch of rebuilds
   void *dEns = nullptr;
   Tile *dTiles = nullptr;
   int nTiles = 0, tilesCap = 0;
@@ -1074,7 +1073,7 @@ static void freeBulk(BulkImpl *b) {
   cudaFree(b->dErr);
   cudaFree(b->dWords);
   cudaFree(b->dOff);
-  cudaFree(b->dRawStage);
+  freeRateScratch(b->rateScratch);
   dropGraph(b);
   if (b->ev0)
     cudaEventDestroy(b->ev0);
@@ -1099,9 +1098,9 @@ int32_t bulkUpdateRates(emcg_handle *h, int model, const double *raw, bool onDev
   void *dm = (char *)b->dModels + (size_t)model * mb;
   if (b->precision == EMCG_FP64)
     return launchRateUpdate<double>(dm, b->dTables[model], b->rates[model], raw, onDevice,
-                                    &b->dRawStage, &b->rawStageCap, b->dErr, b->stream);
+                                    b->rateScratch, b->dErr, b->stream);
   return launchRateUpdate<float>(dm, b->dTables[model], b->rates[model], raw, onDevice,
-                                 &b->dRawStage, &b->rawStageCap, b->dErr, b->stream);
+                                 b->rateScratch, b->dErr, b->stream);
 }
 
 int32_t bulkGetRates(emcg_handle *h, int model, double *tables, double *tau) {

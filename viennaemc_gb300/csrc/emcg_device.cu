@@ -671,8 +671,7 @@ struct DeviceImpl {
   // device
   void *dModel = nullptr, *dTables = nullptr;
   RateLayout rates;            // table layout (rate-table rebuild)
-  double *dRawStage = nullptr; // host rates staged for a rebuild
-  int64_t rawStageCap = 0;
+  RateScratch rateScratch;     // device scratch of rebuilds
   int32_t *dRegion = nullptr, *dNodeContact = nullptr, *dNodeRes = nullptr, *dBnd[4] = {};
   uint8_t *dNodeOhmic = nullptr;
   double *dPot = nullptr, *dNr = nullptr, *dConc = nullptr, *dExp = nullptr;
@@ -760,9 +759,9 @@ int32_t deviceUpdateRates(emcg_handle *h, const double *raw, bool onDevice) {
   EMCG_TRY(devOf(h, &d));
   if (d->precision == EMCG_FP64)
     return launchRateUpdate<double>(d->dModel, d->dTables, d->rates, raw, onDevice,
-                                    &d->dRawStage, &d->rawStageCap, d->dErr, d->stream);
-  return launchRateUpdate<float>(d->dModel, d->dTables, d->rates, raw, onDevice, &d->dRawStage,
-                                 &d->rawStageCap, d->dErr, d->stream);
+                                    d->rateScratch, d->dErr, d->stream);
+  return launchRateUpdate<float>(d->dModel, d->dTables, d->rates, raw, onDevice,
+                                 d->rateScratch, d->dErr, d->stream);
 }
 
 int32_t deviceGetRates(emcg_handle *h, double *tables, double *tau) {
@@ -784,7 +783,8 @@ int32_t destroyDevice(emcg_handle *h) {
   void *ps[] = {d->dModel, d->dTables, d->dRegion, d->dNodeContact, d->dNodeRes, d->dNodeOhmic,
                 d->dPot, d->dNr, d->dConc, d->dExp, d->dEx, d->dEy, d->dN, d->dDrop, d->dBlock,
                 d->dList, d->dListNode, d->dListCount, d->dGList, d->dGNode, d->dKept, d->dResNodes,
-                d->dInjCount, d->dNetto, d->dRemInj, d->dErr, d->dRawStage};
+                d->dInjCount, d->dNetto, d->dRemInj, d->dErr};
+  freeRateScratch(d->rateScratch);
   for (void *p : ps)
     cudaFree(p);
   for (int b = 0; b < 4; b++)

@@ -8,9 +8,9 @@
 //   Gmax  = max over levels of cum_{n-1}
 //   table_t = cum_t / Gmax,  tau = 1 / Gmax
 // in double, then stores the tables level-major in the engine's precision in
-// place of the old ones.  The launch is ordered on the handle's stream, so the
-// next step sees the new tables; a captured step graph reads them through the
-// same pointers.
+// place of the old ones.  The launches are ordered on the handle's stream, so
+// the next step sees the new tables; a captured step graph reads them through
+// the same pointers.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -45,63 +45,99 @@ inline RateLayout rateLayoutOf(const emcg_model_desc &m) {
 
 constexpr int kRenormThreads = 256;
 
-// One block per table set.  Pass 1 forms the last cumulative row per level
-// and its maximum; pass 2 forms the cumulative rows again (the same
-// operations, so the same bits) and stores them divided by the maximum.  A
-// set with a non-finite rate or a maximum that is not positive is left as it
-// was and EMCG_ERR_ARG is recorded (the reference would divide by it).
+// Device scratch of a handle's rebuilds: staged host rates and the per-chunk
+// maxima of pass 1.
+struct RateScratch {
+  double *stage = nullptr;
+  int64_t stageCap = 0;
+  double *part = nullptr;
+  int64_t partCap = 0;
+};
+
+inline void freeRateScratch(RateScratch &S) {
+  cudaFree(S.stage);
+  cudaFree(S.part);
+  S = RateScratch{};
+}
+
+__device__ __forceinline__ double blockMaxOr(double v, int *bad) {
+  __shared__ double w[kRenormThreads / 32];
+  for (int o = 16; o > 0; o >>= 1)
+    v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0)
+    w[threadIdx.x >> 5] = v;
+  *bad = __syncthreads_or(*bad);
+  double m = w[0];
+  for (int i = 1; i < (int)(blockDim.x >> 5); i++)
+    m = fmax(m, w[i]);
+  return m;
+}
+
+// Pass 1, one thread per (table set, level): the last cumulative row and its
+// maximum per chunk of kRenormThreads levels; NaN marks a chunk with a
+// non-finite rate.
 template <class T>
 __global__ void __launch_bounds__(kRenormThreads)
-    renormRatesKernel(const double *__restrict__ raw, ModelK<T> *model, T *tables, int *err) {
-  __shared__ double wmax[kRenormThreads / 32];
-  __shared__ double gmax;
-  const int ts = blockIdx.x;
-  const int nT = model->tsN[ts];
-  if (nT == 0) // no mechanism: the default free-flight time stays (:250-251)
-    return;
-  const int L = model->nLevels;
-  const int64_t off = model->tsOff[ts];
-  const double *r = raw + off;
-  double mx = -INFINITY;
+    rateMaxKernel(const double *__restrict__ raw, const ModelK<T> *__restrict__ model,
+                  double *__restrict__ part, int nChunks) {
+  const int ts = blockIdx.y, ch = blockIdx.x;
+  const int nT = model->tsN[ts], L = model->nLevels;
+  const int l = ch * kRenormThreads + threadIdx.x;
+  double c = -INFINITY;
   int bad = 0;
-  for (int l = threadIdx.x; l < L; l += blockDim.x) {
-    double c = r[l];
-    bad |= !isfinite(c);
+  if (nT > 0 && l < L) {
+    const double *r = raw + model->tsOff[ts] + l;
+    c = r[0];
+    bad = !isfinite(c);
     for (int t = 1; t < nT; t++) {
-      const double x = r[(int64_t)t * L + l];
+      const double x = r[(int64_t)t * L];
       bad |= !isfinite(x);
       c = x + c;
     }
-    mx = fmax(mx, c);
   }
-  for (int o = 16; o > 0; o >>= 1)
-    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0)
-    wmax[threadIdx.x >> 5] = mx;
-  bad = __syncthreads_or(bad);
-  if (threadIdx.x == 0) {
-    double m = wmax[0];
-    for (int w = 1; w < (int)(blockDim.x >> 5); w++)
-      m = fmax(m, wmax[w]);
-    gmax = m;
+  const double m = blockMaxOr(c, &bad);
+  if (threadIdx.x == 0)
+    part[(int64_t)ts * nChunks + ch] = bad ? NAN : m;
+}
+
+// Pass 2: the set's maximum from the chunk maxima, then the cumulative rows
+// again (the same operations, so the same bits) divided by it, stored
+// level-major in the engine's precision; tau = 1 / maximum.  A set with a
+// non-finite rate or a maximum that is not positive is left as it was and
+// EMCG_ERR_ARG is recorded (the reference would divide by it).
+template <class T>
+__global__ void __launch_bounds__(kRenormThreads)
+    rateNormKernel(const double *__restrict__ raw, ModelK<T> *model, T *tables,
+                   const double *__restrict__ part, int nChunks, int *err) {
+  const int ts = blockIdx.y, ch = blockIdx.x;
+  const int nT = model->tsN[ts], L = model->nLevels;
+  if (nT == 0) // no mechanism: the default free-flight time stays (:250-251)
+    return;
+  double g = -INFINITY;
+  bool bad = false;
+  for (int i = 0; i < nChunks; i++) {
+    const double p = part[(int64_t)ts * nChunks + i];
+    bad |= isnan(p);
+    g = fmax(g, p);
   }
-  __syncthreads();
-  const double g = gmax;
   if (bad || !(g > 0.0) || !isfinite(g)) {
-    if (threadIdx.x == 0)
+    if (ch == 0 && threadIdx.x == 0)
       atomicCAS(err, 0, EMCG_ERR_ARG);
     return;
   }
-  T *dst = tables + off;
-  for (int l = threadIdx.x; l < L; l += blockDim.x) {
-    double c = r[l];
-    dst[(int64_t)l * nT] = (T)(c / g);
+  const int l = ch * kRenormThreads + threadIdx.x;
+  if (l < L) {
+    const int64_t off = model->tsOff[ts];
+    const double *r = raw + off + l;
+    T *dst = tables + off + (int64_t)l * nT;
+    double c = r[0];
+    dst[0] = (T)(c / g);
     for (int t = 1; t < nT; t++) {
-      c = r[(int64_t)t * L + l] + c;
-      dst[(int64_t)l * nT + t] = (T)(c / g);
+      c = r[(int64_t)t * L] + c;
+      dst[t] = (T)(c / g);
     }
   }
-  if (threadIdx.x == 0)
+  if (ch == 0 && threadIdx.x == 0)
     model->tauMax[ts] = (T)(1.0 / g);
 }
 
@@ -131,15 +167,31 @@ inline int32_t checkHostRates(const RateLayout &R, const double *raw) {
   return EMCG_OK;
 }
 
-// Launch the rebuild of one model.  raw: host or device doubles (onDevice);
-// host rates go through the handle's staging buffer (grown on demand).
+// Grow a scratch buffer of doubles (after the stream has drained: an earlier
+// rebuild may still read the old one).
+inline int32_t growScratch(double **p, int64_t *cap, int64_t n, cudaStream_t st) {
+  if (*cap >= n)
+    return EMCG_OK;
+  EMCG_CUDA(cudaStreamSynchronize(st));
+  cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  EMCG_CUDA(cudaMalloc(p, (size_t)n * sizeof(double)));
+  *cap = n;
+  return EMCG_OK;
+}
+
+// Launch the rebuild of one model: pass 1 and pass 2 over a grid of
+// (level chunk, table set).  raw: host or device doubles (onDevice); host
+// rates go through the handle's staging buffer.
 template <class T>
 int32_t launchRateUpdate(void *dModel, void *dTables, const RateLayout &R, const double *raw,
-                         bool onDevice, double **stage, int64_t *stageCap, int *dErr,
-                         cudaStream_t st) {
+                         bool onDevice, RateScratch &S, int *dErr, cudaStream_t st) {
   EMCG_CHECK_ARG(raw != nullptr, "rates: raw is NULL");
   if (R.total == 0)
     return EMCG_OK;
+  const int nChunks = (R.nLevels + kRenormThreads - 1) / kRenormThreads;
+  EMCG_TRY(growScratch(&S.part, &S.partCap, (int64_t)R.nTS * nChunks, st));
   const double *src = raw;
   if (onDevice) {
     cudaPointerAttributes a;
@@ -151,20 +203,17 @@ int32_t launchRateUpdate(void *dModel, void *dTables, const RateLayout &R, const
                    "rates: raw is not device memory of the handle's device");
   } else {
     EMCG_TRY(checkHostRates(R, raw));
-    if (*stageCap < R.total) {
-      EMCG_CUDA(cudaStreamSynchronize(st)); // an earlier rebuild may still read it
-      cudaFree(*stage);
-      *stage = nullptr;
-      *stageCap = 0;
-      EMCG_CUDA(cudaMalloc(stage, (size_t)R.total * sizeof(double)));
-      *stageCap = R.total;
-    }
-    EMCG_CUDA(cudaMemcpyAsync(*stage, raw, (size_t)R.total * sizeof(double),
+    EMCG_TRY(growScratch(&S.stage, &S.stageCap, R.total, st));
+    EMCG_CUDA(cudaMemcpyAsync(S.stage, raw, (size_t)R.total * sizeof(double),
                               cudaMemcpyHostToDevice, st));
-    src = *stage;
+    src = S.stage;
   }
-  renormRatesKernel<T><<<R.nTS, kRenormThreads, 0, st>>>(src, (ModelK<T> *)dModel, (T *)dTables,
-                                                         dErr);
+  const dim3 grid(nChunks, R.nTS);
+  rateMaxKernel<T><<<grid, kRenormThreads, 0, st>>>(src, (const ModelK<T> *)dModel, S.part,
+                                                    nChunks);
+  EMCG_CUDA(cudaGetLastError());
+  rateNormKernel<T><<<grid, kRenormThreads, 0, st>>>(src, (ModelK<T> *)dModel, (T *)dTables,
+                                                     S.part, nChunks, dErr);
   EMCG_CUDA(cudaGetLastError());
   return EMCG_OK;
 }
