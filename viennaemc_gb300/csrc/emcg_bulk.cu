@@ -472,19 +472,24 @@ __global__ void bulkInitKernel(StateK<T> st, const ModelK<T> *__restrict__ model
 // Warp-asynchronous variant (float, Philox).  In the lockstep kernel nearly
 // every warp holds a particle with an event in a given step, so the warp runs
 // the scatter path with a few lanes active.  Here each lane runs its own
-// particle from event to event: in one iteration it crosses the step
-// boundaries up to its next event (free flight to the end of the step, the
-// end-of-step bookkeeping, its observables), then the lanes process their
-// events together.  The physics and the random numbers are those of the
-// lockstep kernel: the same free flights, the Philox counter (pid, step, call)
-// restarted at each step, the grain timer at each step end.
+// particle and the warp works in passes.  In a drift pass every lane that can
+// go on flies freely to whichever comes first, the end of its current step
+// (then the end-of-step bookkeeping and its observables) or its next event
+// (then it waits); all of them run the drift together.  Once kEventBatch
+// lanes wait at events, or no lane can go on, a scatter pass scatters the
+// waiting lanes together.  The physics and the random numbers are those of
+// the lockstep kernel: the same free flights, the Philox counter (pid, step,
+// call) restarted at each step, the grain timer at each step end.
 // Observables: a lane writes its per-step values into its own column of a
 // small per-warp window; once every lane of the warp has passed a step, the
 // warp folds that row into the block's float step sums (shared memory), which
 // go to the device's double sums at the end of the launch.  A lane runs at
-// most kAsyncWindow steps ahead of the slowest lane of its warp.
+// most kAsyncWindow steps ahead of the slowest lane of its warp.  Both
+// constants were chosen by measurement on 2^20 electrons.
 // ---------------------------------------------------------------------------
-constexpr int kAsyncWindow = 8;
+constexpr int kAsyncWindow = 12;
+// lanes of a warp that wait at an event before the warp scatters them together
+constexpr int kEventBatch = 6;
 
 __host__ __device__ constexpr size_t asyncSmemBytes(int nWarps, int nSteps, int Q) {
   return (size_t)nSteps * Q * sizeof(float) +
@@ -549,7 +554,8 @@ __global__ void __launch_bounds__(256, MINB)
   int myErr = 0;
   PhiloxSrc<T> rng;
   rng.init(pid, step0, EK.stream, EK.key0, EK.key1);
-  int flushed = 0; // steps folded into the block sums
+  int flushed = 0;  // steps folded into the block sums
+  bool pend = false; // drifted to an event inside step s, not yet scattered
   while (true) {
     const int sMin = __reduce_min_sync(0xffffffffu, s);
     for (; flushed < sMin; flushed++) {
@@ -570,43 +576,55 @@ __global__ void __launch_bounds__(256, MINB)
     if (sMin >= nSteps)
       break;
     const int limit = min(nSteps, flushed + kAsyncWindow);
-    if (s < limit) {
-      // step ends before the next event (bulkParticleStep without an event)
-      while (s < limit && !(tau < dt - tIn)) {
-        const T rem = dt - tIn;
-        driftBulk(M.v[valley], sub, EK.fv[valley][sub], rem, k, E, pos, kN, EK.box);
-        tau -= rem;
-        gtau -= dt;
-        if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
-          gtau = -m_log(rng.ulog()) * M.grainTau;
-        const ValleyK<T> &V = M.v[valley];
-        const T *g = EK.g[valley][sub];
-        const T npf = m_sqrt(T(1) + T(4) * V.alpha * gammaOf(V, E));
-        const int slot = (s % kAsyncWindow) * 32 + lane;
-        winE[slot] = E;
-        winD[slot] = m_div(V.cX * (g[0] * kN[0] + g[1] * kN[1] + g[2] * kN[2]), npf);
-        winVal[slot] = (uint8_t)valley;
-        s++;
-        tIn = T(0);
-        nEv = 0;
-        rng.init(pid, step0 + (uint32_t)s, EK.stream, EK.key0, EK.key1);
-      }
-      // the event inside step s: free flight to it, scattering, new free flight
-      if (s < limit) {
-        int e = 0;
-        if (++nEv > kMaxScatterPerStep) {
-          e = EMCG_ERR_TIMEOUT;
-        } else {
-          driftBulk(M.v[valley], sub, EK.fv[valley][sub], tau, k, E, pos, kN, EK.box);
-          tIn += tau;
-          e = scatterParticle(M, k, E, valley, sub, region, rng);
-          if (!e)
-            tau = -m_log(rng.ulog()) * tauOf(M, valley, region);
-        }
+    // a lane whose free flight ended at an event waits (pend) until enough
+    // lanes of its warp wait too, or no lane can go on: then they scatter
+    // together, so the scatter path runs for several lanes at once
+    const bool can = !pend && s < limit;
+    const unsigned pendMask = __ballot_sync(0xffffffffu, pend);
+    const unsigned canMask = __ballot_sync(0xffffffffu, can);
+    if (pendMask && (__popc(pendMask) >= kEventBatch || !canMask)) {
+      if (pend) { // scattering, new free flight
+        pend = false;
+        const int e = scatterParticle(M, k, E, valley, sub, region, rng);
         if (e) {
           myErr = e;
           live = false;
           s = nSteps;
+        } else {
+          tau = -m_log(rng.ulog()) * tauOf(M, valley, region);
+        }
+      }
+    } else if (can) {
+      // the free flight ends either at the end of step s (bulkParticleStep
+      // without an event) or at the next event inside it; both drift first,
+      // so the warp's lanes drift together
+      const T rem = dt - tIn;
+      const bool ev = tau < rem;
+      if (ev && ++nEv > kMaxScatterPerStep) {
+        myErr = EMCG_ERR_TIMEOUT;
+        live = false;
+        s = nSteps;
+      } else {
+        driftBulk(M.v[valley], sub, EK.fv[valley][sub], ev ? tau : rem, k, E, pos, kN, EK.box);
+        if (ev) {
+          tIn += tau;
+          pend = true;
+        } else { // end of step s: its observables, then step s + 1
+          tau -= rem;
+          gtau -= dt;
+          if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
+            gtau = -m_log(rng.ulog()) * M.grainTau;
+          const ValleyK<T> &V = M.v[valley];
+          const T *g = EK.g[valley][sub];
+          const T npf = m_sqrt(T(1) + T(4) * V.alpha * gammaOf(V, E));
+          const int slot = (s % kAsyncWindow) * 32 + lane;
+          winE[slot] = E;
+          winD[slot] = m_div(V.cX * (g[0] * kN[0] + g[1] * kN[1] + g[2] * kN[2]), npf);
+          winVal[slot] = (uint8_t)valley;
+          s++;
+          tIn = T(0);
+          nEv = 0;
+          rng.init(pid, step0 + (uint32_t)s, EK.stream, EK.key0, EK.key1);
         }
       }
     }
