@@ -502,6 +502,48 @@ inline int asyncMaxSteps(int nWarps, int Q) {
 }
 
 
+// drift() (include/emcParticleDrift.hpp:11-36) with k held in the ellipse
+// frame of the particle's subvalley: the frame changes only at scattering, so
+// k goes to the device frame and back there, not at every free flight.  The
+// displacement is summed in the ellipse frame too (dP) and added to the
+// position by flushPos.  |k| is the same in both frames (R orthonormal).
+// Returns hbar / (mc (1 + 2 alpha E)) at the new energy: the velocity factor
+// of the ellipse-frame k (emcNonParabolicAnistropValley.hpp:185-204, with
+// sqrt(1 + 4 alpha gamma) = 1 + 2 alpha E).
+__device__ __forceinline__ float driftEcs(const ValleyK<float> &V, const float fv[3], float dt,
+                                          float kE[3], float &E, float dP[3]) {
+  float kO[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    kO[i] = kE[i];
+    kE[i] = kO[i] + fv[i] * dt;
+  }
+  E = energyOf(V, kE[0] * kE[0] + kE[1] * kE[1] + kE[2] * kE[2]);
+  const float vf = m_div(V.cX, 1.f + 2.f * E * V.alpha);
+  const float c = vf * dt * 0.5f;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    dP[i] += V.vogt[i] * (kE[i] + kO[i]) * c;
+  return vf;
+}
+
+// The summed displacement into the device frame and the periodic box
+// (basicBulkParticleHandler.hpp:600-613); the sum covers one free flight or
+// less, far below a box length.
+__device__ __forceinline__ void flushPos(const float *R, float dP[3], float pos[3],
+                                         const float box[3]) {
+  float dd[3];
+  toDev(R, dP[0], dP[1], dP[2], dd);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    float c = pos[i] + dd[i];
+    if (c < 0.f || c > box[i])
+      c -= box[i] * floorf(c / box[i]);
+    pos[i] = c;
+    dP[i] = 0.f;
+  }
+}
+
 template <int MINB>
 __global__ void __launch_bounds__(256, MINB)
     bulkStepAsyncKernel(StateK<float> st, const ModelK<float> *__restrict__ models,
@@ -530,12 +572,11 @@ __global__ void __launch_bounds__(256, MINB)
   const uint32_t pid = (uint32_t)(gi - EK.begin);
   const T dt = EK.dt;
 
-  T k[3] = {0, 0, 0}, pos[3] = {0, 0, 0}, kN[3] = {0, 0, 0}, E = 0, tau = 0, gtau = 0;
+  // kE: k in the ellipse frame of the subvalley; dP: displacement in that
+  // frame not yet added to pos
+  T kE[3] = {0, 0, 0}, pos[3] = {0, 0, 0}, dP[3] = {0, 0, 0}, E = 0, tau = 0, gtau = 0;
   int valley = 0, sub = 0, region = 0;
   if (active) {
-    k[0] = st.kx[gi];
-    k[1] = st.ky[gi];
-    k[2] = st.kz[gi];
     pos[0] = st.px[gi];
     pos[1] = st.py[gi];
     pos[2] = st.pz[gi];
@@ -546,6 +587,7 @@ __global__ void __launch_bounds__(256, MINB)
     valley = mt & 0xff;
     sub = (mt >> 8) & 0xff;
     region = mt >> 16;
+    toEcs(M.v[valley].rot[sub], st.kx[gi], st.ky[gi], st.kz[gi], kE);
   }
   bool live = active;    // false once the particle has failed
   int s = live ? 0 : nSteps; // the step the particle is in
@@ -583,8 +625,12 @@ __global__ void __launch_bounds__(256, MINB)
     const unsigned pendMask = __ballot_sync(0xffffffffu, pend);
     const unsigned canMask = __ballot_sync(0xffffffffu, can);
     if (pendMask && (__popc(pendMask) >= kEventBatch || !canMask)) {
-      if (pend) { // scattering, new free flight
+      if (pend) { // scattering (device frame), new free flight
         pend = false;
+        T k[3];
+        const T *R = M.v[valley].rot[sub];
+        toDev(R, kE[0], kE[1], kE[2], k);
+        flushPos(R, dP, pos, EK.box);
         const int e = scatterParticle(M, k, E, valley, sub, region, rng);
         if (e) {
           myErr = e;
@@ -593,6 +639,7 @@ __global__ void __launch_bounds__(256, MINB)
         } else {
           tau = -m_log(rng.ulog()) * tauOf(M, valley, region);
         }
+        toEcs(M.v[valley].rot[sub], k[0], k[1], k[2], kE);
       }
     } else if (can) {
       // the free flight ends either at the end of step s (bulkParticleStep
@@ -605,7 +652,7 @@ __global__ void __launch_bounds__(256, MINB)
         live = false;
         s = nSteps;
       } else {
-        driftBulk(M.v[valley], sub, EK.fv[valley][sub], ev ? tau : rem, k, E, pos, kN, EK.box);
+        const T vf = driftEcs(M.v[valley], EK.fv[valley][sub], ev ? tau : rem, kE, E, dP);
         if (ev) {
           tIn += tau;
           pend = true;
@@ -614,12 +661,10 @@ __global__ void __launch_bounds__(256, MINB)
           gtau -= dt;
           if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
             gtau = -m_log(rng.ulog()) * M.grainTau;
-          const ValleyK<T> &V = M.v[valley];
           const T *g = EK.g[valley][sub];
-          const T npf = m_sqrt(T(1) + T(4) * V.alpha * gammaOf(V, E));
           const int slot = (s % kAsyncWindow) * 32 + lane;
           winE[slot] = E;
-          winD[slot] = m_div(V.cX * (g[0] * kN[0] + g[1] * kN[1] + g[2] * kN[2]), npf);
+          winD[slot] = vf * (g[0] * kE[0] + g[1] * kE[1] + g[2] * kE[2]);
           winVal[slot] = (uint8_t)valley;
           s++;
           tIn = T(0);
@@ -635,6 +680,10 @@ __global__ void __launch_bounds__(256, MINB)
     if (bins[i] != 0.f)
       atomicAdd(&obsE[i], (double)bins[i]);
   if (active) {
+    T k[3];
+    const T *R = M.v[valley].rot[sub];
+    toDev(R, kE[0], kE[1], kE[2], k);
+    flushPos(R, dP, pos, EK.box);
     st.kx[gi] = k[0];
     st.ky[gi] = k[1];
     st.kz[gi] = k[2];

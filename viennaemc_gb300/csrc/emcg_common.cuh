@@ -187,7 +187,8 @@ template <> struct PhiloxSrc<double> {
 
 template <> struct PhiloxSrc<float> {
   uint32_t c0, c1, c2, c3, k0, k1;
-  uint32_t b[4];
+  uint32_t b0, b1, b2, b3; // scalars, not an array: a dynamically indexed
+                           // array would live in local memory
   int nb;
   __device__ __forceinline__ void init(uint32_t pid, uint32_t step,
                                        uint32_t stream, uint32_t key0,
@@ -202,11 +203,16 @@ template <> struct PhiloxSrc<float> {
   }
   __device__ __forceinline__ uint32_t word() {
     if (nb == 0) {
-      philox4x32_10(c0, c1, c2, c3, k0, k1, b);
+      uint32_t o[4];
+      philox4x32_10(c0, c1, c2, c3, k0, k1, o);
+      b0 = o[0];
+      b1 = o[1];
+      b2 = o[2];
+      b3 = o[3];
       c2++;
       nb = 4;
     }
-    uint32_t w = b[4 - nb];
+    const uint32_t w = nb == 4 ? b0 : nb == 3 ? b1 : nb == 2 ? b2 : b3;
     nb--;
     return w;
   }
