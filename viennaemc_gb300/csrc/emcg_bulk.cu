@@ -487,9 +487,9 @@ __global__ void bulkInitKernel(StateK<T> st, const ModelK<T> *__restrict__ model
 // most kAsyncWindow steps ahead of the slowest lane of its warp.  Both
 // constants were chosen by measurement on 2^20 electrons.
 // ---------------------------------------------------------------------------
-constexpr int kAsyncWindow = 12;
+constexpr int kAsyncWindow = 16;
 // lanes of a warp that wait at an event before the warp scatters them together
-constexpr int kEventBatch = 6;
+constexpr int kEventBatch = 8;
 
 __host__ __device__ constexpr size_t asyncSmemBytes(int nWarps, int nSteps, int Q) {
   return (size_t)nSteps * Q * sizeof(float) +
@@ -597,6 +597,7 @@ __global__ void __launch_bounds__(256, MINB)
   PhiloxSrc<T> rng;
   rng.init(pid, step0, EK.stream, EK.key0, EK.key1);
   int flushed = 0;  // steps folded into the block sums
+  int ws = 0;        // window slot of step s (s mod kAsyncWindow)
   bool pend = false; // drifted to an event inside step s, not yet scattered
   while (true) {
     const int sMin = __reduce_min_sync(0xffffffffu, s);
@@ -662,14 +663,15 @@ __global__ void __launch_bounds__(256, MINB)
           if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
             gtau = -m_log(rng.ulog()) * M.grainTau;
           const T *g = EK.g[valley][sub];
-          const int slot = (s % kAsyncWindow) * 32 + lane;
+          const int slot = ws * 32 + lane;
           winE[slot] = E;
           winD[slot] = vf * (g[0] * kE[0] + g[1] * kE[1] + g[2] * kE[2]);
           winVal[slot] = (uint8_t)valley;
           s++;
           tIn = T(0);
           nEv = 0;
-          rng.init(pid, step0 + (uint32_t)s, EK.stream, EK.key0, EK.key1);
+          ws = ws + 1 == kAsyncWindow ? 0 : ws + 1;
+          rng.restart(step0 + (uint32_t)s);
         }
       }
     }

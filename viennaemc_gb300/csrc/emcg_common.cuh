@@ -201,6 +201,12 @@ template <> struct PhiloxSrc<float> {
     k1 = key1;
     nb = 0;
   }
+  // init() for another step of the same particle and stream
+  __device__ __forceinline__ void restart(uint32_t step) {
+    c1 = step;
+    c2 = 0;
+    nb = 0;
+  }
   __device__ __forceinline__ uint32_t word() {
     if (nb == 0) {
       uint32_t o[4];
