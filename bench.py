@@ -666,7 +666,7 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def main(argv=None):
+def build_parser():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5000)
@@ -692,7 +692,11 @@ def main(argv=None):
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
-    args = ap.parse_args(argv)
+    return ap
+
+
+def main(argv=None):
+    args = build_parser().parse_args(argv)
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
