@@ -490,6 +490,11 @@ __global__ void bulkInitKernel(StateK<T> st, const ModelK<T> *__restrict__ model
 constexpr int kAsyncWindow = 16;
 // lanes of a warp that wait at an event before the warp scatters them together
 constexpr int kEventBatch = 8;
+// fixed-point scales of a warp's step sums: energy 2^-20 eV, velocity
+// 0.25 m/s per unit; below kFixMax per lane, 32 lanes stay within int32
+constexpr float kFixE = 1048576.f;
+constexpr float kFixD = 4.f;
+constexpr float kFixMax = 67108864.f;
 
 __host__ __device__ constexpr size_t asyncSmemBytes(int nWarps, int nSteps, int Q) {
   return (size_t)nSteps * Q * sizeof(float) +
@@ -597,6 +602,7 @@ __global__ void __launch_bounds__(256, MINB)
   PhiloxSrc<T> rng;
   rng.init(pid, step0, EK.stream, EK.key0, EK.key1);
   int flushed = 0;  // steps folded into the block sums
+  float accE = 0.f, accD = 0.f, accC = 0.f; // one valley: sums of a step of the 32-step group
   int ws = 0;        // window slot of step s (s mod kAsyncWindow)
   bool pend = false; // drifted to an event inside step s, not yet scattered
   while (true) {
@@ -604,11 +610,37 @@ __global__ void __launch_bounds__(256, MINB)
     for (; flushed < sMin; flushed++) {
       const int slot = (flushed % kAsyncWindow) * 32 + lane;
       for (int v = 0; v < nV; v++) {
-        const bool in = live && winVal[slot] == v;
-        const T e = warpSum(in ? winE[slot] : T(0));
-        const T d = warpSum(in ? winD[slot] : T(0));
+        const bool in = live && (nV == 1 || winVal[slot] == v);
+        const T ev = in ? winE[slot] : T(0), dv = in ? winD[slot] : T(0);
+        // the warp's sums in fixed point, exact and one instruction each
+        // (redux.sync); a step with a value out of range sums in float
+        const T fe = ev * kFixE, fd = dv * kFixD;
+        T e, d;
+        if (__all_sync(0xffffffffu, fabsf(fe) < kFixMax && fabsf(fd) < kFixMax)) {
+          e = (T)(int)__reduce_add_sync(0xffffffffu, (unsigned)__float2int_rn(fe)) *
+              (T(1) / kFixE);
+          d = (T)(int)__reduce_add_sync(0xffffffffu, (unsigned)__float2int_rn(fd)) *
+              (T(1) / kFixD);
+        } else {
+          e = warpSum(ev);
+          d = warpSum(dv);
+        }
         const unsigned c = __popc(__ballot_sync(0xffffffffu, in));
-        if (lane == 0) {
+        if (nV == 1) {
+          // one valley: lane (step mod 32) keeps the step's sums, and the
+          // warp adds 32 steps to the block sums in one go
+          if (lane == (flushed & 31)) {
+            accE = e;
+            accD = d;
+            accC = (float)c;
+          }
+          if ((flushed & 31) == 31) {
+            float *b = bins + (size_t)((flushed & ~31) + lane) * Q;
+            atomicAdd(b + 0, accE);
+            atomicAdd(b + 1, accD);
+            atomicAdd(b + 2, accC);
+          }
+        } else if (lane == 0) {
           float *b = bins + (size_t)flushed * Q + v * 3;
           atomicAdd(b + 0, e);
           atomicAdd(b + 1, d);
@@ -666,7 +698,8 @@ __global__ void __launch_bounds__(256, MINB)
           const int slot = ws * 32 + lane;
           winE[slot] = E;
           winD[slot] = vf * (g[0] * kE[0] + g[1] * kE[1] + g[2] * kE[2]);
-          winVal[slot] = (uint8_t)valley;
+          if (nV > 1)
+            winVal[slot] = (uint8_t)valley;
           s++;
           tIn = T(0);
           nEv = 0;
@@ -675,6 +708,12 @@ __global__ void __launch_bounds__(256, MINB)
         }
       }
     }
+  }
+  if (nV == 1 && lane < (flushed & 31)) { // the last, partial group of steps
+    float *b = bins + (size_t)((flushed & ~31) + lane) * Q;
+    atomicAdd(b + 0, accE);
+    atomicAdd(b + 1, accD);
+    atomicAdd(b + 2, accC);
   }
   __syncthreads();
   double *obsE = obs + (size_t)tl.ens * nSteps * Q;
