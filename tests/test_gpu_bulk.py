@@ -474,3 +474,56 @@ def test_full_size_bulk_properties_and_drift_velocity(engine, oracle):
                           os.cpu_count() or 1, True)
     vd_ref = float((o[-10000:, 0, 1] / o[-10000:, 0, 2]).mean())
     assert abs(vd - vd_ref) <= 0.04 * abs(vd_ref), (vd, vd_ref)
+
+
+def _two_valley_type(engine):
+    """Silicon X valleys (valley 0) and an isotropic valley 0.15 eV above
+    (valley 1, one subvalley), joined by zero-order intervalley phonons in both
+    directions, acoustic phonons in each."""
+    from viennaemc_gb300 import physics as P
+    mat = P.silicon_material()
+    pt = P.Electron(1000, 2.0)
+    P.add_x_valley(pt, 0.19)
+    pt.addValley(P.NonParabolicAnisotropValley([0.3, 0.3, 0.3], pt.getMass(), 1, 0.4, 0.15))
+    for v in (0, 1):
+        pt.addScatterMechanism([0], P.AcousticScatterMechanism(v, 9.0, 300.0, mat.rho,
+                                                               mat.velSound))
+    to1 = {0: [0], 1: [0], 2: [0]}
+    to0 = {0: [0, 1, 2]}
+    for cls in (P.ZeroOrderInterValleyAbsorptionScatterMechanism,
+                P.ZeroOrderInterValleyEmissionScatterMechanism):
+        pt.addScatterMechanism([0], cls("XL", 0, to1, 2e10, 0.03, 300.0, mat.rho, 1))
+        pt.addScatterMechanism([0], cls("LX", 1, to0, 2e10, 0.03, 300.0, mat.rho, 0))
+    pt.initScatterTables()
+    return pt
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_two_valley_kernels_equal_lockstep(engine, mode):
+    """A two-valley model (per-valley observables, intervalley transfer) in the
+    block-queued and warp-asynchronous kernels against the lockstep kernel:
+    trajectories agree bar last-ulp branch flips, per-valley counts and mean
+    energies agree closely, and both valleys are populated."""
+    pt = _two_valley_type(engine)
+    spec = engine.EnsembleSpec(0, 20000, 3e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 23, 0)
+    runs = []
+    for queued in (0, mode):
+        b = engine.BulkBatch([pt], [spec], "fp32")
+        b.set_launch(queued=queued, min_blocks=4, steps_per_launch=40)
+        b.init_particles(0)
+        obs = b.step(300)
+        runs.append((b.get_state(0), obs))
+        b.close()
+    (a, oa), (q, oq) = runs
+    bad = a.valley != q.valley
+    for f in ("kx", "ky", "kz", "energy", "px"):
+        x, y = getattr(a, f), getattr(q, f)
+        bad |= np.abs(x - y) > 2e-5 * np.max(np.abs(x))
+    assert bad.sum() <= a.n // 100, bad.sum()
+    cnt_a, cnt_q = oa[0, :, :, 2], oq[0, :, :, 2]
+    assert np.all(cnt_a.sum(axis=1) == 20000) and np.all(cnt_q.sum(axis=1) == 20000)
+    assert cnt_a[-1, 1] > 100  # the upper valley is populated
+    assert np.max(np.abs(cnt_a - cnt_q)) <= 200
+    ea = oa[0, 100:, :, 0].sum(axis=0) / cnt_a[100:].sum(axis=0)
+    eq = oq[0, 100:, :, 0].sum(axis=0) / cnt_q[100:].sum(axis=0)
+    assert np.allclose(ea, eq, rtol=2e-2)
