@@ -343,7 +343,7 @@ typedef struct {
   uint32_t stream;
   int32_t poisson_max_cycles;   /* Newton / defect-correction iterations */
   double poisson_rtol;          /* relative residual target */
-  int32_t poisson_smooth;       /* red-black sweeps before and after */
+  int32_t poisson_smooth;       /* red-black sweeps before and after (0: 3) */
   int32_t poisson_fp32;         /* 1: float V-cycles in double refinement */
   int32_t round_expected;       /* 1: expected particles at the contacts rounded to
                                    whole particles, as electronVWD

@@ -732,7 +732,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     rel = scale > 0 ? aF / scale : aF;
     if (rel <= rtol || it == maxCycles)
       break;
-    const int nv = rel < M.twoCycleRel ? M.vcycles : 1;
+    // under the update-size rule a Newton step needs only a rough correction
+    const int nv = updTol <= 0. && rel < M.twoCycleRel ? M.vcycles : 1;
     for (int vc = 0; vc < nv; vc++) {
       // one V-cycle: the distributed levels down ...
       const int Ls = M.firstSmall;
@@ -1268,7 +1269,8 @@ static int32_t solveT(PoissonMG &P, double *pot, const double *conc, bool resetB
     rel = scale > 0 ? stats[0] / scale : stats[0];
     if (rel <= rtol || it == maxCycles)
       break;
-    const int nv = rel < P.twoCycleRel ? P.vcyclesPerNewton : 1;
+    // under the update-size rule a Newton step needs only a rough correction
+    const int nv = P.updTol <= 0. && rel < P.twoCycleRel ? P.vcyclesPerNewton : 1;
     for (int k = 0; k < nv; k++)
       vcycle<MT>(P, 0, st);
     updatePotKernel<MT><<<grid, kBlock, 0, st>>>(pot, K0.d, L0.fixed, n, P.stats);
@@ -1327,8 +1329,8 @@ constexpr int kNAMaxDim = 8192;                // nodes per dimension
 constexpr int kNAMaxLevels = 16;               // as the allocating hierarchy
 constexpr int kNAMaxContacts = 64;
 constexpr int kNAMaxDevices = 64;
-constexpr int kNAVcyclesPerNewton = 2; // as PoissonMG's defaults
-constexpr double kNATwoCycleRel = 1e-2;
+constexpr int kNAVcyclesPerNewton = 3; // as PoissonMG's defaults
+constexpr double kNATwoCycleRel = 1e30;
 constexpr int kNALevelNodes = 2 * kNAMaxNodes; // nodes of all levels together
 constexpr int kNA1D = 16 * kNAMaxDim;          // 1-D transfer entries of all levels
 
@@ -1738,7 +1740,7 @@ extern "C" int32_t emcg_poisson_solve_noalloc(const emcg_device_desc *dv, double
     resetBCKernel<<<grid, kBlock, 0, st>>>(d_pot, resMask, d_conc ? resNe : resEq, n);
     EMCG_CUDA(cudaGetLastError());
   }
-  const int pre = smooth > 0 ? smooth : 2, post = pre, coarseSweeps = 40;
+  const int pre = smooth > 0 ? smooth : 3, post = pre, coarseSweeps = 16;
   LevelK<float> K0 = levelK<float>(lev[0]);
   double h_stats[2] = {0, 0};
   double rel = INFINITY;

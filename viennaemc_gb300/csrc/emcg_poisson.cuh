@@ -68,12 +68,17 @@ struct PoissonMG {
   uint8_t *resetMask = nullptr;
   double *resetEq = nullptr, *resetNe = nullptr;
   double *stats = nullptr; // [max|F|, scale, max|d|] as ordered bits
-  int pre = 2, post = 2, coarseSweeps = 40;
+  // red-black sweeps before and after the coarse correction, and sweeps on
+  // the coarsest level
+  int pre = 3, post = 3, coarseSweeps = 16;
   // V-cycles on the correction equation per Newton step once the relative
-  // residual is below twoCycleRel; above it one (while Newton steps are clamped
-  // a more exact linear solve gains nothing)
-  int vcyclesPerNewton = 2;
-  double twoCycleRel = 1e-2;
+  // residual is below twoCycleRel, one above it (and one under the update-size
+  // rule below, which needs only a rough correction).  Measured on the 201 x 101
+  // resistor (device steps of 5e5 electrons): three V-cycles of three sweeps
+  // from the first Newton step take 2 Newton steps per solve and the least
+  // time; two V-cycles of two sweeps from 1e-2 took 4.8 and 14 % longer.
+  int vcyclesPerNewton = 3;
+  double twoCycleRel = 1e30;
   // the reference's SOR stopping rule as an alternative: stop once a Newton
   // update changes no potential by more than updTol (thermal voltages; 0 = off)
   double updTol = 0.;

@@ -167,7 +167,7 @@ class DeviceSimulation:
     def __init__(self, device: Device, particle_type, scheme=NGP, dt=1e-16, seed=1,
                  capacity=None, precision="fp64", carriers_per_particle=1.0,
                  potential_init=False, round_counts=False, tau_region_is_valley=False,
-                 poisson_rtol=1e-8, poisson_max_cycles=60, poisson_fp32=True, poisson_smooth=2,
+                 poisson_rtol=1e-8, poisson_max_cycles=60, poisson_fp32=True, poisson_smooth=0,
                  stream=0, poisson_update_tol=0.0):
         self._lib = L.lib()
         self.device = device
