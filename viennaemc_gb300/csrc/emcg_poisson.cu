@@ -390,7 +390,8 @@ template <class MT> __device__ __forceinline__ void cSync(const CLevel<MT> &L) {
     cg::this_cluster().sync();
 }
 
-template <class MT> __device__ void cSmooth(const CCtx &c, const CLevel<MT> &L, int color) {
+template <class MT> __device__ void cSmooth(const CCtx &c, const CLevel<MT> &Lr, int color) {
+  const CLevel<MT> L = Lr; // a private copy: stores to shared memory cannot alias it
   int r0, r1;
   cOwnRows(c, L, r0, r1);
   const int half = (L.nx + 1) / 2, cnt = half * (r1 - r0);
@@ -419,7 +420,8 @@ template <class MT> __device__ void cSmooth(const CCtx &c, const CLevel<MT> &L, 
 
 // residual r - A d of the correction equation at this CTA's nodes of level F
 // (0 at Dirichlet nodes), as restrictKernel evaluates it
-template <class MT> __device__ void cResidual(const CCtx &c, const CLevel<MT> &F) {
+template <class MT> __device__ void cResidual(const CCtx &c, const CLevel<MT> &Fr) {
+  const CLevel<MT> F = Fr;
   int r0, r1;
   cOwnRows(c, F, r0, r1);
   const int cnt = F.nx * (r1 - r0);
@@ -466,7 +468,8 @@ __device__ __forceinline__ void cRestrictRows(const CCtx &c, const CLevel<MT> &F
 
 // coarse right-hand side P^T (fine residual), reaction by injection, d = 0
 template <class MT>
-__device__ void cRestrict(const CCtx &c, const CLevel<MT> &F, const CLevel<MT> &Cc) {
+__device__ void cRestrict(const CCtx &c, const CLevel<MT> &Fr, const CLevel<MT> &Cr) {
+  const CLevel<MT> F = Fr, Cc = Cr;
   int Y0, Y1;
   cRestrictRows(c, F, Cc, Y0, Y1);
   const int cnt = Cc.nx * (Y1 - Y0);
@@ -505,7 +508,8 @@ __device__ void cRestrict(const CCtx &c, const CLevel<MT> &F, const CLevel<MT> &
 }
 
 template <class MT>
-__device__ void cProlong(const CCtx &c, const CLevel<MT> &F, const CLevel<MT> &Cc) {
+__device__ void cProlong(const CCtx &c, const CLevel<MT> &Fr, const CLevel<MT> &Cr) {
+  const CLevel<MT> F = Fr, Cc = Cr;
   int r0, r1;
   cOwnRows(c, F, r0, r1);
   const int cnt = F.nx * (r1 - r0);
