@@ -4,8 +4,12 @@
 // registers; per-step ensemble observables are reduced warp -> block ->
 // device with double accumulators.
 #include <algorithm>
+#include <atomic>
+#include <climits>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "emcg_common.cuh"
@@ -813,8 +817,9 @@ struct BulkImpl {
   int64_t offCap = 0;
   bool replay = false;
   double lastMs = 0;
-  // host staging for state transfer
-  std::vector<unsigned char> stage;
+  // pinned host staging for state uploads (grown on demand)
+  void *pinned = nullptr;
+  size_t pinnedBytes = 0;
   // graph replay of one launch of steps: [observable reset] -> [step kernel],
   // instantiated per launch shape, the step offset updated before each replay
   bool useGraph = false;
@@ -1182,6 +1187,8 @@ static void freeBulk(BulkImpl *b) {
   cudaFree(b->dWords);
   cudaFree(b->dOff);
   freeRateScratch(b->rateScratch);
+  if (b->pinned)
+    cudaFreeHost(b->pinned);
   dropGraph(b);
   if (b->ev0)
     cudaEventDestroy(b->ev0);
@@ -1331,32 +1338,78 @@ extern "C" int64_t emcg_num_particles(emcg_handle *h, int32_t e) {
   return b->count[e];
 }
 
+// Run f(lo, hi) over [0, n) on up to 8 host threads (one below 64k items).
+template <class F> static void parallelRange(int64_t n, F f) {
+  const int64_t kMinPer = 1 << 16;
+  int nt = (int)std::min<int64_t>(8, std::max<int64_t>(1, n / kMinPer));
+  nt = std::max(1, std::min(nt, (int)std::thread::hardware_concurrency()));
+  if (nt == 1) {
+    f(int64_t(0), n);
+    return;
+  }
+  std::vector<std::thread> th;
+  const int64_t per = (n + nt - 1) / nt;
+  for (int k = 0; k < nt; k++) {
+    const int64_t lo = std::min(n, k * per), hi = std::min(n, lo + per);
+    th.emplace_back([=] { f(lo, hi); });
+  }
+  for (auto &t : th)
+    t.join();
+}
+
+// Upload a host state: converted on the host threads into pinned staging,
+// then one asynchronous copy per field.
 template <class T>
 static int32_t setStateTyped(BulkImpl *b, int e, const emcg_state *s) {
   const int64_t n = s->n, base = b->begin[e];
   const double *src[9] = {s->kx, s->ky, s->kz, s->px, s->py, s->pz, s->energy, s->tau,
                           s->grain_tau};
-  std::vector<T> tmp((size_t)std::max<int64_t>(n, 1));
-  for (int f = 0; f < 9; f++) {
+  for (int f = 0; f < 9; f++)
     EMCG_CHECK_ARG(src[f] != nullptr, "state field %d is NULL", f);
-    for (int64_t i = 0; i < n; i++)
-      tmp[i] = (T)src[f][i];
-    if (n)
-      EMCG_CUDA(cudaMemcpy((T *)b->dState[f] + base, tmp.data(), n * sizeof(T),
-                           cudaMemcpyHostToDevice));
-  }
   EMCG_CHECK_ARG(s->valley && s->sub && s->region, "state index arrays are NULL");
-  std::vector<uint32_t> meta((size_t)std::max<int64_t>(n, 1));
-  for (int64_t i = 0; i < n; i++) {
-    EMCG_CHECK_ARG(s->valley[i] >= 0 && s->valley[i] < b->ensNV[e] && s->sub[i] >= 0 &&
-                       s->sub[i] < EMCG_MAX_DEG && s->region[i] >= 0 &&
-                       s->region[i] < EMCG_MAX_REGIONS,
-                   "particle %lld: valley/sub/region out of range", (long long)i);
-    meta[i] = packMeta(s->valley[i], s->sub[i], s->region[i]);
+  if (n == 0)
+    return EMCG_OK;
+  const size_t need = (size_t)n * (9 * sizeof(T) + sizeof(uint32_t));
+  if (b->pinnedBytes < need) {
+    EMCG_CUDA(cudaStreamSynchronize(b->stream)); // an earlier upload may still read it
+    if (b->pinned)
+      cudaFreeHost(b->pinned);
+    b->pinned = nullptr;
+    b->pinnedBytes = 0;
+    EMCG_CUDA(cudaHostAlloc(&b->pinned, need, cudaHostAllocDefault));
+    b->pinnedBytes = need;
   }
-  if (n)
-    EMCG_CUDA(cudaMemcpy(b->dMeta + base, meta.data(), n * sizeof(uint32_t),
-                         cudaMemcpyHostToDevice));
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  T *stage = static_cast<T *>(b->pinned);
+  uint32_t *meta = reinterpret_cast<uint32_t *>(stage + (size_t)9 * n);
+  const int nv = b->ensNV[e];
+  std::atomic<int64_t> badIdx(INT64_MAX);
+  parallelRange(n, [&](int64_t lo, int64_t hi) {
+    for (int f = 0; f < 9; f++) {
+      T *dst = stage + (size_t)f * n;
+      const double *sp = src[f];
+      for (int64_t i = lo; i < hi; i++)
+        dst[i] = (T)sp[i];
+    }
+    for (int64_t i = lo; i < hi; i++) {
+      const int32_t v = s->valley[i], sb = s->sub[i], r = s->region[i];
+      if (v < 0 || v >= nv || sb < 0 || sb >= EMCG_MAX_DEG || r < 0 || r >= EMCG_MAX_REGIONS) {
+        int64_t cur = badIdx.load();
+        while (i < cur && !badIdx.compare_exchange_weak(cur, i)) {
+        }
+        return;
+      }
+      meta[i] = packMeta(v, sb, r);
+    }
+  });
+  EMCG_CHECK_ARG(badIdx.load() == INT64_MAX, "particle %lld: valley/sub/region out of range",
+                 (long long)badIdx.load());
+  for (int f = 0; f < 9; f++)
+    EMCG_CUDA(cudaMemcpyAsync((T *)b->dState[f] + base, stage + (size_t)f * n, n * sizeof(T),
+                              cudaMemcpyHostToDevice, b->stream));
+  EMCG_CUDA(cudaMemcpyAsync(b->dMeta + base, meta, n * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                            b->stream));
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
   return EMCG_OK;
 }
 
