@@ -168,8 +168,9 @@ def run_engine(args):
     device = _device_bench(args, rank) if args.device_steps > 0 else None
     if device is not None and args.mosfet_steps > 0:
         device["mosfet_sweep"] = _mosfet_bench(args, rank)
+    p2p = _p2p_bench(args, rank) if args.p2p_n > 0 else None
     _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units, h2d, d2h,
-            value64, vd32, vd64, win, k64, wall, clocks, device, batched)
+            value64, vd32, vd64, win, k64, wall, clocks, device, batched, p2p)
     if ws > 1:
         torch.distributed.destroy_process_group()
 
@@ -220,7 +221,7 @@ def _fp64(v, pt, args, N, K, W, per, rank, avg):
 
 
 def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units, h2d, d2h,
-            value64, vd32, vd64, win, k64, wall, clocks, device=None, batched=None):
+            value64, vd32, vd64, win, k64, wall, clocks, device=None, batched=None, p2p=None):
     peak, peak_src = _peaks()
     bpp = BYTES_PER_PARTICLE_STEP["fp32"]
     achieved = bpp * value / 1e9  # algorithmic GB/s (72 B per particle-step)
@@ -259,6 +260,8 @@ def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units,
         line["batched"] = batched
     if device:
         line["device"] = device
+    if p2p:
+        line["p2p_coulomb"] = p2p
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(N, args.cpu_seconds)
     if rank == 0:
@@ -300,6 +303,39 @@ def _rate_rebuild_timing(b, models, reps=50):
             "levels": h.n_levels, "source": "device rates (CUDA tensor)",
             "timing": "host wall clock, call + kernel, %d rebuilds of %d models" %
                       (reps, len(raws))}
+
+
+def _p2p_bench(args, rank):
+    """Particle-particle Coulomb sums of the FMM handlers, direct on the GPU:
+    n electrons and donors in a cube with the 1 nm cutoff; FP32 and FP64 pair
+    terms; the oracle's direct sum on the host cores for a bounded sample of
+    targets."""
+    from viennaemc_gb300 import p2p
+    n = args.p2p_n
+    rs = np.random.default_rng(7 + rank)
+    box = 1e-7
+    pos = rs.random((3, n)) * box
+    q = np.where(np.arange(n) % 2 == 0, -1.0, 1.0) * 1.60219e-19
+    out = {"workload": f"{n} charges (electrons and donors alternating) in a {box:g} m cube, "
+                       "1 nm cutoff, no periodic copies", "pairs": n * (n - 1)}
+    for prec in ("fp32", "fp64"):
+        p2p.coulomb(pos[:, :2048], q[:2048], precision=prec)  # warm-up
+        ms = []
+        for _ in range(3 if prec == "fp32" else 1):
+            _, _, k = p2p.coulomb(pos, q, precision=prec, return_ms=True)
+            ms.append(k)
+        out[prec] = {"kernel_ms": min(ms), "pairs_per_s": n * (n - 1) / (min(ms) / 1e3)}
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle as po
+        po.build()
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        po.p2p_coulomb(pos, q, 1e9, threads=threads)
+        el = time.perf_counter() - t0
+        out["cpu_oracle"] = {"pairs_per_s": n * (n - 1) / el, "cores": threads,
+                             "kind": "port", "sample": f"the same {n} charges, double"}
+    return out
 
 
 def _batched_bench(args, rank):
@@ -692,6 +728,8 @@ def build_parser():
     ap.add_argument("--mosfet-steps", type=int, default=200,
                     help="timed steps of the 8-bias MOSFET batch (0: skip it)")
     ap.add_argument("--fp64-steps", type=int, default=1500)
+    ap.add_argument("--p2p-n", type=int, default=32768,
+                    help="charges of the particle-particle Coulomb leg (0: skip it)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")

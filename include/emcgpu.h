@@ -283,6 +283,29 @@ int32_t emcg_update_rates(emcg_handle *h, int32_t model, const double *raw,
    (n_tablesets doubles, NULL to skip).  Waits for the handle's stream. */
 int32_t emcg_get_rates(emcg_handle *h, int32_t model, double *tables, double *tau);
 
+/* ---- particle-particle Coulomb (FMM handlers) ------------------------- */
+/* The particle-particle sums that scalFMM computes for
+   emcFMMParticleHandler (include/ParticleHandler/emcFMMParticleHandler.hpp:
+   160-167, 381-393) and FMMBulkParticleHandler
+   (examples/bulkSimulationFMM/FMMBulkParticleHandler.hpp:203-205, 433-440),
+   evaluated directly on the GPU.  For every particle i, over every other
+   particle j and every periodic copy of the box, the pair term of
+   FP2PRCutoff::NonMutualParticles (include/ParticleHandler/FMM/
+   FP2PRCutoff.hpp:64-100): force_i += -q_i q_j d / r^3, potential_i +=
+   q_j / r, with d = x_i - x_j rescaled to the cutoff radius when the pair is
+   closer.  These are the container values before the handlers' Coulomb factor.
+   pos: 3 x n doubles (x plane, y plane, z plane) [m]; charge: n [C];
+   inv_cutoff: 1 / cutoff radius [1/m] (1e9: the reference's 1 nm; 0: none);
+   images: copies of the cubic box of width box on each side in x, y and z
+   (0: the box alone; a particle sees its own copies, not itself);
+   precision: EMCG_FP64 (the reference's arithmetic order) or EMCG_FP32
+   (float pair terms, double sums per tile).  force: 3 x n, potential: n;
+   *kernel_ms (may be NULL): device time of the sums. */
+int32_t emcg_p2p_coulomb(const double *pos, const double *charge, int64_t n,
+                         double inv_cutoff, double box, int32_t images,
+                         int32_t precision, double *force, double *potential,
+                         double *kernel_ms);
+
 /* ---- single-particle kernels (known-answer tests of the reference) ----- */
 /* drift() of include/emcParticleDrift.hpp:11-36 for n independent
    particles of valley v of model 0: k, pos (3 x n, SoA) and energy in/out,

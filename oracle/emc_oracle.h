@@ -110,6 +110,15 @@ int32_t oc_build_tables(oc_model *m);
 /* replace the rates of one built (valley, region) table set and
    renormalise it (reinitScatterTables with caller-filled rates) */
 int32_t oc_set_raw_tables(oc_model *m, int32_t valley, int32_t region, const double *raw);
+
+/* particle-particle Coulomb sums of the FMM handlers, direct (emc_oracle_p2p.c):
+   pos 3 x n planes, q n; invCut = 1 / cutoff radius (0: no cutoff); box and
+   images: periodic copies per side; force 3 x n, pot n */
+void oc_p2p_pair(double xt, double yt, double zt, double qt, double xs, double ys, double zs,
+                 double qs, double invCut, double out[4]);
+int32_t oc_p2p_coulomb(const double *pos, const double *q, int64_t n, double invCut,
+                       double box, int32_t images, double *force, double *pot,
+                       int32_t threads);
 int32_t oc_get_raw_table(const oc_model *m, int32_t valley, int32_t region,
                          int32_t idxTable, double *out);
 int32_t oc_get_norm_table(const oc_model *m, int32_t valley, int32_t region,

@@ -72,6 +72,10 @@ def _declare(L):
         getattr(L, fn).argtypes = [vp, i32, i32, i32, P(d)]
     L.oc_set_raw_tables.restype = i32
     L.oc_set_raw_tables.argtypes = [vp, i32, i32, P(d)]
+    L.oc_p2p_pair.restype = None
+    L.oc_p2p_pair.argtypes = [d, d, d, d, d, d, d, d, d, P(d)]
+    L.oc_p2p_coulomb.restype = i32
+    L.oc_p2p_coulomb.argtypes = [P(d), P(d), C.c_int64, d, d, i32, P(d), P(d), i32]
     L.oc_n_tables.restype = i32
     L.oc_n_tables.argtypes = [vp, i32, i32]
     L.oc_table_mech.restype = i32
@@ -546,3 +550,23 @@ class Device:
 def truncate(st: State, n: int) -> State:
     """View of the first n particles (copy)."""
     return st.resize(n)
+
+
+# ---- particle-particle Coulomb (FMM handlers, direct sum) -------------------------
+def p2p_pair(t, qt, s, qs, inv_cutoff=1e9):
+    """NonMutualParticles for one pair: (force x, y, z, potential)."""
+    out = np.zeros(4)
+    lib().oc_p2p_pair(t[0], t[1], t[2], qt, s[0], s[1], s[2], qs, inv_cutoff, dptr(out))
+    return out
+
+
+def p2p_coulomb(pos, q, inv_cutoff=1e9, box=0.0, images=0, threads=0):
+    """Direct Coulomb sums: pos (3, n), q (n,) -> force (3, n), potential (n,)."""
+    p = np.ascontiguousarray(np.asarray(pos, np.float64).reshape(3, -1))
+    qq = np.ascontiguousarray(np.asarray(q, np.float64))
+    n = qq.size
+    f = np.zeros((3, n))
+    pot = np.zeros(n)
+    assert lib().oc_p2p_coulomb(dptr(p.reshape(-1)), dptr(qq), n, inv_cutoff, box, images,
+                                dptr(f.reshape(-1)), dptr(pot), threads) == 0
+    return f, pot

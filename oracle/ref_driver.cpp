@@ -40,6 +40,7 @@
 #include <ValleyTypes/emcNonParabolicAnistropValley.hpp>
 #include <ScatterMechanisms/emcHotPhononFroehlichMechanism.hpp>
 #include <emcPhononBath.hpp>
+#include <ParticleHandler/FMM/FP2PRCutoff.hpp>
 #include <PMSchemes/emcCICScheme.hpp>
 #include <PMSchemes/emcNECScheme.hpp>
 #include <PMSchemes/emcNGPScheme.hpp>
@@ -557,6 +558,57 @@ static int runReinit(int argc, char **argv) {
   return 0;
 }
 
+// The reference's particle-particle pair kernel with the 1 nm cutoff
+// (include/ParticleHandler/FMM/FP2PRCutoff.hpp:18-100), as the FMM handlers'
+// P2P evaluates it: n particles in a cube, each target summed over every
+// other particle in index order with NonMutualParticles, plus the pairs of a
+// MutualParticles call.  args: n box seed
+static int runP2P(int argc, char **argv) {
+  if (argc < 5)
+    return 2;
+  const int n = std::atoi(argv[2]);
+  const double box = std::atof(argv[3]);
+  std::mt19937_64 g(std::strtoull(argv[4], nullptr, 10));
+  std::uniform_real_distribution<double> u(0., 1.);
+  std::vector<double> x(n), y(n), z(n), q(n);
+  for (int i = 0; i < n; i++) {
+    x[i] = u(g) * box;
+    y[i] = u(g) * box;
+    z[i] = u(g) * box;
+    q[i] = (i % 3 == 2 ? 1. : -1.) * constants::q;
+  }
+  // a few pairs closer than the cutoff
+  for (int i = 1; i < n; i += 7) {
+    x[i] = x[i - 1] + 3e-10 * (u(g) - 0.5);
+    y[i] = y[i - 1] + 3e-10 * (u(g) - 0.5);
+    z[i] = z[i - 1] + 3e-10 * (u(g) - 0.5);
+  }
+  std::vector<double> fx(n, 0.), fy(n, 0.), fz(n, 0.), pot(n, 0.);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      if (j != i)
+        FP2PRCutoff::NonMutualParticles<double>(x[i], y[i], z[i], q[i], &fx[i], &fy[i], &fz[i],
+                                                &pot[i], x[j], y[j], z[j], q[j]);
+  rec("x", x);
+  rec("y", y);
+  rec("z", z);
+  rec("q", q);
+  rec("fx", fx);
+  rec("fy", fy);
+  rec("fz", fz);
+  rec("pot", pot);
+  // one MutualParticles call per consecutive pair: both sides of a pair
+  std::vector<double> m(8 * (n / 2), 0.);
+  for (int p = 0; p + 1 < n; p += 2) {
+    double *o = &m[8 * (p / 2)];
+    FP2PRCutoff::MutualParticles<double>(x[p], y[p], z[p], q[p], o + 0, o + 1, o + 2, o + 3,
+                                         x[p + 1], y[p + 1], z[p + 1], q[p + 1], o + 4, o + 5,
+                                         o + 6, o + 7);
+  }
+  rec("mutual", m);
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc < 2) {
     std::fprintf(stderr, "usage: ref_driver {bulk|mt} ...\n");
@@ -577,6 +629,8 @@ int main(int argc, char **argv) {
     rc = runDevice(argc, argv);
   else if (mode == "reinit")
     rc = runReinit(argc, argv);
+  else if (mode == "p2p")
+    rc = runP2P(argc, argv);
   std::cout.rdbuf(orig);
   return rc;
 }

@@ -11,6 +11,8 @@ headers by `make -C oracle ref`, which needs the reference tree) and stores:
                     (offsets into `words`, recorded by the oracle while it
                     reproduced the reference bit for bit).
   mt19937_64.npz    first words of std::mt19937_64(5489) and canonical maps.
+  p2p_cutoff.npz    the reference's particle-particle pair kernel with the 1 nm
+                    cutoff (FP2PRCutoff.hpp), summed directly over 256 particles.
   reinit_hot_phonon.npz
                     rates, normalised tables and tau of an acoustic + hot-phonon
                     Froehlich absorption/emission set before and after the
@@ -18,7 +20,7 @@ headers by `make -C oracle ref`, which needs the reference tree) and stores:
                     advanced in between (the rates change).
 
 Run from the repository root:  python tests/golden/make_golden.py [part ...]
-(parts: mt bulk device output reinit; default all).
+(parts: mt bulk device output reinit p2p; default all).
 """
 from __future__ import annotations
 
@@ -213,6 +215,21 @@ def make_output(case, outdir_name):
     print(f"{outdir_name}: {sorted(os.listdir(dst))}")
 
 
+P2P_CASE = (256, 5e-8, 11)  # particles, cube edge [m], seed
+
+
+def make_p2p():
+    """The reference's 1 nm cutoff pair kernel over 256 particles (every
+    target summed over every other particle in index order), and one mutual
+    call per consecutive pair."""
+    n, box, seed = P2P_CASE
+    d = po.run_ref("p2p", n, box, seed)
+    out = {k: d[k] for k in ("x", "y", "z", "q", "fx", "fy", "fz", "pot", "mutual")}
+    out["params"] = np.array(P2P_CASE, dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, "p2p_cutoff.npz"), **out)
+    print(f"p2p_cutoff: {n} particles in a {box:g} m cube")
+
+
 REINIT_CASE = (1000, 1.0, 20000, 1e-13)  # levels, max energy [eV], emissions, bath dt [s]
 
 
@@ -242,7 +259,7 @@ def make_mt():
 
 if __name__ == "__main__":
     po.build(force=True)
-    parts = set(sys.argv[1:]) or {"mt", "bulk", "device", "output", "reinit"}
+    parts = set(sys.argv[1:]) or {"mt", "bulk", "device", "output", "reinit", "p2p"}
     if "mt" in parts:
         make_mt()
     if "bulk" in parts:
@@ -256,3 +273,5 @@ if __name__ == "__main__":
         make_output(DEVICE_CASES[3], "output_mosfet_necvwd")
     if "reinit" in parts:
         make_reinit()
+    if "p2p" in parts:
+        make_p2p()

@@ -15,7 +15,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 LIB_PATH = os.path.join(PKG, "libemcgpu.so")
-SOURCES = ["emcg_core.cu", "emcg_bulk.cu", "emcg_device.cu", "emcg_poisson.cu"]
+SOURCES = ["emcg_core.cu", "emcg_bulk.cu", "emcg_device.cu", "emcg_poisson.cu", "emcg_p2p.cu"]
 HEADERS = ["emcg_common.cuh", "emcg_host.h", "emcg_model.h", "emcg_poisson.cuh", "emcg_rates.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -240,4 +240,6 @@ _EXTRA_DECLS.extend([
                                     C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     ("emcg_update_rates", [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32]),
     ("emcg_get_rates", [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    ("emcg_p2p_coulomb", [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_int32,
+                          C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
 ])
