@@ -306,6 +306,29 @@ int32_t emcg_p2p_coulomb(const double *pos, const double *charge, int64_t n,
                          int32_t precision, double *force, double *potential,
                          double *kernel_ms);
 
+/* Particle-particle Coulomb steps in the bulk engine: FMMBulkParticleHandler
+   (examples/bulkSimulationFMM/FMMBulkParticleHandler.hpp) on the GPU.
+   enable != 0: every step first forms, for each ensemble, the sums of
+   emcg_p2p_coulomb over its particles (charge of the ensemble) and its fixed
+   charges, for each of its particles (executeFMM, :203-205), and then moves
+   every particle one step with force = charge x field - (ke / eps_r) x force
+   sum (getForceAtParticle, :433-440; ke = 1 / (4 pi eps0) with the
+   reference's constants), the force rotated into each free flight's
+   subvalley frame (moveParticles, :233-277).  inv_cutoff and images as
+   emcg_p2p_coulomb, images over each ensemble's (cubic) box.  Steps then run
+   one launch each; replay is not available.  enable == 0: back to the
+   applied field alone. */
+int32_t emcg_bulk_set_coulomb(emcg_handle *h, int32_t enable, double eps_r,
+                              double inv_cutoff, int32_t images);
+/* Fixed charges of ensemble e (the handler's particle types that do not
+   move, e.g. donors): pos 3 x n planes [m], q n [C]; n = 0 removes them. */
+int32_t emcg_bulk_set_fixed_charges(emcg_handle *h, int32_t e, const double *pos,
+                                    const double *q, int64_t n);
+/* The force sums (3 x n planes, may be NULL) and potential sums (n, may be
+   NULL) of ensemble e's particles from the last Coulomb step (the container
+   values, before the Coulomb factor). */
+int32_t emcg_bulk_get_coulomb(emcg_handle *h, int32_t e, double *force, double *potential);
+
 /* ---- single-particle kernels (known-answer tests of the reference) ----- */
 /* drift() of include/emcParticleDrift.hpp:11-36 for n independent
    particles of valley v of model 0: k, pos (3 x n, SoA) and energy in/out,

@@ -875,6 +875,58 @@ int32_t oc_bulk_run_philox(const oc_model *m, oc_particles *p, double dt,
   return status;
 }
 
+int32_t oc_model_n_valleys(const oc_model *m) { return m->nV; }
+
+/* One Philox step of every particle with its own force (3 x n planes):
+   FMMBulkParticleHandler::moveParticles
+   (examples/bulkSimulationFMM/FMMBulkParticleHandler.hpp:233-277), whose
+   per-particle step is the bulk handler's with that force. */
+int32_t oc_bulk_step_forces(const oc_model *m, oc_particles *p, double dt,
+                            const double *forces, const double box[3],
+                            const double fieldDir[3], uint64_t seed, uint32_t stream,
+                            uint32_t step, int32_t nThreads, double *obs) {
+  int nV = m->nV;
+  int32_t status = 0;
+  const int64_t n = p->n;
+  double tot[OC_MAX_VALLEYS * 3];
+  memset(tot, 0, sizeof(tot));
+#ifdef _OPENMP
+  if (nThreads > 0)
+    omp_set_num_threads(nThreads);
+#pragma omp parallel
+#endif
+  {
+    double acc[OC_MAX_VALLEYS * 3];
+    memset(acc, 0, sizeof(acc));
+    oc_rng r;
+    memset(&r, 0, sizeof(r));
+    r.mode = OC_RNG_PHILOX;
+    r.seed = seed;
+    r.stream = stream;
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (int64_t i = 0; i < n; i++) {
+      dctx d;
+      oci_dctx_init(&d, &r, (uint32_t)i, step, stream);
+      const double f[3] = {forces[i], forces[n + i], forces[2 * n + i]};
+      if (bulk_particle_step(m, p, i, dt, f, box, &d))
+        status = -1;
+      if (obs)
+        accum_obs(m, p, i, fieldDir, acc);
+    }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+    for (int j = 0; j < nV * 3; j++)
+      tot[j] += acc[j];
+  }
+  if (obs)
+    for (int j = 0; j < nV * 3; j++)
+      obs[j] = tot[j];
+  return status;
+}
+
 /* examples/bulkSimulation/basicBulkParticleHandler.hpp:289-347 */
 void oc_observables(const oc_model *m, const oc_particles *p,
                     const double dir[3], double *out) {

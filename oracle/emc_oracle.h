@@ -111,6 +111,22 @@ int32_t oc_build_tables(oc_model *m);
    renormalise it (reinitScatterTables with caller-filled rates) */
 int32_t oc_set_raw_tables(oc_model *m, int32_t valley, int32_t region, const double *raw);
 
+int32_t oc_model_n_valleys(const oc_model *m);
+/* one Philox step of every particle with its own force (3 x n planes) */
+int32_t oc_bulk_step_forces(const oc_model *m, oc_particles *p, double dt,
+                            const double *forces, const double box[3],
+                            const double fieldDir[3], uint64_t seed, uint32_t stream,
+                            uint32_t step, int32_t nThreads, double *obs);
+/* FMMBulkParticleHandler's step loop: Coulomb sums over the particles (charge q)
+   and the fixed charges, then one step with charge x field - ke / epsR x sum;
+   obs: nSteps x nV x 3 (may be NULL) */
+int32_t oc_bulk_run_coulomb(const oc_model *m, oc_particles *p, double dt, double q,
+                            const double field[3], const double box[3],
+                            const double fieldDir[3], const double *fixedPos,
+                            const double *fixedQ, int64_t nFixed, double epsR, double invCut,
+                            int32_t images, uint64_t seed, uint32_t stream, uint32_t step0,
+                            int32_t nSteps, int32_t threads, double *obs);
+
 /* particle-particle Coulomb sums of the FMM handlers, direct (emc_oracle_p2p.c):
    pos 3 x n planes, q n; invCut = 1 / cutoff radius (0: no cutoff); box and
    images: periodic copies per side; force 3 x n, pot n */

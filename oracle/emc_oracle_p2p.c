@@ -18,6 +18,9 @@
 #include <omp.h>
 #endif
 
+#include <stdlib.h>
+#include <string.h>
+
 #include "emc_oracle.h"
 
 void oc_p2p_pair(double xt, double yt, double zt, double qt, double xs, double ys, double zs,
@@ -76,4 +79,53 @@ int32_t oc_p2p_coulomb(const double *pos, const double *q, int64_t n, double inv
     pot[i] = p;
   }
   return 0;
+}
+
+/* FMMBulkParticleHandler's step loop (examples/bulkSimulationFMM/
+   bulkSimulationFMM.cpp:150-168): executeFMM (the Coulomb sums over the moving
+   particles, charge q, and the fixed charges) then moveParticles with
+   force = q field - (ke / epsR) x sum (getForceAtParticle,
+   FMMBulkParticleHandler.hpp:433-440), ke from the reference's constants
+   (include/emcConstants.hpp:9, 21, 27). */
+int32_t oc_bulk_run_coulomb(const oc_model *m, oc_particles *p, double dt, double q,
+                            const double field[3], const double box[3],
+                            const double fieldDir[3], const double *fixedPos,
+                            const double *fixedQ, int64_t nFixed, double epsR, double invCut,
+                            int32_t images, uint64_t seed, uint32_t stream, uint32_t step0,
+                            int32_t nSteps, int32_t threads, double *obs) {
+  const double ke = 1. / (4 * 3.14159265358979323846 * 8.85419e-12);
+  const int64_t n = p->n, mm = n + nFixed;
+  double *src = (double *)malloc(sizeof(double) * (size_t)(4 * mm + 1));
+  double *fc = (double *)malloc(sizeof(double) * (size_t)(3 * mm + 1));
+  double *pot = (double *)malloc(sizeof(double) * (size_t)(mm + 1));
+  double *force = (double *)malloc(sizeof(double) * (size_t)(3 * n + 1));
+  int32_t st = 0;
+  for (int s = 0; s < nSteps && !st; s++) {
+    for (int64_t i = 0; i < n; i++) {
+      src[i] = p->px[i];
+      src[mm + i] = p->py[i];
+      src[2 * mm + i] = p->pz[i];
+      src[3 * mm + i] = q;
+    }
+    for (int64_t j = 0; j < nFixed; j++) {
+      src[n + j] = fixedPos[j];
+      src[mm + n + j] = fixedPos[nFixed + j];
+      src[2 * mm + n + j] = fixedPos[2 * nFixed + j];
+      src[3 * mm + n + j] = fixedQ[j];
+    }
+    if (oc_p2p_coulomb(src, src + 3 * mm, mm, invCut, box[0], images, fc, pot, threads)) {
+      st = -1;
+      break;
+    }
+    for (int64_t i = 0; i < n; i++)
+      for (int v = 0; v < 3; v++)
+        force[v * n + i] = q * field[v] + -(ke / epsR) * fc[v * mm + i];
+    st = oc_bulk_step_forces(m, p, dt, force, box, fieldDir, seed, stream, step0 + (uint32_t)s,
+                             threads, obs ? obs + (size_t)s * oc_model_n_valleys(m) * 3 : NULL);
+  }
+  free(src);
+  free(fc);
+  free(pot);
+  free(force);
+  return st;
 }

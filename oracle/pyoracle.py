@@ -76,6 +76,9 @@ def _declare(L):
     L.oc_p2p_pair.argtypes = [d, d, d, d, d, d, d, d, d, P(d)]
     L.oc_p2p_coulomb.restype = i32
     L.oc_p2p_coulomb.argtypes = [P(d), P(d), C.c_int64, d, d, i32, P(d), P(d), i32]
+    L.oc_bulk_run_coulomb.restype = i32
+    L.oc_bulk_run_coulomb.argtypes = [vp, vp, d, d, P(d), P(d), P(d), P(d), P(d), C.c_int64, d, d,
+                                      i32, C.c_uint64, C.c_uint32, C.c_uint32, i32, i32, P(d)]
     L.oc_n_tables.restype = i32
     L.oc_n_tables.argtypes = [vp, i32, i32]
     L.oc_table_mech.restype = i32
@@ -303,6 +306,23 @@ class Model:
         rc = lib().oc_bulk_run_philox(self.h, C.byref(p), dt, dptr(darr(force)), dptr(darr(box)),
                                       dptr(darr(field_dir)), seed, stream, step0, n_steps,
                                       n_threads, dptr(obs) if want_obs else None)
+        assert rc == 0, rc
+        return obs
+
+    def bulk_run_coulomb(self, st: State, dt, charge, field, box, field_dir, fixed_pos,
+                         fixed_q, eps_r, inv_cutoff, images, seed, stream, step0, n_steps,
+                         n_threads=0, want_obs=True):
+        """FMMBulkParticleHandler's loop: Coulomb sums, then a step with
+        per-particle forces, n_steps times (Philox)."""
+        p = st.cstruct()
+        obs = np.zeros((n_steps, self.nV, 3)) if want_obs else None
+        fp = np.ascontiguousarray(np.asarray(fixed_pos, np.float64).reshape(3, -1))
+        fq = np.ascontiguousarray(np.asarray(fixed_q, np.float64).reshape(-1))
+        rc = lib().oc_bulk_run_coulomb(self.h, C.byref(p), dt, charge, dptr(darr(field)),
+                                       dptr(darr(box)), dptr(darr(field_dir)),
+                                       dptr(fp.reshape(-1)), dptr(fq), fq.size, eps_r,
+                                       inv_cutoff, images, seed, stream, step0, n_steps,
+                                       n_threads, dptr(obs) if want_obs else None)
         assert rc == 0, rc
         return obs
 

@@ -16,7 +16,8 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 LIB_PATH = os.path.join(PKG, "libemcgpu.so")
 SOURCES = ["emcg_core.cu", "emcg_bulk.cu", "emcg_device.cu", "emcg_poisson.cu", "emcg_p2p.cu"]
-HEADERS = ["emcg_common.cuh", "emcg_host.h", "emcg_model.h", "emcg_poisson.cuh", "emcg_rates.cuh"]
+HEADERS = ["emcg_common.cuh", "emcg_host.h", "emcg_model.h", "emcg_poisson.cuh", "emcg_rates.cuh",
+           "emcg_p2p.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 MAX_VALLEYS, MAX_DEG, MAX_MECH, MAX_NF, MAX_REGIONS = 4, 8, 32, 8, 16
@@ -242,4 +243,7 @@ _EXTRA_DECLS.extend([
     ("emcg_get_rates", [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     ("emcg_p2p_coulomb", [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_int32,
                           C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    ("emcg_bulk_set_coulomb", [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_int32]),
+    ("emcg_bulk_set_fixed_charges", [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64]),
+    ("emcg_bulk_get_coulomb", [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
 ])

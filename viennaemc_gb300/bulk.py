@@ -243,6 +243,32 @@ class BulkBatch:
         """The engine's normalised tables (raw layout) and tau per table set."""
         return get_rates(self._lib, self.h, model, self.models[model])
 
+    def set_coulomb(self, eps_r, inv_cutoff=1e9, images=0, enable=True):
+        """Particle-particle Coulomb steps (FMMBulkParticleHandler,
+        examples/bulkSimulationFMM): each step sums the Coulomb force of every
+        ensemble's particles and fixed charges on its particles, then moves
+        them with force = charge x field - (ke / eps_r) x sum."""
+        L.check(self._lib.emcg_bulk_set_coulomb(self.h, int(enable), float(eps_r),
+                                                float(inv_cutoff), int(images)))
+
+    def set_fixed_charges(self, ens: int, pos, q):
+        """Charges of ensemble ens that do not move (donors): pos (3, n), q (n,)."""
+        p = np.ascontiguousarray(np.asarray(pos, np.float64).reshape(3, -1))
+        qq = np.ascontiguousarray(np.asarray(q, np.float64).reshape(-1))
+        if p.shape[1] != qq.size:
+            raise ValueError("pos and q disagree in n")
+        self._fixed_keep = (p, qq)
+        L.check(self._lib.emcg_bulk_set_fixed_charges(self.h, ens, p.ctypes.data_as(C.c_void_p),
+                                                      qq.ctypes.data_as(C.c_void_p), qq.size))
+
+    def get_coulomb(self, ens: int):
+        """(force sums (3, n), potential sums (n,)) of the last Coulomb step."""
+        n = self.num_particles(ens)
+        f, p = np.zeros((3, n)), np.zeros(n)
+        L.check(self._lib.emcg_bulk_get_coulomb(self.h, ens, f.ctypes.data_as(C.c_void_p),
+                                                p.ctypes.data_as(C.c_void_p)))
+        return f, p
+
     def set_replay(self, words, offsets):
         w = np.ascontiguousarray(np.asarray(words, np.uint64))
         o = np.ascontiguousarray(np.asarray(offsets, np.int64))

@@ -15,6 +15,7 @@
 #include "emcg_common.cuh"
 #include "emcg_host.h"
 #include "emcg_model.h"
+#include "emcg_p2p.cuh"
 #include "emcg_rates.cuh"
 
 namespace emcg {
@@ -63,6 +64,52 @@ __device__ __forceinline__ int bulkParticleStep(const ModelK<T> &M, const EnsK<T
     tau += nt;
     driftBulk(M.v[valley], sub, EK.fv[valley][sub], nt < tRem ? nt : tRem, k, E, pos, kN,
               EK.box);
+    tRem -= nt;
+  }
+  tau -= dt;
+  gtau -= dt;
+  if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
+    gtau = -m_log(rng.ulog()) * M.grainTau;
+  return err;
+}
+
+// One particle, one time step with its own force F (FMMBulkParticleHandler::
+// moveParticles, examples/bulkSimulationFMM/FMMBulkParticleHandler.hpp:233-277):
+// the same free flights and scattering as bulkParticleStep, the force rotated
+// into the frame of the current subvalley for each free flight.
+template <class T, class Src>
+__device__ __forceinline__ int bulkParticleStepF(const ModelK<T> &M, const EnsK<T> &EK,
+                                                 const T F[3], T k[3], T pos[3], T &E, T &tau,
+                                                 T &gtau, int &valley, int &sub, int region,
+                                                 T kN[3], Src &rng) {
+  const T dt = EK.dt;
+  int err = 0;
+  auto fvOf = [&](T fv[3]) {
+    const ValleyK<T> &V = M.v[valley];
+    toEcs(V.rot[sub], F[0], F[1], F[2], fv);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      fv[i] *= V.cF[i];
+  };
+  T fv[3];
+  fvOf(fv);
+  driftBulk(M.v[valley], sub, fv, dt < tau ? dt : tau, k, E, pos, kN, EK.box);
+  T tRem = dt - tau;
+  int guard = 0;
+  while (tRem > T(0)) {
+    if (++guard > kMaxScatterPerStep) {
+      err = EMCG_ERR_TIMEOUT;
+      break;
+    }
+    int e = scatterParticle(M, k, E, valley, sub, region, rng);
+    if (e) {
+      err = e;
+      break;
+    }
+    T nt = -m_log(rng.ulog()) * tauOf(M, valley, region);
+    tau += nt;
+    fvOf(fv);
+    driftBulk(M.v[valley], sub, fv, nt < tRem ? nt : tRem, k, E, pos, kN, EK.box);
     tRem -= nt;
   }
   tau -= dt;
@@ -188,6 +235,105 @@ __global__ void __launch_bounds__(256, MINB) bulkStepKernel(StateK<T> st, const 
   recordError(err, myErr);
 }
 
+
+// ---------------------------------------------------------------------------
+// Particle-particle Coulomb steps (FMMBulkParticleHandler,
+// examples/bulkSimulationFMM).  Per step: the sources of each ensemble -- its
+// particles and its fixed charges -- are gathered, the Coulomb sums over them
+// are formed for its particles (emcg_p2p.cuh, in place of executeFMM), and
+// every particle moves one step with force = charge x field + coulFactor x sum
+// (getForceAtParticle, :433-440).
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void coulombGatherKernel(StateK<T> st, int64_t begin, int64_t n, double q,
+                                    const double *__restrict__ fixed, int64_t nf,
+                                    double *__restrict__ src) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, m = n + nf;
+  if (i >= m)
+    return;
+  if (i < n) {
+    src[i] = (double)st.px[begin + i];
+    src[m + i] = (double)st.py[begin + i];
+    src[2 * m + i] = (double)st.pz[begin + i];
+    src[3 * m + i] = q;
+  } else {
+    const int64_t j = i - n;
+    for (int v = 0; v < 4; v++)
+      src[v * m + i] = fixed[v * nf + j];
+  }
+}
+
+// One step of every particle with its own force; obs: [ens][Q] sums of this step.
+template <class T>
+__global__ void __launch_bounds__(256)
+    bulkForceStepKernel(StateK<T> st, const ModelK<T> *__restrict__ models,
+                        const EnsK<T> *__restrict__ ens, const Tile *__restrict__ tiles,
+                        uint32_t step, int nVmax, const double *__restrict__ coulF,
+                        int64_t stride, T coulFactor, double *__restrict__ obs,
+                        int *__restrict__ err) {
+  const Tile tl = tiles[blockIdx.x];
+  const EnsK<T> &EK = ens[tl.ens];
+  const ModelK<T> &M = models[EK.model];
+  const int nV = EK.nV, Q = nVmax * 3, lane = threadIdx.x & 31;
+  const int64_t gi = tl.begin + threadIdx.x;
+  const bool active = gi < tl.end;
+  const uint32_t pid = (uint32_t)(gi - EK.begin);
+  T k[3] = {0, 0, 0}, pos[3] = {0, 0, 0}, kN[3] = {0, 0, 0}, E = 0, tau = 0, gtau = 0;
+  int valley = 0, sub = 0, region = 0, myErr = 0;
+  if (active) {
+    k[0] = st.kx[gi];
+    k[1] = st.ky[gi];
+    k[2] = st.kz[gi];
+    pos[0] = st.px[gi];
+    pos[1] = st.py[gi];
+    pos[2] = st.pz[gi];
+    E = st.E[gi];
+    tau = st.tau[gi];
+    gtau = st.gtau[gi];
+    const uint32_t mt = st.meta[gi];
+    valley = mt & 0xff;
+    sub = (mt >> 8) & 0xff;
+    region = mt >> 16;
+    T F[3];
+#pragma unroll
+    for (int v = 0; v < 3; v++)
+      F[v] = EK.F[v] + coulFactor * (T)coulF[v * stride + gi];
+    PhiloxSrc<T> rng;
+    rng.init(pid, step, EK.stream, EK.key0, EK.key1);
+    myErr = bulkParticleStepF(M, EK, F, k, pos, E, tau, gtau, valley, sub, region, kN, rng);
+  }
+  T vd = T(0);
+  if (active) {
+    const ValleyK<T> &V = M.v[valley];
+    const T *g = EK.g[valley][sub];
+    const T npf = m_sqrt(T(1) + T(4) * V.alpha * gammaOf(V, E));
+    vd = m_div(V.cX * (g[0] * kN[0] + g[1] * kN[1] + g[2] * kN[2]), npf);
+  }
+  for (int v = 0; v < nV; v++) {
+    const bool in = active && valley == v;
+    const T e = warpSum(in ? E : T(0)), d = warpSum(in ? vd : T(0));
+    const unsigned c = __popc(__ballot_sync(0xffffffffu, in));
+    if (lane == 0 && c) {
+      double *o = obs + (size_t)tl.ens * Q + v * 3;
+      atomicAdd(o + 0, (double)e);
+      atomicAdd(o + 1, (double)d);
+      atomicAdd(o + 2, (double)c);
+    }
+  }
+  if (active) {
+    st.kx[gi] = k[0];
+    st.ky[gi] = k[1];
+    st.kz[gi] = k[2];
+    st.px[gi] = pos[0];
+    st.py[gi] = pos[1];
+    st.pz[gi] = pos[2];
+    st.E[gi] = E;
+    st.tau[gi] = tau;
+    st.gtau[gi] = gtau;
+    st.meta[gi] = packMeta(valley, sub, region);
+  }
+  recordError(err, myErr);
+}
 
 // ---------------------------------------------------------------------------
 // Queued variant (Philox only).  The block's particles live in shared memory
@@ -820,6 +966,14 @@ struct BulkImpl {
   // pinned host staging for state uploads (grown on demand)
   void *pinned = nullptr;
   size_t pinnedBytes = 0;
+  // particle-particle Coulomb steps (FMMBulkParticleHandler)
+  bool coulomb = false;
+  double coulEpsR = 1., coulInvCut = 1e9;
+  int coulImages = 0, sms = 0;
+  std::vector<int64_t> nFixed;       // fixed charges per ensemble
+  std::vector<double *> dFixed;      // their x, y, z, q planes
+  double *dSrc = nullptr, *dPart = nullptr, *dCoulF = nullptr;
+  int64_t srcCap = 0, partCap = 0;
   // graph replay of one launch of steps: [observable reset] -> [step kernel],
   // instantiated per launch shape, the step offset updated before each replay
   bool useGraph = false;
@@ -885,8 +1039,11 @@ static void buildEnsK(const emcg_ensemble_desc &d, const ModelK<T> &M,
       }
     }
   }
-  for (int i = 0; i < 3; i++)
+  for (int i = 0; i < 3; i++) {
     E.box[i] = (T)d.box[i];
+    E.F[i] = (T)F[i];
+  }
+  E.charge = (T)d.charge;
   E.dt = (T)d.dt;
   E.key0 = (uint32_t)d.seed;
   E.key1 = (uint32_t)(d.seed >> 32);
@@ -1062,8 +1219,93 @@ template <class T> static int32_t graphFor(BulkImpl *b, int ns, size_t smem, siz
   return EMCG_OK;
 }
 
+// Grow a device buffer of doubles to n (after draining the stream).
+static int32_t growDoubles(BulkImpl *b, double **p, int64_t *cap, int64_t n) {
+  if (*cap >= n)
+    return EMCG_OK;
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  EMCG_CUDA(cudaMalloc(p, (size_t)std::max<int64_t>(n, 1) * sizeof(double)));
+  *cap = n;
+  return EMCG_OK;
+}
+
+// reference constants (include/emcConstants.hpp:9, 21, 27)
+constexpr double kCoulombKe = 1. / (4 * 3.14159265358979323846 * 8.85419e-12);
+
+// Steps with particle-particle Coulomb forces, one per launch.
+template <class T>
+static int32_t coulombStepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHost) {
+  EMCG_TRY(ensureTiles(b));
+  const int Q = b->nVmax * 3;
+  if (!b->sms) {
+    int dev = 0;
+    EMCG_CUDA(cudaGetDevice(&dev));
+    EMCG_CUDA(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  int64_t srcNeed = 1, partNeed = 1;
+  for (int e = 0; e < b->nEns; e++) {
+    const int64_t n = b->count[e], m = n + b->nFixed[e];
+    srcNeed = std::max(srcNeed, 4 * m);
+    partNeed = std::max(partNeed, 4 * n * (int64_t)p2pChunks(std::max<int64_t>(n, 1), b->sms));
+  }
+  EMCG_TRY(growDoubles(b, &b->dSrc, &b->srcCap, srcNeed));
+  EMCG_TRY(growDoubles(b, &b->dPart, &b->partCap, partNeed));
+  if (!b->dCoulF) {
+    EMCG_CUDA(cudaMalloc(&b->dCoulF, (size_t)std::max<int64_t>(b->totalCap, 1) * 4 *
+                                         sizeof(double)));
+    EMCG_CUDA(cudaMemsetAsync(b->dCoulF, 0, (size_t)std::max<int64_t>(b->totalCap, 1) * 4 *
+                                                 sizeof(double), b->stream));
+  }
+  if ((size_t)b->nEns * Q > b->obsCap) {
+    dropGraph(b);
+    cudaFree(b->dObs);
+    b->dObs = nullptr;
+    EMCG_CUDA(cudaMalloc(&b->dObs, (size_t)b->nEns * Q * sizeof(double)));
+    b->obsCap = (size_t)b->nEns * Q;
+  }
+  StateK<T> st = stateOf<T>(b);
+  const T coulFactor = (T)(-kCoulombKe / b->coulEpsR);
+  EMCG_CUDA(cudaEventRecord(b->ev0, b->stream));
+  for (int s = 0; s < nSteps; s++) {
+    EMCG_CUDA(cudaMemsetAsync(b->dObs, 0, (size_t)b->nEns * Q * sizeof(double), b->stream));
+    for (int e = 0; e < b->nEns; e++) {
+      const int64_t n = b->count[e], nf = b->nFixed[e], m = n + nf;
+      if (n == 0)
+        continue;
+      coulombGatherKernel<T><<<(unsigned)((m + 255) / 256), 256, 0, b->stream>>>(
+          st, b->begin[e], n, b->ens[e].charge, b->dFixed[e], nf, b->dSrc);
+      EMCG_CUDA(cudaGetLastError());
+      EMCG_CUDA(p2pLaunch<T>(b->dSrc, b->dSrc + m, b->dSrc + 2 * m, b->dSrc + 3 * m, m, n,
+                             b->coulInvCut, b->ens[e].box[0], b->coulImages,
+                             p2pChunks(n, b->sms), b->dPart, b->dCoulF + b->begin[e],
+                             b->totalCap, b->stream));
+    }
+    if (b->nTiles > 0) {
+      bulkForceStepKernel<T><<<b->nTiles, b->blockThreads, 0, b->stream>>>(
+          st, (const ModelK<T> *)b->dModels, (const EnsK<T> *)b->dEns, b->dTiles,
+          step0 + (uint32_t)s, b->nVmax, b->dCoulF, b->totalCap, coulFactor, b->dObs, b->dErr);
+      EMCG_CUDA(cudaGetLastError());
+    }
+    if (obsHost)
+      for (int e = 0; e < b->nEns; e++)
+        EMCG_CUDA(cudaMemcpyAsync(obsHost + ((size_t)e * nSteps + s) * Q, b->dObs + (size_t)e * Q,
+                                  (size_t)Q * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  }
+  EMCG_CUDA(cudaEventRecord(b->ev1, b->stream));
+  EMCG_CUDA(cudaEventSynchronize(b->ev1));
+  float ms = 0;
+  EMCG_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+  b->lastMs = ms;
+  return readError(b);
+}
+
 template <class T>
 static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHost) {
+  if (b->coulomb && !b->replay)
+    return coulombStepTyped<T>(b, nSteps, step0, obsHost);
   EMCG_TRY(ensureTiles(b));
   const int Q = b->nVmax * 3;
   int per = b->stepsPerLaunch > 0 ? b->stepsPerLaunch : nSteps;
@@ -1189,6 +1431,11 @@ static void freeBulk(BulkImpl *b) {
   freeRateScratch(b->rateScratch);
   if (b->pinned)
     cudaFreeHost(b->pinned);
+  for (double *p : b->dFixed)
+    cudaFree(p);
+  cudaFree(b->dSrc);
+  cudaFree(b->dPart);
+  cudaFree(b->dCoulF);
   dropGraph(b);
   if (b->ev0)
     cudaEventDestroy(b->ev0);
@@ -1279,6 +1526,8 @@ extern "C" int32_t emcg_bulk_create(const emcg_model_desc *models, int32_t n_mod
   b->count.assign(n_ens, 0);
   b->cap.resize(n_ens);
   b->ensNV.resize(n_ens);
+  b->nFixed.assign(n_ens, 0);
+  b->dFixed.assign(n_ens, nullptr);
   int64_t off = 0;
   for (int e = 0; e < n_ens; e++) {
     b->begin[e] = off;
@@ -1623,6 +1872,70 @@ extern "C" int32_t emcg_bulk_set_graph(emcg_handle *h, int32_t enable) {
   b->useGraph = enable != 0;
   if (!b->useGraph)
     dropGraph(b);
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_bulk_set_coulomb(emcg_handle *h, int32_t enable, double eps_r,
+                                         double inv_cutoff, int32_t images) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  if (enable) {
+    EMCG_CHECK_ARG(eps_r > 0 && std::isfinite(eps_r), "eps_r must be positive");
+    EMCG_CHECK_ARG(inv_cutoff >= 0 && std::isfinite(inv_cutoff), "inv_cutoff must be >= 0");
+    EMCG_CHECK_ARG(images >= 0 && images <= 8, "images must be in [0, 8]");
+    if (images > 0)
+      for (int e = 0; e < b->nEns; e++) {
+        const double *bx = b->ens[e].box;
+        EMCG_CHECK_ARG(bx[0] == bx[1] && bx[1] == bx[2],
+                       "ensemble %d: periodic copies need a cubic box", e);
+      }
+    EMCG_CHECK_ARG(!b->replay, "Coulomb steps run on Philox streams; clear replay first");
+  }
+  b->coulomb = enable != 0;
+  b->coulEpsR = eps_r;
+  b->coulInvCut = inv_cutoff;
+  b->coulImages = images;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_bulk_set_fixed_charges(emcg_handle *h, int32_t e, const double *pos,
+                                               const double *q, int64_t n) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(e >= 0 && e < b->nEns, "ensemble %d out of range", e);
+  EMCG_CHECK_ARG(n >= 0 && (n == 0 || (pos && q)), "bad fixed charges");
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  cudaFree(b->dFixed[e]);
+  b->dFixed[e] = nullptr;
+  b->nFixed[e] = 0;
+  if (n == 0)
+    return EMCG_OK;
+  std::vector<double> planes((size_t)4 * n);
+  std::memcpy(planes.data(), pos, (size_t)3 * n * sizeof(double));
+  std::memcpy(planes.data() + 3 * n, q, (size_t)n * sizeof(double));
+  for (double v : planes)
+    EMCG_CHECK_ARG(std::isfinite(v), "fixed charges: non-finite value");
+  EMCG_CUDA(cudaMalloc(&b->dFixed[e], planes.size() * sizeof(double)));
+  EMCG_CUDA(cudaMemcpy(b->dFixed[e], planes.data(), planes.size() * sizeof(double),
+                       cudaMemcpyHostToDevice));
+  b->nFixed[e] = n;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_bulk_get_coulomb(emcg_handle *h, int32_t e, double *force,
+                                         double *potential) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(e >= 0 && e < b->nEns, "ensemble %d out of range", e);
+  EMCG_CHECK_ARG(b->dCoulF, "no Coulomb step has run");
+  const int64_t n = b->count[e];
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  for (int v = 0; v < 4; v++) {
+    double *dst = v < 3 ? (force ? force + (size_t)v * n : nullptr) : potential;
+    if (dst && n)
+      EMCG_CUDA(cudaMemcpy(dst, b->dCoulF + (size_t)v * b->totalCap + b->begin[e],
+                           (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+  }
   return EMCG_OK;
 }
 

@@ -63,6 +63,8 @@ template <class T> struct EnsK {
   T g[EMCG_MAX_VALLEYS][EMCG_MAX_DEG][3];  // vogt o (R dir): v.dir = cX g.k_ecs / npf
   T box[3];
   T dt;
+  T F[3];   // applied force charge x field [N] (particle-particle Coulomb steps)
+  T charge; // [C]
   uint32_t key0, key1, stream, pad_;
 };
 
