@@ -117,3 +117,23 @@ def test_coulomb_argument_checks(engine):
     with pytest.raises(ValueError):
         b.set_fixed_charges(0, np.zeros((3, 4)), np.zeros(3))
     b.close()
+
+
+def test_fmm_bulk_handler_mirror(engine):
+    """The handler mirror: electrons from the doping, as many fixed donors,
+    the Coulomb interaction on, the reference's call sequence."""
+    pt = engine.physics.silicon_electron("jacoboni")
+    h = engine.FMMBulkParticleHandler((1e-7,) * 3, pt, (1, 0, 0), 1e6, images=0,
+                                      eps_r=EPS_R, doping=1e24, seed=4, precision="fp32",
+                                      dt=1e-16)
+    h.generateInitialParticles(spacing=(1e-8,) * 3)
+    assert 500 < h.getNrParticles(0) < 1500 and h.donors.shape[1] == h.getNrParticles(0)
+    assert h.getNrRepeatedBoxes() == 1
+    for _ in range(3):
+        h.executeFMM()
+        h.moveParticles(1e-16)
+        h.resetForcesAndPotential()
+        h.rearrangeTree()
+    f, p = h.getCoulomb()
+    assert f.shape == (3, h.getNrParticles(0)) and np.all(np.isfinite(f))
+    assert np.isfinite(h.getAvgEnergy(0)).all() and h.getValleyOccupationProbability(0)[0] == 1

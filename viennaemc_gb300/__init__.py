@@ -12,7 +12,8 @@ from .physics import (Electron, NonParabolicAnisotropValley, AcousticScatterMech
                       FirstOrderInterValleyAbsorptionScatterMechanism,
                       FirstOrderInterValleyEmissionScatterMechanism, CoulombScatterMechanism,
                       silicon_electron, silicon_material, thermal_voltage)
-from .bulk import BulkBatch, BulkParticleHandler, EnsembleSpec, ParticleState
+from .bulk import (BulkBatch, BulkParticleHandler, EnsembleSpec, FMMBulkParticleHandler,
+                   ParticleState)
 
 build = _lib.build
 __all__ = ["Electron", "NonParabolicAnisotropValley", "AcousticScatterMechanism",
@@ -21,4 +22,5 @@ __all__ = ["Electron", "NonParabolicAnisotropValley", "AcousticScatterMechanism"
            "FirstOrderInterValleyAbsorptionScatterMechanism",
            "FirstOrderInterValleyEmissionScatterMechanism", "CoulombScatterMechanism",
            "silicon_electron", "silicon_material", "thermal_voltage", "BulkBatch",
-           "BulkParticleHandler", "EnsembleSpec", "ParticleState", "build"]
+           "BulkParticleHandler", "EnsembleSpec", "FMMBulkParticleHandler", "ParticleState",
+           "build"]

@@ -426,3 +426,64 @@ class BulkParticleHandler:
         if self._batch is not None:
             self._batch.set_state(0, ParticleState(0))
         self.n = 0
+
+
+class FMMBulkParticleHandler(BulkParticleHandler):
+    """FMMBulkParticleHandler (examples/bulkSimulationFMM/FMMBulkParticleHandler.hpp)
+    on the GPU: bulk electrons with particle-particle Coulomb forces, the
+    donors as fixed charges.  The FMM's sums are formed directly on the GPU
+    in every step; images is the number of periodic copies of the box on each
+    side (scalFMM's periodicity parameter repeats the box in its own way; this
+    sums over (2 images + 1)^3 boxes).
+
+    handler = FMMBulkParticleHandler(maxPos, electronType, fieldDir, fieldStrength,
+                                     images, eps_r=11.8, doping=1e24)
+    handler.generateInitialParticles(spacing)      # electrons and donors
+    handler.executeFMM(); handler.moveParticles(dt)
+    handler.getAvgEnergy(0), getAvgDriftVelocity(0), getValleyOccupationProbability(0)
+    """
+
+    def __init__(self, max_pos, particle_type: Electron, field_dir, field_strength=0.0,
+                 images=0, eps_r=11.8, doping=0.0, inv_cutoff=1e9, seed=0,
+                 temperature=300.0, precision="fp64", capacity=None, dt=1e-16):
+        super().__init__(max_pos, particle_type, field_dir, field_strength, seed, temperature,
+                         precision, capacity, dt)
+        self.images = int(images)
+        self.eps_r = float(eps_r)
+        self.doping = float(doping)
+        self.inv_cutoff = float(inv_cutoff)
+        self.donors = np.zeros((3, 0))
+
+    def generateInitialParticles(self, spacing=None, doping=None, n=None):
+        """Electrons (the node-based counts of the doping, or n uniform) and as
+        many donors as electrons, uniform in the box (addParticle with the
+        reference's initParticlePos, :155-176, :446-460)."""
+        super().generateInitialParticles(spacing, self.doping if doping is None else doping, n)
+        rs = np.random.default_rng(self.seed + 1)
+        self.donors = rs.random((3, self.n)) * np.asarray(self.max_pos)[:, None]
+        self._apply()
+
+    def _apply(self):
+        b = self._batch
+        b.set_fixed_charges(0, self.donors, np.full(self.donors.shape[1], -self.type.getCharge()))
+        b.set_coulomb(self.eps_r, self.inv_cutoff, self.images)
+
+    def set_state(self, st: ParticleState):
+        super().set_state(st)
+        self._apply()
+
+    def getNrRepeatedBoxes(self):
+        return (2 * self.images + 1) ** 3
+
+    def executeFMM(self):
+        """The Coulomb sums run inside each step (moveParticles)."""
+
+    def resetForcesAndPotential(self):
+        """Nothing to reset: the sums are formed afresh in every step."""
+
+    def rearrangeTree(self):
+        """No tree: the direct sums need no arrangement."""
+
+    def getCoulomb(self):
+        """Force and potential sums of the last step (container values)."""
+        return self._batch.get_coulomb(0)
