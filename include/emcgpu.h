@@ -452,7 +452,7 @@ int32_t emcg_device_poisson_mode(emcg_handle *h, int32_t mode, int32_t *cluster_
    relative-residual target, Newton-step limit, update tolerance [V]. */
 int32_t emcg_device_set_poisson(emcg_handle *h, double rtol, int32_t max_cycles,
                                 double update_tol);
-/* Newton / V-cycles and Poisson solves of the last emcg_device_step call. */
+/* Newton steps (*cycles) and Poisson solves of the last emcg_device_step call. */
 int32_t emcg_device_poisson_counts(emcg_handle *h, int64_t *cycles, int64_t *solves);
 
 /* Poisson solve that allocates nothing.  No counterpart in the reference: it

@@ -1295,7 +1295,7 @@ static int32_t solveT(PoissonMG &P, double *pot, const double *conc, bool resetB
   if (cycles)
     *cycles = it;
   if (!updStop && !(rel <= rtol)) {
-    setError("Poisson: relative residual %.3e after %d V-cycles (target %.1e)", rel, it, rtol);
+    setError("Poisson: relative residual %.3e after %d Newton steps (target %.1e)", rel, it, rtol);
     return EMCG_ERR_NONCONVERGED;
   }
   return EMCG_OK;
@@ -1775,7 +1775,7 @@ extern "C" int32_t emcg_poisson_solve_noalloc(const emcg_device_desc *dv, double
   if (cycles)
     *cycles = it;
   if (!(rel <= rtol)) {
-    setError("Poisson: relative residual %.3e after %d V-cycles (target %.1e)", rel, it, rtol);
+    setError("Poisson: relative residual %.3e after %d Newton steps (target %.1e)", rel, it, rtol);
     return EMCG_ERR_NONCONVERGED;
   }
   return EMCG_OK;

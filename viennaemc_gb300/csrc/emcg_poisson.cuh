@@ -9,7 +9,7 @@
 // exp(phi) (equilibrium), G the gate Robin coefficient.  The reference's
 // lexicographic SOR reaches the fixed point of this equation; here it is
 // solved by Newton / defect correction in double precision whose correction
-// equation J d = -F is solved approximately by one or two multigrid V-cycles
+// equation J d = -F is solved approximately by a few multigrid V-cycles
 // per iteration (red-black Gauss-Seidel, bilinear transfer, finite-volume
 // coarse operators), in float or double.  The solve stops when
 // max|F| <= rtol * max(hP (|C| + n + p)), the scale taken at the first
@@ -97,7 +97,7 @@ int32_t poissonCreate(PoissonMG &P, const PoissonSetup &S, bool fp32, int smooth
 void poissonFree(PoissonMG &P);
 // Solve for pot (device, normalised).  conc == nullptr: equilibrium.
 // Returns EMCG_OK / EMCG_ERR_NONCONVERGED / EMCG_ERR_CUDA; outputs the final
-// relative residual and the number of V-cycles.
+// relative residual and the number of Newton steps.
 int32_t poissonSolve(PoissonMG &P, double *pot, const double *conc, bool resetBC,
                      double rtol, int maxCycles, cudaStream_t st, double *relRes,
                      int *cycles);
