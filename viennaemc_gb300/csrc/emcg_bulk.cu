@@ -664,7 +664,11 @@ inline int asyncMaxSteps(int nWarps, int Q) {
 // position by flushPos.  |k| is the same in both frames (R orthonormal).
 // Returns hbar / (mc (1 + 2 alpha E)) at the new energy: the velocity factor
 // of the ellipse-frame k (emcNonParabolicAnistropValley.hpp:185-204, with
-// sqrt(1 + 4 alpha gamma) = 1 + 2 alpha E).
+// sqrt(1 + 4 alpha gamma) = 1 + 2 alpha E).  With g = hbar^2 k^2 / (mc q) and
+// s = sqrt(1 + 2 alpha g), E = g / (1 + s) (:109-113) and 1 + 2 alpha E = s, so
+// one reciprocal square root serves the energy and the velocity factor.  dP
+// sums (k_old + k_new) c without the Herring-Vogt factors, which flushPos
+// applies: they are constant until the valley changes.
 __device__ __forceinline__ float driftEcs(const ValleyK<float> &V, const float fv[3], float dt,
                                           float kE[3], float &E, float dP[3]) {
   float kO[3];
@@ -673,22 +677,25 @@ __device__ __forceinline__ float driftEcs(const ValleyK<float> &V, const float f
     kO[i] = kE[i];
     kE[i] = kO[i] + fv[i] * dt;
   }
-  E = energyOf(V, kE[0] * kE[0] + kE[1] * kE[1] + kE[2] * kE[2]);
-  const float vf = m_div(V.cX, 1.f + 2.f * E * V.alpha);
-  const float c = vf * dt * 0.5f;
+  const float g = V.cE * (kE[0] * kE[0] + kE[1] * kE[1] + kE[2] * kE[2]);
+  const float t = fmaf(2.f * V.alpha, g, 1.f);
+  const float rs = rsqrtf(t);
+  E = m_div(g, 1.f + t * rs);
+  const float vf = V.cX * rs;
+  const float c = vf * (0.5f * dt);
 #pragma unroll
   for (int i = 0; i < 3; i++)
-    dP[i] += V.vogt[i] * (kE[i] + kO[i]) * c;
+    dP[i] = fmaf(kE[i] + kO[i], c, dP[i]);
   return vf;
 }
 
 // The summed displacement into the device frame and the periodic box
 // (basicBulkParticleHandler.hpp:600-613); the sum covers one free flight or
 // less, far below a box length.
-__device__ __forceinline__ void flushPos(const float *R, float dP[3], float pos[3],
-                                         const float box[3]) {
+__device__ __forceinline__ void flushPos(const float *R, const float vogt[3], float dP[3],
+                                         float pos[3], const float box[3]) {
   float dd[3];
-  toDev(R, dP[0], dP[1], dP[2], dd);
+  toDev(R, dP[0] * vogt[0], dP[1] * vogt[1], dP[2] * vogt[2], dd);
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     float c = pos[i] + dd[i];
@@ -813,7 +820,7 @@ __global__ void __launch_bounds__(256, MINB)
         T k[3];
         const T *R = M.v[valley].rot[sub];
         toDev(R, kE[0], kE[1], kE[2], k);
-        flushPos(R, dP, pos, EK.box);
+        flushPos(R, M.v[valley].vogt, dP, pos, EK.box);
         const int e = scatterParticle(M, k, E, valley, sub, region, rng);
         if (e) {
           myErr = e;
@@ -874,7 +881,7 @@ __global__ void __launch_bounds__(256, MINB)
     T k[3];
     const T *R = M.v[valley].rot[sub];
     toDev(R, kE[0], kE[1], kE[2], k);
-    flushPos(R, dP, pos, EK.box);
+    flushPos(R, M.v[valley].vogt, dP, pos, EK.box);
     st.kx[gi] = k[0];
     st.ky[gi] = k[1];
     st.kz[gi] = k[2];
@@ -1304,7 +1311,7 @@ static int32_t coulombStepTyped(BulkImpl *b, int nSteps, uint32_t step0, double 
 
 template <class T>
 static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHost) {
-  if (b->coulomb && !b->replay)
+  if (b->coulomb) // set_coulomb and set_replay exclude each other
     return coulombStepTyped<T>(b, nSteps, step0, obsHost);
   EMCG_TRY(ensureTiles(b));
   const int Q = b->nVmax * 3;
@@ -1795,6 +1802,7 @@ extern "C" int32_t emcg_set_replay(emcg_handle *h, const uint64_t *words, int64_
   }
   EMCG_CHECK_ARG(b->precision == EMCG_FP64, "replay needs the FP64 engine");
   EMCG_CHECK_ARG(b->nEns == 1, "replay needs exactly one ensemble");
+  EMCG_CHECK_ARG(!b->coulomb, "replay does not run Coulomb steps; switch them off first");
   EMCG_CHECK_ARG(offsets && n_offsets == b->count[0] + 1,
                  "replay: need n+1 = %lld offsets, got %lld", (long long)(b->count[0] + 1),
                  (long long)n_offsets);
