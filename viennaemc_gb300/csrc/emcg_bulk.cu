@@ -634,12 +634,14 @@ __global__ void bulkInitKernel(StateK<T> st, const ModelK<T> *__restrict__ model
 // small per-warp window; once every lane of the warp has passed a step, the
 // warp folds that row into the block's float step sums (shared memory), which
 // go to the device's double sums at the end of the launch.  A lane runs at
-// most kAsyncWindow steps ahead of the slowest lane of its warp.  Both
-// constants were chosen by measurement on 2^20 electrons.
+// most kAsyncWindow steps ahead of the slowest lane of its warp.  The three
+// constants below were chosen by measurement on 2^20 and 2^22 electrons.
 // ---------------------------------------------------------------------------
-constexpr int kAsyncWindow = 16;
+constexpr int kAsyncWindow = 20;
 // lanes of a warp that wait at an event before the warp scatters them together
 constexpr int kEventBatch = 8;
+// free flights a lane may take in one drift pass
+constexpr int kPassActions = 3;
 // fixed-point scales of a warp's step sums: energy 2^-20 eV, velocity
 // 0.25 m/s per unit; below kFixMax per lane, 32 lanes stay within int32
 constexpr float kFixE = 1048576.f;
@@ -831,37 +833,40 @@ __global__ void __launch_bounds__(256, MINB)
         }
         toEcs(M.v[valley].rot[sub], k[0], k[1], k[2], kE);
       }
-    } else if (can) {
-      // the free flight ends either at the end of step s (bulkParticleStep
-      // without an event) or at the next event inside it; both drift first,
-      // so the warp's lanes drift together
-      const T rem = dt - tIn;
-      const bool ev = tau < rem;
-      if (ev && ++nEv > kMaxScatterPerStep) {
-        myErr = EMCG_ERR_TIMEOUT;
-        live = false;
-        s = nSteps;
-      } else {
-        const T vf = driftEcs(M.v[valley], EK.fv[valley][sub], ev ? tau : rem, kE, E, dP);
-        if (ev) {
-          tIn += tau;
-          pend = true;
-        } else { // end of step s: its observables, then step s + 1
-          tau -= rem;
-          gtau -= dt;
-          if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
-            gtau = -m_log(rng.ulog()) * M.grainTau;
-          const T *g = EK.g[valley][sub];
-          const int slot = ws * 32 + lane;
-          winE[slot] = E;
-          winD[slot] = vf * (g[0] * kE[0] + g[1] * kE[1] + g[2] * kE[2]);
-          if (nV > 1)
-            winVal[slot] = (uint8_t)valley;
-          s++;
-          tIn = T(0);
-          nEv = 0;
-          ws = ws + 1 == kAsyncWindow ? 0 : ws + 1;
-          rng.restart(step0 + (uint32_t)s);
+    } else {
+      // up to kPassActions free flights per lane and pass: each ends either at
+      // the end of step s (bulkParticleStep without an event) or at the next
+      // event inside it; both drift first, so the warp's lanes drift together
+#pragma unroll 1
+      for (int act = 0; act < kPassActions && !pend && s < limit; act++) {
+        const T rem = dt - tIn;
+        const bool ev = tau < rem;
+        if (ev && ++nEv > kMaxScatterPerStep) {
+          myErr = EMCG_ERR_TIMEOUT;
+          live = false;
+          s = nSteps;
+        } else {
+          const T vf = driftEcs(M.v[valley], EK.fv[valley][sub], ev ? tau : rem, kE, E, dP);
+          if (ev) {
+            tIn += tau;
+            pend = true;
+          } else { // end of step s: its observables, then step s + 1
+            tau -= rem;
+            gtau -= dt;
+            if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
+              gtau = -m_log(rng.ulog()) * M.grainTau;
+            const T *g = EK.g[valley][sub];
+            const int slot = ws * 32 + lane;
+            winE[slot] = E;
+            winD[slot] = vf * (g[0] * kE[0] + g[1] * kE[1] + g[2] * kE[2]);
+            if (nV > 1)
+              winVal[slot] = (uint8_t)valley;
+            s++;
+            tIn = T(0);
+            nEv = 0;
+            ws = ws + 1 == kAsyncWindow ? 0 : ws + 1;
+            rng.restart(step0 + (uint32_t)s);
+          }
         }
       }
     }
