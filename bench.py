@@ -448,7 +448,7 @@ def _device_bench(args, rank):
            "value": 0.5 * (n0 + n1) * K / (step_ms / 1e3), "unit": UNIT,
            "ms_per_step": step_ms / K, "poisson_ms_per_solve": pois_ms / K,
            "poisson_newton_per_solve": cycles / max(solves, 1),
-           "poisson": "double Newton steps, each with 2 float multigrid V-cycles; stop at 1e-8 "
+           "poisson": "double Newton steps, each with 3 float multigrid V-cycles; stop at 1e-8 "
                       "relative residual",
            "wall_s": wall, "current_A": [float(c) for c in cur]}
     if rank == 0 and not args.no_cpu_baseline:

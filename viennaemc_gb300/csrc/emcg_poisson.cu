@@ -282,6 +282,13 @@ template <> LevelK<double> levelK<double>(const MGLevel &l) {
 constexpr int kClusterThreads = 512;
 constexpr int kMaxCluster = 16;
 constexpr int kSmallNodes = 4096;
+// levels below the finest of at most this many nodes (all held by CTA 0) are
+// worked by warp 0 alone, its phases ending in __syncwarp instead of a
+// barrier of the whole CTA
+#ifndef EMCG_WARP_NODES
+#define EMCG_WARP_NODES 64
+#endif
+constexpr int kWarpNodes = EMCG_WARP_NODES;
 constexpr size_t kClusterSmemMax = 227 * 1024;
 
 // q = t / d for 0 <= t and t * d < 2^32, by one wide multiply (m = ceil(2^32 / d))
@@ -295,7 +302,8 @@ struct FastDiv {
 
 template <class MT> struct CLevel {
   int nx, ny, small, rowsPer; // small: all rows in CTA 0; else rowsPer rows per CTA
-  int nCls, ncx, ncy, pad_;   // ncx, ncy: next level's size (0 on the coarsest)
+  int nCls, ncx, ncy, warp;   // ncx, ncy: next level's size (0 on the coarsest);
+                              // warp: worked by warp 0 of CTA 0 alone
   FastDiv byNx, byHalf, byRows; // nx, (nx + 1) / 2 and rowsPer
   // byte offsets in dynamic shared memory: this CTA's rows of d, r, rho, the
   // residual and the class index, the class table (8 MT per class) and the
@@ -382,68 +390,119 @@ __device__ __forceinline__ Coef<MT> cCoef(const CCtx &c, const CLevel<MT> &L, ui
 }
 
 // end of a phase over level L: cluster barrier for a distributed level, block
-// barrier for one held by CTA 0
+// barrier for one held by CTA 0, warp barrier for one worked by warp 0
 template <class MT> __device__ __forceinline__ void cSync(const CLevel<MT> &L) {
-  if (L.small)
+  if (L.warp)
+    __syncwarp();
+  else if (L.small)
     __syncthreads();
   else
     cg::this_cluster().sync();
 }
 
-template <class MT> __device__ void cSmooth(const CCtx &c, const CLevel<MT> &Lr, int color) {
-  const CLevel<MT> L = Lr; // a private copy: stores to shared memory cannot alias it
+// threads that take no part in a phase over level L (warp-level levels: all
+// but warp 0), and the stride of the threads that do
+template <class MT> __device__ __forceinline__ bool cIdle(const CLevel<MT> &L) {
+  return L.warp && threadIdx.x >= 32;
+}
+template <class MT> __device__ __forceinline__ int cStride(const CLevel<MT> &L) {
+  return L.warp ? 32 : (int)blockDim.x;
+}
+
+// row accessors of a phase; kS: the row is in this CTA's shared memory (its
+// own rows, or any row of a level held whole by CTA 0 in a phase that runs
+// there), so the accesses compile to shared-memory loads and stores rather
+// than generic ones
+template <bool kS, class T, class MT>
+__device__ __forceinline__ T *cRowT(const CCtx &c, const CLevel<MT> &L, unsigned off, int y) {
+  if (kS)
+    return reinterpret_cast<T *>(c.smem + off) + (size_t)y * L.nx;
+  return cRow<T>(c, L, off, y);
+}
+template <bool kS, class T, class MT>
+__device__ __forceinline__ T *cRowNearT(const CCtx &c, const CLevel<MT> &L, unsigned off, int ly) {
+  if (kS)
+    return reinterpret_cast<T *>(c.smem + off) + (size_t)ly * L.nx;
+  return cRowNear<T>(c, L, off, ly);
+}
+
+template <bool kS, class MT>
+__device__ __forceinline__ void cSmoothT(const CCtx &c, const CLevel<MT> &L, int color) {
   int r0, r1;
   cOwnRows(c, L, r0, r1);
-  const int half = (L.nx + 1) / 2, cnt = half * (r1 - r0);
-  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+  const int half = (L.nx + 1) / 2, cnt = half * (r1 - r0), stride = cStride(L);
+  for (int t = threadIdx.x; t < cnt; t += stride) {
     const int ly = L.byHalf.div(t), y = r0 + ly;
     const int x = 2 * (t - ly * half) + ((y + color) & 1);
     if (x >= L.nx)
       continue;
-    const Coef<MT> K = cCoef(c, L, cRowNear<uint8_t>(c, L, L.offCls, ly)[x]);
+    // row ly is this CTA's own; its neighbours are too, but at a band edge
+    const Coef<MT> K = cCoef(c, L, cRowNearT<true, uint8_t>(c, L, L.offCls, ly)[x]);
     if (K.fixed != MT(0))
       continue;
-    MT *d = cRowNear<MT>(c, L, L.offD, ly);
-    MT s = cRowNear<MT>(c, L, L.offR, ly)[x];
+    MT *d = cRowNearT<true, MT>(c, L, L.offD, ly);
+    MT s = cRowNearT<true, MT>(c, L, L.offR, ly)[x];
     if (x > 0)
       s += K.cw * d[x - 1];
     if (x < L.nx - 1)
       s += K.ce * d[x + 1];
     if (y > 0)
-      s += K.cs * cRowNear<MT>(c, L, L.offD, ly - 1)[x];
+      s += K.cs * (kS || ly > 0 ? cRowNearT<true, MT>(c, L, L.offD, ly - 1)[x]
+                                : cRowNearT<false, MT>(c, L, L.offD, ly - 1)[x]);
     if (y < L.ny - 1)
-      s += K.cn * cRowNear<MT>(c, L, L.offD, ly + 1)[x];
-    d[x] = mgDiv(s, K.diag0 + K.area * cRowNear<MT>(c, L, L.offRho, ly)[x]);
+      s += K.cn * (kS || ly + 1 < L.rowsPer ? cRowNearT<true, MT>(c, L, L.offD, ly + 1)[x]
+                                            : cRowNearT<false, MT>(c, L, L.offD, ly + 1)[x]);
+    d[x] = mgDiv(s, K.diag0 + K.area * cRowNearT<true, MT>(c, L, L.offRho, ly)[x]);
   }
+}
+template <class MT> __device__ void cSmooth(const CCtx &c, const CLevel<MT> &Lr, int color) {
+  const CLevel<MT> L = Lr; // a private copy: stores to shared memory cannot alias it
+  if (cIdle(L))
+    return;
+  if (L.small)
+    cSmoothT<true>(c, L, color);
+  else
+    cSmoothT<false>(c, L, color);
   cSync(L);
 }
 
 // residual r - A d of the correction equation at this CTA's nodes of level F
 // (0 at Dirichlet nodes), as restrictKernel evaluates it
-template <class MT> __device__ void cResidual(const CCtx &c, const CLevel<MT> &Fr) {
-  const CLevel<MT> F = Fr;
+template <bool kS, class MT>
+__device__ __forceinline__ void cResidualT(const CCtx &c, const CLevel<MT> &F) {
   int r0, r1;
   cOwnRows(c, F, r0, r1);
-  const int cnt = F.nx * (r1 - r0);
-  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+  const int cnt = F.nx * (r1 - r0), stride = cStride(F);
+  for (int t = threadIdx.x; t < cnt; t += stride) {
     const int ly = F.byNx.div(t), y = r0 + ly, x = t - ly * F.nx;
-    const Coef<MT> K = cCoef(c, F, cRowNear<uint8_t>(c, F, F.offCls, ly)[x]);
+    const Coef<MT> K = cCoef(c, F, cRowNearT<true, uint8_t>(c, F, F.offCls, ly)[x]);
     MT res = MT(0);
     if (K.fixed == MT(0)) {
-      const MT *d = cRowNear<MT>(c, F, F.offD, ly);
-      MT a = (K.diag0 + K.area * cRowNear<MT>(c, F, F.offRho, ly)[x]) * d[x];
+      const MT *d = cRowNearT<true, MT>(c, F, F.offD, ly);
+      MT a = (K.diag0 + K.area * cRowNearT<true, MT>(c, F, F.offRho, ly)[x]) * d[x];
       if (x > 0)
         a -= K.cw * d[x - 1];
       if (x < F.nx - 1)
         a -= K.ce * d[x + 1];
       if (y > 0)
-        a -= K.cs * cRowNear<MT>(c, F, F.offD, ly - 1)[x];
+        a -= K.cs * (kS || ly > 0 ? cRowNearT<true, MT>(c, F, F.offD, ly - 1)[x]
+                                  : cRowNearT<false, MT>(c, F, F.offD, ly - 1)[x]);
       if (y < F.ny - 1)
-        a -= K.cn * cRowNear<MT>(c, F, F.offD, ly + 1)[x];
-      res = cRowNear<MT>(c, F, F.offR, ly)[x] - a;
+        a -= K.cn * (kS || ly + 1 < F.rowsPer ? cRowNearT<true, MT>(c, F, F.offD, ly + 1)[x]
+                                              : cRowNearT<false, MT>(c, F, F.offD, ly + 1)[x]);
+      res = cRowNearT<true, MT>(c, F, F.offR, ly)[x] - a;
     }
-    cRowNear<MT>(c, F, F.offRes, ly)[x] = res;
+    cRowNearT<true, MT>(c, F, F.offRes, ly)[x] = res;
   }
+}
+template <class MT> __device__ void cResidual(const CCtx &c, const CLevel<MT> &Fr) {
+  const CLevel<MT> F = Fr;
+  if (cIdle(F))
+    return;
+  if (F.small)
+    cResidualT<true>(c, F);
+  else
+    cResidualT<false>(c, F);
   cSync(F);
 }
 
@@ -467,18 +526,18 @@ __device__ __forceinline__ void cRestrictRows(const CCtx &c, const CLevel<MT> &F
 }
 
 // coarse right-hand side P^T (fine residual), reaction by injection, d = 0
-template <class MT>
-__device__ void cRestrict(const CCtx &c, const CLevel<MT> &Fr, const CLevel<MT> &Cr) {
-  const CLevel<MT> F = Fr, Cc = Cr;
+template <bool kS, class MT>
+__device__ __forceinline__ void cRestrictT(const CCtx &c, const CLevel<MT> &F,
+                                        const CLevel<MT> &Cc) {
   int Y0, Y1;
   cRestrictRows(c, F, Cc, Y0, Y1);
-  const int cnt = Cc.nx * (Y1 - Y0);
-  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+  const int cnt = Cc.nx * (Y1 - Y0), stride = cStride(F);
+  for (int t = threadIdx.x; t < cnt; t += stride) {
     const int q = Cc.byNx.div(t), Y = Y0 + q, X = t - q * Cc.nx;
-    cRow<MT>(c, Cc, Cc.offD, Y)[X] = MT(0);
-    cRow<MT>(c, Cc, Cc.offRho, Y)[X] =
-        cRow<MT>(c, F, F.offRho, cTab<int>(c, F.offMapY)[Y])[cTab<int>(c, F.offMapX)[X]];
-    const Coef<MT> KC = cCoef(c, Cc, cRow<uint8_t>(c, Cc, Cc.offCls, Y)[X]);
+    cRowT<kS, MT>(c, Cc, Cc.offD, Y)[X] = MT(0);
+    cRowT<kS, MT>(c, Cc, Cc.offRho, Y)[X] =
+        cRowT<kS, MT>(c, F, F.offRho, cTab<int>(c, F.offMapY)[Y])[cTab<int>(c, F.offMapX)[X]];
+    const Coef<MT> KC = cCoef(c, Cc, cRowT<kS, uint8_t>(c, Cc, Cc.offCls, Y)[X]);
     MT acc = MT(0);
     if (KC.fixed == MT(0)) {
       MT wxs[3];
@@ -493,7 +552,7 @@ __device__ void cRestrict(const CCtx &c, const CLevel<MT> &Fr, const CLevel<MT> 
         const MT wy = (MT)cTab<float>(c, F.offRyW)[3 * Y + b];
         if (wy == MT(0))
           continue;
-        const MT *res = cRow<MT>(c, F, F.offRes, cTab<int>(c, F.offRyI)[3 * Y + b]);
+        const MT *res = cRowT<kS, MT>(c, F, F.offRes, cTab<int>(c, F.offRyI)[3 * Y + b]);
 #pragma unroll
         for (int a = 0; a < 3; a++) {
           if (wxs[a] == MT(0))
@@ -502,50 +561,73 @@ __device__ void cRestrict(const CCtx &c, const CLevel<MT> &Fr, const CLevel<MT> 
         }
       }
     }
-    cRow<MT>(c, Cc, Cc.offR, Y)[X] = acc;
+    cRowT<kS, MT>(c, Cc, Cc.offR, Y)[X] = acc;
   }
+}
+template <class MT>
+__device__ void cRestrict(const CCtx &c, const CLevel<MT> &Fr, const CLevel<MT> &Cr) {
+  const CLevel<MT> F = Fr, Cc = Cr;
+  if (cIdle(F))
+    return;
+  if (F.small)
+    cRestrictT<true>(c, F, Cc);
+  else
+    cRestrictT<false>(c, F, Cc);
   cSync(F);
 }
 
-template <class MT>
-__device__ void cProlong(const CCtx &c, const CLevel<MT> &Fr, const CLevel<MT> &Cr) {
-  const CLevel<MT> F = Fr, Cc = Cr;
+template <bool kS, class MT>
+__device__ __forceinline__ void cProlongT(const CCtx &c, const CLevel<MT> &F,
+                                        const CLevel<MT> &Cc) {
   int r0, r1;
   cOwnRows(c, F, r0, r1);
-  const int cnt = F.nx * (r1 - r0);
-  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+  const int cnt = F.nx * (r1 - r0), stride = cStride(F);
+  for (int t = threadIdx.x; t < cnt; t += stride) {
     const int ly = F.byNx.div(t), y = r0 + ly, x = t - ly * F.nx;
-    if (cCoef(c, F, cRowNear<uint8_t>(c, F, F.offCls, ly)[x]).fixed != MT(0))
+    if (cCoef(c, F, cRowNearT<true, uint8_t>(c, F, F.offCls, ly)[x]).fixed != MT(0))
       continue;
     const int X0 = cTab<int>(c, F.offPxI)[x], Y0 = cTab<int>(c, F.offPyI)[y];
     const MT wx = (MT)cTab<float>(c, F.offPxW)[x], wy = (MT)cTab<float>(c, F.offPyW)[y];
-    const MT *c0 = cRow<MT>(c, Cc, Cc.offD, Y0);
+    const MT *c0 = cRowT<kS, MT>(c, Cc, Cc.offD, Y0);
     MT v = wx * wy * c0[X0];
     if (wx < MT(1))
       v += (MT(1) - wx) * wy * c0[X0 + 1];
     if (wy < MT(1)) {
-      const MT *c1 = cRow<MT>(c, Cc, Cc.offD, Y0 + 1);
+      const MT *c1 = cRowT<kS, MT>(c, Cc, Cc.offD, Y0 + 1);
       v += wx * (MT(1) - wy) * c1[X0];
       if (wx < MT(1))
         v += (MT(1) - wx) * (MT(1) - wy) * c1[X0 + 1];
     }
-    cRowNear<MT>(c, F, F.offD, ly)[x] += v;
+    cRowNearT<true, MT>(c, F, F.offD, ly)[x] += v;
   }
+}
+template <class MT>
+__device__ void cProlong(const CCtx &c, const CLevel<MT> &Fr, const CLevel<MT> &Cr) {
+  const CLevel<MT> F = Fr, Cc = Cr;
+  if (cIdle(F))
+    return;
+  if (F.small)
+    cProlongT<true>(c, F, Cc);
+  else
+    cProlongT<false>(c, F, Cc);
   cSync(F);
 }
 
 // coarsest level (held by CTA 0): red-black sweeps, in the registers of warp 0
-// when it has at most 32 nodes, else by the block with block barriers
+// when it has at most 32 nodes, else by the threads of the level (warp 0 or the
+// block) with their barriers
 template <class MT> __device__ void cCoarse(const CCtx &c, const CLevel<MT> &L, int sweeps) {
+  if (cIdle(L))
+    return;
   const int n = L.nx * L.ny;
   if (n <= 32) {
     if (threadIdx.x < 32) {
       const int i = threadIdx.x, x = i % L.nx, y = i / L.nx;
       const bool live = i < n;
-      const Coef<MT> K = cCoef(c, L, live ? cRow<uint8_t>(c, L, L.offCls, y)[x] : 0);
-      MT *dp = live ? cRow<MT>(c, L, L.offD, y) + x : nullptr;
-      const MT r = live ? cRow<MT>(c, L, L.offR, y)[x] : MT(0);
-      const MT den = live ? K.diag0 + K.area * cRow<MT>(c, L, L.offRho, y)[x] : MT(1);
+      const Coef<MT> K = cCoef(c, L, live ? cRowT<true, uint8_t>(c, L, L.offCls, y)[x] : 0);
+      MT *dp = live ? cRowT<true, MT>(c, L, L.offD, y) + x : nullptr;
+      const MT r = live ? cRowT<true, MT>(c, L, L.offR, y)[x] : MT(0);
+      const MT den = live ? K.diag0 + K.area * cRowT<true, MT>(c, L, L.offRho, y)[x] : MT(1);
       const bool upd = live && K.fixed == MT(0);
       MT d = live ? *dp : MT(0);
       for (int it = 0; it < sweeps; it++) {
@@ -571,29 +653,30 @@ template <class MT> __device__ void cCoarse(const CCtx &c, const CLevel<MT> &L, 
       if (live)
         *dp = d;
     }
-    __syncthreads();
+    cSync(L);
     return;
   }
+  const int stride = cStride(L);
   for (int it = 0; it < sweeps; it++) {
     for (int color = 0; color < 2; color++) {
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      for (int i = threadIdx.x; i < n; i += stride) {
         const int x = i % L.nx, y = i / L.nx;
-        const Coef<MT> K = cCoef(c, L, cRow<uint8_t>(c, L, L.offCls, y)[x]);
+        const Coef<MT> K = cCoef(c, L, cRowT<true, uint8_t>(c, L, L.offCls, y)[x]);
         if (((x + y) & 1) != color || K.fixed != MT(0))
           continue;
-        MT *d = cRow<MT>(c, L, L.offD, y);
-        MT s = cRow<MT>(c, L, L.offR, y)[x];
+        MT *d = cRowT<true, MT>(c, L, L.offD, y);
+        MT s = cRowT<true, MT>(c, L, L.offR, y)[x];
         if (x > 0)
           s += K.cw * d[x - 1];
         if (x < L.nx - 1)
           s += K.ce * d[x + 1];
         if (y > 0)
-          s += K.cs * cRow<MT>(c, L, L.offD, y - 1)[x];
+          s += K.cs * cRowT<true, MT>(c, L, L.offD, y - 1)[x];
         if (y < L.ny - 1)
-          s += K.cn * cRow<MT>(c, L, L.offD, y + 1)[x];
-        d[x] = mgDiv(s, K.diag0 + K.area * cRow<MT>(c, L, L.offRho, y)[x]);
+          s += K.cn * cRowT<true, MT>(c, L, L.offD, y + 1)[x];
+        d[x] = mgDiv(s, K.diag0 + K.area * cRowT<true, MT>(c, L, L.offRho, y)[x]);
       }
-      __syncthreads();
+      cSync(L);
     }
   }
 }
@@ -703,10 +786,11 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     double aF = 0., sc = 0.;
     for (int t = threadIdx.x; t < nOwn; t += blockDim.x) {
       const int ly = L0.byNx.div(t), y = p0 + ly, x = t - ly * nx, i = y * nx + x;
-      MT *d0 = cRowNear<MT>(c, L0, L0.offD, ly), *r0 = cRowNear<MT>(c, L0, L0.offR, ly);
-      MT *rho0 = cRowNear<MT>(c, L0, L0.offRho, ly);
+      MT *d0 = cRowNearT<true, MT>(c, L0, L0.offD, ly);
+      MT *r0 = cRowNearT<true, MT>(c, L0, L0.offR, ly);
+      MT *rho0 = cRowNearT<true, MT>(c, L0, L0.offRho, ly);
       d0[x] = MT(0);
-      if (cCoef(c, L0, cRowNear<uint8_t>(c, L0, L0.offCls, ly)[x]).fixed != MT(0)) {
+      if (cCoef(c, L0, cRowNearT<true, uint8_t>(c, L0, L0.offCls, ly)[x]).fixed != MT(0)) {
         r0[x] = MT(0);
         rho0[x] = MT(0);
         continue;
@@ -761,6 +845,9 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
         }
         cCoarse(c, M.L[M.nLev - 1], M.coarseSweeps);
         for (int l = M.nLev - 2; l >= Ls; l--) {
+          // the CTA reads what warp 0 wrote on the level below
+          if (M.L[l + 1].warp && !M.L[l].warp)
+            __syncthreads();
           cProlong(c, M.L[l], M.L[l + 1]);
           for (int s = 0; s < M.post; s++) {
             cSmooth(c, M.L[l], 1);
@@ -783,10 +870,10 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     double upd = 0.;
     for (int t = threadIdx.x; t < nOwn; t += blockDim.x) {
       const int ly = L0.byNx.div(t), x = t - ly * nx;
-      if (cCoef(c, L0, cRowNear<uint8_t>(c, L0, L0.offCls, ly)[x]).fixed != MT(0))
+      if (cCoef(c, L0, cRowNearT<true, uint8_t>(c, L0, L0.offCls, ly)[x]).fixed != MT(0))
         continue;
-      const double v =
-          fmin(kMaxNewtonStep, fmax(-kMaxNewtonStep, (double)cRowNear<MT>(c, L0, L0.offD, ly)[x]));
+      const double v = fmin(kMaxNewtonStep,
+                            fmax(-kMaxNewtonStep, (double)cRowNearT<true, MT>(c, L0, L0.offD, ly)[x]));
       pot[(size_t)(p0 + ly) * nx + x] += v;
       upd = fmax(upd, fabs(v));
     }
@@ -835,6 +922,7 @@ template <class MT> CMG<MT> clusterDesc(const PoissonMG &P, int CL, size_t *byte
     c.nx = P.L[l].nx;
     c.ny = P.L[l].ny;
     c.small = l >= M.firstSmall ? 1 : 0;
+    c.warp = l >= 1 && c.small && c.nx * c.ny <= kWarpNodes ? 1 : 0;
   }
   // bands: level 0 split evenly (rounded to even rows when a distributed
   // level follows), each next distributed level on half the rows of the level
