@@ -466,6 +466,105 @@ template <class MT> __device__ void cSmooth(const CCtx &c, const CLevel<MT> &Lr,
   cSync(L);
 }
 
+// Several red-black sweeps over level L with each thread's nodes held in
+// registers: a thread keeps the same nodes over the sweeps, so their position,
+// class, right-hand side and diagonal are read once, and a half sweep reads
+// only the neighbours' corrections.  The arithmetic is cSmoothT's.
+constexpr int kSweepNodes = 3; // nodes of one colour per thread
+template <bool kS, int K, class MT>
+__device__ __forceinline__ void cHalfSweep(const CCtx &c, const CLevel<MT> &L, int r0,
+                                           const int (&pos)[2][kSweepNodes],
+                                           const int (&cl)[2][kSweepNodes],
+                                           const MT (&rr)[2][kSweepNodes],
+                                           const MT (&den)[2][kSweepNodes]) {
+#pragma unroll
+  for (int j = 0; j < kSweepNodes; j++) {
+    if (pos[K][j] < 0)
+      continue;
+    const int ly = pos[K][j] >> 16, x = pos[K][j] & 0xffff, y = r0 + ly;
+    const Coef<MT> C = cCoef(c, L, cl[K][j]);
+    MT *d = cRowNearT<true, MT>(c, L, L.offD, ly);
+    MT s = rr[K][j];
+    if (x > 0)
+      s += C.cw * d[x - 1];
+    if (x < L.nx - 1)
+      s += C.ce * d[x + 1];
+    if (y > 0)
+      s += C.cs * (kS || ly > 0 ? cRowNearT<true, MT>(c, L, L.offD, ly - 1)[x]
+                                : cRowNearT<false, MT>(c, L, L.offD, ly - 1)[x]);
+    if (y < L.ny - 1)
+      s += C.cn * (kS || ly + 1 < L.rowsPer ? cRowNearT<true, MT>(c, L, L.offD, ly + 1)[x]
+                                            : cRowNearT<false, MT>(c, L, L.offD, ly + 1)[x]);
+    d[x] = mgDiv(s, den[K][j]);
+  }
+  cSync(L);
+}
+
+template <bool kS, class MT>
+__device__ __forceinline__ void cSweepsHeld(const CCtx &c, const CLevel<MT> &L, int r0, int r1,
+                                            int sweeps, int first) {
+  const int half = (L.nx + 1) / 2, cnt = half * (r1 - r0), stride = cStride(L);
+  int pos[2][kSweepNodes], cl[2][kSweepNodes];
+  MT rr[2][kSweepNodes], den[2][kSweepNodes];
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+#pragma unroll
+    for (int j = 0; j < kSweepNodes; j++) {
+      pos[k][j] = -1;
+      cl[k][j] = 0;
+      rr[k][j] = MT(0);
+      den[k][j] = MT(1);
+      const int t = threadIdx.x + j * stride;
+      if (t >= cnt)
+        continue;
+      const int ly = L.byHalf.div(t), y = r0 + ly;
+      const int x = 2 * (t - ly * half) + ((y + k) & 1);
+      if (x >= L.nx)
+        continue;
+      const int q = cRowNearT<true, uint8_t>(c, L, L.offCls, ly)[x];
+      const Coef<MT> K = cCoef(c, L, q);
+      if (K.fixed != MT(0))
+        continue;
+      pos[k][j] = (ly << 16) | x;
+      cl[k][j] = q;
+      rr[k][j] = cRowNearT<true, MT>(c, L, L.offR, ly)[x];
+      den[k][j] = K.diag0 + K.area * cRowNearT<true, MT>(c, L, L.offRho, ly)[x];
+    }
+  }
+  for (int s = 0; s < sweeps; s++) {
+    if (first == 0) {
+      cHalfSweep<kS, 0>(c, L, r0, pos, cl, rr, den);
+      cHalfSweep<kS, 1>(c, L, r0, pos, cl, rr, den);
+    } else {
+      cHalfSweep<kS, 1>(c, L, r0, pos, cl, rr, den);
+      cHalfSweep<kS, 0>(c, L, r0, pos, cl, rr, den);
+    }
+  }
+}
+
+// `sweeps` red-black sweeps over level L, colour `first` first; every CTA
+// passes the same 2 * sweeps barriers whichever form its rows take
+template <class MT>
+__device__ void cSmoothSweeps(const CCtx &c, const CLevel<MT> &Lr, int sweeps, int first) {
+  const CLevel<MT> L = Lr;
+  if (cIdle(L))
+    return;
+  int r0, r1;
+  cOwnRows(c, L, r0, r1);
+  const int cnt = (L.nx + 1) / 2 * (r1 - r0);
+  if (cnt <= kSweepNodes * cStride(L) && L.nx <= 0xffff && r1 - r0 <= 0x7fff) {
+    if (L.small)
+      cSweepsHeld<true>(c, L, r0, r1, sweeps, first);
+    else
+      cSweepsHeld<false>(c, L, r0, r1, sweeps, first);
+    return;
+  }
+  for (int s = 0; s < sweeps; s++) {
+    cSmooth(c, L, first);
+    cSmooth(c, L, 1 - first);
+  }
+}
+
 // residual r - A d of the correction equation at this CTA's nodes of level F
 // (0 at Dirichlet nodes), as restrictKernel evaluates it
 template <bool kS, class MT>
@@ -826,20 +925,14 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
       // one V-cycle: the distributed levels down ...
       const int Ls = M.firstSmall;
       for (int l = 0; l < Ls; l++) {
-        for (int s = 0; s < M.pre; s++) {
-          cSmooth(c, M.L[l], 0);
-          cSmooth(c, M.L[l], 1);
-        }
+        cSmoothSweeps(c, M.L[l], M.pre, 0);
         cResidual(c, M.L[l]);
         cRestrict(c, M.L[l], M.L[l + 1]);
       }
       // ... the levels held by CTA 0 ...
       if (rank == 0) {
         for (int l = Ls; l + 1 < M.nLev; l++) {
-          for (int s = 0; s < M.pre; s++) {
-            cSmooth(c, M.L[l], 0);
-            cSmooth(c, M.L[l], 1);
-          }
+          cSmoothSweeps(c, M.L[l], M.pre, 0);
           cResidual(c, M.L[l]);
           cRestrict(c, M.L[l], M.L[l + 1]);
         }
@@ -849,20 +942,14 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
           if (M.L[l + 1].warp && !M.L[l].warp)
             __syncthreads();
           cProlong(c, M.L[l], M.L[l + 1]);
-          for (int s = 0; s < M.post; s++) {
-            cSmooth(c, M.L[l], 1);
-            cSmooth(c, M.L[l], 0);
-          }
+          cSmoothSweeps(c, M.L[l], M.post, 1);
         }
       }
       cluster.sync();
       // ... and the distributed levels up
       for (int l = Ls - 1; l >= 0; l--) {
         cProlong(c, M.L[l], M.L[l + 1]);
-        for (int s = 0; s < M.post; s++) {
-          cSmooth(c, M.L[l], 1);
-          cSmooth(c, M.L[l], 0);
-        }
+        cSmoothSweeps(c, M.L[l], M.post, 1);
       }
     }
     // clamped Newton update of this CTA's rows (updatePotKernel); the cluster
