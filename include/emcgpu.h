@@ -425,7 +425,10 @@ int32_t emcg_device_contacts(emcg_handle *h, uint32_t step, int32_t *rem_inj);
 int32_t emcg_device_assign(emcg_handle *h);
 /* performEMCStep (include/emcSimulation.hpp:164-193) n_steps times; netto
    (n_steps x n_contacts, may be NULL) receives removed - (injected - deleted)
-   per step and contact, as emcSimulationResults::updateCurrent consumes. */
+   per step and contact, as emcSimulationResults::updateCurrent consumes.
+   The single-launch Poisson solve of a step is checked at the end of that
+   step: EMCG_ERR_NONCONVERGED returns after the step whose solve missed its
+   target, its particle phase done on the potential the solve reached. */
 int32_t emcg_device_step(emcg_handle *h, int32_t n_steps, uint32_t step0, int32_t *netto);
 /* generateInitialParticles (include/ParticleHandler/emcAbstractParticleHandler.hpp:
    133-148): counts from exp(potential) Ni (potential_based) or the doping. */

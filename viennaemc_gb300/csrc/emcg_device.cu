@@ -1350,15 +1350,18 @@ extern "C" int32_t emcg_device_step(emcg_handle *h, int32_t n_steps, uint32_t st
   d->poissonCycles = d->poissonSolves = 0;
   for (int s = 0; s < n_steps; s++) {
     EMCG_CUDA(cudaEventRecord(d->ev[0], d->stream));
-    double rel;
-    int cyc;
-    int32_t ps = poissonRun(d, false, d->bcReset, &rel, &cyc);
+    // the cluster solve is only enqueued: the step's particle kernels follow
+    // it on the stream at once, and its outcome is read at the end of the step
+    double rel = 0.;
+    int cyc = 0;
+    bool queued = false;
+    EMCG_CUDA(cudaEventRecord(d->ev[2], d->stream));
+    int32_t ps = poissonEnqueue(d->mg, d->dPot, d->dConc, d->bcReset, d->cfg.poisson_rtol,
+                                d->cfg.poisson_max_cycles, d->stream, &queued, &rel, &cyc);
+    EMCG_CUDA(cudaEventRecord(d->ev[3], d->stream));
     d->bcReset = false;
     if (ps)
       return ps;
-    poisMs += d->poissonMs;
-    d->poissonCycles += cyc;
-    d->poissonSolves++;
     EMCG_TRY(d->precision == EMCG_FP64 ? efieldT<double>(d) : efieldT<float>(d));
     EMCG_CUDA(cudaMemsetAsync(d->dNetto, 0, (nc + 1) * sizeof(int32_t), d->stream));
     EMCG_CUDA(cudaMemsetAsync(d->dRemInj, 0, (nc + 1) * sizeof(int32_t), d->stream));
@@ -1377,6 +1380,15 @@ extern "C" int32_t emcg_device_step(emcg_handle *h, int32_t n_steps, uint32_t st
     float ms = 0;
     cudaEventElapsedTime(&ms, d->ev[0], d->ev[1]);
     stepMs += ms;
+    cudaEventElapsedTime(&ms, d->ev[2], d->ev[3]);
+    d->poissonMs = ms;
+    poisMs += ms;
+    if (queued)
+      ps = poissonFinish(d->mg, d->cfg.poisson_rtol, &rel, &cyc);
+    d->poissonCycles += cyc;
+    d->poissonSolves++;
+    if (ps)
+      return ps;
     EMCG_TRY(readErr(d));
     if (netto)
       for (int c = 0; c < nc; c++)

@@ -1402,6 +1402,37 @@ void poissonFree(PoissonMG &P) {
   void *ps[] = {P.C, P.gSum, P.gVeq, P.gVne, P.resetMask, P.resetEq, P.resetNe, P.stats};
   for (void *p : ps)
     cudaFree(p);
+  if (P.hStats)
+    cudaFreeHost(P.hStats);
+  P.hStats = nullptr;
+}
+
+// the single-launch cluster solve, enqueued on st
+template <class MT>
+static int32_t clusterLaunch(PoissonMG &P, double *pot, const double *conc, double rtol,
+                             int maxCycles, cudaStream_t st) {
+  size_t bytes = 0;
+  const CMG<MT> M = clusterDesc<MT>(P, P.clusterSize, &bytes);
+  cudaLaunchAttribute at;
+  cudaLaunchConfig_t cfg = clusterConfig<MT>(P.clusterSize, bytes, st, &at);
+  EMCG_CUDA(cudaLaunchKernelEx(&cfg, poissonClusterKernel<MT>, M, pot, conc, P.C, P.gSum,
+                               conc ? P.gVne : P.gVeq, P.hF[0], P.hF[1], P.hP, rtol, maxCycles,
+                               P.updTol, P.stats));
+  return EMCG_OK;
+}
+
+// the outcome of a solve from its statistics
+static int32_t solveOutcome(double rel, int it, bool updStop, double rtol, double *relRes,
+                            int *cycles) {
+  if (relRes)
+    *relRes = rel;
+  if (cycles)
+    *cycles = it;
+  if (!updStop && !(rel <= rtol)) {
+    setError("Poisson: relative residual %.3e after %d Newton steps (target %.1e)", rel, it, rtol);
+    return EMCG_ERR_NONCONVERGED;
+  }
+  return EMCG_OK;
 }
 
 template <class MT>
@@ -1421,13 +1452,7 @@ static int32_t solveT(PoissonMG &P, double *pot, const double *conc, bool resetB
   bool updStop = false;
   const bool cluster = P.useCluster && P.clusterSize > 0;
   if (cluster) {
-    size_t bytes = 0;
-    const CMG<MT> M = clusterDesc<MT>(P, P.clusterSize, &bytes);
-    cudaLaunchAttribute at;
-    cudaLaunchConfig_t cfg = clusterConfig<MT>(P.clusterSize, bytes, st, &at);
-    EMCG_CUDA(cudaLaunchKernelEx(&cfg, poissonClusterKernel<MT>, M, pot, conc, P.C, P.gSum,
-                                 conc ? P.gVne : P.gVeq, P.hF[0], P.hF[1], P.hP, rtol, maxCycles,
-                                 P.updTol, P.stats));
+    EMCG_TRY(clusterLaunch<MT>(P, pot, conc, rtol, maxCycles, st));
     EMCG_CUDA(cudaMemcpyAsync(stats, P.stats, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     EMCG_CUDA(cudaStreamSynchronize(st));
     rel = stats[0];
@@ -1465,21 +1490,39 @@ static int32_t solveT(PoissonMG &P, double *pot, const double *conc, bool resetB
       }
     }
   }
-  if (relRes)
-    *relRes = rel;
-  if (cycles)
-    *cycles = it;
-  if (!updStop && !(rel <= rtol)) {
-    setError("Poisson: relative residual %.3e after %d Newton steps (target %.1e)", rel, it, rtol);
-    return EMCG_ERR_NONCONVERGED;
-  }
-  return EMCG_OK;
+  return solveOutcome(rel, it, updStop, rtol, relRes, cycles);
 }
 
 int32_t poissonSolve(PoissonMG &P, double *pot, const double *conc, bool resetBC, double rtol,
                      int maxCycles, cudaStream_t st, double *relRes, int *cycles) {
   return P.fp32 ? solveT<float>(P, pot, conc, resetBC, rtol, maxCycles, st, relRes, cycles)
                 : solveT<double>(P, pot, conc, resetBC, rtol, maxCycles, st, relRes, cycles);
+}
+
+int32_t poissonEnqueue(PoissonMG &P, double *pot, const double *conc, bool resetBC, double rtol,
+                       int maxCycles, cudaStream_t st, bool *queued, double *relRes,
+                       int *cycles) {
+  *queued = false;
+  if (!(P.useCluster && P.clusterSize > 0))
+    return poissonSolve(P, pot, conc, resetBC, rtol, maxCycles, st, relRes, cycles);
+  if (!P.hStats)
+    EMCG_CUDA(cudaMallocHost(&P.hStats, 3 * sizeof(double)));
+  if (resetBC) {
+    const int n = P.S.nx * P.S.ny;
+    resetBCKernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(
+        pot, P.resetMask, conc ? P.resetNe : P.resetEq, n);
+    EMCG_CUDA(cudaGetLastError());
+  }
+  EMCG_TRY(P.fp32 ? clusterLaunch<float>(P, pot, conc, rtol, maxCycles, st)
+                  : clusterLaunch<double>(P, pot, conc, rtol, maxCycles, st));
+  EMCG_CUDA(cudaMemcpyAsync(P.hStats, P.stats, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  *queued = true;
+  return EMCG_OK;
+}
+
+int32_t poissonFinish(PoissonMG &P, double rtol, double *relRes, int *cycles) {
+  EMCG_CHECK_ARG(P.hStats, "no enqueued Poisson solve");
+  return solveOutcome(P.hStats[0], (int)P.hStats[1], P.hStats[2] != 0., rtol, relRes, cycles);
 }
 
 } // namespace emcg

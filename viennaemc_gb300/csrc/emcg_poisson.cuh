@@ -90,6 +90,9 @@ struct PoissonMG {
   int clusterSize = 0;
   size_t clusterSmem = 0;
   bool useCluster = true;
+  // pinned copy of a cluster solve's [relative residual, Newton steps,
+  // stopped by the update rule], written by the stream (poissonEnqueue)
+  double *hStats = nullptr;
 };
 
 int32_t poissonCreate(PoissonMG &P, const PoissonSetup &S, bool fp32, int smooth,
@@ -101,5 +104,13 @@ void poissonFree(PoissonMG &P);
 int32_t poissonSolve(PoissonMG &P, double *pot, const double *conc, bool resetBC,
                      double rtol, int maxCycles, cudaStream_t st, double *relRes,
                      int *cycles);
+// The cluster solve without waiting for it: enqueues the solve and the copy
+// of its statistics on st and returns *queued = true; poissonFinish, once st
+// has passed that copy, gives what poissonSolve returns.  Where the grid has
+// no cluster solve it runs poissonSolve and returns *queued = false.
+int32_t poissonEnqueue(PoissonMG &P, double *pot, const double *conc, bool resetBC, double rtol,
+                       int maxCycles, cudaStream_t st, bool *queued, double *relRes,
+                       int *cycles);
+int32_t poissonFinish(PoissonMG &P, double rtol, double *relRes, int *cycles);
 
 } // namespace emcg
