@@ -284,11 +284,10 @@ constexpr int kMaxCluster = 16;
 constexpr int kSmallNodes = 4096;
 // levels below the finest of at most this many nodes (all held by CTA 0) are
 // worked by warp 0 alone, its phases ending in __syncwarp instead of a
-// barrier of the whole CTA
-#ifndef EMCG_WARP_NODES
-#define EMCG_WARP_NODES 64
-#endif
-constexpr int kWarpNodes = EMCG_WARP_NODES;
+// barrier of the whole CTA.  Measured on the 201 x 101 resistor: 64 nodes
+// (8x5 and coarser) -0.3 %, 128 nodes +5 %, 512 nodes +31 % against none:
+// one warp walks a larger level's nodes one after another.
+constexpr int kWarpNodes = 64;
 constexpr size_t kClusterSmemMax = 227 * 1024;
 
 // q = t / d for 0 <= t and t * d < 2^32, by one wide multiply (m = ceil(2^32 / d))
