@@ -199,27 +199,30 @@ def test_full_device_steps_run_and_conserve_count(engine):
         sim.close()
 
 
-def _resistor_201x101():
+def _resistor_201x101(scale=1):
     from viennaemc_gb300 import device as D
     from viennaemc_gb300.physics import silicon_material
-    dev = D.Device(silicon_material(), (100e-9, 50e-9), (0.5e-9, 0.5e-9))
+    lx, ly = 100e-9 * scale, 50e-9 * scale
+    dev = D.Device(silicon_material(), (lx, ly), (0.5e-9, 0.5e-9))
     dev.setDeviceWidth(1e-4)
-    dev.addConstantDopingRegion((0, 0), (100e-9, 50e-9), 1e24)
-    dev.addOhmicContact(D.XMAX, 0.0, (0,), (50e-9,))
-    dev.addOhmicContact(D.XMIN, 0.5, (0,), (50e-9,))
+    dev.addConstantDopingRegion((0, 0), (lx, ly), 1e24)
+    dev.addOhmicContact(D.XMAX, 0.0, (0,), (ly,))
+    dev.addOhmicContact(D.XMIN, 0.5, (0,), (ly,))
     return dev
 
 
-@pytest.mark.parametrize("case", DEVICE_CASES + ["resistor_201x101"])
+# resistor_401x201: a CTA's band of the finest level holds more nodes than the
+# register-held sweeps take, so those sweeps run one phase per half sweep
+@pytest.mark.parametrize("case", DEVICE_CASES + ["resistor_201x101", "resistor_401x201"])
 def test_poisson_cluster_equals_multilaunch(engine, case):
     """The single-launch cluster solve and the one-launch-per-phase solve
     evaluate the same expressions on the same values: same cycles, same
     potential (1e-13 thermal voltages)."""
     from viennaemc_gb300 import _lib as L
     from viennaemc_gb300 import device as D
-    if case == "resistor_201x101":
+    if case.startswith("resistor_"):
         from viennaemc_gb300 import physics as P
-        dev = _resistor_201x101()
+        dev = _resistor_201x101(2 if case == "resistor_401x201" else 1)
         pt = P.silicon_electron("refbulk", n_levels=1000, max_energy=4.0, regions=[0],
                                 coulomb=True, region_doping=dev.getDopingRegionDoping)
         sim = D.DeviceSimulation(dev, pt, scheme=D.CIC, dt=1e-16, seed=5, precision="fp32",
@@ -233,7 +236,7 @@ def test_poisson_cluster_equals_multilaunch(engine, case):
                             poisson_max_cycles=200)
         pot0, conc = g["pot_init"], g["conc0"]
     assert sim.poisson_mode() >= 1
-    if case == "resistor_201x101":
+    if case.startswith("resistor_"):
         assert sim.poisson_mode() > 1  # distributed over several CTAs
     out = {}
     for mode in (1, 0):
@@ -345,3 +348,25 @@ def test_initial_particles_beyond_capacity_are_rejected(engine):
         small.init_particles()
     assert ei.value.status == -1 and "capacity" in str(ei.value)
     small.close()
+
+
+def test_step_reports_a_solve_that_missed_its_target(engine):
+    """The device step checks its enqueued Poisson solve at the end of the
+    step: a Newton-step limit too small for the target is reported there."""
+    from viennaemc_gb300 import _lib as L
+    from viennaemc_gb300 import device as D
+    from viennaemc_gb300 import physics as P
+    dev = _resistor_201x101()
+    pt = P.silicon_electron("refbulk", n_levels=1000, max_energy=4.0, regions=[0],
+                            coulomb=True, region_doping=dev.getDopingRegionDoping)
+    sim = D.DeviceSimulation(dev, pt, scheme=D.CIC, dt=1e-16, seed=5, precision="fp32",
+                             poisson_rtol=1e-8, poisson_max_cycles=60)
+    sim.calcEquilibriumCharacteristics()
+    sim.performEMCStep(2)
+    sim.set_poisson(rtol=1e-30, max_cycles=1)
+    with pytest.raises(L.EmcgError):
+        sim.performEMCStep(1)
+    sim.set_poisson(rtol=1e-8, max_cycles=60)
+    sim.performEMCStep(2)  # the handle stays usable
+    assert sim.num_particles() > 0
+    sim.close()
