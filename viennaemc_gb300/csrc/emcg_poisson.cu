@@ -469,7 +469,9 @@ template <class MT> __device__ void cSmooth(const CCtx &c, const CLevel<MT> &Lr,
 // registers: a thread keeps the same nodes over the sweeps, so their position,
 // class, right-hand side and diagonal are read once, and a half sweep reads
 // only the neighbours' corrections.  The arithmetic is cSmoothT's.
-constexpr int kSweepNodes = 3; // nodes of one colour per thread
+// nodes of one colour per thread.  Six, for the 2,814-node bands of a 401 x 201
+// grid, spilled registers: 0.5 % faster there, 1.4 % slower on 201 x 101.
+constexpr int kSweepNodes = 3;
 template <bool kS, int K, class MT>
 __device__ __forceinline__ void cHalfSweep(const CCtx &c, const CLevel<MT> &L, int r0,
                                            const int (&pos)[2][kSweepNodes],
