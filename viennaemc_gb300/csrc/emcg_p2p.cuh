@@ -18,8 +18,8 @@
 // split into chunks over a second grid dimension and the chunks' partial sums
 // are added in order afterwards.  The pair arithmetic runs in the engine's
 // precision (float: rsqrt), each tile's partial sums go to double
-// accumulators.  The work is n^2 pair terms of about 20 operations: bound by
-// the FP32 (or FP64) pipes, not by memory.
+// accumulators.  The work is n^2 pair terms of about 15 (float) or 20
+// (double) operations: bound by the FP32 (or FP64) pipes, not by memory.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -71,6 +71,33 @@ __device__ __forceinline__ void pairTerm(T xi, T yi, T zi, T qi, const Src4<T> &
   acc[1] += dy * -inv2;
   acc[2] += dz * -inv2;
   acc[3] += inv * s.q;
+}
+
+// The float form of the same term in fewer operations.  Closer than the
+// cutoff the reference rescales d to the cutoff's length and takes 1/r and
+// 1/r^2 at the cutoff, so the force factor d / r'^3 becomes d (1/r) (1/cut)^2
+// and the potential term q_j / cut: with c = min(1/r, 1/cut) the terms are
+// d (1/r) c^2 q_j and c q_j on either side of the cutoff.  The target's charge
+// and the force's sign are applied to the tile's sums, not to every pair.
+__device__ __forceinline__ void pairTermF(float xi, float yi, float zi, const Src4<float> &s,
+                                          float invCut, float acc[4]) {
+  const float dx = xi - s.x, dy = yi - s.y, dz = zi - s.z;
+  const float inv = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+  const float c = fminf(inv, invCut);
+  const float w = inv * c * c * s.q;
+  acc[0] = fmaf(dx, w, acc[0]);
+  acc[1] = fmaf(dy, w, acc[1]);
+  acc[2] = fmaf(dz, w, acc[2]);
+  acc[3] = fmaf(c, s.q, acc[3]);
+}
+
+template <class T>
+__device__ __forceinline__ void pairTermAny(T xi, T yi, T zi, T qi, const Src4<T> &s, T invCut,
+                                            T cut, T invCut2, T acc[4]) {
+  if constexpr (sizeof(T) == 4)
+    pairTermF(xi, yi, zi, s, invCut, acc);
+  else
+    pairTerm<T>(xi, yi, zi, qi, s, invCut, cut, invCut2, acc);
 }
 
 // Grid (target blocks, source chunks): each thread sums the sources of its
@@ -125,7 +152,7 @@ __global__ void __launch_bounds__(kP2PThreads)
               const Src4<T> s = tile[k];
 #pragma unroll
               for (int u = 0; u < kP2PTargets; u++)
-                pairTerm<T>(xi[u], yi[u], zi[u], qi[u], s, invCut, cut, invCut2, acc[u]);
+                pairTermAny<T>(xi[u], yi[u], zi[u], qi[u], s, invCut, cut, invCut2, acc[u]);
             }
           } else {
             for (int k = 0; k < cnt; k++) {
@@ -133,14 +160,18 @@ __global__ void __launch_bounds__(kP2PThreads)
 #pragma unroll
               for (int u = 0; u < kP2PTargets; u++)
                 if (k != self[u])
-                  pairTerm<T>(xi[u], yi[u], zi[u], qi[u], s, invCut, cut, invCut2, acc[u]);
+                  pairTermAny<T>(xi[u], yi[u], zi[u], qi[u], s, invCut, cut, invCut2, acc[u]);
             }
           }
 #pragma unroll
-          for (int u = 0; u < kP2PTargets; u++)
+          for (int u = 0; u < kP2PTargets; u++) {
+            // float sums leave out the target's charge and the force's sign
+            const double g = sizeof(T) == 4 ? -(double)qi[u] : 1.0;
 #pragma unroll
-            for (int v = 0; v < 4; v++)
-              F[u][v] += (double)acc[u][v];
+            for (int v = 0; v < 3; v++)
+              F[u][v] += g * (double)acc[u][v];
+            F[u][3] += (double)acc[u][3];
+          }
         }
       }
   double *out = part + (size_t)blockIdx.y * 4 * nTgt;
