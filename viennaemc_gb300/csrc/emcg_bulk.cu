@@ -708,7 +708,7 @@ __device__ __forceinline__ void flushPos(const float *R, const float vogt[3], fl
   }
 }
 
-template <int MINB>
+template <int MINB, bool kOne>
 __global__ void __launch_bounds__(256, MINB)
     bulkStepAsyncKernel(StateK<float> st, const ModelK<float> *__restrict__ models,
                         const EnsK<float> *__restrict__ ens, const Tile *__restrict__ tiles,
@@ -730,7 +730,7 @@ __global__ void __launch_bounds__(256, MINB)
   const Tile tl = tiles[blockIdx.x];
   const EnsK<T> &EK = ens[tl.ens];
   const ModelK<T> &M = models[EK.model];
-  const int nV = EK.nV;
+  const int nV = kOne ? 1 : EK.nV;
   const int64_t gi = tl.begin + threadIdx.x;
   const bool active = gi < tl.end;
   const uint32_t pid = (uint32_t)(gi - EK.begin);
@@ -846,7 +846,8 @@ __global__ void __launch_bounds__(256, MINB)
           live = false;
           s = nSteps;
         } else {
-          const T vf = driftEcs(M.v[valley], EK.fv[valley][sub], ev ? tau : rem, kE, E, dP);
+          const int vd = kOne ? 0 : valley;
+          const T vf = driftEcs(M.v[vd], EK.fv[vd][sub], ev ? tau : rem, kE, E, dP);
           if (ev) {
             tIn += tau;
             pend = true;
@@ -855,7 +856,7 @@ __global__ void __launch_bounds__(256, MINB)
             gtau -= dt;
             if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
               gtau = -m_log(rng.ulog()) * M.grainTau;
-            const T *g = EK.g[valley][sub];
+            const T *g = EK.g[vd][sub];
             const int slot = ws * 32 + lane;
             winE[slot] = E;
             winD[slot] = vf * (g[0] * kE[0] + g[1] * kE[1] + g[2] * kE[2]);
@@ -905,9 +906,17 @@ __global__ void __launch_bounds__(256, MINB)
 template <int MINB> int32_t asyncSmemOptIn(size_t bytes) {
   if (bytes <= 48 * 1024)
     return EMCG_OK;
-  EMCG_CUDA(cudaFuncSetAttribute(bulkStepAsyncKernel<MINB>,
+  EMCG_CUDA(cudaFuncSetAttribute(bulkStepAsyncKernel<MINB, false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  EMCG_CUDA(cudaFuncSetAttribute(bulkStepAsyncKernel<MINB, true>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   return EMCG_OK;
+}
+
+// the warp-asynchronous kernel for a register cap; kOne: every ensemble of the
+// batch has one valley, so the drift reads that valley's constants once
+template <int MINB> static auto asyncKernel(bool one) {
+  return one ? bulkStepAsyncKernel<MINB, true> : bulkStepAsyncKernel<MINB, false>;
 }
 
 // drift() known-answer kernel: independent particles, per-particle force/dt
@@ -1146,11 +1155,12 @@ template <class T> static void *stepKernelFn(const BulkImpl *b, bool *queued) {
   *queued = b->queued != 0;
   if constexpr (sizeof(T) == 4) {
     if (b->queued == 2) {
+      const bool one = b->nVmax == 1;
       if (b->minBlocks >= 4 && b->blockThreads <= 256)
-        return (void *)bulkStepAsyncKernel<4>;
+        return (void *)asyncKernel<4>(one);
       if (b->minBlocks == 3 && b->blockThreads <= 256)
-        return (void *)bulkStepAsyncKernel<3>;
-      return (void *)bulkStepAsyncKernel<1>;
+        return (void *)asyncKernel<3>(one);
+      return (void *)asyncKernel<1>(one);
     }
   }
   if (b->queued) {
@@ -1364,15 +1374,15 @@ static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHos
             const size_t asmem = asyncSmemBytes(b->blockThreads / 32, ns, Q);
             if (b->minBlocks >= 4 && b->blockThreads <= 256) {
               EMCG_TRY(asyncSmemOptIn<4>(asmem));
-              bulkStepAsyncKernel<4><<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
+              asyncKernel<4>(b->nVmax == 1)<<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
                   st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
             } else if (b->minBlocks == 3 && b->blockThreads <= 256) {
               EMCG_TRY(asyncSmemOptIn<3>(asmem));
-              bulkStepAsyncKernel<3><<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
+              asyncKernel<3>(b->nVmax == 1)<<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
                   st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
             } else {
               EMCG_TRY(asyncSmemOptIn<1>(asmem));
-              bulkStepAsyncKernel<1><<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
+              asyncKernel<1>(b->nVmax == 1)<<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
                   st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
             }
           }
