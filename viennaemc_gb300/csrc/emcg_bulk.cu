@@ -837,6 +837,14 @@ __global__ void __launch_bounds__(256, MINB)
       // up to kPassActions free flights per lane and pass: each ends either at
       // the end of step s (bulkParticleStep without an event) or at the next
       // event inside it; both drift first, so the warp's lanes drift together
+      // the subvalley's force and field direction, read once per pass
+      const int vd = kOne ? 0 : valley;
+      T fvl[3], gl[3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        fvl[i] = EK.fv[vd][sub][i];
+        gl[i] = EK.g[vd][sub][i];
+      }
 #pragma unroll 1
       for (int act = 0; act < kPassActions && !pend && s < limit; act++) {
         const T rem = dt - tIn;
@@ -846,8 +854,7 @@ __global__ void __launch_bounds__(256, MINB)
           live = false;
           s = nSteps;
         } else {
-          const int vd = kOne ? 0 : valley;
-          const T vf = driftEcs(M.v[vd], EK.fv[vd][sub], ev ? tau : rem, kE, E, dP);
+          const T vf = driftEcs(M.v[vd], fvl, ev ? tau : rem, kE, E, dP);
           if (ev) {
             tIn += tau;
             pend = true;
@@ -856,10 +863,9 @@ __global__ void __launch_bounds__(256, MINB)
             gtau -= dt;
             if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
               gtau = -m_log(rng.ulog()) * M.grainTau;
-            const T *g = EK.g[vd][sub];
             const int slot = ws * 32 + lane;
             winE[slot] = E;
-            winD[slot] = vf * (g[0] * kE[0] + g[1] * kE[1] + g[2] * kE[2]);
+            winD[slot] = vf * (gl[0] * kE[0] + gl[1] * kE[1] + gl[2] * kE[2]);
             if (nV > 1)
               winVal[slot] = (uint8_t)valley;
             s++;
