@@ -238,6 +238,12 @@ int32_t emcg_set_launch(emcg_handle *h, int32_t block_threads,
    per-step sums in float in an order that varies from run to run: particle
    states are reproducible bit for bit, observables to float rounding. */
 int32_t emcg_set_scatter_mode(emcg_handle *h, int32_t queued);
+/* Tuning of the warp-asynchronous kernel: free flights a lane may take in one
+   drift pass before the warp checks its waiting lanes again, in [1, 20]
+   (default 5).  Only the schedule changes: particle states are the same bit
+   for bit.  No reference counterpart. */
+int32_t emcg_set_pass_actions(emcg_handle *h, int32_t n);
+int32_t emcg_get_pass_actions(emcg_handle *h, int32_t *n);
 
 /* Tuning: register cap of the step kernel, as the minimum number of resident
    256-thread blocks per SM (1 = uncapped, 3 or 4); capped variants apply to
@@ -250,10 +256,12 @@ int32_t emcg_bulk_set_graph(emcg_handle *h, int32_t enable);
 /* Autotuner: runs trial_steps steps (from step0, advancing the ensembles --
    use it as warm-up) with each candidate launch shape (block threads 128 /
    256, register cap 1 / 3 / 4 resident blocks per SM, lockstep,
-   block-queued or, for float, warp-asynchronous scatter), twice: in a
-   forward and then a backward pass over the shapes.  It keeps the shape of
-   least total device time.  *steps_used = steps run (2 x shapes x
-   trial_steps); outputs may be NULL.  No reference counterpart. */
+   block-queued or, for float, warp-asynchronous scatter with 3 or 5 free
+   flights per pass), twice: in a forward and then a backward pass over the
+   shapes.  It keeps the shape of least total device time (its pass actions:
+   emcg_get_pass_actions).  *steps_used = steps run (2 x shapes x
+   trial_steps: 13 float shapes, 8 double); outputs may be NULL.  No
+   reference counterpart. */
 int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint32_t step0,
                            int32_t *steps_used, int32_t *block_threads, int32_t *min_blocks,
                            int32_t *queued);

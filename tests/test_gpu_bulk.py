@@ -397,14 +397,14 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(engine):
     b = _sweep_batch(engine)
     b.set_launch(256, 20)
     cfg = b.autotune(10)
-    assert cfg["steps_used"] == 220  # 11 float shapes x 10 steps, forward and backward
+    assert cfg["steps_used"] == 260  # 13 float shapes x 10 steps, forward and backward
     assert cfg["block_threads"] in (128, 256) and cfg["min_blocks"] in (1, 3, 4)
-    assert cfg["queued"] in (0, 1, 2)
+    assert cfg["queued"] in (0, 1, 2) and cfg["pass_actions"] in (3, 5)
     o = b.step(20)
     b.close()
     b2 = _sweep_batch(engine)
     b2.set_launch(256, 20)
-    b2.step(220)
+    b2.step(260)
     o2 = b2.step(20)
     b2.close()
     cnt, cnt2 = o[..., 2].sum(axis=-1), o2[..., 2].sum(axis=-1)
@@ -527,3 +527,30 @@ def test_two_valley_kernels_equal_lockstep(engine, mode):
     ea = oa[0, 100:, :, 0].sum(axis=0) / cnt_a[100:].sum(axis=0)
     eq = oq[0, 100:, :, 0].sum(axis=0) / cnt_q[100:].sum(axis=0)
     assert np.allclose(ea, eq, rtol=2e-2)
+
+
+def test_pass_actions_change_only_the_schedule(engine):
+    """Free flights per drift pass of the warp-asynchronous kernel (1, the
+    default 5, 20): the same particle states bit for bit, the same counts, and
+    step sums equal to float rounding; out-of-range settings are refused."""
+    outs = []
+    for n in (1, 5, 20):
+        b = _sweep_batch(engine)
+        b.set_launch(256, 40, 4, queued=2, pass_actions=n)
+        assert b.pass_actions() == n
+        o = b.step(80)
+        outs.append((o, [b.get_state(e) for e in range(len(b.specs))]))
+        b.close()
+    for o, states in outs[1:]:
+        assert np.array_equal(o[..., 2], outs[0][0][..., 2])
+        for c in (0, 1):
+            a, r = o[..., c], outs[0][0][..., c]
+            assert np.allclose(a, r, rtol=1e-5, atol=1e-6 * np.abs(r).max())
+        for a, r in zip(states, outs[0][1]):
+            for f in ("kx", "ky", "kz", "energy", "px", "py", "pz", "tau"):
+                assert np.array_equal(getattr(a, f), getattr(r, f)), f
+    b = _sweep_batch(engine)
+    for bad in (0, 21):
+        with pytest.raises(engine._lib.EmcgError):
+            b.set_launch(pass_actions=bad)
+    b.close()

@@ -161,6 +161,10 @@ def _declare(L):
     L.emcg_set_launch.argtypes = [vp, i32, i32]
     L.emcg_set_scatter_mode.restype = i32
     L.emcg_set_scatter_mode.argtypes = [vp, i32]
+    L.emcg_set_pass_actions.restype = i32
+    L.emcg_set_pass_actions.argtypes = [vp, i32]
+    L.emcg_get_pass_actions.restype = i32
+    L.emcg_get_pass_actions.argtypes = [vp, C.POINTER(i32)]
     L.emcg_set_occupancy.restype = i32
     L.emcg_set_occupancy.argtypes = [vp, i32]
     L.emcg_drift_kat.restype = i32

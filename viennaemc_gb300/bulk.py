@@ -201,12 +201,21 @@ class BulkBatch:
         self._earr[ens] = d
 
     # ---- dynamics ------------------------------------------------------------
-    def set_launch(self, block_threads=0, steps_per_launch=0, min_blocks=0, queued=None):
+    def set_launch(self, block_threads=0, steps_per_launch=0, min_blocks=0, queued=None,
+                   pass_actions=None):
         L.check(self._lib.emcg_set_launch(self.h, block_threads, steps_per_launch))
         if min_blocks:
             L.check(self._lib.emcg_set_occupancy(self.h, min_blocks))
         if queued is not None:
             L.check(self._lib.emcg_set_scatter_mode(self.h, int(queued)))
+        if pass_actions is not None:
+            L.check(self._lib.emcg_set_pass_actions(self.h, int(pass_actions)))
+
+    def pass_actions(self) -> int:
+        """Free flights per drift pass of the warp-asynchronous kernel."""
+        n = C.c_int32()
+        L.check(self._lib.emcg_get_pass_actions(self.h, C.byref(n)))
+        return n.value
 
     def set_graph(self, enable: bool = True):
         """Replay each launch of steps from an instantiated CUDA graph."""
@@ -222,7 +231,7 @@ class BulkBatch:
                                              C.byref(blk), C.byref(mb), C.byref(q)))
         self.step_index = s0 + used.value
         return {"block_threads": blk.value, "min_blocks": mb.value, "queued": q.value,
-                "steps_used": used.value}
+                "pass_actions": self.pass_actions(), "steps_used": used.value}
 
     def step(self, n_steps: int = 1, observables: bool = True, step0: int | None = None):
         """Advance all ensembles; returns sums [ens, step, valley, {E, v.dir, count}]."""

@@ -640,8 +640,11 @@ __global__ void bulkInitKernel(StateK<T> st, const ModelK<T> *__restrict__ model
 constexpr int kAsyncWindow = 20;
 // lanes of a warp that wait at an event before the warp scatters them together
 constexpr int kEventBatch = 8;
-// free flights a lane may take in one drift pass
-constexpr int kPassActions = 3;
+// free flights a lane may take in one drift pass, by default (set per handle:
+// emcg_set_pass_actions).  Measured on 2^20 electrons, 2000 steps: 3 gave
+// 8.90e10, 4 9.00e10, 5 9.06e10, 6 9.02e10, 8 8.70e10, 20 6.79e10; on the
+// 64-ensemble sweep 5 was 3.6 % slower than 3, so the autotuner tries both.
+constexpr int kPassActions = 5;
 // fixed-point scales of a warp's step sums: energy 2^-20 eV, velocity
 // 0.25 m/s per unit; below kFixMax per lane, 32 lanes stay within int32
 constexpr float kFixE = 1048576.f;
@@ -712,7 +715,7 @@ template <int MINB, bool kOne>
 __global__ void __launch_bounds__(256, MINB)
     bulkStepAsyncKernel(StateK<float> st, const ModelK<float> *__restrict__ models,
                         const EnsK<float> *__restrict__ ens, const Tile *__restrict__ tiles,
-                        int nSteps, uint32_t step0, int chunk, int nVmax,
+                        int nSteps, uint32_t step0, int chunk, int nVmax, int passActions,
                         double *__restrict__ obs, int *__restrict__ err) {
   using T = float;
   extern __shared__ __align__(16) unsigned char smemRaw[];
@@ -834,7 +837,7 @@ __global__ void __launch_bounds__(256, MINB)
         toEcs(M.v[valley].rot[sub], k[0], k[1], k[2], kE);
       }
     } else {
-      // up to kPassActions free flights per lane and pass: each ends either at
+      // up to passActions free flights per lane and pass: each ends either at
       // the end of step s (bulkParticleStep without an event) or at the next
       // event inside it; both drift first, so the warp's lanes drift together
       // the subvalley's force and field direction, read once per pass
@@ -846,7 +849,7 @@ __global__ void __launch_bounds__(256, MINB)
         gl[i] = EK.g[vd][sub][i];
       }
 #pragma unroll 1
-      for (int act = 0; act < kPassActions && !pend && s < limit; act++) {
+      for (int act = 0; act < passActions && !pend && s < limit; act++) {
         const T rem = dt - tIn;
         const bool ev = tau < rem;
         if (ev && ++nEv > kMaxScatterPerStep) {
@@ -982,6 +985,7 @@ struct BulkImpl {
   int blockThreads = 256;
   int minBlocks = 1; // register cap variant of the step kernel (1, 3 or 4)
   int queued = 0; // step kernel: 0 lockstep, 1 block-queued, 2 warp-asynchronous (float)
+  int passActions = kPassActions; // warp-asynchronous kernel: free flights per drift pass
   int stepsPerLaunch = 0;
   int chunk = 16;
   uint64_t *dWords = nullptr;
@@ -1008,7 +1012,7 @@ struct BulkImpl {
   cudaGraphExec_t gexec = nullptr;
   cudaGraphNode_t gKernel = nullptr;
   cudaKernelNodeParams gKp = {};
-  int gNs = -1, gBlock = 0, gMinb = 0, gQueued = -1, gTiles = -1;
+  int gNs = -1, gBlock = 0, gMinb = 0, gQueued = -1, gTiles = -1, gPass = -1;
   alignas(16) unsigned char gArgs[256] = {};
   void *gParams[12] = {};
 };
@@ -1023,6 +1027,7 @@ template <class T> struct StepArgs {
   uint32_t step0;
   int chunk;
   int nVmax;
+  int pass;
   double *obs;
   const uint64_t *words;
   const int64_t *off;
@@ -1186,7 +1191,7 @@ template <class T> static void *stepKernelFn(const BulkImpl *b, bool *queued) {
 // (Re)build the graph of one launch of ns steps for the current configuration.
 template <class T> static int32_t graphFor(BulkImpl *b, int ns, size_t smem, size_t qsmem) {
   if (b->gexec && b->gNs == ns && b->gBlock == b->blockThreads && b->gMinb == b->minBlocks &&
-      b->gQueued == b->queued && b->gTiles == b->nTiles)
+      b->gQueued == b->queued && b->gTiles == b->nTiles && b->gPass == b->passActions)
     return EMCG_OK;
   dropGraph(b);
   static_assert(sizeof(StepArgs<T>) <= sizeof(b->gArgs), "step arguments exceed the buffer");
@@ -1199,6 +1204,7 @@ template <class T> static int32_t graphFor(BulkImpl *b, int ns, size_t smem, siz
   a.step0 = 0;
   a.chunk = b->chunk;
   a.nVmax = b->nVmax;
+  a.pass = b->passActions;
   a.obs = b->dObs;
   a.words = nullptr;
   a.off = nullptr;
@@ -1209,7 +1215,12 @@ template <class T> static int32_t graphFor(BulkImpl *b, int ns, size_t smem, siz
                     &a.chunk, &a.nVmax, &a.obs, &a.words, &a.off, &a.err};
   void *que[10] = {&a.st, &a.mp, &a.ep, &a.tiles, &a.ns, &a.step0, &a.chunk, &a.nVmax, &a.obs,
                    &a.err};
-  if (queued)
+  void *asy[11] = {&a.st,    &a.mp,    &a.ep,   &a.tiles, &a.ns, &a.step0,
+                   &a.chunk, &a.nVmax, &a.pass, &a.obs,   &a.err};
+  static_assert(sizeof(asy) <= sizeof(b->gParams), "kernel parameters exceed the buffer");
+  if (b->queued == 2 && sizeof(T) == 4)
+    std::memcpy(b->gParams, asy, sizeof(asy));
+  else if (queued)
     std::memcpy(b->gParams, que, sizeof(que));
   else
     std::memcpy(b->gParams, lock, sizeof(lock));
@@ -1243,6 +1254,7 @@ template <class T> static int32_t graphFor(BulkImpl *b, int ns, size_t smem, siz
   b->gBlock = b->blockThreads;
   b->gMinb = b->minBlocks;
   b->gQueued = b->queued;
+  b->gPass = b->passActions;
   b->gTiles = b->nTiles;
   return EMCG_OK;
 }
@@ -1381,15 +1393,18 @@ static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHos
             if (b->minBlocks >= 4 && b->blockThreads <= 256) {
               EMCG_TRY(asyncSmemOptIn<4>(asmem));
               asyncKernel<4>(b->nVmax == 1)<<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
-                  st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
+                  st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->passActions,
+                  b->dObs, b->dErr);
             } else if (b->minBlocks == 3 && b->blockThreads <= 256) {
               EMCG_TRY(asyncSmemOptIn<3>(asmem));
               asyncKernel<3>(b->nVmax == 1)<<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
-                  st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
+                  st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->passActions,
+                  b->dObs, b->dErr);
             } else {
               EMCG_TRY(asyncSmemOptIn<1>(asmem));
               asyncKernel<1>(b->nVmax == 1)<<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
-                  st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
+                  st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->passActions,
+                  b->dObs, b->dErr);
             }
           }
         } else if (b->queued) {
@@ -1868,6 +1883,22 @@ extern "C" int32_t emcg_set_scatter_mode(emcg_handle *h, int32_t queued) {
   return EMCG_OK;
 }
 
+extern "C" int32_t emcg_set_pass_actions(emcg_handle *h, int32_t n) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(n >= 1 && n <= kAsyncWindow, "pass actions must be in [1, %d]", kAsyncWindow);
+  b->passActions = n;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_get_pass_actions(emcg_handle *h, int32_t *n) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(n, "NULL output");
+  *n = b->passActions;
+  return EMCG_OK;
+}
+
 extern "C" int32_t emcg_set_occupancy(emcg_handle *h, int32_t min_blocks_per_sm) {
   BulkImpl *b;
   EMCG_TRY(bulkOf(h, &b));
@@ -1981,16 +2012,19 @@ extern "C" int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint3
   // that the ensembles' warming up from the initial distribution (events get
   // more frequent) weighs on every shape alike; the least total device time
   // wins
+  // (the warp-asynchronous kernel with 3 and with 5 free flights per pass)
   struct Cand {
-    int block, minb, queued;
+    int block, minb, queued, pass;
   };
-  const Cand cands[] = {{256, 4, 0}, {256, 3, 0}, {256, 1, 0}, {128, 4, 0}, {128, 1, 0},
-                        {256, 4, 1}, {256, 3, 1}, {128, 4, 1}, {256, 4, 2}, {256, 3, 2},
-                        {128, 4, 2}};
-  const int nCands = b->precision == EMCG_FP32 ? 11 : 8; // mode 2 is float only
-  const int keepPer = b->stepsPerLaunch;
+  const Cand cands[] = {{256, 4, 0, 0}, {256, 3, 0, 0}, {256, 1, 0, 0}, {128, 4, 0, 0},
+                        {128, 1, 0, 0}, {256, 4, 1, 0}, {256, 3, 1, 0}, {128, 4, 1, 0},
+                        {256, 4, 2, 3}, {256, 3, 2, 3}, {128, 4, 2, 3}, {256, 4, 2, 5},
+                        {128, 4, 2, 5}};
+  constexpr int kCands = sizeof(cands) / sizeof(cands[0]);
+  const int nCands = b->precision == EMCG_FP32 ? kCands : 8; // mode 2 is float only
+  const int keepPer = b->stepsPerLaunch, keepPass = b->passActions;
   b->stepsPerLaunch = trial_steps;
-  double ms[11] = {};
+  double ms[kCands] = {};
   uint32_t s = step0;
   for (int pass = 0; pass < 2 * nCands; pass++) {
     const int ci = pass < nCands ? pass : 2 * nCands - 1 - pass;
@@ -2000,11 +2034,13 @@ extern "C" int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint3
     b->blockThreads = c.block;
     b->minBlocks = c.minb;
     b->queued = c.queued;
+    b->passActions = c.pass ? c.pass : keepPass;
     int32_t st = b->precision == EMCG_FP64 ? stepTyped<double>(b, trial_steps, s, nullptr)
                                            : stepTyped<float>(b, trial_steps, s, nullptr);
     s += trial_steps;
     if (st != EMCG_OK) {
       b->stepsPerLaunch = keepPer;
+      b->passActions = keepPass;
       return st;
     }
     ms[ci] += b->lastMs;
@@ -2019,6 +2055,7 @@ extern "C" int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint3
   b->blockThreads = bestC.block;
   b->minBlocks = bestC.minb;
   b->queued = bestC.queued;
+  b->passActions = bestC.pass ? bestC.pass : keepPass;
   b->stepsPerLaunch = keepPer;
   if (steps_used)
     *steps_used = (int32_t)(s - step0);
