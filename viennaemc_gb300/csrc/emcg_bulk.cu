@@ -639,7 +639,9 @@ __global__ void bulkInitKernel(StateK<T> st, const ModelK<T> *__restrict__ model
 // ---------------------------------------------------------------------------
 constexpr int kAsyncWindow = 20;
 // lanes of a warp that wait at an event before the warp scatters them together
-constexpr int kEventBatch = 8;
+// (with five free flights per pass, 7 ran 0.9 % faster than 8 on 2^20
+// electrons and the same on the 64-ensemble sweep)
+constexpr int kEventBatch = 7;
 // free flights a lane may take in one drift pass, by default (set per handle:
 // emcg_set_pass_actions).  Measured on 2^20 electrons, 2000 steps: 3 gave
 // 8.90e10, 4 9.00e10, 5 9.06e10, 6 9.02e10, 8 8.70e10, 20 6.79e10; on the
