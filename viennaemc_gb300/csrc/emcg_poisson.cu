@@ -501,9 +501,39 @@ __device__ __forceinline__ void cHalfSweep(const CCtx &c, const CLevel<MT> &L, i
   cSync(L);
 }
 
+// residual r - A d at the held nodes of colour K (cResidualT's arithmetic;
+// the Dirichlet nodes' zeros are written once, at the start of the launch)
+template <bool kS, int K, class MT>
+__device__ __forceinline__ void cResidualHeld(const CCtx &c, const CLevel<MT> &L, int r0,
+                                              const int (&pos)[2][kSweepNodes],
+                                              const int (&cl)[2][kSweepNodes],
+                                              const MT (&rr)[2][kSweepNodes],
+                                              const MT (&den)[2][kSweepNodes]) {
+#pragma unroll
+  for (int j = 0; j < kSweepNodes; j++) {
+    if (pos[K][j] < 0)
+      continue;
+    const int ly = pos[K][j] >> 16, x = pos[K][j] & 0xffff, y = r0 + ly;
+    const Coef<MT> C = cCoef(c, L, cl[K][j]);
+    const MT *d = cRowNearT<true, MT>(c, L, L.offD, ly);
+    MT a = den[K][j] * d[x];
+    if (x > 0)
+      a -= C.cw * d[x - 1];
+    if (x < L.nx - 1)
+      a -= C.ce * d[x + 1];
+    if (y > 0)
+      a -= C.cs * (kS || ly > 0 ? cRowNearT<true, MT>(c, L, L.offD, ly - 1)[x]
+                                : cRowNearT<false, MT>(c, L, L.offD, ly - 1)[x]);
+    if (y < L.ny - 1)
+      a -= C.cn * (kS || ly + 1 < L.rowsPer ? cRowNearT<true, MT>(c, L, L.offD, ly + 1)[x]
+                                            : cRowNearT<false, MT>(c, L, L.offD, ly + 1)[x]);
+    cRowNearT<true, MT>(c, L, L.offRes, ly)[x] = rr[K][j] - a;
+  }
+}
+
 template <bool kS, class MT>
 __device__ __forceinline__ void cSweepsHeld(const CCtx &c, const CLevel<MT> &L, int r0, int r1,
-                                            int sweeps, int first) {
+                                            int sweeps, int first, bool residual) {
   const int half = (L.nx + 1) / 2, cnt = half * (r1 - r0), stride = cStride(L);
   int pos[2][kSweepNodes], cl[2][kSweepNodes];
   MT rr[2][kSweepNodes], den[2][kSweepNodes];
@@ -541,12 +571,19 @@ __device__ __forceinline__ void cSweepsHeld(const CCtx &c, const CLevel<MT> &L, 
       cHalfSweep<kS, 0>(c, L, r0, pos, cl, rr, den);
     }
   }
+  if (residual) {
+    cResidualHeld<kS, 0>(c, L, r0, pos, cl, rr, den);
+    cResidualHeld<kS, 1>(c, L, r0, pos, cl, rr, den);
+    cSync(L);
+  }
 }
 
-// `sweeps` red-black sweeps over level L, colour `first` first; every CTA
-// passes the same 2 * sweeps barriers whichever form its rows take
+// `sweeps` red-black sweeps over level L, colour `first` first, then (residual)
+// the residual of the correction equation; every CTA passes the same
+// 2 * sweeps (+ 1) barriers whichever form its rows take
 template <class MT>
-__device__ void cSmoothSweeps(const CCtx &c, const CLevel<MT> &Lr, int sweeps, int first) {
+__device__ void cSmoothSweeps(const CCtx &c, const CLevel<MT> &Lr, int sweeps, int first,
+                              bool residual = false) {
   const CLevel<MT> L = Lr;
   if (cIdle(L))
     return;
@@ -555,15 +592,17 @@ __device__ void cSmoothSweeps(const CCtx &c, const CLevel<MT> &Lr, int sweeps, i
   const int cnt = (L.nx + 1) / 2 * (r1 - r0);
   if (cnt <= kSweepNodes * cStride(L) && L.nx <= 0xffff && r1 - r0 <= 0x7fff) {
     if (L.small)
-      cSweepsHeld<true>(c, L, r0, r1, sweeps, first);
+      cSweepsHeld<true>(c, L, r0, r1, sweeps, first, residual);
     else
-      cSweepsHeld<false>(c, L, r0, r1, sweeps, first);
+      cSweepsHeld<false>(c, L, r0, r1, sweeps, first, residual);
     return;
   }
   for (int s = 0; s < sweeps; s++) {
     cSmooth(c, L, first);
     cSmooth(c, L, 1 - first);
   }
+  if (residual)
+    cResidual(c, L);
 }
 
 // residual r - A d of the correction equation at this CTA's nodes of level F
@@ -856,6 +895,11 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     uint8_t *cl = reinterpret_cast<uint8_t *>(smem + L.offCls);
     for (int k = threadIdx.x; k < L.nx * (r1 - r0); k += blockDim.x)
       cl[k] = L.cls[(size_t)r0 * L.nx + k];
+    if (l + 1 < M.nLev) { // the residual of Dirichlet nodes stays 0
+      MT *res = reinterpret_cast<MT *>(smem + L.offRes);
+      for (int k = threadIdx.x; k < L.nx * (r1 - r0); k += blockDim.x)
+        res[k] = MT(0);
+    }
     if (L.ncx > 0) {
       stage(L.offPxI, L.pxIdx, L.nx);
       stage(L.offPxW, L.pxW, L.nx);
@@ -926,15 +970,13 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
       // one V-cycle: the distributed levels down ...
       const int Ls = M.firstSmall;
       for (int l = 0; l < Ls; l++) {
-        cSmoothSweeps(c, M.L[l], M.pre, 0);
-        cResidual(c, M.L[l]);
+        cSmoothSweeps(c, M.L[l], M.pre, 0, true);
         cRestrict(c, M.L[l], M.L[l + 1]);
       }
       // ... the levels held by CTA 0 ...
       if (rank == 0) {
         for (int l = Ls; l + 1 < M.nLev; l++) {
-          cSmoothSweeps(c, M.L[l], M.pre, 0);
-          cResidual(c, M.L[l]);
+          cSmoothSweeps(c, M.L[l], M.pre, 0, true);
           cRestrict(c, M.L[l], M.L[l + 1]);
         }
         cCoarse(c, M.L[M.nLev - 1], M.coarseSweeps);
