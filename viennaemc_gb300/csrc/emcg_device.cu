@@ -370,33 +370,71 @@ __global__ void gatherListKernel(const int32_t *__restrict__ list,
   }
 }
 
-// One warp per reservoir node walks the reservoir particles in index order:
-// the r-th particle at the node (r from 0) stays while r * carriers is below
-// the expected number there, the rest are marked for removal
-// (emcBasicParticleHandler::handleOhmicContacts, :158-192).
+// Ranking of the particles on reservoir nodes (emcBasicParticleHandler::
+// handleOhmicContacts, :158-192): the r-th particle at a node (r from 0, in
+// particle order) stays while r * carriers is below the expected number there,
+// the rest are marked for removal.  The gathered list (particle order) is cut
+// into kRankChunks chunks; a warp per (node, chunk) counts the node's entries
+// in its chunk (contactCountKernel), then ranks them from the counts of the
+// earlier chunks (contactRankKernel), so no warp walks the whole list.
+constexpr int kRankChunks = 16;
+
+__device__ __forceinline__ void rankChunk(int R, int c, int &j0, int &j1) {
+  const int len = (R + kRankChunks - 1) / kRankChunks;
+  j0 = min(R, c * len);
+  j1 = min(R, j0 + len);
+}
+
+__global__ void contactCountKernel(const int32_t *__restrict__ gNode,
+                                   const int64_t *__restrict__ total,
+                                   const int32_t *__restrict__ resNodes, int nRes,
+                                   int32_t *__restrict__ chunkCount) {
+  const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= nRes * kRankChunks)
+    return;
+  const int r = w / kRankChunks, c = w - r * kRankChunks;
+  const int g = resNodes[r];
+  int j0, j1;
+  rankChunk((int)*total, c, j0, j1);
+  int cnt = 0;
+  for (int base = j0; base < j1; base += 32) {
+    const int j = base + lane;
+    cnt += __popc(__ballot_sync(0xffffffffu, j < j1 && gNode[j] == g));
+  }
+  if (lane == 0)
+    chunkCount[w] = cnt;
+}
+
 __global__ void contactRankKernel(const int32_t *__restrict__ gList,
                                   const int32_t *__restrict__ gNode,
                                   const int64_t *__restrict__ total,
                                   const int32_t *__restrict__ resNodes, int nRes,
                                   const double *__restrict__ expNr, double nrC,
                                   const int32_t *__restrict__ nodeContact,
+                                  const int32_t *__restrict__ chunkCount,
                                   uint8_t *__restrict__ drop, int32_t *__restrict__ kept,
                                   int32_t *__restrict__ remInj) {
   const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
-  if (w >= nRes)
+  if (w >= nRes * kRankChunks)
     return;
-  const int g = resNodes[w];
+  const int r = w / kRankChunks, c = w - r * kRankChunks;
+  const int g = resNodes[r];
   const double e = expNr[g];
-  const int R = (int)*total;
-  int seen = 0, nKept = 0, nDrop = 0;
-  for (int base = 0; base < R; base += 32) {
+  int j0, j1;
+  rankChunk((int)*total, c, j0, j1);
+  int seen = 0; // the node's entries in the earlier chunks
+  for (int q = 0; q < c; q++)
+    seen += chunkCount[r * kRankChunks + q];
+  int nKept = 0, nDrop = 0;
+  for (int base = j0; base < j1; base += 32) {
     const int j = base + lane;
-    const bool mine = j < R && gNode[j] == g;
+    const bool mine = j < j1 && gNode[j] == g;
     const unsigned m = __ballot_sync(0xffffffffu, mine);
     if (mine) {
-      const int r = seen + __popc(m & ((1u << lane) - 1u));
-      if ((double)r * nrC < e)
+      const int rk = seen + __popc(m & ((1u << lane) - 1u));
+      if ((double)rk * nrC < e)
         nKept++;
       else {
         drop[gList[j]] = 1;
@@ -411,7 +449,8 @@ __global__ void contactRankKernel(const int32_t *__restrict__ gList,
     nDrop += __shfl_xor_sync(0xffffffffu, nDrop, o);
   }
   if (lane == 0) {
-    kept[g] = nKept;
+    if (nKept)
+      atomicAdd(&kept[g], nKept);
     if (nDrop)
       atomicAdd(&remInj[nodeContact[g]], -nDrop);
   }
@@ -686,6 +725,7 @@ struct DeviceImpl {
   int32_t *dBlock = nullptr;  // per compaction block counts / offsets
   int32_t *dList = nullptr, *dListNode = nullptr, *dListCount = nullptr;
   int32_t *dKept = nullptr;
+  int32_t *dChunkCount = nullptr; // [reservoir node][kRankChunks] (contact ranking)
   int32_t *dGList = nullptr, *dGNode = nullptr; // reservoir particles in index order
   int32_t *dResNodes = nullptr, *dInjCount = nullptr;
   int32_t *dNetto = nullptr, *dRemInj = nullptr;
@@ -782,7 +822,8 @@ int32_t destroyDevice(emcg_handle *h) {
   poissonFree(d->mg);
   void *ps[] = {d->dModel, d->dTables, d->dRegion, d->dNodeContact, d->dNodeRes, d->dNodeOhmic,
                 d->dPot, d->dNr, d->dConc, d->dExp, d->dEx, d->dEy, d->dN, d->dDrop, d->dBlock,
-                d->dList, d->dListNode, d->dListCount, d->dGList, d->dGNode, d->dKept, d->dResNodes,
+                d->dList, d->dListNode, d->dListCount, d->dGList, d->dGNode, d->dKept,
+                d->dChunkCount, d->dResNodes,
                 d->dInjCount, d->dNetto, d->dRemInj, d->dErr};
   freeRateScratch(d->rateScratch);
   for (void *p : ps)
@@ -996,6 +1037,8 @@ extern "C" int32_t emcg_device_create(const emcg_model_desc *model, const emcg_d
        cudaMalloc(&d->dGList, cap * sizeof(int32_t)) == cudaSuccess &&
        cudaMalloc(&d->dGNode, cap * sizeof(int32_t)) == cudaSuccess &&
        cudaMalloc(&d->dKept, n * sizeof(int32_t)) == cudaSuccess &&
+       cudaMalloc(&d->dChunkCount, (d->resNodesH.size() + 1) * kRankChunks * sizeof(int32_t)) ==
+           cudaSuccess &&
        cudaMalloc(&d->dInjCount, (d->resNodesH.size() + 1) * sizeof(int32_t)) == cudaSuccess &&
        cudaMalloc(&d->dNetto, (d->nContacts + 1) * sizeof(int32_t)) == cudaSuccess &&
        cudaMalloc(&d->dRemInj, (d->nContacts + 1) * sizeof(int32_t)) == cudaSuccess &&
@@ -1169,10 +1212,15 @@ template <class T> static int32_t contactsT(DeviceImpl *d, uint32_t step) {
   scanBlocksKernel<<<1, 1024, 0, st>>>(d->dListCount, nb, d->dN + 3);
   gatherListKernel<<<nb, 256, 0, st>>>(d->dList, d->dListNode, d->dListCount, nb, d->dN + 3,
                                        d->dGList, d->dGNode);
-  if (nRes > 0)
-    contactRankKernel<<<(nRes * 32 + 255) / 256, 256, 0, st>>>(
-        d->dGList, d->dGNode, d->dN + 3, d->dResNodes, nRes, d->dExp,
-        d->cfg.carriers_per_particle, d->dNodeContact, d->dDrop, d->dKept, d->dRemInj);
+  if (nRes > 0) {
+    const unsigned rb = (unsigned)(((int64_t)nRes * kRankChunks * 32 + 255) / 256);
+    contactCountKernel<<<rb, 256, 0, st>>>(d->dGNode, d->dN + 3, d->dResNodes, nRes,
+                                           d->dChunkCount);
+    contactRankKernel<<<rb, 256, 0, st>>>(d->dGList, d->dGNode, d->dN + 3, d->dResNodes, nRes,
+                                          d->dExp, d->cfg.carriers_per_particle,
+                                          d->dNodeContact, d->dChunkCount, d->dDrop, d->dKept,
+                                          d->dRemInj);
+  }
   EMCG_CUDA(cudaGetLastError());
   EMCG_TRY(compact(d));
   if (nRes == 0)
