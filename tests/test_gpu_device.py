@@ -199,6 +199,37 @@ def test_full_device_steps_run_and_conserve_count(engine):
         sim.close()
 
 
+def test_device_step_equals_its_stages(engine):
+    """performEMCStep (one compaction per step, the Poisson solve enqueued)
+    gives what its stages called one by one give: Poisson, E field, move
+    (compacting), contacts (compacting), assignment -- same potential, same
+    particles bit for bit, same contact counts, FP64 and FP32."""
+    g = golden(DEVICE_CASES[0])
+    K = 6
+    for precision in ("fp64", "fp32"):
+        a, _, _ = _sim(engine, g, DEVICE_CASES[0], precision=precision, seed=3)
+        b, _, _ = _sim(engine, g, DEVICE_CASES[0], precision=precision, seed=3)
+        a.calcEquilibriumCharacteristics()
+        b.calcEquilibriumCharacteristics()
+        s0 = b.step_index
+        net_a = a.performEMCStep(K)
+        rows = []
+        for s in range(K):
+            b.poisson(equilibrium=False, reset_bc=(s == 0))
+            b.efield()
+            n = b.move(step=s0 + s)
+            ri = b.contacts(step=s0 + s)
+            b.assign()
+            rows.append(n - ri)
+        assert np.array_equal(net_a, np.array(rows)), precision
+        assert np.array_equal(a.potential, b.potential), precision
+        sa, sb = a.get_state(), b.get_state()
+        for f in ("kx", "ky", "kz", "energy", "px", "py", "tau", "valley", "sub", "region"):
+            assert np.array_equal(getattr(sa, f), getattr(sb, f)), (precision, f)
+        a.close()
+        b.close()
+
+
 def _resistor_201x101(scale=1):
     from viennaemc_gb300 import device as D
     from viennaemc_gb300.physics import silicon_material

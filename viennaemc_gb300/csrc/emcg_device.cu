@@ -332,12 +332,13 @@ __global__ void compactScatterKernel(StateK<T> src, StateK<T> dst, const uint8_t
 // list of the particles sitting at reservoir nodes, in index order
 template <class T>
 __global__ void reservoirListKernel(StateK<T> st, DevK G, const int64_t *__restrict__ nPtr,
+                                    const uint8_t *__restrict__ skip,
                                     int32_t *__restrict__ list, int32_t *__restrict__ listNode,
                                     int32_t *__restrict__ listCount) {
   const int64_t n = *nPtr;
   const int64_t i = (int64_t)blockIdx.x * kCB + threadIdx.x;
   int node = -1;
-  if (i < n) {
+  if (i < n && !(skip && skip[i])) { // skip: removed by the move, not yet compacted
     int cx = clampi(roundIdx<T>(st.px[i], G.hx, G.invhx), 0, G.nx - 1);
     int cy = clampi(roundIdx<T>(st.py[i], G.hy, G.invhy), 0, G.ny - 1);
     int g = cy * G.nx + cx;
@@ -1156,7 +1157,9 @@ static int32_t compact(DeviceImpl *d) {
   return EMCG_OK;
 }
 
-template <class T> static int32_t moveT(DeviceImpl *d, uint32_t step) {
+// compactAfter = false: the removed particles stay marked in dDrop for the
+// contact handling's single compaction (device step)
+template <class T> static int32_t moveT(DeviceImpl *d, uint32_t step, bool compactAfter = true) {
   const int nb = (int)((d->capacity + 255) / 256);
   const emcg_device_config &c = d->cfg;
   uint32_t k0 = (uint32_t)c.seed, k1 = (uint32_t)(c.seed >> 32);
@@ -1196,18 +1199,23 @@ template <class T> static int32_t moveT(DeviceImpl *d, uint32_t step) {
 #undef EMCG_MOVE
   EMCG_CUDA(cudaGetLastError());
   d->replay[0] = false;
-  return compact(d);
+  return compactAfter ? compact(d) : EMCG_OK;
 }
 
-template <class T> static int32_t contactsT(DeviceImpl *d, uint32_t step) {
+// movedDrops: the move's removals are still marked in dDrop (moveT without its
+// compaction); the reservoir list skips them and one compaction removes both.
+// The ranks are those of the compacted order, since compaction is stable.
+template <class T> static int32_t contactsT(DeviceImpl *d, uint32_t step, bool movedDrops = false) {
   const int nb = d->nBlocks();
   const int n = d->nx * d->ny;
   cudaStream_t st = d->stream;
   DevK G = devK(d);
   const int nRes = (int)d->resNodesH.size();
-  EMCG_CUDA(cudaMemsetAsync(d->dDrop, 0, d->capacity, st));
+  if (!movedDrops)
+    EMCG_CUDA(cudaMemsetAsync(d->dDrop, 0, d->capacity, st));
   EMCG_CUDA(cudaMemsetAsync(d->dKept, 0, n * sizeof(int32_t), st));
-  reservoirListKernel<T><<<nb, kCB, 0, st>>>(devState<T>(d, d->cur), G, d->dN, d->dList,
+  reservoirListKernel<T><<<nb, kCB, 0, st>>>(devState<T>(d, d->cur), G, d->dN,
+                                             movedDrops ? d->dDrop : nullptr, d->dList,
                                              d->dListNode, d->dListCount);
   scanBlocksKernel<<<1, 1024, 0, st>>>(d->dListCount, nb, d->dN + 3);
   gatherListKernel<<<nb, 256, 0, st>>>(d->dList, d->dListNode, d->dListCount, nb, d->dN + 3,
@@ -1413,9 +1421,11 @@ extern "C" int32_t emcg_device_step(emcg_handle *h, int32_t n_steps, uint32_t st
     EMCG_TRY(d->precision == EMCG_FP64 ? efieldT<double>(d) : efieldT<float>(d));
     EMCG_CUDA(cudaMemsetAsync(d->dNetto, 0, (nc + 1) * sizeof(int32_t), d->stream));
     EMCG_CUDA(cudaMemsetAsync(d->dRemInj, 0, (nc + 1) * sizeof(int32_t), d->stream));
-    EMCG_TRY(d->precision == EMCG_FP64 ? moveT<double>(d, step0 + s) : moveT<float>(d, step0 + s));
-    EMCG_TRY(d->precision == EMCG_FP64 ? contactsT<double>(d, step0 + s)
-                                       : contactsT<float>(d, step0 + s));
+    // one compaction per step, after the contacts (the move's removals wait marked)
+    EMCG_TRY(d->precision == EMCG_FP64 ? moveT<double>(d, step0 + s, false)
+                                       : moveT<float>(d, step0 + s, false));
+    EMCG_TRY(d->precision == EMCG_FP64 ? contactsT<double>(d, step0 + s, true)
+                                       : contactsT<float>(d, step0 + s, true));
     EMCG_TRY(d->precision == EMCG_FP64 ? assignT<double>(d) : assignT<float>(d));
     EMCG_CUDA(cudaEventRecord(d->ev[1], d->stream));
     if (netto) {
