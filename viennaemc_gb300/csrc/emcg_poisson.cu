@@ -272,8 +272,13 @@ template <> LevelK<double> levelK<double>(const MGLevel &l) {
 //    the level's distinct coefficient tuples; they and the transfer tables are
 //    staged once per launch;
 //  - levels with at most kSmallNodes nodes live whole in CTA 0, which runs the
-//    coarse part of every V-cycle alone with block barriers, the coarsest grid
-//    in the registers of one warp;
+//    coarse part of every V-cycle alone with block barriers (warp barriers on
+//    levels of at most kWarpNodes, which warp 0 works alone), the coarsest
+//    grid in the registers of one warp;
+//  - rows in a CTA's own shared memory are addressed from the kernel's
+//    shared-memory base, so their loads and stores are shared-memory
+//    instructions rather than generic ones; the sweeps keep each thread's nodes
+//    in registers (cSweepsHeld);
 //  - phases over distributed levels are separated by cluster barriers
 //    (release / acquire).
 // Every phase evaluates the expressions of the corresponding multi-launch
@@ -469,8 +474,10 @@ template <class MT> __device__ void cSmooth(const CCtx &c, const CLevel<MT> &Lr,
 // registers: a thread keeps the same nodes over the sweeps, so their position,
 // class, right-hand side and diagonal are read once, and a half sweep reads
 // only the neighbours' corrections.  The arithmetic is cSmoothT's.
-// nodes of one colour per thread.  Six, for the 2,814-node bands of a 401 x 201
-// grid, spilled registers: 0.5 % faster there, 1.4 % slower on 201 x 101.
+//
+// kSweepNodes: nodes of one colour per thread.  Six, for the 2,814-node bands
+// of a 401 x 201 grid, spilled registers: 0.5 % faster there, 1.4 % slower on
+// 201 x 101.
 constexpr int kSweepNodes = 3;
 template <bool kS, int K, class MT>
 __device__ __forceinline__ void cHalfSweep(const CCtx &c, const CLevel<MT> &L, int r0,
