@@ -421,15 +421,15 @@ __device__ __forceinline__ int scatterParticle(const ModelK<T> &M, T k[3],
   const T *row = M.tables + M.tsOff[ts] + (int64_t)L * nT;
   if (rnd > ldg(row + nT - 1))
     return 0; // self-scattering
-  T lo = T(0);
-  for (int t = 0; t < nT; t++) {
-    T hi = ldg(row + t);
-    if (rnd >= lo && rnd < hi) {
-      applyMechanism(M, M.m[M.tsMech[ts][t]], k, E, valley, sub, region, rng);
-      break;
-    }
-    lo = hi;
-  }
+  // the first t with row[t-1] <= rnd < row[t] (row[-1] = 0): the row is
+  // cumulative, so nondecreasing, and t is the number of entries <= rnd.  The
+  // loads are independent, so the search costs one load latency, not nT.
+  int t = 0;
+#pragma unroll 4
+  for (int q = 0; q < nT; q++)
+    t += ldg(row + q) <= rnd ? 1 : 0;
+  if (t < nT) // t = nT: rnd equals the last entry, no mechanism (as the loop above)
+    applyMechanism(M, M.m[M.tsMech[ts][t]], k, E, valley, sub, region, rng);
   return 0;
 }
 
