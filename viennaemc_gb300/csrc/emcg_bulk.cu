@@ -634,10 +634,15 @@ __global__ void bulkInitKernel(StateK<T> st, const ModelK<T> *__restrict__ model
 // small per-warp window; once every lane of the warp has passed a step, the
 // warp folds that row into the block's float step sums (shared memory), which
 // go to the device's double sums at the end of the launch.  A lane runs at
-// most kAsyncWindow steps ahead of the slowest lane of its warp.  The three
+// most a window's length of steps ahead of the slowest lane of its warp.  The
 // constants below were chosen by measurement on 2^20 and 2^22 electrons.
 // ---------------------------------------------------------------------------
+// window length with several valleys (the window also keeps each step's
+// valley), and with one valley: 24 steps of E and v.dir per lane still let 4
+// blocks of 256 threads share an SM at 500 steps per launch (+2.2 % on 2^20
+// electrons, +1.4 % on the sweep against 20)
 constexpr int kAsyncWindow = 20;
+constexpr int kAsyncWindowOne = 24;
 // lanes of a warp that wait at an event before the warp scatters them together
 // (with five free flights per pass, 7 ran 0.9 % faster than 8 on 2^20
 // electrons and the same on the 64-ensemble sweep)
@@ -653,13 +658,18 @@ constexpr float kFixE = 1048576.f;
 constexpr float kFixD = 4.f;
 constexpr float kFixMax = 67108864.f;
 
+// the windows of a block: Q = 3 (one valley) holds E and v.dir per slot,
+// more valleys also the slot's valley
+__host__ __device__ constexpr size_t asyncWindowBytes(int nWarps, int Q) {
+  return Q == 3 ? (size_t)nWarps * kAsyncWindowOne * 32 * (2 * sizeof(float))
+                : (size_t)nWarps * kAsyncWindow * 32 * (2 * sizeof(float) + 1);
+}
 __host__ __device__ constexpr size_t asyncSmemBytes(int nWarps, int nSteps, int Q) {
-  return (size_t)nSteps * Q * sizeof(float) +
-         (size_t)nWarps * kAsyncWindow * 32 * (2 * sizeof(float) + 1);
+  return (size_t)nSteps * Q * sizeof(float) + asyncWindowBytes(nWarps, Q);
 }
 // steps per launch whose block sums fit beside the windows in 64 KB
 inline int asyncMaxSteps(int nWarps, int Q) {
-  const long rest = 65536 - (long)nWarps * kAsyncWindow * 32 * (2 * (long)sizeof(float) + 1);
+  const long rest = 65536 - (long)asyncWindowBytes(nWarps, Q);
   return (int)std::max(1L, rest / (long)(Q * sizeof(float)));
 }
 
@@ -724,11 +734,12 @@ __global__ void __launch_bounds__(256, MINB)
   const int Q = nVmax * 3;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nWarps = blockDim.x >> 5;
   float *bins = reinterpret_cast<float *>(smemRaw); // [nSteps][Q] block sums
-  float *winE = bins + (size_t)nSteps * Q + (size_t)warp * kAsyncWindow * 64; // [W][32]
-  float *winD = winE + kAsyncWindow * 32;                                    // [W][32]
+  constexpr int W = kOne ? kAsyncWindowOne : kAsyncWindow;
+  float *winE = bins + (size_t)nSteps * Q + (size_t)warp * W * 64; // [W][32]
+  float *winD = winE + W * 32;                                    // [W][32]
   uint8_t *winVal = reinterpret_cast<uint8_t *>(bins + (size_t)nSteps * Q +
-                                                (size_t)nWarps * kAsyncWindow * 64) +
-                    warp * kAsyncWindow * 32; // [W][32]
+                                                (size_t)nWarps * W * 64) +
+                    warp * W * 32; // [W][32], several valleys only
   for (int i = threadIdx.x; i < nSteps * Q; i += blockDim.x)
     bins[i] = 0.f;
   __syncthreads();
@@ -767,12 +778,12 @@ __global__ void __launch_bounds__(256, MINB)
   rng.init(pid, step0, EK.stream, EK.key0, EK.key1);
   int flushed = 0;  // steps folded into the block sums
   float accE = 0.f, accD = 0.f, accC = 0.f; // one valley: sums of a step of the 32-step group
-  int ws = 0;        // window slot of step s (s mod kAsyncWindow)
+  int ws = 0;        // window slot of step s (s mod W)
   bool pend = false; // drifted to an event inside step s, not yet scattered
   while (true) {
     const int sMin = __reduce_min_sync(0xffffffffu, s);
     for (; flushed < sMin; flushed++) {
-      const int slot = (flushed % kAsyncWindow) * 32 + lane;
+      const int slot = (flushed % W) * 32 + lane;
       for (int v = 0; v < nV; v++) {
         const bool in = live && (nV == 1 || winVal[slot] == v);
         const T ev = in ? winE[slot] : T(0), dv = in ? winD[slot] : T(0);
@@ -814,7 +825,7 @@ __global__ void __launch_bounds__(256, MINB)
     }
     if (sMin >= nSteps)
       break;
-    const int limit = min(nSteps, flushed + kAsyncWindow);
+    const int limit = min(nSteps, flushed + W);
     // a lane whose free flight ended at an event waits (pend) until enough
     // lanes of its warp wait too, or no lane can go on: then they scatter
     // together, so the scatter path runs for several lanes at once
@@ -876,7 +887,7 @@ __global__ void __launch_bounds__(256, MINB)
             s++;
             tIn = T(0);
             nEv = 0;
-            ws = ws + 1 == kAsyncWindow ? 0 : ws + 1;
+            ws = ws + 1 == W ? 0 : ws + 1;
             rng.restart(step0 + (uint32_t)s);
           }
         }
