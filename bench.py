@@ -124,7 +124,7 @@ def run_engine(args):
     spec = EnsembleSpec(0, N, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 1234 + rank, 0, 300.0)
     b = BulkBatch([pt], [spec], "fp32")
     b.set_launch(args.block, per, args.min_blocks,
-                 queued=args.scatter_mode)
+                 queued=args.scatter_mode, pass_actions=args.pass_actions)
     b.init_particles(0)
     # warm-up (untimed)
     b.step(W)
@@ -181,7 +181,8 @@ def _e2e(v, pt, spec, args, N, K):
     from viennaemc_gb300.bulk import BulkBatch
     st = _host_state(v, N)
     b2 = BulkBatch([pt], [spec], "fp32")
-    b2.set_launch(args.block, args.steps_per_launch, args.min_blocks)
+    b2.set_launch(args.block, args.steps_per_launch, args.min_blocks,
+                  pass_actions=args.pass_actions)
     # warm-up through the same calls (untimed): first-call staging allocation
     b2.set_state(0, st)
     b2.step(max(args.warmup, 3))
@@ -715,6 +716,9 @@ def build_parser():
     ap.add_argument("--steps-per-launch", type=int, default=500)
     ap.add_argument("--block", type=int, default=256)
     ap.add_argument("--min-blocks", type=int, default=4, help="register cap variant (1, 3, 4)")
+    ap.add_argument("--pass-actions", type=int, default=None,
+                    help="free flights per drift pass of the warp-asynchronous kernel "
+                         "(default: the library's)")
     ap.add_argument("--scatter-mode", type=int, default=2, choices=(0, 1, 2),
                     help="step kernel: 0 lockstep, 1 block-queued, 2 warp-asynchronous")
     ap.add_argument("--batch-steps", type=int, default=4000,

@@ -240,7 +240,7 @@ int32_t emcg_set_launch(emcg_handle *h, int32_t block_threads,
 int32_t emcg_set_scatter_mode(emcg_handle *h, int32_t queued);
 /* Tuning of the warp-asynchronous kernel: free flights a lane may take in one
    drift pass before the warp checks its waiting lanes again, in [1, 20]
-   (default 5).  Only the schedule changes: particle states are the same bit
+   (default 6).  Only the schedule changes: particle states are the same bit
    for bit.  No reference counterpart. */
 int32_t emcg_set_pass_actions(emcg_handle *h, int32_t n);
 int32_t emcg_get_pass_actions(emcg_handle *h, int32_t *n);
@@ -256,7 +256,7 @@ int32_t emcg_bulk_set_graph(emcg_handle *h, int32_t enable);
 /* Autotuner: runs trial_steps steps (from step0, advancing the ensembles --
    use it as warm-up) with each candidate launch shape (block threads 128 /
    256, register cap 1 / 3 / 4 resident blocks per SM, lockstep,
-   block-queued or, for float, warp-asynchronous scatter with 3 or 5 free
+   block-queued or, for float, warp-asynchronous scatter with 3 or 6 free
    flights per pass), twice: in a forward and then a backward pass over the
    shapes.  It keeps the shape of least total device time (its pass actions:
    emcg_get_pass_actions).  *steps_used = steps run (2 x shapes x

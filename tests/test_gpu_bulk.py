@@ -399,7 +399,7 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(engine):
     cfg = b.autotune(10)
     assert cfg["steps_used"] == 260  # 13 float shapes x 10 steps, forward and backward
     assert cfg["block_threads"] in (128, 256) and cfg["min_blocks"] in (1, 3, 4)
-    assert cfg["queued"] in (0, 1, 2) and cfg["pass_actions"] in (3, 5)
+    assert cfg["queued"] in (0, 1, 2) and cfg["pass_actions"] in (3, 6)
     o = b.step(20)
     b.close()
     b2 = _sweep_batch(engine)
@@ -530,11 +530,11 @@ def test_two_valley_kernels_equal_lockstep(engine, mode):
 
 
 def test_pass_actions_change_only_the_schedule(engine):
-    """Free flights per drift pass of the warp-asynchronous kernel (1, the
-    default 5, 20): the same particle states bit for bit, the same counts, and
+    """Free flights per drift pass of the warp-asynchronous kernel (1, 5, the
+    default 6, 20): the same particle states bit for bit, the same counts, and
     step sums equal to float rounding; out-of-range settings are refused."""
     outs = []
-    for n in (1, 5, 20):
+    for n in (1, 5, 6, 20):
         b = _sweep_batch(engine)
         b.set_launch(256, 40, 4, queued=2, pass_actions=n)
         assert b.pass_actions() == n

@@ -648,10 +648,12 @@ constexpr int kAsyncWindowOne = 24;
 // electrons and the same on the 64-ensemble sweep)
 constexpr int kEventBatch = 7;
 // free flights a lane may take in one drift pass, by default (set per handle:
-// emcg_set_pass_actions).  Measured on 2^20 electrons, 2000 steps: 3 gave
-// 8.90e10, 4 9.00e10, 5 9.06e10, 6 9.02e10, 8 8.70e10, 20 6.79e10; on the
-// 64-ensemble sweep 5 was 3.6 % slower than 3, so the autotuner tries both.
-constexpr int kPassActions = 5;
+// emcg_set_pass_actions).  Measured on 2^20 electrons, 2000 steps, 20-step
+// window: 3 gave 8.90e10, 4 9.00e10, 5 9.06e10, 6 9.02e10, 8 8.70e10, 20
+// 6.79e10; with the 24-step one-valley window 4 gave 9.11e10, 5 9.30e10, 6
+// 9.34e10, 7 9.28e10.  On the 64-ensemble sweep 5 was 3.6 % slower than 3, so
+// the autotuner tries 3 and 6.
+constexpr int kPassActions = 6;
 // fixed-point scales of a warp's step sums: energy 2^-20 eV, velocity
 // 0.25 m/s per unit; below kFixMax per lane, 32 lanes stay within int32
 constexpr float kFixE = 1048576.f;
@@ -2025,14 +2027,14 @@ extern "C" int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint3
   // that the ensembles' warming up from the initial distribution (events get
   // more frequent) weighs on every shape alike; the least total device time
   // wins
-  // (the warp-asynchronous kernel with 3 and with 5 free flights per pass)
+  // (the warp-asynchronous kernel with 3 and with 6 free flights per pass)
   struct Cand {
     int block, minb, queued, pass;
   };
   const Cand cands[] = {{256, 4, 0, 0}, {256, 3, 0, 0}, {256, 1, 0, 0}, {128, 4, 0, 0},
                         {128, 1, 0, 0}, {256, 4, 1, 0}, {256, 3, 1, 0}, {128, 4, 1, 0},
-                        {256, 4, 2, 3}, {256, 3, 2, 3}, {128, 4, 2, 3}, {256, 4, 2, 5},
-                        {128, 4, 2, 5}};
+                        {256, 4, 2, 3}, {256, 3, 2, 3}, {128, 4, 2, 3}, {256, 4, 2, 6},
+                        {128, 4, 2, 6}};
   constexpr int kCands = sizeof(cands) / sizeof(cands[0]);
   const int nCands = b->precision == EMCG_FP32 ? kCands : 8; // mode 2 is float only
   const int keepPer = b->stepsPerLaunch, keepPass = b->passActions;
