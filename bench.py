@@ -125,6 +125,7 @@ def run_engine(args):
     b = BulkBatch([pt], [spec], "fp32")
     b.set_launch(args.block, per, args.min_blocks,
                  queued=args.scatter_mode, pass_actions=args.pass_actions)
+    args.pass_actions_used = b.pass_actions()
     b.init_particles(0)
     # warm-up (untimed)
     b.step(W)
@@ -236,6 +237,7 @@ def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units,
                    "particles": N, "steps_per_launch": per, "block_threads": args.block,
                    "min_blocks_per_sm": args.min_blocks,
                    "scatter_kernel": kernel,
+                   "pass_actions": getattr(args, "pass_actions_used", None),
                    "l2": "flushed (256 MB write) between timed launches",
                    "observables": "per-step FP64 sums of E, v.dir, count"},
         "e2e": {"value": e2e_units / e2e_s if e2e_units else None, "unit": UNIT,
