@@ -146,7 +146,11 @@ __global__ void __launch_bounds__(kP2PThreads)
             self[u] = central && i >= t0 && i < t0 + cnt ? (int)(i - t0) : -1;
           }
           T acc[kP2PTargets][4] = {};
-          if (self[0] < 0 && self[1] < 0) {
+          bool anySelf = false;
+#pragma unroll
+          for (int u = 0; u < kP2PTargets; u++)
+            anySelf |= self[u] >= 0;
+          if (!anySelf) {
 #pragma unroll 4
             for (int k = 0; k < cnt; k++) {
               const Src4<T> s = tile[k];
