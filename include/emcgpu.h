@@ -9,8 +9,9 @@
  *
  * The reference interface each entry point replaces is cited beside it
  * (paths relative to the ViennaEMC project root).  A maintainer binds this
- * header from the reference's C++ through the adapter shown in
- * INTEGRATION.md; the Python package viennaemc_gb300 binds it with ctypes.
+ * header from the reference's C++ through the adapter classes of
+ * include/emcgpu_reference.hpp; the Python package viennaemc_gb300 binds it
+ * with ctypes.
  *
  * Units are SI throughout (m, s, J, kg, V/m) except energies in eV, exactly
  * as in the reference.  Particle state crosses the boundary as
@@ -474,20 +475,31 @@ int32_t emcg_device_poisson_counts(emcg_handle *h, int64_t *cycles, int64_t *sol
    Works on caller-owned device arrays of nx * ny doubles: d_pot (in/out) is
    the potential in thermal voltages and d_conc the electron concentration
    normalised to ni (the units of EMCG_GRID_POTENTIAL / EMCG_GRID_CONC), or
-   NULL for the equilibrium equation.  reset_bc, the smoothing sweeps (0 = 2),
+   NULL for the equilibrium equation.  reset_bc, the smoothing sweeps (0 = 3),
    rtol and max_cycles mean what they mean for emcg_device_create's
    configuration and emcg_device_poisson.  cuda_stream may be NULL (default
    stream); the call returns after the solve has finished on that stream.
-   Working memory is one fixed device array of about 21 MB in this library,
-   reserved when its device code is loaded: grids of up to 131072 nodes and
-   8192 nodes per dimension, at most 64 contacts (ohmic or gate); larger
-   inputs return EMCG_ERR_ARG and touch nothing.  Every call rebuilds the
-   array's contents, including the statistics that must start at zero.
-   The first call on each device looks the array's address up
-   (cudaGetSymbolAddress, with that device current); make it before any
-   stream capture begins on that device.  All calls share the array: calls whose work can overlap on a device, from
+   Working memory is one fixed device array of about 21 MB in this library:
+   grids of up to 131072 nodes and 8192 nodes per dimension, at most 64
+   contacts (ohmic or gate); larger inputs return EMCG_ERR_ARG and touch
+   nothing.  Every call rebuilds the array's contents, including the
+   statistics that must start at zero.
+   The array belongs to this library's device code, which CUDA loads onto a
+   device lazily by default: at the library's first kernel launch there or
+   at the first call of this function, whichever comes first
+   (CUDA_MODULE_LOADING=EAGER loads it when the context is created).  A
+   caller whose memory pool will claim the rest of the GPU should therefore
+   make one call at start-up, before the pool takes the device.
+   The first call on each device also looks the array's address up
+   (cudaGetSymbolAddress, with that device current) and keeps it for the
+   life of the process; make it before any stream capture begins on that
+   device.  The kept address is not valid after cudaDeviceReset on that
+   device: do not call this function again after such a reset.
+   All calls share the array: calls whose work can overlap on a device, from
    several host threads or on several streams, race and corrupt each other's
-   results; serialise them. */
+   results; serialise them.
+   A potential, concentration or correction that is not finite (NaN or Inf)
+   at some node ends the solve with EMCG_ERR_NONCONVERGED. */
 int32_t emcg_poisson_solve_noalloc(const emcg_device_desc *dev, double *d_pot,
                                    const double *d_conc, int32_t reset_bc, int32_t smooth,
                                    double rtol, int32_t max_cycles, void *cuda_stream,

@@ -84,3 +84,20 @@ def test_noalloc_rejects_oversize_grid(engine):
     assert s == -1  # EMCG_ERR_ARG
     assert "no-allocation" in L.lib().emcg_last_error().decode()
     assert np.array_equal(out, pot)
+
+
+def test_noalloc_reports_non_finite_concentration(engine):
+    """A NaN in the caller's concentration ends the solve as not converged
+    (the residual maxima would otherwise drop it)."""
+    from viennaemc_gb300 import _lib as L
+    g = golden(DEVICE_CASES[0])
+    sim, dev, pt = _sim(engine, g, DEVICE_CASES[0])
+    desc = dev.desc()
+    conc = np.array(g["conc0"], np.float64)
+    conc[len(conc) // 2] = np.nan
+    s, _, _, _ = _noalloc(desc, g["pot_eq"], conc)
+    assert s == -4 and "non-finite" in L.lib().emcg_last_error().decode()
+    s, _, rel, _ = _noalloc(desc, g["pot_eq"], g["conc0"])
+    L.check(s)
+    assert rel <= RTOL
+    sim.close()

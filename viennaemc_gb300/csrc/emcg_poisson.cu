@@ -92,6 +92,11 @@ __global__ void nonlinResidualKernel(const double *__restrict__ pot, const doubl
       aF = fabs(F);
       if (withScale)
         sc = hP * (fabs(C[i]) + n + p);
+      // a NaN would vanish in the maxima (fmax drops it): a non-finite
+      // residual or scale term counts as an infinite residual, which ends
+      // the solve as not converged
+      if (!isfinite(F) || !isfinite(sc))
+        aF = INFINITY;
     }
   }
   double m1 = blockMax(aF);
@@ -111,9 +116,13 @@ __global__ void updatePotKernel(double *__restrict__ pot, const MT *__restrict__
   double a = 0.;
   if (i < n && !fixed[i]) {
     double v = (double)d[i];
-    v = fmin(kMaxNewtonStep, fmax(-kMaxNewtonStep, v));
+    // the clamp would turn a NaN correction into -kMaxNewtonStep (fmax drops
+    // NaN): a non-finite correction is passed on, so that the next residual
+    // reports it
+    if (isfinite(v))
+      v = fmin(kMaxNewtonStep, fmax(-kMaxNewtonStep, v));
     pot[i] += v;
-    a = fabs(v);
+    a = isfinite(v) ? fabs(v) : INFINITY;
   }
   double m = blockMax(a);
   if (threadIdx.x == 0)
@@ -962,6 +971,10 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
       aF = fmax(aF, fabs(F));
       if (it == 0)
         sc = fmax(sc, hP * (fabs(C[i]) + n + p));
+      // a NaN would vanish in the maxima: non-finite values count as an
+      // infinite residual, which ends the solve as not converged
+      if (!isfinite(F) || !isfinite(p) || !isfinite(n))
+        aF = INFINITY;
     }
     // its cluster barrier also orders the writes above; the maxima are next
     // written after the V-cycle's barriers, when every CTA has read them
@@ -969,7 +982,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     if (it == 0)
       scale = sc;
     rel = scale > 0 ? aF / scale : aF;
-    if (rel <= rtol || it == maxCycles)
+    if (rel <= rtol || it == maxCycles || !isfinite(rel))
       break;
     // under the update-size rule a Newton step needs only a rough correction
     const int nv = updTol <= 0. && rel < M.twoCycleRel ? M.vcycles : 1;
@@ -1009,10 +1022,11 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
       const int ly = L0.byNx.div(t), x = t - ly * nx;
       if (cCoef(c, L0, cRowNearT<true, uint8_t>(c, L0, L0.offCls, ly)[x]).fixed != MT(0))
         continue;
-      const double v = fmin(kMaxNewtonStep,
-                            fmax(-kMaxNewtonStep, (double)cRowNearT<true, MT>(c, L0, L0.offD, ly)[x]));
+      double v = (double)cRowNearT<true, MT>(c, L0, L0.offD, ly)[x];
+      if (isfinite(v)) // a non-finite correction is passed on to the next residual
+        v = fmin(kMaxNewtonStep, fmax(-kMaxNewtonStep, v));
       pot[(size_t)(p0 + ly) * nx + x] += v;
-      upd = fmax(upd, fabs(v));
+      upd = isfinite(v) ? fmax(upd, fabs(v)) : INFINITY;
     }
     if (updTol > 0.) {
       // the maxima of this rule use their own slot (offRed + 16)
@@ -1478,6 +1492,11 @@ static int32_t solveOutcome(double rel, int it, bool updStop, double rtol, doubl
     *relRes = rel;
   if (cycles)
     *cycles = it;
+  if (!std::isfinite(rel)) {
+    setError("Poisson: non-finite residual after %d Newton steps (NaN or Inf in the potential, "
+             "the concentration or a correction)", it);
+    return EMCG_ERR_NONCONVERGED;
+  }
   if (!updStop && !(rel <= rtol)) {
     setError("Poisson: relative residual %.3e after %d Newton steps (target %.1e)", rel, it, rtol);
     return EMCG_ERR_NONCONVERGED;
@@ -1521,7 +1540,7 @@ static int32_t solveT(PoissonMG &P, double *pot, const double *conc, bool resetB
     if (it == 0)
       scale = stats[1];
     rel = scale > 0 ? stats[0] / scale : stats[0];
-    if (rel <= rtol || it == maxCycles)
+    if (rel <= rtol || it == maxCycles || !std::isfinite(rel))
       break;
     // under the update-size rule a Newton step needs only a rough correction
     const int nv = P.updTol <= 0. && rel < P.twoCycleRel ? P.vcyclesPerNewton : 1;
@@ -2030,7 +2049,7 @@ extern "C" int32_t emcg_poisson_solve_noalloc(const emcg_device_desc *dv, double
     if (it == 0)
       scale = h_stats[1];
     rel = scale > 0 ? h_stats[0] / scale : h_stats[0];
-    if (rel <= rtol || it == max_cycles)
+    if (rel <= rtol || it == max_cycles || !std::isfinite(rel))
       break;
     const int nv = rel < kNATwoCycleRel ? kNAVcyclesPerNewton : 1;
     for (int k = 0; k < nv; k++)
@@ -2042,6 +2061,11 @@ extern "C" int32_t emcg_poisson_solve_noalloc(const emcg_device_desc *dv, double
     *rel_residual = rel;
   if (cycles)
     *cycles = it;
+  if (!std::isfinite(rel)) {
+    setError("Poisson: non-finite residual after %d Newton steps (NaN or Inf in the potential, "
+             "the concentration or a correction)", it);
+    return EMCG_ERR_NONCONVERGED;
+  }
   if (!(rel <= rtol)) {
     setError("Poisson: relative residual %.3e after %d Newton steps (target %.1e)", rel, it, rtol);
     return EMCG_ERR_NONCONVERGED;
