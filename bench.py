@@ -152,8 +152,6 @@ def run_engine(args):
     clocks = sampler.stop()
     ms, units = reduce_over_ranks(kernel_ms, float(N) * K, ws)
     value = units / (ms / 1e3)
-    obs = np.concatenate(obs_all, axis=1)
-    avg = BulkBatch.averages(obs, [N])
     b.close()
 
     if args.skip_e2e:
@@ -161,17 +159,17 @@ def run_engine(args):
     else:
         e2e_s, e2e_units, h2d, d2h = _e2e(v, pt, spec, args, N, K)
     if args.fp64_steps > 0:
-        value64, vd32, vd64, win, k64 = _fp64(v, pt, args, N, K, W, per, rank, avg)
+        value64, precision, k64 = _precision(v, pt, args, N, per, rank)
     else:
-        value64 = vd32 = vd64 = k64 = None
-        win = slice(0, 0)
+        value64 = precision = k64 = None
+    small = _small_bench(args, rank) if args.small_steps > 0 else None
     batched = _batched_bench(args, rank) if args.batch_steps > 0 else None
     device = _device_bench(args, rank) if args.device_steps > 0 else None
     if device is not None and args.mosfet_steps > 0:
         device["mosfet_sweep"] = _mosfet_bench(args, rank)
     p2p = _p2p_bench(args, rank) if args.p2p_n > 0 else None
     _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units, h2d, d2h,
-            value64, vd32, vd64, win, k64, wall, clocks, device, batched, p2p)
+            value64, precision, k64, wall, clocks, device, batched, p2p, small)
     if ws > 1:
         torch.distributed.destroy_process_group()
 
@@ -194,36 +192,118 @@ def _e2e(v, pt, spec, args, N, K):
     e2e_s = time.perf_counter() - t0
     b2.close()
     e2e_units = float(N) * K
-    h2d = N * (9 * 4 + 4) / K
+    h2d = N * (9 * 8 + 3 * 4) / K
     d2h = o2.shape[-2] * 3 * 8
     return e2e_s, e2e_units, h2d, d2h
 
 
-def _fp64(v, pt, args, N, K, W, per, rank, avg):
-    """Plain FP64 engine on the same configuration, and the FP32 v_d error."""
+def _run_steps(b, k, per):
+    """k steps in launches of at most per; (per-step sums, kernel ms)."""
+    ms, obs = 0.0, []
+    for d0 in range(0, k, per):
+        obs.append(b.step(min(per, k - d0)))
+        ms += b.last_kernel_ms()
+    return np.concatenate(obs, axis=1), ms
+
+
+def _run_snapshots(b, k, per, win, every=100):
+    """k steps in launches of at most per, with the subvalley occupancy of
+    the ensemble taken every `every` steps inside the window; (per-step sums,
+    kernel ms, mean occupancy, final state)."""
+    ms, obs, occ, done = 0.0, [], [], 0
+    while done < k:
+        ns = min(per, k - done)
+        if done >= win.start:
+            ns = min(ns, every)
+        elif done + ns > win.start:
+            ns = win.start - done
+        obs.append(b.step(ns))
+        ms += b.last_kernel_ms()
+        done += ns
+        if done > win.start and (done - win.start) % every == 0:
+            st = b.get_state(0)
+            occ.append(np.bincount(np.asarray(st.sub), minlength=3)[:3] / max(st.n, 1))
+    return np.concatenate(obs, axis=1), ms, np.mean(occ, axis=0), b.get_state(0)
+
+
+def _observables(obs, occ, n, win):
+    """Mean drift velocity and energy over the step window, and the mean
+    subvalley occupancy of the snapshots in it (the valley repopulation a
+    field along <100> drives)."""
+    from viennaemc_gb300.bulk import BulkBatch
+    a = BulkBatch.averages(obs, [n])
+    return {"drift_velocity": float(a["drift_velocity"][0, win, 0].mean()),
+            "energy": float(a["energy"][0, win, 0].mean()),
+            "subvalley_occupancy": [float(x) for x in occ]}
+
+
+def _precision(v, pt, args, N, per, rank):
+    """The FP32 engine against its precision oracle, the FP64 engine run from the
+    same initial electrons with the same seed and the same random numbers
+    (EMCG_ENS_FLOAT_DRAWS), per observable; the seed-to-seed sigma of the FP32
+    observables (extra seeds) beside it; and the plain FP64 engine's speed."""
     from viennaemc_gb300.bulk import BulkBatch, EnsembleSpec
-    k64 = min(K, args.fp64_steps)
-    spec64 = EnsembleSpec(0, N, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 999 + rank, 0, 300.0)
-    b64 = BulkBatch([pt], [spec64], "fp64")
-    b64.set_launch(args.block, per)
-    b64.init_particles(0)
-    b64.step(W)
-    ms64 = 0.0
-    obs64 = []
-    for d0 in range(0, k64, per):
-        obs64.append(b64.step(min(per, k64 - d0)))
-        ms64 += b64.last_kernel_ms()
-    b64.close()
-    a64 = BulkBatch.averages(np.concatenate(obs64, axis=1), [N])
+    k64 = args.fp64_steps
     win = slice(max(0, k64 - 500), k64)
-    vd32 = float(avg["drift_velocity"][0, win, 0].mean())
-    vd64 = float(a64["drift_velocity"][0, win, 0].mean())
-    value64 = N * k64 / (ms64 / 1e3)
-    return value64, vd32, vd64, win, k64
+    seed = 4321 + rank
+
+    def spec(s, fd=False):
+        return EnsembleSpec(0, N, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, s, 0, 300.0, fd)
+    b32 = BulkBatch([pt], [spec(seed)], "fp32")
+    b32.set_launch(args.block, per, args.min_blocks, queued=args.scatter_mode)
+    b32.init_particles(0)
+    st0 = b32.get_state(0)
+    o32, _, occ32, s32 = _run_snapshots(b32, k64, per, win)
+    b32.close()
+    b64 = BulkBatch([pt], [spec(seed, True)], "fp64")
+    b64.set_launch(args.block, per)
+    b64.set_state(0, st0)
+    o64, _, occ64, s64 = _run_snapshots(b64, k64, per, win)
+    b64.close()
+    r32, r64 = _observables(o32, occ32, N, win), _observables(o64, occ64, N, win)
+    # electrons still on the same path: same subvalley, energy within float
+    # rounding grown over the run (the others branched on a rounding)
+    same = (s32.sub == s64.sub) & (np.abs(s32.energy - s64.energy)
+                                   <= 1e-3 * np.abs(s64.energy) + 1e-5)
+    # seed-to-seed spread of one FP32 run's observables
+    extra = []
+    for k in range(args.precision_seeds):
+        b = BulkBatch([pt], [spec(seed + 1 + k)], "fp32")
+        b.set_launch(args.block, per, args.min_blocks, queued=args.scatter_mode)
+        b.init_particles(0)
+        o, _, occ, _ = _run_snapshots(b, k64, per, win)
+        extra.append(_observables(o, occ, N, win))
+        b.close()
+    out = {"oracle": "FP64 engine, same initial electrons, same seed, same random numbers "
+                     "(float draws widened to double)",
+           "steps": k64, "window_steps": [win.start, win.stop],
+           "occupancy": "mean of 5 snapshots of the ensemble, every 100 steps in the window",
+           "same_path_fraction": float(same.mean()), "observables": {}}
+    for key in ("drift_velocity", "energy"):
+        x32, x64 = r32[key], r64[key]
+        sd = float(np.std([e[key] for e in extra + [r32]], ddof=1)) if extra else None
+        out["observables"][key] = {"fp32": x32, "fp64": x64, "rel": abs(x32 - x64) / abs(x64),
+                                   "seed_sigma_rel": sd / abs(x64) if sd is not None else None}
+    o32v, o64v = np.array(r32["subvalley_occupancy"]), np.array(r64["subvalley_occupancy"])
+    sd = (np.std([e["subvalley_occupancy"] for e in extra + [r32]], axis=0, ddof=1).max()
+          if extra else None)
+    out["observables"]["subvalley_occupancy"] = {
+        "fp32": r32["subvalley_occupancy"], "fp64": r64["subvalley_occupancy"],
+        "abs": float(np.abs(o32v - o64v).max()),
+        "seed_sigma_abs": float(sd) if sd is not None else None}
+    out["seeds_for_sigma"] = len(extra) + 1
+    # the plain FP64 engine (its own 64-bit draws) on the same workload: speed
+    b = BulkBatch([pt], [spec(999 + rank)], "fp64")
+    b.set_launch(args.block, per)
+    b.set_state(0, st0)
+    _, ms_plain = _run_steps(b, k64, per)
+    b.close()
+    return N * k64 / (ms_plain / 1e3), out, k64
 
 
 def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units, h2d, d2h,
-            value64, vd32, vd64, win, k64, wall, clocks, device=None, batched=None, p2p=None):
+            value64, precision, k64, wall, clocks, device=None, batched=None, p2p=None,
+            small=None):
     peak, peak_src = _peaks()
     bpp = BYTES_PER_PARTICLE_STEP["fp32"]
     achieved = bpp * value / 1e9  # algorithmic GB/s (72 B per particle-step)
@@ -254,11 +334,11 @@ def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units,
     if value64:
         line["fp64_engine"] = {"value": value64, "unit": UNIT, "steps": k64,
                                "fp32_speedup": value / value64}
-        line["vd_error"] = {"fp32_mps": vd32, "fp64_mps": vd64,
-                            "rel": abs(vd32 - vd64) / abs(vd64) if vd64 else None,
-                            "window_steps": [win.start, win.stop]}
+        line["fp32_error"] = precision
     if clocks:
         line["clocks"] = clocks
+    if small:
+        line["small"] = small
     if batched:
         line["batched"] = batched
     if device:
@@ -341,6 +421,43 @@ def _p2p_bench(args, rank):
     return out
 
 
+def _small_bench(args, rank):
+    """The plain method's small case: bulk Si, 10,000 electrons, 1e5 V/m
+    along <100>, dt 1 fs, 3,000 steps, FP64 engine; the FP32 engine beside
+    it; the reference algorithm (oracle port, FP64) on the host cores for the
+    same workload."""
+    import viennaemc_gb300 as v
+    from viennaemc_gb300.bulk import BulkBatch, EnsembleSpec
+    n, K, per = 10000, args.small_steps, 500
+    pt = silicon_model(v, "fp64")
+    out = {"workload": "bulk Si, 10,000 electrons, 1e5 V/m <100>, dt 1 fs, 3,000 steps, FP64",
+           "particles": n, "steps": K}
+    for prec, block in (("fp64", 64), ("fp32", 64)):
+        spec = EnsembleSpec(0, n, 1e5, (1, 0, 0), (1e-6,) * 3, 1e-15, 77 + rank, 0, 300.0)
+        b = BulkBatch([pt], [spec], prec)
+        b.set_launch(block, per)
+        b.init_particles(0)
+        o, ms, occ, _ = _run_snapshots(b, K, per, slice(K // 2, K), every=K // 10)
+        r = _observables(o, occ, n, slice(K // 2, K))
+        b.close()
+        out[prec] = {"value": n * K / (ms / 1e3), "unit": UNIT, "kernel_ms": ms,
+                     "block_threads": block, **r}
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle as po
+        po.build()
+        threads = os.cpu_count() or 1
+        m = po.silicon_model("jacoboni")
+        st = _oracle_state(po, n)
+        t0 = time.perf_counter()
+        m.bulk_run_philox(st, 1e-15, [-1.60219e-19 * 1e5, 0, 0], [1e-6] * 3, [1, 0, 0], 7, 0,
+                          0, K, threads, True)
+        el = time.perf_counter() - t0
+        out["cpu_reference"] = {"value": n * K / el, "unit": UNIT, "cores": threads,
+                                "kind": "port", "sample": "the whole workload, FP64"}
+    return out
+
+
 def _batched_bench(args, rank):
     """The velocity-field sweep in one launch per chunk of steps: FP32 state,
     autotuned launch shape, CUDA-graph replay; the plain FP64 engine on the same
@@ -378,35 +495,59 @@ def _batched_bench(args, rank):
            "l2": "working set larger than L2 (%.0f MB of particle state)" % (ntot * 40 / 1e6),
            "rate_rebuild": rebuild}
     if args.batch_fp64_steps > 0:
-        # plain FP64 engine on the same batch from the same seeds: speed and v_d
-        k64 = args.batch_fp64_steps
-        runs = {}
-        for prec in ("fp32", "fp64"):
-            bb = BulkBatch(models, specs, prec)
-            for e in range(len(specs)):
-                bb.init_particles(e)
-            bb.set_launch(256, min(k64, args.steps_per_launch))
-            t_ms, o = 0.0, []
-            for d0 in range(0, k64, args.steps_per_launch):
-                o.append(bb.step(min(args.steps_per_launch, k64 - d0)))
-                t_ms += bb.last_kernel_ms()
-            bb.close()
-            runs[prec] = (t_ms, np.concatenate(o, axis=1))
-        win = slice(k64 // 2, k64)
-        errs = []
-        for e, sp in enumerate(specs):
-            if sp.n_particles < 200000 or sp.field_strength < 1e5:
-                continue
-            a = [BulkBatch.averages(runs[p][1][e:e + 1], [sp.n_particles])["drift_velocity"]
-                 [0, win, 0].mean() for p in ("fp32", "fp64")]
-            errs.append(abs(a[0] - a[1]) / abs(a[1]))
-        out["fp64_engine"] = {"value": ntot * k64 / (runs["fp64"][0] / 1e3), "steps": k64,
-                              "fp32_speedup_same_steps": runs["fp64"][0] / runs["fp32"][0]}
-        out["vd_error"] = {"max_rel": max(errs) if errs else None,
-                           "ensembles_compared": len(errs),
-                           "rule": ">= 2e5 particles and >= 1e5 V/m, mean v_d over steps "
-                                   f"{win.start}-{win.stop}"}
+        out.update(_batched_precision(args, models, specs, ntot))
     return out
+
+
+def _batched_precision(args, models, specs, ntot):
+    """The sweep's FP32 run against the FP64 engine from the same initial
+    electrons with the same seeds and random numbers (float draws), per
+    ensemble: mean energy and drift velocity over the second half of the
+    steps; and the plain FP64 engine's speed on the same batch."""
+    import dataclasses
+    from viennaemc_gb300.bulk import BulkBatch
+    k64, per = args.batch_fp64_steps, args.steps_per_launch
+    b32 = BulkBatch(models, specs, "fp32")
+    for e in range(len(specs)):
+        b32.init_particles(e)
+    st0 = [b32.get_state(e) for e in range(len(specs))]
+    b32.set_launch(256, min(k64, per))
+    o32, ms32 = _run_steps(b32, k64, per)
+    s32 = [b32.get_state(e) for e in range(len(specs))]
+    b32.close()
+    runs = {}
+    for mode, fd in (("same_draws", True), ("plain", False)):
+        b64 = BulkBatch(models, [dataclasses.replace(s, float_draws=fd) for s in specs], "fp64")
+        for e in range(len(specs)):
+            b64.set_state(e, st0[e])
+        b64.set_launch(256, min(k64, per))
+        runs[mode] = _run_steps(b64, k64, per)
+        if fd:
+            s64 = [b64.get_state(e) for e in range(len(specs))]
+        b64.close()
+    win = slice(k64 // 2, k64)
+    e_err, v_err, same = [], [], []
+    for e, sp in enumerate(specs):
+        a, r = s32[e], s64[e]
+        same.append(float(((a.sub == r.sub) & (np.abs(a.energy - r.energy)
+                                                <= 1e-3 * np.abs(r.energy) + 1e-5)).mean()))
+        a32 = BulkBatch.averages(o32[e:e + 1], [sp.n_particles])
+        a64 = BulkBatch.averages(runs["same_draws"][0][e:e + 1], [sp.n_particles])
+        e32, e64 = a32["energy"][0, win, 0].mean(), a64["energy"][0, win, 0].mean()
+        e_err.append(abs(e32 - e64) / e64)
+        if sp.field_strength >= 1e5:
+            v32, v64 = (a["drift_velocity"][0, win, 0].mean() for a in (a32, a64))
+            v_err.append(abs(v32 - v64) / abs(v64))
+    return {"fp64_engine": {"value": ntot * k64 / (runs["plain"][1] / 1e3), "steps": k64,
+                            "fp32_speedup_same_steps": runs["plain"][1] / ms32},
+            "fp32_error": {"oracle": "FP64 engine, same initial electrons, seeds and random "
+                                     "numbers (float draws widened to double)",
+                           "energy_max_rel": float(max(e_err)), "ensembles": len(e_err),
+                           "drift_velocity_max_rel": float(max(v_err)),
+                           "drift_velocity_ensembles": len(v_err),
+                           "same_path_fraction_min": float(min(same)),
+                           "window_steps": [win.start, win.stop],
+                           "rule": "energy: every ensemble; drift velocity: fields >= 1e5 V/m"}}
 
 
 def resistor_device(D, P):
@@ -471,14 +612,15 @@ def _device_bench(args, rank):
     return out
 
 
-def mosfet_device(D, P, vds, vgs=1.0):
+def mosfet_device(D, P, vds, vgs=1.0, width=1.3e-6):
     """2-D Si n-MOSFET: 200 nm x 100 nm at 0.5 nm (401 x 201 nodes), gate
     length 50 nm over 1 nm SiO2 (eps_r 3.9, barrier Eg/2), source and drain
     Nd = 1e26 m^-3 to 20 nm depth, channel and bulk Na = 1e24 m^-3, substrate
-    contact at the back; the contact layout of the reference mosfet2D."""
+    contact at the back; the contact layout of the reference mosfet2D.  The
+    device width sets the superparticle count (about 3.9e5 at 1.3 um)."""
     mat = P.silicon_material()
     dev = D.Device(mat, (200e-9, 100e-9), (0.5e-9, 0.5e-9))
-    dev.setDeviceWidth(1.3e-6)
+    dev.setDeviceWidth(width)
     dev.addConstantDopingRegion((0, 20e-9), (200e-9, 100e-9), -1e24)
     dev.addConstantDopingRegion((0, 0), (75e-9, 20e-9), 1e26)
     dev.addConstantDopingRegion((75e-9, 0), (125e-9, 20e-9), -1e24)
@@ -490,14 +632,21 @@ def mosfet_device(D, P, vds, vgs=1.0):
     return dev
 
 
+# uneven superparticle counts of the eight bias points, 2e5 .. 6e5 (device
+# width in proportion), in an order unrelated to the bias
+MOSFET_COUNTS = (4.3e5, 2.0e5, 6.0e5, 3.1e5, 5.4e5, 2.6e5, 4.9e5, 3.6e5)
+
+
 def _mosfet_bench(args, rank):
-    """Eight drain biases 0..1 V at Vgs = 1 V stepped together (one engine per
-    bias, each on its own stream), FP32 particles, per-step Poisson to 1e-8."""
+    """Eight drain biases 0..1 V at Vgs = 1 V stepped together as one batch
+    of uneven ensembles (2e5 to 6e5 superparticles, one engine per bias, each
+    on its own stream), FP32 particles, per-step Poisson to 1e-8."""
     from viennaemc_gb300 import device as D
     from viennaemc_gb300 import physics as P
-    sims = []
+    sims, widths = [], []
     for k, vds in enumerate(np.linspace(0.0, 1.0, 8)):
-        dev = mosfet_device(D, P, float(vds))
+        widths.append(1.3e-6 * MOSFET_COUNTS[k] / 3.9e5)
+        dev = mosfet_device(D, P, float(vds), width=widths[-1])
         regs = list(range(dev.n_regions))
         pt = P.silicon_electron("refbulk", n_levels=1000, max_energy=4.0, regions=regs,
                                 coulomb=True, region_doping=dev.getDopingRegionDoping,
@@ -521,11 +670,13 @@ def _mosfet_bench(args, rank):
         s.close()
     tot = sum(0.5 * (a + b) for a, b in zip(n0, n1))
     return {"workload": "Si n-MOSFET 401 x 201 nodes (0.5 nm), Lg 50 nm, 1 nm SiO2, S/D 1e26, "
-                        "channel 1e24, Vgs 1 V, Vds = 0..1 V in 8 steps, one engine per bias",
+                        "channel 1e24, Vgs 1 V, Vds = 0..1 V in 8 steps, one engine per bias, "
+                        "uneven superparticle counts 2e5-6e5",
             "steps": K, "particles": n1, "wall_ms_per_step": 1e3 * wall / K,
             "value": tot * K / wall, "unit": UNIT,
             "device_ms_per_step_each": step, "poisson_ms_per_solve_each": pois,
             "drain_current_A": drain,
+            "drain_current_A_per_m": [i / w for i, w in zip(drain, widths)],
             "note": "value = particles of all 8 engines x steps / wall time of the batch "
                     "(host-timed, the engines overlap on the GPU)"}
 
@@ -601,10 +752,11 @@ def rel_residual(dev, pot, conc):
 
 
 def _host_state(v, N):
-    """A host-side Maxwellian state (the public API's input form)."""
+    """A host-side Maxwellian state (the public API's input form), in
+    page-locked memory."""
     rs = np.random.default_rng(5)
     from viennaemc_gb300.bulk import ParticleState
-    st = ParticleState(N)
+    st = ParticleState(N, pinned=True)
     E = -1.5 * (1.38066e-23 / 1.60219e-19 * 300.0) * np.log(rs.uniform(1e-6, 1, N))
     k = np.sqrt(2 * 0.2586 * 9.11e-31 * E * (1 + 0.5 * E) * 1.60219e-19) / 1.05459e-34
     ct = 1 - 2 * rs.random(N)
@@ -734,6 +886,10 @@ def build_parser():
     ap.add_argument("--mosfet-steps", type=int, default=200,
                     help="timed steps of the 8-bias MOSFET batch (0: skip it)")
     ap.add_argument("--fp64-steps", type=int, default=1500)
+    ap.add_argument("--small-steps", type=int, default=3000,
+                    help="steps of the 10,000-electron FP64 case (0: skip it)")
+    ap.add_argument("--precision-seeds", type=int, default=4,
+                    help="extra FP32 seeds for the seed-to-seed sigma of the observables")
     ap.add_argument("--p2p-n", type=int, default=32768,
                     help="charges of the particle-particle Coulomb leg (0: skip it)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)

@@ -128,7 +128,8 @@ typedef struct {
 /* One bulk ensemble (basicBulkParticleHandler,
    examples/bulkSimulation/basicBulkParticleHandler.hpp:93-120):
    force = charge * field (:186), periodic box [0, box] (:600-613),
-   field_dir = normalised field direction for the drift velocity (:326-347). */
+   field_dir = normalised field direction for the drift velocity (:326-347).
+   flags: EMCG_ENS_FLOAT_DRAWS or 0 (see below). */
 typedef struct {
   int32_t model;      /* index into the handle's models */
   int32_t pad_;
@@ -140,8 +141,17 @@ typedef struct {
   double dt;          /* s */
   uint64_t seed;
   uint32_t stream;
-  uint32_t pad2_;
+  uint32_t flags;
 } emcg_ensemble_desc;
+
+/* Ensemble flag, no reference counterpart: the double engine draws its random
+   numbers as the float engine does -- one 32-bit Philox word per draw, the
+   float engine's uniform (24 bits) or pick, widened to double -- in place of
+   one 64-bit word per draw.  With the same seed, stream and initial state the
+   two engines then consume the same numbers, and their results differ by the
+   arithmetic alone: the double run is the float run's precision oracle.  The
+   float engine ignores the flag. */
+#define EMCG_ENS_FLOAT_DRAWS 1u
 
 /* Host-side structure-of-arrays particle state (emcParticle +
    positionsParticles, include/emcParticle.hpp:10-18). */
@@ -162,6 +172,13 @@ typedef struct emcg_handle emcg_handle;
    include/emcMessage.hpp:43-66, which aborts). */
 const char *emcg_last_error(void);
 int32_t emcg_version(void);
+
+/* Page-locked host memory for particle states (no reference counterpart):
+   state uploads (emcg_set_state) and downloads from such memory run at the
+   full host-link rate; from ordinary memory CUDA stages them.  bytes = 0
+   gives NULL. */
+int32_t emcg_host_alloc(int64_t bytes, void **ptr);
+int32_t emcg_host_free(void *ptr);
 
 /* ---- bulk engine (examples/bulkSimulation/basicBulkParticleHandler.hpp) -- */
 

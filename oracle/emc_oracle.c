@@ -166,6 +166,19 @@ uint64_t oci_draw_u64(dctx *d) {
     }
     w = d->buf[2 - d->nbuf];
     d->nbuf--;
+  } else if (d->mode == OC_RNG_PHILOX32) {
+    /* the engine's float source: o[0], o[1], o[2], o[3] of each block */
+    if (d->nbuf == 0) {
+      uint32_t o[4];
+      oc_philox4x32_10(d->ctr, d->key, o);
+      d->ctr[2]++;
+      d->buf[0] = (uint64_t)o[0] | ((uint64_t)o[1] << 32);
+      d->buf[1] = (uint64_t)o[2] | ((uint64_t)o[3] << 32);
+      d->nbuf = 4;
+    }
+    const uint64_t b = d->buf[(4 - d->nbuf) >> 1];
+    w = (d->nbuf & 1) ? (b >> 32) : (b & 0xFFFFFFFFu);
+    d->nbuf--;
   } else {
     if (d->r->pos < d->r->nwords) {
       w = d->r->words[d->r->pos++];
@@ -186,10 +199,27 @@ uint64_t oci_draw_u64(dctx *d) {
 }
 
 /* std::uniform_real_distribution<double>(a, b)(rng) = canonical*(b-a)+a
-   (bits/random.h uniform_real_distribution::operator()) */
-double oci_draw_u01(dctx *d) { return oc_canonical(oci_draw_u64(d)) * (1.0 - 0.0) + 0.0; }
+   (bits/random.h uniform_real_distribution::operator()).  OC_RNG_PHILOX32:
+   the engine's float draws, a 24-bit uniform from the top of one 32-bit word
+   and U[1e-6, 1) by one float fused multiply-add, widened to double. */
+static float draw_f32(dctx *d) { return (float)(oci_draw_u64(d) >> 8) * 0x1p-24f; }
+double oci_draw_u01(dctx *d) {
+  if (d->mode == OC_RNG_PHILOX32)
+    return (double)draw_f32(d);
+  return oc_canonical(oci_draw_u64(d)) * (1.0 - 0.0) + 0.0;
+}
 double oci_draw_ulog(dctx *d) {
+  if (d->mode == OC_RNG_PHILOX32)
+    return (double)fmaf(draw_f32(d), 1.f - 1e-6f, 1e-6f);
   return oc_canonical(oci_draw_u64(d)) * (1. - 1e-6) + 1e-6;
+}
+/* rng() % n of the reference; OC_RNG_PHILOX32: the engine's float pick, the
+   high word of the 32-bit draw times n */
+uint32_t oci_draw_pick(dctx *d, uint32_t n) {
+  const uint64_t w = oci_draw_u64(d);
+  if (d->mode == OC_RNG_PHILOX32)
+    return (uint32_t)((w * (uint64_t)n) >> 32);
+  return (uint32_t)(w % (uint64_t)n);
 }
 
 /* ======================================================================== */
@@ -679,8 +709,7 @@ static void mech_scatter(const oc_model *m, const oc_mech *me, double *k,
   case OC_ZERO_IV_EMI:
   case OC_FIRST_IV_EMI: { /* ...ZeroOrder...hpp:247-257, 390-400 etc. */
     *valley = me->finalValley;
-    uint64_t w = oci_draw_u64(d);
-    *sub = me->finalSub[*sub][w % (uint64_t)me->nF];
+    *sub = me->finalSub[*sub][oci_draw_pick(d, (uint32_t)me->nF)];
     if (me->kind == OC_ZERO_IV_ABS || me->kind == OC_FIRST_IV_ABS)
       *E += (me->p1 - me->deltaValley);
     else
@@ -830,7 +859,7 @@ int32_t oc_bulk_run_philox(const oc_model *m, oc_particles *p, double dt,
                            const double force[3], const double box[3],
                            const double fieldDir[3], uint64_t seed,
                            uint32_t stream, uint32_t step0, int32_t nSteps,
-                           int32_t nThreads, double *obs) {
+                           int32_t nThreads, double *obs, int32_t words32) {
   int nV = m->nV;
   int32_t status = 0;
 #ifdef _OPENMP
@@ -848,7 +877,7 @@ int32_t oc_bulk_run_philox(const oc_model *m, oc_particles *p, double dt,
       memset(acc, 0, sizeof(acc));
       oc_rng r;
       memset(&r, 0, sizeof(r));
-      r.mode = OC_RNG_PHILOX;
+      r.mode = words32 ? OC_RNG_PHILOX32 : OC_RNG_PHILOX;
       r.seed = seed;
       r.stream = stream;
 #ifdef _OPENMP

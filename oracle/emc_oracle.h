@@ -45,7 +45,9 @@ enum {
 enum {
   OC_RNG_MT = 0,     /* one sequential std::mt19937_64 (reference, no OpenMP) */
   OC_RNG_PHILOX = 1, /* Philox4x32-10, counter (particle, step, call, stream) */
-  OC_RNG_REPLAY = 2  /* consume a recorded flat word log sequentially */
+  OC_RNG_REPLAY = 2, /* consume a recorded flat word log sequentially */
+  OC_RNG_PHILOX32 = 3 /* Philox4x32-10 as the engine's float draws: one 32-bit
+                         word per draw, 24-bit uniforms, multiply-high picks */
 };
 
 typedef struct oc_model oc_model;
@@ -168,7 +170,7 @@ int32_t oc_bulk_run_philox(const oc_model *m, oc_particles *p, double dt,
                            const double force[3], const double box[3],
                            const double fieldDir[3], uint64_t seed,
                            uint32_t stream, uint32_t step0, int32_t nSteps,
-                           int32_t nThreads, double *obs);
+                           int32_t nThreads, double *obs, int32_t words32);
 /* reference per-valley observables: out[v*3 + 0] = avg E, 1 = avg v.dir,
    2 = occupation probability */
 void oc_observables(const oc_model *m, const oc_particles *p,

@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
 
 ACOUSTIC, ZERO_IV_ABS, ZERO_IV_EMI, FIRST_IV_ABS, FIRST_IV_EMI, COULOMB = range(6)
-RNG_MT, RNG_PHILOX, RNG_REPLAY = range(3)
+RNG_MT, RNG_PHILOX, RNG_REPLAY, RNG_PHILOX32 = range(4)
 
 _lib = None
 
@@ -103,7 +103,7 @@ def _declare(L):
     L.oc_bulk_step.argtypes = [vp, P(Particles), d, P(d), P(d), P(Rng), u32, P(i64)]
     L.oc_bulk_run_philox.restype = i32
     L.oc_bulk_run_philox.argtypes = [vp, P(Particles), d, P(d), P(d), P(d), u64, u32, u32,
-                                     i32, i32, P(d)]
+                                     i32, i32, P(d), i32]
     L.oc_observables.argtypes = [vp, P(Particles), P(d), P(d)]
     L.oc_bulk_init.restype = i64
     L.oc_bulk_init.argtypes = [vp, P(d), P(d), d, P(Rng), P(Particles), i64]
@@ -300,12 +300,13 @@ class Model:
         return rc, off
 
     def bulk_run_philox(self, st: State, dt, force, box, field_dir, seed, stream, step0,
-                        n_steps, n_threads=0, want_obs=True):
+                        n_steps, n_threads=0, want_obs=True, words32=False):
+        """words32: draw as the engine's float source (one 32-bit word per draw)."""
         p = st.cstruct()
         obs = np.zeros((n_steps, self.nV, 3)) if want_obs else None
         rc = lib().oc_bulk_run_philox(self.h, C.byref(p), dt, dptr(darr(force)), dptr(darr(box)),
                                       dptr(darr(field_dir)), seed, stream, step0, n_steps,
-                                      n_threads, dptr(obs) if want_obs else None)
+                                      n_threads, dptr(obs) if want_obs else None, int(words32))
         assert rc == 0, rc
         return obs
 

@@ -26,14 +26,14 @@ def _eng_field(f):
     return ENG.get(f, f)
 
 
-def _batch(engine, g, precision="fp64", n=None, seed=1, stream=0):
+def _batch(engine, g, precision="fp64", n=None, seed=1, stream=0, float_draws=False):
     name, T, nL, maxE, mt = case_model(g)
     pt = engine.physics.silicon_electron(name, temperature=T, n_levels=nL, max_energy=maxE, mt=mt)
     fld = g["applied_field"]
     strength = float(np.sqrt(np.sum(fld * fld)))
     spec = engine.EnsembleSpec(0, n if n is not None else len(g["s0_E"]), strength,
                                tuple(g["field_dir"]), (float(g["box"]),) * 3, float(g["dt"]),
-                               seed, stream, T)
+                               seed, stream, T, float_draws)
     return engine.BulkBatch([pt], [spec], precision)
 
 
@@ -147,6 +147,73 @@ def test_philox_fp64_matches_oracle(engine, oracle):
     b.close()
 
 
+def test_float_draws_fp64_matches_oracle(engine, oracle):
+    """The double engine drawing as the float engine (EMCG_ENS_FLOAT_DRAWS: one
+    32-bit Philox word per draw, 24-bit uniforms, multiply-high picks) against
+    the oracle drawing the same way: states within 1e-12 after 100 steps."""
+    m = oracle.silicon_model("jacoboni")
+    rng = oracle.RngState(oracle.RNG_MT, 98)
+    st = m.bulk_init([2e-6] * 3, [2e-7] * 3, 4e20, rng)
+    g = {"applied_field": np.array([-1e6, 0, 0]), "field_dir": np.array([-1.0, 0, 0]),
+         "box": np.array(2e-6), "dt": np.array(1e-15), "s0_E": st.E,
+         "raw": np.zeros((13, 1)), "params": np.array([300, 1000, 1.0, 0, 0, 0, 0, 0, 0, 0, 0.19])}
+    seed, stream, steps = 0xFEED_0042, 5, 100
+    b = _batch(engine, g, seed=seed, stream=stream, float_draws=True)
+    b.set_state(0, _oracle_state_to_engine(engine, st))
+    obs = b.step(steps, step0=9)
+    ref = st.copy()
+    oobs = m.bulk_run_philox(ref, 1e-15, [1.60219e-19 * 1e6, 0, 0], [2e-6] * 3, [-1.0, 0, 0],
+                             seed, stream, 9, steps, n_threads=1, words32=True)
+    # the 64-bit draws take another path
+    other = st.copy()
+    m.bulk_run_philox(other, 1e-15, [1.60219e-19 * 1e6, 0, 0], [2e-6] * 3, [-1.0, 0, 0],
+                      seed, stream, 9, steps, n_threads=1)
+    got = b.get_state(0)
+    bad = np.zeros(st.n, bool)
+    for f in FIELDS_F:
+        a, r = getattr(got, _eng_field(f)), getattr(ref, f)
+        bad |= np.abs(a - r) > 1e-12 * np.max(np.abs(r))
+    for f in ("valley", "sub"):
+        bad |= getattr(got, f) != getattr(ref, f)
+    assert bad.sum() <= max(1, st.n // 1000), bad.sum()
+    # every event draws a new free flight: tau tells the two draw modes apart
+    assert np.mean(np.abs(other.tau - ref.tau) > 1e-6 * np.abs(ref.tau).max()) > 0.9
+    assert np.allclose(obs[0, :, 0, 2], oobs[:, 0, 2])
+    assert np.allclose(obs[0, :, 0, 0], oobs[:, 0, 0], rtol=1e-9)
+    b.close()
+
+
+def test_fp32_equals_fp64_with_the_same_draws(engine):
+    """The float engine and the double engine with float draws, from the same
+    initial electrons and the same Philox seed, consume the same random
+    numbers and sample the same directions: after 600 steps almost every
+    electron still follows the same path (same subvalley, energy within the
+    float rounding grown over the run) -- the few others branched on a float
+    rounding -- and the mean energy and drift velocity agree to float
+    precision, far below their seed-to-seed noise."""
+    pt = engine.physics.silicon_electron("jacoboni")
+    n, steps = 20000, 600
+    spec32 = engine.EnsembleSpec(0, n, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 77, 1)
+    spec64 = engine.EnsembleSpec(0, n, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 77, 1,
+                                 float_draws=True)
+    b32 = engine.BulkBatch([pt], [spec32], "fp32")
+    b32.init_particles(0)
+    st0 = b32.get_state(0)
+    b64 = engine.BulkBatch([pt], [spec64], "fp64")
+    b64.set_state(0, st0)
+    o32, o64 = b32.step(steps), b64.step(steps)
+    a, r = b32.get_state(0), b64.get_state(0)
+    b32.close()
+    b64.close()
+    same = (a.sub == r.sub) & (np.abs(a.energy - r.energy) <= 1e-3 * np.abs(r.energy) + 1e-5)
+    assert same.mean() >= 0.99, same.mean()
+    A32, A64 = (engine.BulkBatch.averages(o, [n]) for o in (o32, o64))
+    e32, e64 = A32["energy"][0, -300:, 0].mean(), A64["energy"][0, -300:, 0].mean()
+    v32, v64 = (A["drift_velocity"][0, -300:, 0].mean() for A in (A32, A64))
+    assert abs(e32 - e64) <= 5e-4 * e64, (e32, e64)
+    assert abs(v32 - v64) <= 2e-3 * abs(v64), (v32, v64)
+
+
 def test_init_fp64_matches_oracle(engine, oracle):
     m = oracle.silicon_model("jacoboni")
     n, ext, spacing = 500, np.array([6, 6, 6]), np.array([1e-7] * 3)
@@ -236,13 +303,32 @@ def _steady(engine, precision, n, steps, seed, field=1e6, direction=(1, 0, 0), m
 
 
 def test_fp32_matches_fp64_within_one_percent(engine):
+    """The headline's bound: FP32 drift velocity and mean energy within 1 % of
+    the FP64 oracle, 2^16 electrons, 1500 steps at 1e6 V/m, steady window of
+    500 steps.  The oracle is the FP64 engine from the same initial electrons
+    with the same seed and random numbers, so the difference is that of the
+    arithmetic alone and the electrons that branched on a float rounding
+    (measured on 2^16 electrons: 0.2 % in drift velocity; the seed-to-seed
+    noise of this ensemble is about 0.6 %)."""
+    pt = engine.physics.silicon_electron("jacoboni")
     n, steps = 1 << 16, 1500
-    v64, e64 = _steady(engine, "fp64", n, steps, 11)
-    v32, e32 = _steady(engine, "fp32", n, steps, 12)
-    vd64, vd32 = v64[-500:].mean(), v32[-500:].mean()
-    ee64, ee32 = e64[-500:].mean(), e32[-500:].mean()
+    spec = engine.EnsembleSpec(0, n, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 11, 0)
+    b32 = engine.BulkBatch([pt], [spec], "fp32")
+    b32.init_particles(0)
+    b64 = engine.BulkBatch([pt], [engine.EnsembleSpec(0, n, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15,
+                                                      11, 0, float_draws=True)], "fp64")
+    b64.set_state(0, b32.get_state(0))
+    a32 = engine.BulkBatch.averages(b32.step(steps), [n])
+    a64 = engine.BulkBatch.averages(b64.step(steps), [n])
+    b32.close()
+    b64.close()
+    vd32, vd64 = (a["drift_velocity"][0, -500:, 0].mean() for a in (a32, a64))
+    ee32, ee64 = (a["energy"][0, -500:, 0].mean() for a in (a32, a64))
     assert abs(vd32 - vd64) <= 0.01 * abs(vd64), (vd32, vd64)
     assert abs(ee32 - ee64) <= 0.01 * ee64, (ee32, ee64)
+    # the electrons that branched on a float rounding (a few percent after 1500
+    # steps) carry their own noise: well inside the bound all the same
+    assert abs(vd32 - vd64) <= 5e-3 * abs(vd64) and abs(ee32 - ee64) <= 1e-3 * ee64
     # electrons drift against the field
     assert vd64 < 0 and 4e4 < abs(vd64) < 2e5
 
@@ -553,4 +639,36 @@ def test_pass_actions_change_only_the_schedule(engine):
     for bad in (0, 21):
         with pytest.raises(engine._lib.EmcgError):
             b.set_launch(pass_actions=bad)
+    b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_state_upload_checks_indices_and_keeps_the_old_state(engine, precision):
+    """emcg_set_state copies the caller's arrays to the device and converts
+    them there: a subvalley out of range is refused with the first bad
+    particle's index and leaves the ensemble as it was; a page-locked host
+    state uploads the same values."""
+    pt = engine.physics.silicon_electron("jacoboni")
+    spec = engine.EnsembleSpec(0, 1000, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 5, 0)
+    b = engine.BulkBatch([pt], [spec], precision)
+    b.init_particles(0)
+    st = b.get_state(0)
+    bad = engine.ParticleState.from_arrays(**{f: getattr(st, f) for f in
+                                              engine.bulk.STATE_F + engine.bulk.STATE_I})
+    bad.sub[17] = 9
+    bad.sub[400] = -1
+    bad.kx[:] = 0.0
+    with pytest.raises(engine._lib.EmcgError) as ei:
+        b.set_state(0, bad)
+    assert ei.value.status == -1 and "particle 17" in str(ei.value)
+    now = b.get_state(0)
+    for f in engine.bulk.STATE_F + engine.bulk.STATE_I:
+        assert np.array_equal(getattr(now, f), getattr(st, f)), f
+    pinned = engine.ParticleState(st.n, pinned=True)
+    for f in engine.bulk.STATE_F + engine.bulk.STATE_I:
+        getattr(pinned, f)[:] = getattr(st, f)
+    pinned.kx *= 0.5
+    b.set_state(0, pinned)
+    now = b.get_state(0)
+    assert np.array_equal(now.kx, st.kx * 0.5) and np.array_equal(now.sub, st.sub)
     b.close()

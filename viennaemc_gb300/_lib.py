@@ -108,7 +108,7 @@ class EnsembleDesc(C.Structure):
     _fields_ = [("model", C.c_int32), ("pad_", C.c_int32), ("capacity", C.c_int64),
                 ("field", C.c_double * 3), ("charge", C.c_double), ("field_dir", C.c_double * 3),
                 ("box", C.c_double * 3), ("dt", C.c_double), ("seed", C.c_uint64),
-                ("stream", C.c_uint32), ("pad2_", C.c_uint32)]
+                ("stream", C.c_uint32), ("flags", C.c_uint32)]
 
 
 class StateDesc(C.Structure):
@@ -167,6 +167,10 @@ def _declare(L):
     L.emcg_get_pass_actions.argtypes = [vp, C.POINTER(i32)]
     L.emcg_set_occupancy.restype = i32
     L.emcg_set_occupancy.argtypes = [vp, i32]
+    L.emcg_host_alloc.restype = i32
+    L.emcg_host_alloc.argtypes = [i64, C.POINTER(vp)]
+    L.emcg_host_free.restype = i32
+    L.emcg_host_free.argtypes = [vp]
     L.emcg_drift_kat.restype = i32
     L.emcg_drift_kat.argtypes = [vp, i32, i64, P(i32), P(d), P(d), P(d), P(d), P(d)]
     for name, args in _EXTRA_DECLS:

@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -30,10 +31,32 @@ def _ip(a):
 
 
 class ParticleState:
-    """Host structure-of-arrays particle state (float64 / int32)."""
+    """Host structure-of-arrays particle state (float64 / int32).
 
-    def __init__(self, n: int):
+    pinned: the arrays live in one page-locked block (emcg_host_alloc), so
+    uploads and downloads run at the full host-link rate."""
+
+    def __init__(self, n: int, pinned: bool = False):
         self.n = int(n)
+        self._block = None
+        if pinned and self.n:
+            lib = L.lib()
+            nb = self.n * (8 * len(STATE_F) + 4 * len(STATE_I))
+            p = C.c_void_p()
+            L.check(lib.emcg_host_alloc(nb, C.byref(p)))
+            self._block = p
+            self._finalizer = weakref.finalize(self, lib.emcg_host_free, p)
+            raw = np.ctypeslib.as_array((C.c_uint8 * nb).from_address(p.value))
+            off = 0
+            for f in STATE_F:
+                setattr(self, f, raw[off:off + 8 * self.n].view(np.float64))
+                off += 8 * self.n
+            for f in STATE_I:
+                setattr(self, f, raw[off:off + 4 * self.n].view(np.int32))
+                off += 4 * self.n
+            for f in STATE_F + STATE_I:
+                getattr(self, f)[:] = 0
+            return
         for f in STATE_F:
             setattr(self, f, np.zeros(self.n, np.float64))
         for f in STATE_I:
@@ -109,6 +132,8 @@ class EnsembleSpec:
     seed: int
     stream: int = 0
     temperature: float = 300.0
+    # the double engine draws as the float engine (EMCG_ENS_FLOAT_DRAWS)
+    float_draws: bool = False
 
 
 class BulkBatch:
@@ -150,6 +175,7 @@ class BulkBatch:
         d.dt = sp.dt
         d.seed = sp.seed
         d.stream = sp.stream
+        d.flags = 1 if sp.float_draws else 0
 
     def close(self):
         if getattr(self, "h", None):

@@ -4,12 +4,10 @@
 // registers; per-step ensemble observables are reduced warp -> block ->
 // device with double accumulators.
 #include <algorithm>
-#include <atomic>
 #include <climits>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
-#include <thread>
 #include <vector>
 
 #include "emcg_common.cuh"
@@ -181,7 +179,7 @@ __global__ void __launch_bounds__(256, MINB) bulkStepKernel(StateK<T> st, const 
           myErr = EMCG_ERR_REPLAY;
       } else {
         PhiloxSrc<T> src;
-        src.init(pid, step0 + (uint32_t)s, EK.stream, EK.key0, EK.key1);
+        src.init(pid, step0 + (uint32_t)s, EK.stream, EK.key0, EK.key1, EK.floatDraws);
         myErr = bulkParticleStep(M, EK, k, pos, E, tau, gtau, valley, sub, region, kN, src);
       }
     }
@@ -299,7 +297,7 @@ __global__ void __launch_bounds__(256)
     for (int v = 0; v < 3; v++)
       F[v] = EK.F[v] + coulFactor * (T)coulF[v * stride + gi];
     PhiloxSrc<T> rng;
-    rng.init(pid, step, EK.stream, EK.key0, EK.key1);
+    rng.init(pid, step, EK.stream, EK.key0, EK.key1, EK.floatDraws);
     myErr = bulkParticleStepF(M, EK, F, k, pos, E, tau, gtau, valley, sub, region, kN, rng);
   }
   T vd = T(0);
@@ -444,7 +442,8 @@ __global__ void __launch_bounds__(256, MINB)
       int valley = mt & 0xff, sub = (mt >> 8) & 0xff, region = mt >> 16;
       T tRem = dt - tau;
       PhiloxSrc<T> rng;
-      rng.init((uint32_t)(tl.begin + p - EK.begin), step, EK.stream, EK.key0, EK.key1);
+      rng.init((uint32_t)(tl.begin + p - EK.begin), step, EK.stream, EK.key0, EK.key1,
+               EK.floatDraws);
       int guard = 0, e = 0;
       while (tRem > T(0)) {
         if (++guard > kMaxScatterPerStep) {
@@ -486,7 +485,7 @@ __global__ void __launch_bounds__(256, MINB)
       int sub = (mt >> 8) & 0xff;
       if (gtau <= T(0)) {
         PhiloxSrc<T> rng;
-        rng.init((uint32_t)(gi - EK.begin), step, EK.stream, EK.key0, EK.key1);
+        rng.init((uint32_t)(gi - EK.begin), step, EK.stream, EK.key0, EK.key1, EK.floatDraws);
         rng.c2 = 0x40000000u;
         gtau = -m_log(rng.ulog()) * M.grainTau;
       }
@@ -1009,9 +1008,11 @@ struct BulkImpl {
   int64_t offCap = 0;
   bool replay = false;
   double lastMs = 0;
-  // pinned host staging for state uploads (grown on demand)
-  void *pinned = nullptr;
-  size_t pinnedBytes = 0;
+  // device staging of state uploads, the caller's arrays as they are (grown
+  // on demand), and the first bad particle index the conversion found
+  void *dStage = nullptr;
+  size_t stageBytes = 0;
+  unsigned long long *dBad = nullptr;
   // particle-particle Coulomb steps (FMMBulkParticleHandler)
   bool coulomb = false;
   double coulEpsR = 1., coulInvCut = 1e9;
@@ -1095,6 +1096,7 @@ static void buildEnsK(const emcg_ensemble_desc &d, const ModelK<T> &M,
   E.key0 = (uint32_t)d.seed;
   E.key1 = (uint32_t)(d.seed >> 32);
   E.stream = d.stream;
+  E.floatDraws = (d.flags & EMCG_ENS_FLOAT_DRAWS) ? 1u : 0u;
   (void)M;
 }
 
@@ -1487,8 +1489,8 @@ static void freeBulk(BulkImpl *b) {
   cudaFree(b->dWords);
   cudaFree(b->dOff);
   freeRateScratch(b->rateScratch);
-  if (b->pinned)
-    cudaFreeHost(b->pinned);
+  cudaFree(b->dStage);
+  cudaFree(b->dBad);
   for (double *p : b->dFixed)
     cudaFree(p);
   cudaFree(b->dSrc);
@@ -1645,27 +1647,38 @@ extern "C" int64_t emcg_num_particles(emcg_handle *h, int32_t e) {
   return b->count[e];
 }
 
-// Run f(lo, hi) over [0, n) on up to 8 host threads (one below 64k items).
-template <class F> static void parallelRange(int64_t n, F f) {
-  const int64_t kMinPer = 1 << 16;
-  int nt = (int)std::min<int64_t>(8, std::max<int64_t>(1, n / kMinPer));
-  nt = std::max(1, std::min(nt, (int)std::thread::hardware_concurrency()));
-  if (nt == 1) {
-    f(int64_t(0), n);
+// Upload check: the first particle whose valley, subvalley or region is out
+// of range (the caller's int32 indices, copied to the device as they are).
+__global__ void stateCheckKernel(int64_t n, const int32_t *__restrict__ idx, int nValleys,
+                                 unsigned long long *__restrict__ bad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
     return;
-  }
-  std::vector<std::thread> th;
-  const int64_t per = (n + nt - 1) / nt;
-  for (int k = 0; k < nt; k++) {
-    const int64_t lo = std::min(n, k * per), hi = std::min(n, lo + per);
-    th.emplace_back([=] { f(lo, hi); });
-  }
-  for (auto &t : th)
-    t.join();
+  const int32_t v = idx[i], sb = idx[n + i], r = idx[2 * n + i];
+  if (v < 0 || v >= nValleys || sb < 0 || sb >= EMCG_MAX_DEG || r < 0 || r >= EMCG_MAX_REGIONS)
+    atomicMin(bad, (unsigned long long)i);
 }
 
-// Upload a host state: converted on the host threads into pinned staging,
-// then one asynchronous copy per field.
+// Upload conversion into the engine's precision and packed meta; nothing is
+// written if the check found a bad particle, so the old state stays.
+template <class T>
+__global__ void stateConvertKernel(StateK<T> st, int64_t base, int64_t n,
+                                   const double *__restrict__ src,
+                                   const int32_t *__restrict__ idx,
+                                   const unsigned long long *__restrict__ bad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || *bad != ~0ull)
+    return;
+  T *dst[9] = {st.kx, st.ky, st.kz, st.px, st.py, st.pz, st.E, st.tau, st.gtau};
+#pragma unroll
+  for (int f = 0; f < 9; f++)
+    dst[f][base + i] = (T)src[(size_t)f * n + i];
+  st.meta[base + i] = packMeta(idx[i], idx[n + i], idx[2 * n + i]);
+}
+
+// Upload a host state: one asynchronous copy per field of the caller's arrays
+// into device staging (at the full host link rate when the caller's memory is
+// pinned), then one conversion kernel.
 template <class T>
 static int32_t setStateTyped(BulkImpl *b, int e, const emcg_state *s) {
   const int64_t n = s->n, base = b->begin[e];
@@ -1676,47 +1689,35 @@ static int32_t setStateTyped(BulkImpl *b, int e, const emcg_state *s) {
   EMCG_CHECK_ARG(s->valley && s->sub && s->region, "state index arrays are NULL");
   if (n == 0)
     return EMCG_OK;
-  const size_t need = (size_t)n * (9 * sizeof(T) + sizeof(uint32_t));
-  if (b->pinnedBytes < need) {
+  const size_t need = (size_t)n * (9 * sizeof(double) + 3 * sizeof(int32_t));
+  if (b->stageBytes < need) {
     EMCG_CUDA(cudaStreamSynchronize(b->stream)); // an earlier upload may still read it
-    if (b->pinned)
-      cudaFreeHost(b->pinned);
-    b->pinned = nullptr;
-    b->pinnedBytes = 0;
-    EMCG_CUDA(cudaHostAlloc(&b->pinned, need, cudaHostAllocDefault));
-    b->pinnedBytes = need;
+    cudaFree(b->dStage);
+    b->dStage = nullptr;
+    b->stageBytes = 0;
+    EMCG_CUDA(cudaMalloc(&b->dStage, need));
+    b->stageBytes = need;
   }
-  EMCG_CUDA(cudaStreamSynchronize(b->stream));
-  T *stage = static_cast<T *>(b->pinned);
-  uint32_t *meta = reinterpret_cast<uint32_t *>(stage + (size_t)9 * n);
-  const int nv = b->ensNV[e];
-  std::atomic<int64_t> badIdx(INT64_MAX);
-  parallelRange(n, [&](int64_t lo, int64_t hi) {
-    for (int f = 0; f < 9; f++) {
-      T *dst = stage + (size_t)f * n;
-      const double *sp = src[f];
-      for (int64_t i = lo; i < hi; i++)
-        dst[i] = (T)sp[i];
-    }
-    for (int64_t i = lo; i < hi; i++) {
-      const int32_t v = s->valley[i], sb = s->sub[i], r = s->region[i];
-      if (v < 0 || v >= nv || sb < 0 || sb >= EMCG_MAX_DEG || r < 0 || r >= EMCG_MAX_REGIONS) {
-        int64_t cur = badIdx.load();
-        while (i < cur && !badIdx.compare_exchange_weak(cur, i)) {
-        }
-        return;
-      }
-      meta[i] = packMeta(v, sb, r);
-    }
-  });
-  EMCG_CHECK_ARG(badIdx.load() == INT64_MAX, "particle %lld: valley/sub/region out of range",
-                 (long long)badIdx.load());
+  if (!b->dBad)
+    EMCG_CUDA(cudaMalloc(&b->dBad, sizeof(unsigned long long)));
+  double *dsrc = static_cast<double *>(b->dStage);
+  int32_t *didx = reinterpret_cast<int32_t *>(dsrc + (size_t)9 * n);
   for (int f = 0; f < 9; f++)
-    EMCG_CUDA(cudaMemcpyAsync((T *)b->dState[f] + base, stage + (size_t)f * n, n * sizeof(T),
+    EMCG_CUDA(cudaMemcpyAsync(dsrc + (size_t)f * n, src[f], n * sizeof(double),
                               cudaMemcpyHostToDevice, b->stream));
-  EMCG_CUDA(cudaMemcpyAsync(b->dMeta + base, meta, n * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                            b->stream));
+  const int32_t *isrc[3] = {s->valley, s->sub, s->region};
+  for (int f = 0; f < 3; f++)
+    EMCG_CUDA(cudaMemcpyAsync(didx + (size_t)f * n, isrc[f], n * sizeof(int32_t),
+                              cudaMemcpyHostToDevice, b->stream));
+  EMCG_CUDA(cudaMemsetAsync(b->dBad, 0xff, sizeof(unsigned long long), b->stream));
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  stateCheckKernel<<<grid, 256, 0, b->stream>>>(n, didx, b->ensNV[e], b->dBad);
+  stateConvertKernel<T><<<grid, 256, 0, b->stream>>>(stateOf<T>(b), base, n, dsrc, didx, b->dBad);
+  EMCG_CUDA(cudaGetLastError());
+  unsigned long long bad = 0;
+  EMCG_CUDA(cudaMemcpyAsync(&bad, b->dBad, sizeof(bad), cudaMemcpyDeviceToHost, b->stream));
   EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  EMCG_CHECK_ARG(bad == ~0ull, "particle %llu: valley/sub/region out of range", bad);
   return EMCG_OK;
 }
 

@@ -65,7 +65,8 @@ template <class T> struct EnsK {
   T dt;
   T F[3];   // applied force charge x field [N] (particle-particle Coulomb steps)
   T charge; // [C]
-  uint32_t key0, key1, stream, pad_;
+  uint32_t key0, key1, stream;
+  uint32_t floatDraws; // EMCG_ENS_FLOAT_DRAWS: the double engine draws as the float one
 };
 
 struct Tile {
@@ -104,9 +105,14 @@ __device__ __forceinline__ void m_sincos2pi(double u, double *s, double *c) {
   *c = cos(phi);
 }
 __device__ __forceinline__ void m_sincos2pi(float u, float *s, float *c) {
-  // angle in [-pi, pi) keeps the SFU in its accurate range; the azimuth is
-  // uniform either way
-  __sincosf(6.2831853f * (u - 0.5f), s, c);
+  // the angle 2 pi u - pi in [-pi, pi) keeps the SFU in its accurate range;
+  // sin and cos of 2 pi u are their negatives, so a draw gives the same
+  // direction as in the double engine (the float and double engines stay on
+  // the same path when they consume the same numbers)
+  float sm, cm;
+  __sincosf(6.2831853f * (u - 0.5f), &sm, &cm);
+  *s = -sm;
+  *c = -cm;
 }
 
 template <class T> __device__ __forceinline__ T ldg(const T *p) { return __ldg(p); }
@@ -149,13 +155,16 @@ __device__ __forceinline__ double canonical53(uint64_t w) {
 // float:  32-bit words (four per call).
 template <class T> struct PhiloxSrc;
 
+// Double draws: one 64-bit word per draw.  With f32 set (EMCG_ENS_FLOAT_DRAWS)
+// one 32-bit word per draw and exactly the float source's values, widened.
 template <> struct PhiloxSrc<double> {
   uint32_t c0, c1, c2, c3, k0, k1;
   uint64_t b0, b1;
   int nb;
+  bool f32;
   __device__ __forceinline__ void init(uint32_t pid, uint32_t step,
                                        uint32_t stream, uint32_t key0,
-                                       uint32_t key1) {
+                                       uint32_t key1, uint32_t floatDraws = 0) {
     c0 = pid;
     c1 = step;
     c2 = 0;
@@ -163,25 +172,44 @@ template <> struct PhiloxSrc<double> {
     k0 = key0;
     k1 = key1;
     nb = 0;
+    f32 = floatDraws != 0;
+  }
+  __device__ __forceinline__ void block() {
+    uint32_t o[4];
+    philox4x32_10(c0, c1, c2, c3, k0, k1, o);
+    c2++;
+    b0 = (uint64_t)o[0] | ((uint64_t)o[1] << 32);
+    b1 = (uint64_t)o[2] | ((uint64_t)o[3] << 32);
   }
   __device__ __forceinline__ uint64_t word() {
     if (nb == 0) {
-      uint32_t o[4];
-      philox4x32_10(c0, c1, c2, c3, k0, k1, o);
-      c2++;
-      b0 = (uint64_t)o[0] | ((uint64_t)o[1] << 32);
-      b1 = (uint64_t)o[2] | ((uint64_t)o[3] << 32);
+      block();
       nb = 2;
     }
     uint64_t w = (nb == 2) ? b0 : b1;
     nb--;
     return w;
   }
-  __device__ __forceinline__ uint32_t pick(uint32_t n) {
-    return (uint32_t)(word() % (uint64_t)n);
+  // the float source's word sequence: o[0], o[1], o[2], o[3] of each block
+  __device__ __forceinline__ uint32_t word32() {
+    if (nb == 0) {
+      block();
+      nb = 4;
+    }
+    const uint32_t w = nb == 4 ? (uint32_t)b0 : nb == 3 ? (uint32_t)(b0 >> 32)
+                     : nb == 2 ? (uint32_t)b1 : (uint32_t)(b1 >> 32);
+    nb--;
+    return w;
   }
-  __device__ __forceinline__ double u01() { return canonical53(word()); }
+  __device__ __forceinline__ uint32_t pick(uint32_t n) {
+    return f32 ? __umulhi(word32(), n) : (uint32_t)(word() % (uint64_t)n);
+  }
+  __device__ __forceinline__ double u01() {
+    return f32 ? (double)((float)(word32() >> 8) * 0x1p-24f) : canonical53(word());
+  }
   __device__ __forceinline__ double ulog() {
+    if (f32)
+      return (double)fmaf((float)(word32() >> 8) * 0x1p-24f, 1.f - 1e-6f, 1e-6f);
     return __dadd_rn(__dmul_rn(canonical53(word()), 1. - 1e-6), 1e-6);
   }
   __device__ __forceinline__ bool failed() const { return false; }
@@ -194,7 +222,7 @@ template <> struct PhiloxSrc<float> {
   int nb;
   __device__ __forceinline__ void init(uint32_t pid, uint32_t step,
                                        uint32_t stream, uint32_t key0,
-                                       uint32_t key1) {
+                                       uint32_t key1, uint32_t = 0) {
     c0 = pid;
     c1 = step;
     c2 = 0;

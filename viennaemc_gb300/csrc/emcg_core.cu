@@ -36,6 +36,21 @@ extern "C" const char *emcg_last_error(void) {
 
 extern "C" int32_t emcg_version(void) { return 100; }
 
+extern "C" int32_t emcg_host_alloc(int64_t bytes, void **ptr) {
+  EMCG_CHECK_ARG(ptr && bytes >= 0, "bad host allocation request");
+  *ptr = nullptr;
+  if (bytes == 0)
+    return EMCG_OK;
+  EMCG_CUDA(cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocDefault));
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_host_free(void *ptr) {
+  if (ptr)
+    EMCG_CUDA(cudaFreeHost(ptr));
+  return EMCG_OK;
+}
+
 extern "C" int32_t emcg_update_rates(emcg_handle *h, int32_t model, const double *raw,
                                      int32_t raw_on_device) {
   EMCG_CHECK_ARG(h, "handle is NULL");
