@@ -147,6 +147,7 @@ def run_engine(args):
         obs_all.append(b.step(ns))
         kernel_ms += b.last_kernel_ms()
         done += ns
+    args.block_used = b.launch()["block_threads"]
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
@@ -308,13 +309,19 @@ def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units,
     bpp = BYTES_PER_PARTICLE_STEP["fp32"]
     achieved = bpp * value / 1e9  # algorithmic GB/s (72 B per particle-step)
     kernel = {0: "lockstep", 1: "block-queued", 2: "warp-asynchronous"}[args.scatter_mode]
-    traffic = _profiled_traffic(N, kernel)
+    ns_launch = min(per, K)  # steps of each timed launch
+    prof = _profiled(kernel, ns_launch)
+    traffic = prof["dram_bytes_per_electron"] * N if prof else None
+    sms, sm_mhz = _sm_count(), (clocks or {}).get("sm_mhz") or 2070.0
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "bulk Si, 2^20 electrons, 1e6 V/m <100>, dt 1 fs, 5000 steps",
-                   "particles": N, "steps_per_launch": per, "block_threads": args.block,
+        "config": {"workload": "bulk Si, 2^20 electrons, 1e6 V/m <100>, dt 1 fs (the "
+                               "5000-step configuration; the timed steps below)",
+                   "particles": N, "steps_timed": K, "launches_timed": n_launch,
+                   "steps_per_launch": ns_launch,
+                   "block_threads": getattr(args, "block_used", args.block),
                    "min_blocks_per_sm": args.min_blocks,
                    "scatter_kernel": kernel,
                    "pass_actions": getattr(args, "pass_actions_used", None),
@@ -327,10 +334,22 @@ def _report(args, ws, rank, N, K, W, per, ms, value, n_launch, e2e_s, e2e_units,
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_src,
                      "bytes_per_unit": bpp, "unit_of_work": "particle-step",
-                     "algorithmic_bytes_per_launch": bpp * N * per,
-                     "traffic_per": "launch of steps_per_launch steps"},
+                     "algorithmic_bytes_per_launch": bpp * N * ns_launch,
+                     "traffic_per": "timed launch (steps_per_launch steps), from the ncu "
+                                    "capture of the closest launch length",
+                     "traffic_source": prof["source"] if prof else None},
         "wall_s": wall,
     }
+    if prof:
+        # the kernel's real limit: instruction issue (one warp instruction per
+        # scheduler and cycle, four schedulers per SM)
+        ipu = prof["warp_instructions_per_particle_step"]
+        ipeak = sms * 4 * sm_mhz * 1e6
+        line["roofline_issue"] = {"bound": "issue", "achieved": ipu * value, "peak": ipeak,
+                                  "unit": "warp instructions/s", "frac": ipu * value / ipeak,
+                                  "instructions_per_unit": ipu, "unit_of_work": "particle-step",
+                                  "peak_basis": f"{sms} SMs x 4 schedulers x {sm_mhz:.0f} MHz",
+                                  "source": prof["source"]}
     if value64:
         line["fp64_engine"] = {"value": value64, "unit": UNIT, "steps": k64,
                                "fp32_speedup": value / value64}
@@ -771,17 +790,26 @@ def _host_state(v, N):
     return st
 
 
-def _profiled_traffic(n_electrons, kernel):
-    """DRAM bytes of one bench launch of the bulk kernel, from the committed
-    ncu capture of that kernel (bytes per electron per launch, scaled to this
-    launch); None when no capture of the kernel is committed."""
-    p = os.path.join(ROOT, "profiles", "bulk_step_fp32_traffic.json")
+def _profiled(kernel, steps):
+    """The committed ncu figures of the bulk kernel's launch closest in length
+    to `steps` steps: DRAM bytes per electron per launch (the fused kernel
+    reads and writes the state once per launch) and issued warp instructions
+    per particle-step; None when no capture of the kernel is committed."""
+    p = os.path.join(ROOT, "profiles", "bulk_step_fp32_counters.json")
     try:
         with open(p) as f:
-            k = json.load(f)["kernels"][kernel]
-        return float(k["dram_bytes_per_electron_per_launch"]) * n_electrons
+            caps = json.load(f)["kernels"][kernel]["launches"]
+        return min(caps, key=lambda c: abs(np.log(c["steps"] / max(steps, 1))))
     except (OSError, KeyError, ValueError):
         return None
+
+
+def _sm_count():
+    try:
+        import torch
+        return torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        return 152
 
 
 def cpu_baseline(N, seconds):
@@ -868,7 +896,8 @@ def build_parser():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--n", type=int, default=1 << 20)
     ap.add_argument("--steps-per-launch", type=int, default=500)
-    ap.add_argument("--block", type=int, default=256)
+    ap.add_argument("--block", type=int, default=-1,
+                    help="threads per block (-1: the library's choice for the launch length)")
     ap.add_argument("--min-blocks", type=int, default=4, help="register cap variant (1, 3, 4)")
     ap.add_argument("--pass-actions", type=int, default=None,
                     help="free flights per drift pass of the warp-asynchronous kernel "

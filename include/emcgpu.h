@@ -237,10 +237,15 @@ int32_t emcg_set_replay(emcg_handle *h, const uint64_t *words, int64_t nwords,
 /* Per-launch timing of the last emcg_bulk_step (device milliseconds). */
 int32_t emcg_last_kernel_ms(emcg_handle *h, double *ms);
 
-/* Tuning: threads per block (multiple of 32, <= 1024) and steps fused per
+/* Tuning: threads per block (multiple of 32, <= 1024; -1 = automatic, the
+   default: 256, or 128 for launches of the warp-asynchronous kernel shorter
+   than 100 steps, whose blocks' warps end far apart) and steps fused per
    kernel launch (observables flushed every chunk). 0 keeps the current. */
 int32_t emcg_set_launch(emcg_handle *h, int32_t block_threads,
                         int32_t steps_per_launch);
+/* The block size of the last launch (or the set one) and the steps per
+   launch setting (0: all steps of a call in one launch). */
+int32_t emcg_get_launch(emcg_handle *h, int32_t *block_threads, int32_t *steps_per_launch);
 
 /* Tuning, the step kernel: 0 lockstep (each warp advances its particles
    step by step and handles their events; the default of the double engine);

@@ -159,6 +159,8 @@ def _declare(L):
     L.emcg_last_kernel_ms.argtypes = [vp, P(d)]
     L.emcg_set_launch.restype = i32
     L.emcg_set_launch.argtypes = [vp, i32, i32]
+    L.emcg_get_launch.restype = i32
+    L.emcg_get_launch.argtypes = [vp, C.POINTER(i32), C.POINTER(i32)]
     L.emcg_set_scatter_mode.restype = i32
     L.emcg_set_scatter_mode.argtypes = [vp, i32]
     L.emcg_set_pass_actions.restype = i32

@@ -237,6 +237,12 @@ class BulkBatch:
         if pass_actions is not None:
             L.check(self._lib.emcg_set_pass_actions(self.h, int(pass_actions)))
 
+    def launch(self) -> dict:
+        """Block size of the last launch and the steps-per-launch setting."""
+        blk, per = C.c_int32(), C.c_int32()
+        L.check(self._lib.emcg_get_launch(self.h, C.byref(blk), C.byref(per)))
+        return {"block_threads": blk.value, "steps_per_launch": per.value}
+
     def pass_actions(self) -> int:
         """Free flights per drift pass of the warp-asynchronous kernel."""
         n = C.c_int32()

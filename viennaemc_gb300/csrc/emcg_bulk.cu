@@ -997,6 +997,7 @@ struct BulkImpl {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int blockThreads = 256;
+  bool autoBlock = true; // block size chosen per launch (emcg_set_launch, -1)
   int minBlocks = 1; // register cap variant of the step kernel (1, 3 or 4)
   int queued = 0; // step kernel: 0 lockstep, 1 block-queued, 2 warp-asynchronous (float)
   int passActions = kPassActions; // warp-asynchronous kernel: free flights per drift pass
@@ -1359,10 +1360,27 @@ static int32_t coulombStepTyped(BulkImpl *b, int nSteps, uint32_t step0, double 
   return readError(b);
 }
 
+// Launches of the warp-asynchronous kernel shorter than this run in 128-thread
+// blocks when the block size is automatic.  A block keeps its SM resources
+// until its slowest warp ends, and over few steps the warps of a block end far
+// apart: measured on 2^20 electrons, 20-step launches took 0.312 ms in blocks
+// of 128 threads (0.311 in 64) against 0.334 ms in 256; 100-step launches were
+// even; 500-step launches took 5.81 ms in 128 against 5.64 ms in 256.
+constexpr int kShortLaunchSteps = 100;
+
 template <class T>
 static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHost) {
   if (b->coulomb) // set_coulomb and set_replay exclude each other
     return coulombStepTyped<T>(b, nSteps, step0, obsHost);
+  if (b->autoBlock) {
+    const bool asyncK = b->queued == 2 && sizeof(T) == 4 && !b->replay;
+    const int first = std::min(b->stepsPerLaunch > 0 ? b->stepsPerLaunch : nSteps, nSteps);
+    const int want = asyncK && first < kShortLaunchSteps ? 128 : 256;
+    if (want != b->blockThreads) {
+      b->blockThreads = want;
+      b->tilesDirty = true;
+    }
+  }
   EMCG_TRY(ensureTiles(b));
   const int Q = b->nVmax * 3;
   int per = b->stepsPerLaunch > 0 ? b->stepsPerLaunch : nSteps;
@@ -1928,17 +1946,31 @@ extern "C" int32_t emcg_set_launch(emcg_handle *h, int32_t block_threads,
                                    int32_t steps_per_launch) {
   BulkImpl *b;
   EMCG_TRY(bulkOf(h, &b));
-  if (block_threads) {
+  if (block_threads == -1) {
+    b->autoBlock = true;
+  } else if (block_threads) {
     EMCG_CHECK_ARG(block_threads % 32 == 0 && block_threads >= 32 && block_threads <= 1024,
-                   "block_threads must be a multiple of 32 in [32, 1024]");
+                   "block_threads must be -1 or a multiple of 32 in [32, 1024]");
     if (block_threads != b->blockThreads)
       b->tilesDirty = true;
     b->blockThreads = block_threads;
+    b->autoBlock = false;
   }
   if (steps_per_launch) {
     EMCG_CHECK_ARG(steps_per_launch > 0, "steps_per_launch must be positive");
     b->stepsPerLaunch = steps_per_launch;
   }
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_get_launch(emcg_handle *h, int32_t *block_threads,
+                                   int32_t *steps_per_launch) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  if (block_threads)
+    *block_threads = b->blockThreads;
+  if (steps_per_launch)
+    *steps_per_launch = b->stepsPerLaunch;
   return EMCG_OK;
 }
 
@@ -2039,6 +2071,7 @@ extern "C" int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint3
   constexpr int kCands = sizeof(cands) / sizeof(cands[0]);
   const int nCands = b->precision == EMCG_FP32 ? kCands : 8; // mode 2 is float only
   const int keepPer = b->stepsPerLaunch, keepPass = b->passActions;
+  b->autoBlock = false; // the tuner sets the block size
   b->stepsPerLaunch = trial_steps;
   double ms[kCands] = {};
   uint32_t s = step0;
