@@ -18,7 +18,14 @@
 //   emcgpu::DeviceDesc, emcgpu::GpuDeviceSimulation
 //                            a 2-D reference emcDevice as the engine's device
 //                            description, and emcSimulation's equilibrium /
-//                            performEMCStep on the GPU.
+//                            performEMCStep on the GPU, the engine's fast
+//                            path (every grid stays on the GPU).
+//   emcgpu::GpuEngine, GpuPMScheme, GpuPoissonSolver, GpuParticleHandler
+//                            plugins of the reference's own interfaces
+//                            (emcAbstractPMScheme, emcAbstractSolver,
+//                            emcAbstractParticleHandler), so that the stock
+//                            emcSimulation runs on the GPU with its template
+//                            arguments swapped and nothing else changed.
 //
 // Every status returned by the C ABI other than EMCG_OK is turned into the
 // reference's own error path (emcMessage::addError, which aborts).
@@ -35,7 +42,17 @@
 #include <tuple>
 #include <vector>
 
+#include <fstream>
+#include <iostream>
+
+#include <PMSchemes/emcAbstractPMScheme.hpp>
+#include <PMSchemes/emcCICScheme.hpp>
+#include <PMSchemes/emcNECScheme.hpp>
+#include <PMSchemes/emcNGPScheme.hpp>
+#include <ParticleHandler/emcAbstractParticleHandler.hpp>
 #include <ParticleType/emcParticleType.hpp>
+#include <PoissonSolver/emcAbstractSolver.hpp>
+#include <emcParticleInitialization.hpp>
 #include <ScatterMechanisms/emcAcousticScatterMechanism.hpp>
 #include <ScatterMechanisms/emcCoulombScatterMechanism.hpp>
 #include <ScatterMechanisms/emcFirstOrderInterValleyScatterMechanism.hpp>
@@ -490,6 +507,386 @@ private:
   emcg_handle *h_ = nullptr;
   int nc_ = 0;
   uint32_t step_ = 0;
+};
+
+// ---------------------------------------------------------------------------
+// Plugins of the reference's interfaces for its stock emcSimulation
+// (include/emcSimulation.hpp:28-47 static_asserts these bases):
+//
+//   using Engine  = emcgpu::GpuEngine<T, Dev>;
+//   using PM      = emcgpu::GpuPMScheme<T, Dev, emcNGPScheme<T, Dev>>;
+//   using Handler = emcgpu::GpuParticleHandler<T, Dev, PM>;
+//   using Solver  = emcgpu::GpuPoissonSolver<T, Dev, Handler>;
+//   emcSimulation<T, Dev, Solver, Handler, PM> simulation(param, device, solver, pm);
+//
+// The three share one device engine (GpuEngine), created at its first use.
+// The host grids emcSimulation passes between them (potential, field,
+// particle counts, concentration) cross the boundary at every call, so the
+// reference's results, averages and output files are its own; the particles
+// stay on the GPU.  The initial particles are made by the reference's
+// emcAbstractParticleHandler::generateInitialParticles (its counts and its
+// random-number stream) through addParticle, and uploaded before the first
+// move; moves, contacts and injection then run on the GPU engine.
+// ---------------------------------------------------------------------------
+
+// EMCG_PM_* of a reference PM scheme class
+template <class S> struct PmKindOf {
+  static constexpr int value = -1;
+};
+template <class T, class D> struct PmKindOf<emcNGPScheme<T, D>> {
+  static constexpr int value = EMCG_PM_NGP;
+};
+template <class T, class D> struct PmKindOf<emcCICScheme<T, D>> {
+  static constexpr int value = EMCG_PM_CIC;
+};
+template <class T, class D> struct PmKindOf<emcNECScheme<T, D>> {
+  static constexpr int value = EMCG_PM_NEC;
+};
+
+// The device engine behind the plugins: one particle type (index 0) on a 2-D
+// device.  cfg: dt (= emcSimulationParameter's step time), Poisson settings,
+// capacity (0: from the device's doping); the PM scheme, charge, seed and
+// carriers per particle are set by the plugins.
+template <class T, class DeviceType> class GpuEngine {
+public:
+  using Grid = emcGrid<T, 2>;
+
+  GpuEngine(const DeviceType &device, ModelBuilder<T, DeviceType> &model, emcg_device_config cfg,
+            int precision = EMCG_FP32)
+      : dd_(device), model_(model), cfg_(cfg), precision_(precision) {
+    if (cfg_.capacity == 0) { // 1.6 x the doping's carriers, as the Python host
+      double sum = 0;
+      const emcg_device_desc &d = dd_.desc();
+      for (int i = 0; i < d.nx * d.ny; i++)
+        sum += std::abs(d.doping[i]);
+      cfg_.capacity = (int64_t)(1.6 * std::max(sum, 1.) * device.getCellVolume()) + 4096;
+    }
+  }
+  ~GpuEngine() {
+    if (h_)
+      emcg_destroy(h_);
+  }
+  GpuEngine(const GpuEngine &) = delete;
+  GpuEngine &operator=(const GpuEngine &) = delete;
+
+  // settings, before the engine's first use
+  emcg_device_config &config() {
+    if (h_)
+      emcMessage::getInstance()
+          .addError("libemcgpu: the engine's settings are fixed at its first use")
+          .print();
+    return cfg_;
+  }
+
+  emcg_handle *handle() {
+    if (!h_) {
+      cfg_.charge = model_.particleType().getCharge();
+      const emcg_model_desc &md = model_.desc();
+      check(emcg_device_create(&md, &dd_.desc(), &cfg_, precision_, &h_));
+    }
+    return h_;
+  }
+  const emcg_device_config &settings() const { return cfg_; }
+  int nContacts() const { return dd_.desc().n_contacts; }
+
+  void toGrid(int which, const Grid &g) {
+    buf_.assign(g.begin(), g.end());
+    check(emcg_device_set_grid(handle(), which, buf_.data()));
+  }
+  void fromGrid(int which, Grid &g) {
+    buf_.resize(g.getSize());
+    check(emcg_device_get_grid(handle(), which, buf_.data()));
+    std::copy(buf_.begin(), buf_.end(), g.begin());
+  }
+
+  uint32_t step = 0; // Philox step counter of moves and injection
+
+private:
+  DeviceDesc<T, DeviceType> dd_;
+  ModelBuilder<T, DeviceType> &model_;
+  emcg_device_config cfg_;
+  int precision_;
+  emcg_handle *h_ = nullptr;
+  std::vector<double> buf_;
+};
+
+// emcAbstractPMScheme on the GPU engine: the field from the potential
+// (calcEField, include/PMSchemes/emcEFieldCalculation.hpp) on the GPU; the
+// single-particle host methods (assignToMesh, interpolateForce), which
+// emcSimulation itself never calls, from the reference scheme HostScheme.
+// Copies share the engine (emcSimulation keeps a copy).
+template <class T, class DeviceType, class HostScheme, int Kind = PmKindOf<HostScheme>::value>
+class GpuPMScheme : public emcAbstractPMScheme<T, DeviceType> {
+  static_assert(Kind >= 0, "give the engine's EMCG_PM_* kind of this PM scheme");
+  static constexpr SizeType Dim = DeviceType::Dimension;
+
+public:
+  using Engine = GpuEngine<T, DeviceType>;
+
+  explicit GpuPMScheme(std::shared_ptr<Engine> engine, HostScheme host = HostScheme())
+      : engine_(std::move(engine)), host_(std::move(host)) {
+    engine_->config().pm_scheme = Kind;
+  }
+
+  void assignToMesh(const std::array<T, Dim> &pos, SizeType nrCarriers,
+                    const std::array<T, Dim> &spacing,
+                    emcGrid<T, Dim> &grid) const override {
+    host_.assignToMesh(pos, nrCarriers, spacing, grid);
+  }
+  void assignToMesh(const std::vector<std::array<T, Dim>> &position, SizeType nrCarriers,
+                    const std::array<T, Dim> &spacing,
+                    emcGrid<T, Dim> &grid) const override {
+    host_.assignToMesh(position, nrCarriers, spacing, grid);
+  }
+  std::array<T, 3> interpolateForce(const std::vector<emcGrid<T, Dim>> &eField,
+                                    const std::array<T, Dim> &pos,
+                                    const std::array<T, Dim> &spacing,
+                                    T charge) const override {
+    return host_.interpolateForce(eField, pos, spacing, charge);
+  }
+  // the potential to the engine, its field back into eField
+  void calcEField(std::vector<emcGrid<T, Dim>> &eField, const emcGrid<T, Dim> &potential,
+                  const DeviceType &) const override {
+    engine_->toGrid(EMCG_GRID_POTENTIAL, potential);
+    check(emcg_device_efield(engine_->handle()));
+    engine_->fromGrid(EMCG_GRID_EX, eField[0]);
+    engine_->fromGrid(EMCG_GRID_EY, eField[1]);
+  }
+
+  std::shared_ptr<Engine> engine() const { return engine_; }
+
+private:
+  std::shared_ptr<Engine> engine_;
+  HostScheme host_;
+};
+
+// emcAbstractSolver on the GPU engine: the multigrid / double-precision
+// defect-correction solve of the reference's discrete equation
+// (include/PoissonSolver/emcSORSolver.hpp:49-197), on the potential and
+// concentration that emcSimulation hands over.
+template <class T, class DeviceType, class ParticleHandler>
+class GpuPoissonSolver : public emcAbstractSolver<T, DeviceType, ParticleHandler> {
+  using GridType = typename emcAbstractSolver<T, DeviceType, ParticleHandler>::GridType;
+
+public:
+  using Engine = GpuEngine<T, DeviceType>;
+
+  explicit GpuPoissonSolver(std::shared_ptr<Engine> engine) : engine_(std::move(engine)) {}
+
+  void calcEquilibriumPotential(GridType &pot, const DeviceType &, bool resetBC = true) override {
+    engine_->toGrid(EMCG_GRID_POTENTIAL, pot);
+    double rel = 0;
+    int32_t cycles = 0;
+    check(emcg_device_poisson(engine_->handle(), 1, resetBC ? 1 : 0, &rel, &cycles));
+    engine_->fromGrid(EMCG_GRID_POTENTIAL, pot);
+  }
+  void calcNonEquilibriumPotential(GridType &pot, const DeviceType &, const GridType &eConc,
+                                   bool resetBC = true) override {
+    engine_->toGrid(EMCG_GRID_POTENTIAL, pot);
+    engine_->toGrid(EMCG_GRID_CONC, eConc);
+    double rel = 0;
+    int32_t cycles = 0;
+    check(emcg_device_poisson(engine_->handle(), 0, resetBC ? 1 : 0, &rel, &cycles));
+    engine_->fromGrid(EMCG_GRID_POTENTIAL, pot);
+  }
+  // the background potential of the FMM handlers: particle-particle forces
+  // are not part of the device engine
+  void calcBackgroundPotential(GridType &, const DeviceType &, ParticleHandler &,
+                               bool = true) override {
+    emcMessage::getInstance()
+        .addError("libemcgpu: the device engine has no particle-particle (FMM) interaction")
+        .print();
+  }
+
+private:
+  std::shared_ptr<Engine> engine_;
+};
+
+// emcAbstractParticleHandler on the GPU engine, constructed by emcSimulation
+// as it constructs emcBasicParticleHandler
+// (include/ParticleHandler/emcBasicParticleHandler.hpp:51-59): one particle
+// type (index 0) that moves and is injected.
+template <class T, class DeviceType, class PMScheme>
+class GpuParticleHandler : public emcAbstractParticleHandler<T, DeviceType, PMScheme, 2> {
+  using Base = emcAbstractParticleHandler<T, DeviceType, PMScheme, 2>;
+  using typename Base::MapIdxToParticleTypes;
+  using typename Base::NettoParticleCounter;
+  using typename Base::SizeVec;
+  using typename Base::ValueVec;
+
+public:
+  GpuParticleHandler(const DeviceType &device, PMScheme &pmScheme, MapIdxToParticleTypes &types,
+                     SizeType nrCarriersPerParticle, SizeType seed)
+      : Base(device, pmScheme, nrCarriersPerParticle, types, seed),
+        engine_(pmScheme.engine()), spacing_(device.getSpacing()),
+        extent_(device.getGridExtent()) {
+    if (types.size() != 1 || !types.count(0) || !types.at(0)->isMoved())
+      emcMessage::getInstance()
+          .addError("libemcgpu: one moving particle type, with index 0")
+          .print();
+    emcg_device_config &c = engine_->config();
+    c.seed = seed;
+    c.carriers_per_particle = (double)nrCarriersPerParticle;
+  }
+
+  bool calcsPartPartInteraction() const override { return false; }
+
+  SizeType getNrParticles(SizeType = 0) const {
+    return pending_.empty() && engine_ ? (SizeType)emcg_num_particles(engine_->handle(), 0)
+                                       : pending_.size();
+  }
+
+  void printNrParticles() const override {
+    std::cout << "\t" << getNrParticles() << " " << Base::idxTypeToPartType.at(0)->getName()
+              << "\n";
+  }
+
+  void assignParticlesToMesh(SizeType, emcGrid<T, 2> &gridNrParticles) override {
+    upload();
+    check(emcg_device_assign(engine_->handle()));
+    engine_->fromGrid(EMCG_GRID_NRPART, gridNrParticles);
+  }
+
+  // the engine moves its particles in its own field (the one calcEField just
+  // computed from the same potential); removed particles per contact
+  NettoParticleCounter driftScatterParticles(T tStep, std::vector<emcGrid<T, 2>> &) override {
+    upload();
+    if (tStep != engine_->settings().dt)
+      emcMessage::getInstance()
+          .addError("libemcgpu: the step time differs from the engine's dt")
+          .print();
+    auto counter = Base::initNettoParticleCounter();
+    std::vector<int32_t> n((size_t)std::max(engine_->nContacts(), 1), 0);
+    check(emcg_device_move(engine_->handle(), engine_->step, n.data()));
+    for (size_t c = 0; c < counter[0].size(); c++)
+      counter[0][c] = n[c];
+    return counter;
+  }
+
+  // deletion of excess particles and injection at the ohmic contacts on the
+  // GPU; injected minus deleted per contact
+  NettoParticleCounter handleOhmicContacts() override {
+    auto counter = Base::initNettoParticleCounter();
+    std::vector<int32_t> n((size_t)std::max(engine_->nContacts(), 1), 0);
+    check(emcg_device_contacts(engine_->handle(), engine_->step, n.data()));
+    engine_->step++;
+    for (size_t c = 0; c < counter[0].size(); c++)
+      counter[0][c] = n[c];
+    return counter;
+  }
+
+  // the particle dump of emcBasicParticleHandler::print (:194-216)
+  void print(std::string namePrefix, std::string nameSuffix) override {
+    const auto &type = Base::idxTypeToPartType.at(0);
+    const State st = download();
+    std::ofstream os(namePrefix + type->getName() + nameSuffix + ".txt");
+    os << Base::device.getMaxPos() << "\n";
+    for (size_t i = 0; i < st.n; i++) {
+      const std::array<T, 2> pos = {st.px[i], st.py[i]};
+      const std::array<T, 3> k = {st.kx[i], st.ky[i], st.kz[i]};
+      os << i << " " << pos << " " << k << " " << st.energy[i] << " " << st.sub[i] << " "
+         << st.valley[i] << " " << st.tau[i];
+      if (i + 1 < st.n)
+        os << "\n";
+    }
+  }
+
+  // emcBasicParticleHandler::getChannelDriftCurrent (:224-238), from the
+  // downloaded particles
+  T getChannelDriftCurrent(SizeType idxType, T x0, T x1, T channelLength) const {
+    const auto &type = Base::idxTypeToPartType.at(idxType);
+    const State st = download();
+    T sumVx = 0;
+    for (size_t i = 0; i < st.n; i++) {
+      if (st.px[i] < x0 || st.px[i] > x1)
+        continue;
+      const std::array<T, 3> k = {st.kx[i], st.ky[i], st.kz[i]};
+      sumVx += type->getValley(st.valley[i])->getVelocity(k, st.energy[i], st.sub[i])[0];
+    }
+    return constants::q * Base::nrCarriersPerPart * sumVx / channelLength;
+  }
+
+protected:
+  // the reference's particle making (initParticlePos and the particle type's
+  // generateInitialParticle / generateInjectedParticle), kept on the host
+  // until the next call that needs the engine
+  void addParticle(SizeType idxType, const SizeVec &coord, emcRNG &rng,
+                   bool isInitial) override {
+    const std::array<T, 2> pos = initParticlePos(coord, extent_, spacing_, rng);
+    const auto &type = Base::idxTypeToPartType.at(idxType);
+    emcParticle<T> p = isInitial ? type->generateInitialParticle(coord, Base::device, rng)
+                                 : type->generateInjectedParticle(coord, Base::device, rng);
+    pending_.push_back({pos, p});
+  }
+
+private:
+  struct State {
+    size_t n = 0;
+    std::vector<double> kx, ky, kz, px, py, pz, energy, tau, gtau;
+    std::vector<int32_t> valley, sub, region;
+    void resize(size_t m) {
+      n = m;
+      for (auto *v : {&kx, &ky, &kz, &px, &py, &pz, &energy, &tau, &gtau})
+        v->assign(m, 0.);
+      for (auto *v : {&valley, &sub, &region})
+        v->assign(m, 0);
+    }
+    emcg_state desc() {
+      emcg_state s{};
+      s.kx = kx.data();
+      s.ky = ky.data();
+      s.kz = kz.data();
+      s.px = px.data();
+      s.py = py.data();
+      s.pz = pz.data();
+      s.energy = energy.data();
+      s.tau = tau.data();
+      s.grain_tau = gtau.data();
+      s.valley = valley.data();
+      s.sub = sub.data();
+      s.region = region.data();
+      s.n = (int64_t)n;
+      return s;
+    }
+  };
+
+  void upload() {
+    if (pending_.empty())
+      return;
+    State st;
+    st.resize(pending_.size());
+    for (size_t i = 0; i < pending_.size(); i++) {
+      const auto &[pos, p] = pending_[i];
+      st.kx[i] = p.k[0];
+      st.ky[i] = p.k[1];
+      st.kz[i] = p.k[2];
+      st.px[i] = pos[0];
+      st.py[i] = pos[1];
+      st.energy[i] = p.energy;
+      st.tau[i] = p.tau;
+      st.gtau[i] = p.grainTau;
+      st.valley[i] = (int32_t)p.valley;
+      st.sub[i] = (int32_t)p.subValley;
+      st.region[i] = (int32_t)p.region;
+    }
+    const emcg_state s = st.desc();
+    check(emcg_set_state(engine_->handle(), 0, &s));
+    pending_.clear();
+  }
+
+  State download() const {
+    State st;
+    const int64_t n = emcg_num_particles(engine_->handle(), 0);
+    st.resize((size_t)std::max<int64_t>(n, 0));
+    emcg_state s = st.desc();
+    check(emcg_get_state(engine_->handle(), 0, &s));
+    return st;
+  }
+
+  std::shared_ptr<GpuEngine<T, DeviceType>> engine_;
+  ValueVec spacing_;
+  SizeVec extent_;
+  std::vector<std::pair<std::array<T, 2>, emcParticle<T>>> pending_;
 };
 
 } // namespace emcgpu

@@ -1,16 +1,30 @@
-"""The C++ drop-in adapter (include/emcgpu_reference.hpp) against the Python
-host builder: compiled with the reference's headers where the reference tree
-is present (it is not on GPU hosts), it must produce the same engine
-descriptor from the reference's own mechanism classes."""
+"""The C++ drop-in adapter (include/emcgpu_reference.hpp), compiled with the
+reference's headers where the reference tree is present (it is not on GPU
+hosts; oracle/Makefile names where it is):
+
+* against the Python host builder: the same engine descriptor from the
+  reference's own mechanism classes and device;
+* the plugins of the reference's interfaces under its stock emcSimulation,
+  run against a recording stand-in of libemcgpu: the reference's step loop
+  calls the engine in the reference's order and the engine's results reach
+  the reference's results and output files.
+"""
 import os
 import subprocess
 
 import numpy as np
 import pytest
 
-from conftest import ROOT
+from conftest import ROOT, golden
 
-REF = os.environ.get("VIENNAEMC_INCLUDE", "/root/reference")
+
+def _reference_tree():
+    out = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "print-ref"],
+                         capture_output=True, text=True)
+    return out.stdout.strip() if out.returncode == 0 else ""
+
+
+REF = _reference_tree()
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include")),
@@ -114,3 +128,76 @@ def test_adapter_raw_rates_match_host_refill(tmp_path):
     assert len(lines) == (n + 88) // 89
     for _, i, v in lines:
         assert float.fromhex(v) == raw[int(i)], i
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include")),
+                    reason="reference headers not available")
+def test_stock_emcsimulation_runs_on_the_gpu_plugins(tmp_path):
+    """emcSimulation<T, emcDevice<T, 2>, GpuPoissonSolver, GpuParticleHandler,
+    GpuPMScheme> compiles (its static_asserts accept the plugin bases) and its
+    execute() runs through the plugins (tests/adapter/emcsim_plugins.cpp, the
+    fixtures' 21 x 11-node resistor, seed 42, 6 steps of which 2 transient).
+    Against the recording stand-in (tests/adapter/stub_emcgpu.cpp):
+    - the engine is created once, with the NGP scheme, the step time, the seed
+      and the particle type's charge;
+    - the initial particles are the reference's own (its counts and random
+      stream through addParticle): the particle dump of the plugin handler
+      equals the reference's initial electrons of the fixture;
+    - every step calls Poisson (reset only in the first), the field, move,
+      contacts and assignment in emcSimulation::performEMCStep's order, with
+      the step counter advancing;
+    - the concentration the solver hands over is the reference's own
+      (updateCurrentParticleConcentrations of the engine's 2 particles per
+      node), and the potentials follow the engine's values;
+    - the current file carries the engine's netto counts (removed 3 - c minus
+      injected c + 1) and the reference's running current."""
+    stub = tmp_path / "stub"
+    stub.mkdir()
+    inc = os.path.join(ROOT, "include")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-w", "-shared", "-fPIC", f"-I{inc}",
+                    os.path.join(ROOT, "tests", "adapter", "stub_emcgpu.cpp"), "-o",
+                    str(stub / "libemcgpu.so")], check=True)
+    exe = tmp_path / "emcsim_plugins"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-w", f"-I{REF}/include", f"-I{inc}",
+                    os.path.join(ROOT, "tests", "adapter", "emcsim_plugins.cpp"), "-o", str(exe),
+                    f"-L{stub}", "-lemcgpu", f"-Wl,-rpath,{stub}"], check=True)
+    log = tmp_path / "calls.txt"
+    env = dict(os.environ, EMCG_STUB_LOG=str(log))
+    subprocess.run([str(exe), "res", "6"], cwd=tmp_path, env=env, check=True,
+                   capture_output=True)
+    calls = [l.split() for l in log.read_text().splitlines()]
+    create = [c for c in calls if c[0] == "create"]
+    assert len(create) == 1
+    kv = dict(x.split("=") for x in create[0][4:])
+    assert create[0][1:4] == ["21", "11", "2"] and kv["pm"] == "0" and kv["seed"] == "42"
+    assert float.fromhex(kv["dt"]) == 1e-15 and float.fromhex(kv["charge"]) == -1.60219e-19
+    # the initial electrons: the reference's own (tests/golden, seed 42)
+    g = golden("device_resistor_ngp.npz")
+    states = [c for c in calls if c[0] == "state"]
+    assert len(states) == 1 and int(states[0][2]) == len(g["s0_E"])
+    dump = np.loadtxt(tmp_path / "resElectronsEq.txt", skiprows=1)
+    assert dump.shape[0] == len(g["s0_E"])
+    for col, f in ((1, "px"), (2, "py"), (3, "kx"), (4, "ky"), (5, "kz"), (6, "E"), (9, "tau")):
+        assert np.allclose(dump[:, col], g[f"s0_{f}"], rtol=6e-6, atol=0), f  # 6 digits
+    assert np.array_equal(dump[:, 7].astype(int), g["s0_sub"])
+    # the step loop, in performEMCStep's order
+    seq = [c[0] if c[0] not in ("poisson", "move", "contacts", "set", "get") else " ".join(c[:2])
+           + (" " + c[2] if c[0] == "poisson" else "") for c in calls]
+    first = seq.index("move 0")
+    step = ["set 0", "set 4", "poisson 0 1", "get 0", "set 0", "efield", "get 1", "get 2",
+            "move 0", "contacts 0", "assign", "get 3"]
+    assert seq[first - 8:first + 4] == step
+    for s in range(1, 6):
+        i = seq.index(f"move {s}")
+        assert seq[i - 8:i + 4] == [x.replace("poisson 0 1", "poisson 0 0")
+                                    .replace("move 0", f"move {s}")
+                                    .replace("contacts 0", f"contacts {s}") for x in step]
+    assert "move 6" not in seq
+    # the concentration from 2 particles per node, interior node 118
+    conc = [float.fromhex(c[3]) for c in calls if c[:2] == ["set", "4"]]
+    assert len(conc) == 6 and np.allclose(conc, 2 / (1e-9 * 1e-9 * 3e-7) / 1.45e16, rtol=1e-12)
+    # the current file: time, netto per contact, running current per contact
+    cur = np.loadtxt(tmp_path / "resElectronsCurrent.txt")
+    assert cur.shape == (4, 5)
+    assert np.array_equal(cur[:, 1:3], np.tile([2, 0], (4, 1)))
+    assert np.allclose(cur[:, 3], 2 * -1.60219e-19 / 1e-15, rtol=1e-5) and np.all(cur[:, 4] == 0)
