@@ -401,3 +401,46 @@ def test_step_reports_a_solve_that_missed_its_target(engine):
     sim.performEMCStep(2)  # the handle stays usable
     assert sim.num_particles() > 0
     sim.close()
+
+
+def test_deposition_is_reproducible_bit_for_bit(engine):
+    """The 201 x 101 resistor with about 5e5 electrons (CIC, FP32), 20 steps
+    from the same seed, twice: the deposition sums fixed-point weights with
+    integer atomics, so the assigned charge, the concentration and the
+    potential are equal bit for bit, whatever order the atomics ran in; and
+    the assigned charge equals a host sum of the same particles' CIC weights
+    to within float rounding."""
+    from viennaemc_gb300 import _lib as L
+    from viennaemc_gb300 import device as D
+    from viennaemc_gb300 import physics as P
+    out = []
+    for _ in range(2):
+        dev = _resistor_201x101()
+        pt = P.silicon_electron("refbulk", n_levels=1000, max_energy=4.0, regions=[0],
+                                coulomb=True, region_doping=dev.getDopingRegionDoping)
+        sim = D.DeviceSimulation(dev, pt, scheme=D.CIC, dt=1e-16, seed=77, precision="fp32",
+                                 poisson_rtol=1e-8, poisson_max_cycles=60)
+        sim.calcEquilibriumCharacteristics()
+        sim.performEMCStep(20)
+        out.append((sim.get_grid(L.GRID_NRPART), sim.concentration, sim.potential,
+                    sim.get_state()))
+        sim.close()
+    (nr, conc, pot, st), (nr2, conc2, pot2, _) = out
+    assert st.n > 400000
+    assert np.array_equal(nr, nr2) and np.array_equal(conc, conc2) and np.array_equal(pot, pot2)
+    # the reference's CIC weights (the lower node gets w = pos / h - floor,
+    # emcCICScheme.hpp:30-66) summed on the host
+    h = 0.5e-9
+    px, py = st.px.astype(np.float32), st.py.astype(np.float32)
+    fx, fy = px * np.float32(1.0 / h), py * np.float32(1.0 / h)  # as the float engine
+    mx, my = np.floor(fx).astype(int), np.floor(fy).astype(int)
+    wx, wy = (fx - mx).astype(np.float64), (fy - my).astype(np.float64)
+    ref = np.zeros((101, 201))
+    for dx, dy, w in ((0, 0, wx * wy), (1, 0, (1 - wx) * wy), (0, 1, wx * (1 - wy)),
+                      (1, 1, (1 - wx) * (1 - wy))):
+        x, y = mx + dx, my + dy
+        ok = (x >= 0) & (x < 201) & (y >= 0) & (y < 101)
+        np.add.at(ref, (y[ok], x[ok]), w[ok])
+    # the float engine forms its weights in float
+    assert np.allclose(nr.reshape(101, 201), ref, rtol=0, atol=2e-6), \
+        np.abs(nr.reshape(101, 201) - ref).max()
