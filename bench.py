@@ -176,24 +176,25 @@ def run_engine(args):
 
 
 def _e2e(v, pt, spec, args, N, K):
-    """End to end through the C ABI: host state in, per-step observables out."""
+    """End to end through the C ABI: the host state in, in the float engine's
+    own layout in page-locked memory, per-step observables out."""
     import torch
-    from viennaemc_gb300.bulk import BulkBatch
-    st = _host_state(v, N)
+    from viennaemc_gb300.bulk import BulkBatch, ParticleStateF32
+    st = ParticleStateF32.from_state(_host_state(v, N), pinned=True)
     b2 = BulkBatch([pt], [spec], "fp32")
     b2.set_launch(args.block, args.steps_per_launch, args.min_blocks,
                   pass_actions=args.pass_actions)
     # warm-up through the same calls (untimed): first-call staging allocation
-    b2.set_state(0, st)
+    b2.set_state_f32(0, st)
     b2.step(max(args.warmup, 3))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    b2.set_state(0, st)
+    b2.set_state_f32(0, st)
     o2 = b2.step(K)
     e2e_s = time.perf_counter() - t0
     b2.close()
     e2e_units = float(N) * K
-    h2d = N * (9 * 8 + 3 * 4) / K
+    h2d = N * (9 * 4 + 4) / K
     d2h = o2.shape[-2] * 3 * 8
     return e2e_s, e2e_units, h2d, d2h
 

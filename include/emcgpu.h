@@ -204,6 +204,25 @@ int32_t emcg_set_state(emcg_handle *h, int32_t ens, const emcg_state *s);
 int32_t emcg_get_state(emcg_handle *h, int32_t ens, emcg_state *s);
 int64_t emcg_num_particles(emcg_handle *h, int32_t ens);
 
+/* The same for a bulk engine in the float engine's own layout (no reference
+   counterpart): float fields and one packed word per particle,
+   meta = valley | subvalley << 8 | region << 16.  40 bytes per particle cross
+   the host link instead of 84, a host that keeps its ensembles in floats
+   uploads them at half the cost (a double engine widens them).  The check of
+   emcg_set_state applies: a field out of range is refused with the first bad
+   particle's index and nothing is written. */
+typedef struct {
+  float *kx, *ky, *kz;
+  float *px, *py, *pz;
+  float *energy;
+  float *tau;
+  float *grain_tau;
+  uint32_t *meta;
+  int64_t n;
+} emcg_state_f32;
+int32_t emcg_set_state_f32(emcg_handle *h, int32_t ens, const emcg_state_f32 *s);
+int32_t emcg_get_state_f32(emcg_handle *h, int32_t ens, emcg_state_f32 *s);
+
 /* Generate n initial particles of ensemble e on the GPU (Philox stream
    (seed, stream), counter = (particle, 0xFFFFFFFF, call, stream)):
    emcElectron::generateInitialParticle + initParticlePos

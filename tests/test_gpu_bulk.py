@@ -672,3 +672,39 @@ def test_state_upload_checks_indices_and_keeps_the_old_state(engine, precision):
     now = b.get_state(0)
     assert np.array_equal(now.kx, st.kx * 0.5) and np.array_equal(now.sub, st.sub)
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_float_layout_state_upload(engine, precision):
+    """emcg_set_state_f32 / emcg_get_state_f32: the float engine's own layout
+    (float fields, packed meta) uploads the same electrons as emcg_set_state
+    with doubles, so the steps that follow give the same states; a packed
+    subvalley out of range is refused and leaves the ensemble as it was."""
+    pt = engine.physics.silicon_electron("jacoboni")
+    spec = engine.EnsembleSpec(0, 3000, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 9, 0)
+    src = engine.BulkBatch([pt], [spec], "fp32")
+    src.init_particles(0)
+    st = src.get_state(0)
+    f32 = src.get_state_f32(0)
+    src.close()
+    assert np.array_equal(f32.kx, st.kx.astype(np.float32))
+    assert np.array_equal(f32.meta & 0xff00, (st.sub.astype(np.uint32) << 8))
+    outs = []
+    for how in ("f64", "f32"):
+        b = engine.BulkBatch([pt], [spec], precision)
+        if how == "f64":
+            b.set_state(0, st)
+        else:
+            b.set_state_f32(0, engine.ParticleStateF32.from_state(st, pinned=True))
+        b.step(30)
+        outs.append(b.get_state(0))
+        bad = engine.ParticleStateF32.from_state(st)
+        bad.meta[5] |= 9 << 8
+        with pytest.raises(engine._lib.EmcgError) as ei:
+            b.set_state_f32(0, bad)
+        assert ei.value.status == -1 and "particle 5" in str(ei.value)
+        after = b.get_state(0)
+        assert np.array_equal(after.kx, outs[-1].kx) and np.array_equal(after.sub, outs[-1].sub)
+        b.close()
+    for f in ("kx", "ky", "kz", "energy", "px", "tau"):
+        assert np.array_equal(getattr(outs[0], f), getattr(outs[1], f)), f

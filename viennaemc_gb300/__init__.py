@@ -13,7 +13,7 @@ from .physics import (Electron, NonParabolicAnisotropValley, AcousticScatterMech
                       FirstOrderInterValleyEmissionScatterMechanism, CoulombScatterMechanism,
                       silicon_electron, silicon_material, thermal_voltage)
 from .bulk import (BulkBatch, BulkParticleHandler, EnsembleSpec, FMMBulkParticleHandler,
-                   ParticleState)
+                   ParticleState, ParticleStateF32)
 
 build = _lib.build
 __all__ = ["Electron", "NonParabolicAnisotropValley", "AcousticScatterMechanism",

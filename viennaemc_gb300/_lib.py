@@ -111,6 +111,12 @@ class EnsembleDesc(C.Structure):
                 ("stream", C.c_uint32), ("flags", C.c_uint32)]
 
 
+class StateF32Desc(C.Structure):
+    _fields_ = [(n, C.POINTER(C.c_float)) for n in
+                ("kx", "ky", "kz", "px", "py", "pz", "energy", "tau", "grain_tau")] + \
+               [("meta", C.POINTER(C.c_uint32)), ("n", C.c_int64)]
+
+
 class StateDesc(C.Structure):
     _fields_ = [(n, C.POINTER(C.c_double)) for n in
                 ("kx", "ky", "kz", "px", "py", "pz", "energy", "tau", "grain_tau")] + \
@@ -147,6 +153,10 @@ def _declare(L):
     L.emcg_set_state.argtypes = [vp, i32, P(StateDesc)]
     L.emcg_get_state.restype = i32
     L.emcg_get_state.argtypes = [vp, i32, P(StateDesc)]
+    L.emcg_set_state_f32.restype = i32
+    L.emcg_set_state_f32.argtypes = [vp, i32, P(StateF32Desc)]
+    L.emcg_get_state_f32.restype = i32
+    L.emcg_get_state_f32.argtypes = [vp, i32, P(StateF32Desc)]
     L.emcg_num_particles.restype = i64
     L.emcg_num_particles.argtypes = [vp, i32]
     L.emcg_bulk_init.restype = i32

@@ -81,6 +81,45 @@ class ParticleState:
         return d
 
 
+class ParticleStateF32:
+    """Host particle state in the float engine's own layout (emcg_state_f32):
+    float fields and meta = valley | subvalley << 8 | region << 16, 40 bytes a
+    particle; pinned: one page-locked block (emcg_host_alloc)."""
+
+    def __init__(self, n: int, pinned: bool = False):
+        self.n = int(n)
+        nb = self.n * (4 * len(STATE_F) + 4)
+        if pinned and self.n:
+            lib = L.lib()
+            p = C.c_void_p()
+            L.check(lib.emcg_host_alloc(nb, C.byref(p)))
+            self._finalizer = weakref.finalize(self, lib.emcg_host_free, p)
+            raw = np.ctypeslib.as_array((C.c_uint8 * nb).from_address(p.value))
+            raw[:] = 0
+        else:
+            raw = np.zeros(max(nb, 1), np.uint8)
+        for k, f in enumerate(STATE_F):
+            setattr(self, f, raw[4 * k * self.n:4 * (k + 1) * self.n].view(np.float32))
+        self.meta = raw[4 * len(STATE_F) * self.n:nb].view(np.uint32)
+
+    @classmethod
+    def from_state(cls, st: "ParticleState", pinned: bool = False) -> "ParticleStateF32":
+        s = cls(st.n, pinned)
+        for f in STATE_F:
+            getattr(s, f)[:] = getattr(st, f)
+        s.meta[:] = (np.asarray(st.valley, np.uint32) | (np.asarray(st.sub, np.uint32) << 8) |
+                     (np.asarray(st.region, np.uint32) << 16))
+        return s
+
+    def desc(self) -> L.StateF32Desc:
+        d = L.StateF32Desc()
+        for f in STATE_F:
+            setattr(d, f, getattr(self, f).ctypes.data_as(C.POINTER(C.c_float)))
+        d.meta = self.meta.ctypes.data_as(C.POINTER(C.c_uint32))
+        d.n = self.n
+        return d
+
+
 def update_rates(lib, h, model: int, raw, particle_type) -> object:
     """emcg_update_rates: raw is a host array, a CUDA float64 tensor (device
     rates), or None (refill from the particle type's mechanisms).  Returns
@@ -208,6 +247,17 @@ class BulkBatch:
     def set_state(self, ens: int, st: ParticleState):
         d = st.desc()
         L.check(self._lib.emcg_set_state(self.h, ens, C.byref(d)))
+
+    def set_state_f32(self, ens: int, st: ParticleStateF32):
+        """Upload in the float engine's own layout (emcg_set_state_f32)."""
+        L.check(self._lib.emcg_set_state_f32(self.h, ens, C.byref(st.desc())))
+
+    def get_state_f32(self, ens: int, out: ParticleStateF32 | None = None) -> ParticleStateF32:
+        n = self.num_particles(ens)
+        out = out if out is not None and out.n == n else ParticleStateF32(n)
+        d = out.desc()
+        L.check(self._lib.emcg_get_state_f32(self.h, ens, C.byref(d)))
+        return out
 
     def get_state(self, ens: int) -> ParticleState:
         n = self._lib.emcg_num_particles(self.h, ens)

@@ -1739,6 +1739,111 @@ static int32_t setStateTyped(BulkImpl *b, int e, const emcg_state *s) {
   return EMCG_OK;
 }
 
+// The float layout: staged as it is, meta checked on the device, the fields
+// and meta written (a double engine widens them) only if every particle is in
+// range.
+__global__ void metaCheckKernel(int64_t n, const uint32_t *__restrict__ meta, int nValleys,
+                                unsigned long long *__restrict__ bad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const uint32_t m = meta[i];
+  if ((int)(m & 0xff) >= nValleys || ((m >> 8) & 0xff) >= EMCG_MAX_DEG ||
+      (m >> 16) >= EMCG_MAX_REGIONS)
+    atomicMin(bad, (unsigned long long)i);
+}
+
+template <class T>
+__global__ void stateConvertF32Kernel(StateK<T> st, int64_t base, int64_t n,
+                                      const float *__restrict__ src,
+                                      const uint32_t *__restrict__ meta,
+                                      const unsigned long long *__restrict__ bad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || *bad != ~0ull)
+    return;
+  T *dst[9] = {st.kx, st.ky, st.kz, st.px, st.py, st.pz, st.E, st.tau, st.gtau};
+#pragma unroll
+  for (int f = 0; f < 9; f++)
+    dst[f][base + i] = (T)src[(size_t)f * n + i];
+  st.meta[base + i] = meta[i];
+}
+
+template <class T>
+static int32_t setStateF32Typed(BulkImpl *b, int e, const emcg_state_f32 *s) {
+  const int64_t n = s->n, base = b->begin[e];
+  const float *src[9] = {s->kx, s->ky, s->kz, s->px, s->py, s->pz, s->energy, s->tau,
+                         s->grain_tau};
+  for (int f = 0; f < 9; f++)
+    EMCG_CHECK_ARG(src[f] != nullptr, "state field %d is NULL", f);
+  EMCG_CHECK_ARG(s->meta, "state meta array is NULL");
+  if (n == 0)
+    return EMCG_OK;
+  const size_t need = (size_t)n * (9 * sizeof(float) + sizeof(uint32_t));
+  if (b->stageBytes < need) {
+    EMCG_CUDA(cudaStreamSynchronize(b->stream));
+    cudaFree(b->dStage);
+    b->dStage = nullptr;
+    b->stageBytes = 0;
+    EMCG_CUDA(cudaMalloc(&b->dStage, need));
+    b->stageBytes = need;
+  }
+  if (!b->dBad)
+    EMCG_CUDA(cudaMalloc(&b->dBad, sizeof(unsigned long long)));
+  float *dsrc = static_cast<float *>(b->dStage);
+  uint32_t *dmeta = reinterpret_cast<uint32_t *>(dsrc + (size_t)9 * n);
+  for (int f = 0; f < 9; f++)
+    EMCG_CUDA(cudaMemcpyAsync(dsrc + (size_t)f * n, src[f], n * sizeof(float),
+                              cudaMemcpyHostToDevice, b->stream));
+  EMCG_CUDA(cudaMemcpyAsync(dmeta, s->meta, n * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                            b->stream));
+  EMCG_CUDA(cudaMemsetAsync(b->dBad, 0xff, sizeof(unsigned long long), b->stream));
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  metaCheckKernel<<<grid, 256, 0, b->stream>>>(n, dmeta, b->ensNV[e], b->dBad);
+  stateConvertF32Kernel<T><<<grid, 256, 0, b->stream>>>(stateOf<T>(b), base, n, dsrc, dmeta,
+                                                        b->dBad);
+  EMCG_CUDA(cudaGetLastError());
+  unsigned long long bad = 0;
+  EMCG_CUDA(cudaMemcpyAsync(&bad, b->dBad, sizeof(bad), cudaMemcpyDeviceToHost, b->stream));
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  EMCG_CHECK_ARG(bad == ~0ull, "particle %llu: valley/sub/region out of range", bad);
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_set_state_f32(emcg_handle *h, int32_t e, const emcg_state_f32 *s) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(s && e >= 0 && e < b->nEns, "bad ensemble or state");
+  EMCG_CHECK_ARG(s->n >= 0 && s->n <= b->cap[e], "ensemble %d: %lld particles exceed capacity %lld",
+                 e, (long long)s->n, (long long)b->cap[e]);
+  int32_t r = b->precision == EMCG_FP64 ? setStateF32Typed<double>(b, e, s)
+                                        : setStateF32Typed<float>(b, e, s);
+  if (r)
+    return r;
+  b->count[e] = s->n;
+  b->tilesDirty = true;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_get_state_f32(emcg_handle *h, int32_t e, emcg_state_f32 *s) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(s && e >= 0 && e < b->nEns, "bad ensemble or state");
+  EMCG_CHECK_ARG(b->precision == EMCG_FP32, "a double engine's state is read with emcg_get_state");
+  const int64_t n = b->count[e], base = b->begin[e];
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  float *dst[9] = {s->kx, s->ky, s->kz, s->px, s->py, s->pz, s->energy, s->tau, s->grain_tau};
+  for (int f = 0; f < 9; f++)
+    if (dst[f] && n)
+      EMCG_CUDA(cudaMemcpyAsync(dst[f], static_cast<float *>(b->dState[f]) + base,
+                                n * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
+  if (s->meta && n)
+    EMCG_CUDA(cudaMemcpyAsync(s->meta, b->dMeta + base, n * sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, b->stream));
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  s->n = n;
+  return EMCG_OK;
+}
+
 extern "C" int32_t emcg_set_state(emcg_handle *h, int32_t e, const emcg_state *s) {
   if (h && h->kind == 2) {
     EMCG_CHECK_ARG(e == 0, "a device engine has one ensemble");
