@@ -175,8 +175,9 @@ int32_t emcg_version(void);
 
 /* Page-locked host memory for particle states (no reference counterpart):
    state uploads (emcg_set_state) and downloads from such memory run at the
-   full host-link rate; from ordinary memory CUDA stages them.  bytes = 0
-   gives NULL. */
+   full host-link rate; from ordinary memory CUDA stages them.  The block is
+   mapped into the device's address space, so emcg_bulk_step_from_host reads
+   it from inside the step kernel.  bytes = 0 gives NULL. */
 int32_t emcg_host_alloc(int64_t bytes, void **ptr);
 int32_t emcg_host_free(void *ptr);
 
@@ -244,6 +245,21 @@ int32_t emcg_bulk_init(emcg_handle *h, int32_t ens, int64_t n,
    getValleyOccupationProbability (:289-347) are sum/count and count/N. */
 int32_t emcg_bulk_step(emcg_handle *h, int32_t n_steps, uint32_t step0,
                        double *obs);
+
+/* emcg_set_state_f32(h, ens, s) followed by emcg_bulk_step(h, n_steps,
+   step0, obs), with the upload fused into the first launch: when the engine
+   is a float one stepping with the warp-asynchronous kernel and every array
+   of s lies inside an emcg_host_alloc block, each thread of that launch reads
+   its particle's start state from host memory over the host link, so the
+   transfer overlaps the steps instead of preceding them (the reference's
+   setParticles + moveParticles pair, :58-59 and :181-225).  Other engines and
+   other host memory take the two calls.  In the fused form a particle whose
+   valley, subvalley or region is out of range is neither stepped nor stored:
+   the call returns EMCG_ERR_ARG and the ensemble's state is unspecified until
+   it is set again. */
+int32_t emcg_bulk_step_from_host(emcg_handle *h, int32_t ens,
+                                 const emcg_state_f32 *s, int32_t n_steps,
+                                 uint32_t step0, double *obs);
 
 /* Replay mode: the next emcg_bulk_step (n_steps must be 1) of ensemble 0
    consumes words[offsets[i] .. offsets[i+1]) for particle i instead of

@@ -708,3 +708,57 @@ def test_float_layout_state_upload(engine, precision):
         b.close()
     for f in ("kx", "ky", "kz", "energy", "px", "tau"):
         assert np.array_equal(getattr(outs[0], f), getattr(outs[1], f)), f
+
+
+@pytest.mark.parametrize("steps_per_launch", [0, 8])
+def test_step_from_host_equals_upload_then_step(engine, steps_per_launch):
+    """emcg_bulk_step_from_host: the first launch reads ensemble 1's start
+    state from page-locked host memory (the upload fused into the kernel); the
+    states equal those of emcg_set_state_f32 + emcg_bulk_step bit for bit and
+    the observable sums agree to the order of the blocks' double adds, while
+    ensemble 0 starts from its device state.  Ordinary host memory takes the
+    two-call path with the same result.  A packed valley out of range is
+    reported, and the engine steps normally once the state is set again."""
+    pt = engine.physics.silicon_electron("jacoboni")
+    specs = [engine.EnsembleSpec(0, 2000, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 9, 0),
+             engine.EnsembleSpec(0, 3000, 5e5, (0, 1, 0), (1e-6,) * 3, 1e-15, 9, 1)]
+    src = engine.BulkBatch([pt], specs, "fp32")
+    src.init_particles(0)
+    src.init_particles(1)
+    st0 = src.get_state_f32(0)
+    st1 = src.get_state_f32(1)
+    src.close()
+    outs = []
+    for how in ("two_calls", "fused", "ordinary_memory"):
+        b = engine.BulkBatch([pt], specs, "fp32")
+        b.set_launch(steps_per_launch=steps_per_launch)
+        b.set_state_f32(0, st0)
+        host = engine.ParticleStateF32(st1.n, pinned=how == "fused")
+        for f in engine.bulk.STATE_F + ("meta",):
+            getattr(host, f)[:] = getattr(st1, f)
+        if how == "two_calls":
+            b.set_state_f32(1, host)
+            obs = b.step(20, step0=7)
+        else:
+            obs = b.step_from_host(1, host, 20, step0=7)
+        outs.append((obs, b.get_state_f32(0), b.get_state_f32(1)))
+        if how == "fused":
+            bad = engine.ParticleStateF32(st1.n, pinned=True)
+            for f in engine.bulk.STATE_F + ("meta",):
+                getattr(bad, f)[:] = getattr(st1, f)
+            bad.meta[11] = (bad.meta[11] & ~np.uint32(0xff)) | np.uint32(3)
+            with pytest.raises(engine._lib.EmcgError) as ei:
+                b.step_from_host(1, bad, 4)
+            # the fused form's message: the two-call form names the particle
+            assert ei.value.status == -1 and "unspecified" in str(ei.value)
+            b.set_state_f32(1, host)
+            again = b.step(5)
+            assert np.isfinite(again).all() and again[1, :, 0, 2].min() == st1.n
+        b.close()
+    ref = outs[0]
+    for obs, s0, s1 in outs[1:]:
+        np.testing.assert_allclose(obs, ref[0], rtol=1e-12, atol=1e-300)
+        for f in engine.bulk.STATE_F + ("meta",):
+            assert np.array_equal(getattr(s0, f), getattr(ref[1], f)), f
+            assert np.array_equal(getattr(s1, f), getattr(ref[2], f)), f
+    assert ref[0][1, :, 0, 2].min() == st1.n

@@ -157,6 +157,8 @@ def _declare(L):
     L.emcg_set_state_f32.argtypes = [vp, i32, P(StateF32Desc)]
     L.emcg_get_state_f32.restype = i32
     L.emcg_get_state_f32.argtypes = [vp, i32, P(StateF32Desc)]
+    L.emcg_bulk_step_from_host.restype = i32
+    L.emcg_bulk_step_from_host.argtypes = [vp, i32, P(StateF32Desc), i32, u32, P(C.c_double)]
     L.emcg_num_particles.restype = i64
     L.emcg_num_particles.argtypes = [vp, i32]
     L.emcg_bulk_init.restype = i32

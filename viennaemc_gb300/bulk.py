@@ -323,6 +323,19 @@ class BulkBatch:
         self.step_index = s0 + n_steps
         return obs
 
+    def step_from_host(self, ens: int, st: ParticleStateF32, n_steps: int = 1,
+                       observables: bool = True, step0: int | None = None):
+        """set_state_f32(ens, st) then step(n_steps) in one call
+        (emcg_bulk_step_from_host): with st in page-locked memory the first
+        launch reads the start state from host memory, the upload overlapping
+        the steps."""
+        s0 = self.step_index if step0 is None else int(step0)
+        obs = np.zeros((len(self.specs), n_steps, self.nVmax, 3)) if observables else None
+        L.check(self._lib.emcg_bulk_step_from_host(self.h, ens, C.byref(st.desc()), n_steps, s0,
+                                                   _dp(obs) if observables else None))
+        self.step_index = s0 + n_steps
+        return obs
+
     def reinit_scatter_tables(self, model: int = 0, raw=None):
         """emcScatterHandler::reinitScatterTables (include/emcScatterHandler.hpp:
         100-108) of model `model` on the GPU, before the next step: raw are the

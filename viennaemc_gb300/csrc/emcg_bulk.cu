@@ -726,7 +726,8 @@ __device__ __forceinline__ void flushPos(const float *R, const float vogt[3], fl
 
 template <int MINB, bool kOne>
 __global__ void __launch_bounds__(256, MINB)
-    bulkStepAsyncKernel(StateK<float> st, const ModelK<float> *__restrict__ models,
+    bulkStepAsyncKernel(StateK<float> st, StateK<float> src, int srcEns,
+                        const ModelK<float> *__restrict__ models,
                         const EnsK<float> *__restrict__ ens, const Tile *__restrict__ tiles,
                         int nSteps, uint32_t step0, int chunk, int nVmax, int passActions,
                         double *__restrict__ obs, int *__restrict__ err) {
@@ -749,7 +750,7 @@ __global__ void __launch_bounds__(256, MINB)
   const ModelK<T> &M = models[EK.model];
   const int nV = kOne ? 1 : EK.nV;
   const int64_t gi = tl.begin + threadIdx.x;
-  const bool active = gi < tl.end;
+  bool active = gi < tl.end;
   const uint32_t pid = (uint32_t)(gi - EK.begin);
   const T dt = EK.dt;
 
@@ -757,24 +758,32 @@ __global__ void __launch_bounds__(256, MINB)
   // frame not yet added to pos
   T kE[3] = {0, 0, 0}, pos[3] = {0, 0, 0}, dP[3] = {0, 0, 0}, E = 0, tau = 0, gtau = 0;
   int valley = 0, sub = 0, region = 0;
+  int myErr = 0;
   if (active) {
-    pos[0] = st.px[gi];
-    pos[1] = st.py[gi];
-    pos[2] = st.pz[gi];
-    E = st.E[gi];
-    tau = st.tau[gi];
-    gtau = st.gtau[gi];
-    uint32_t mt = st.meta[gi];
+    // the start state: ensemble srcEns's page-locked host arrays (read over
+    // the host link, the upload fused into the launch), else the device state
+    const StateK<float> ld = tl.ens == srcEns ? src : st;
+    const uint32_t mt = ld.meta[gi];
     valley = mt & 0xff;
     sub = (mt >> 8) & 0xff;
     region = mt >> 16;
-    toEcs(M.v[valley].rot[sub], st.kx[gi], st.ky[gi], st.kz[gi], kE);
+    if (valley >= nV || sub >= EMCG_MAX_DEG || region >= EMCG_MAX_REGIONS) {
+      active = false; // an unchecked host state: neither stepped nor stored
+      myErr = EMCG_ERR_ARG;
+    } else {
+      pos[0] = ld.px[gi];
+      pos[1] = ld.py[gi];
+      pos[2] = ld.pz[gi];
+      E = ld.E[gi];
+      tau = ld.tau[gi];
+      gtau = ld.gtau[gi];
+      toEcs(M.v[valley].rot[sub], ld.kx[gi], ld.ky[gi], ld.kz[gi], kE);
+    }
   }
   bool live = active;    // false once the particle has failed
   int s = live ? 0 : nSteps; // the step the particle is in
   T tIn = 0;             // time already spent inside step s
   int nEv = 0;           // events in step s (bounded)
-  int myErr = 0;
   PhiloxSrc<T> rng;
   rng.init(pid, step0, EK.stream, EK.key0, EK.key1);
   int flushed = 0;  // steps folded into the block sums
@@ -1031,12 +1040,14 @@ struct BulkImpl {
   cudaKernelNodeParams gKp = {};
   int gNs = -1, gBlock = 0, gMinb = 0, gQueued = -1, gTiles = -1, gPass = -1;
   alignas(16) unsigned char gArgs[256] = {};
-  void *gParams[12] = {};
+  void *gParams[14] = {};
 };
 
 // arguments of the step kernels, in parameter order
 template <class T> struct StepArgs {
   StateK<T> st;
+  StateK<T> src; // the warp-asynchronous kernel's start state (st: the device's)
+  int srcEns;
   const ModelK<T> *mp;
   const EnsK<T> *ep;
   const Tile *tiles;
@@ -1215,6 +1226,8 @@ template <class T> static int32_t graphFor(BulkImpl *b, int ns, size_t smem, siz
   static_assert(sizeof(StepArgs<T>) <= sizeof(b->gArgs), "step arguments exceed the buffer");
   StepArgs<T> &a = *reinterpret_cast<StepArgs<T> *>(b->gArgs);
   a.st = stateOf<T>(b);
+  a.src = a.st;
+  a.srcEns = -1;
   a.mp = (const ModelK<T> *)b->dModels;
   a.ep = (const EnsK<T> *)b->dEns;
   a.tiles = b->dTiles;
@@ -1233,8 +1246,8 @@ template <class T> static int32_t graphFor(BulkImpl *b, int ns, size_t smem, siz
                     &a.chunk, &a.nVmax, &a.obs, &a.words, &a.off, &a.err};
   void *que[10] = {&a.st, &a.mp, &a.ep, &a.tiles, &a.ns, &a.step0, &a.chunk, &a.nVmax, &a.obs,
                    &a.err};
-  void *asy[11] = {&a.st,    &a.mp,    &a.ep,   &a.tiles, &a.ns, &a.step0,
-                   &a.chunk, &a.nVmax, &a.pass, &a.obs,   &a.err};
+  void *asy[13] = {&a.st,   &a.src,   &a.srcEns, &a.mp,   &a.ep,  &a.tiles, &a.ns,
+                   &a.step0, &a.chunk, &a.nVmax,  &a.pass, &a.obs, &a.err};
   static_assert(sizeof(asy) <= sizeof(b->gParams), "kernel parameters exceed the buffer");
   if (b->queued == 2 && sizeof(T) == 4)
     std::memcpy(b->gParams, asy, sizeof(asy));
@@ -1368,8 +1381,73 @@ static int32_t coulombStepTyped(BulkImpl *b, int nSteps, uint32_t step0, double 
 // even; 500-step launches took 5.81 ms in 128 against 5.64 ms in 256.
 constexpr int kShortLaunchSteps = 100;
 
+// One launch of ns steps over the tiles [tiles, tiles + nT) (the direct form;
+// graph replay builds its own node).
 template <class T>
-static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHost) {
+static int32_t launchStepTiles(BulkImpl *b, const StateK<T> &st, int ns, uint32_t s0,
+                               const Tile *tiles, int nT, size_t smem, bool async,
+                               const StateK<T> &src, int srcEns) {
+  const int Q = b->nVmax * 3;
+  const ModelK<T> *mp = (const ModelK<T> *)b->dModels;
+  const EnsK<T> *ep = (const EnsK<T> *)b->dEns;
+  if (b->replay) {
+    if constexpr (sizeof(T) == 8)
+      bulkStepKernel<T, true, 1><<<nT, b->blockThreads, smem, b->stream>>>(
+          st, mp, ep, tiles, ns, s0, b->chunk, b->nVmax, b->dObs, b->dWords,
+          b->dOff, b->dErr);
+  } else if (async) {
+    if constexpr (sizeof(T) == 4) {
+      const size_t asmem = asyncSmemBytes(b->blockThreads / 32, ns, Q);
+      if (b->minBlocks >= 4 && b->blockThreads <= 256) {
+        EMCG_TRY(asyncSmemOptIn<4>(asmem));
+        asyncKernel<4>(b->nVmax == 1)<<<nT, b->blockThreads, asmem, b->stream>>>(
+            st, src, srcEns, mp, ep, tiles, ns, s0, b->chunk, b->nVmax, b->passActions,
+            b->dObs, b->dErr);
+      } else if (b->minBlocks == 3 && b->blockThreads <= 256) {
+        EMCG_TRY(asyncSmemOptIn<3>(asmem));
+        asyncKernel<3>(b->nVmax == 1)<<<nT, b->blockThreads, asmem, b->stream>>>(
+            st, src, srcEns, mp, ep, tiles, ns, s0, b->chunk, b->nVmax, b->passActions,
+            b->dObs, b->dErr);
+      } else {
+        EMCG_TRY(asyncSmemOptIn<1>(asmem));
+        asyncKernel<1>(b->nVmax == 1)<<<nT, b->blockThreads, asmem, b->stream>>>(
+            st, src, srcEns, mp, ep, tiles, ns, s0, b->chunk, b->nVmax, b->passActions,
+            b->dObs, b->dErr);
+      }
+    }
+  } else if (b->queued) {
+    const size_t qsmem = ((smem + 15) & ~size_t(15)) + blockStateBytes<T>(b->blockThreads);
+    if (b->minBlocks >= 4 && b->blockThreads <= 256)
+      bulkStepQueuedKernel<T, 4><<<nT, b->blockThreads, qsmem, b->stream>>>(
+          st, mp, ep, tiles, ns, s0, b->chunk, b->nVmax, b->dObs, b->dErr);
+    else if (b->minBlocks == 3 && b->blockThreads <= 256)
+      bulkStepQueuedKernel<T, 3><<<nT, b->blockThreads, qsmem, b->stream>>>(
+          st, mp, ep, tiles, ns, s0, b->chunk, b->nVmax, b->dObs, b->dErr);
+    else
+      bulkStepQueuedKernel<T, 1><<<nT, b->blockThreads, qsmem, b->stream>>>(
+          st, mp, ep, tiles, ns, s0, b->chunk, b->nVmax, b->dObs, b->dErr);
+  } else if (b->minBlocks >= 4 && b->blockThreads <= 256) {
+    bulkStepKernel<T, false, 4><<<nT, b->blockThreads, smem, b->stream>>>(
+        st, mp, ep, tiles, ns, s0, b->chunk, b->nVmax, b->dObs, nullptr,
+        nullptr, b->dErr);
+  } else if (b->minBlocks == 3 && b->blockThreads <= 256) {
+    bulkStepKernel<T, false, 3><<<nT, b->blockThreads, smem, b->stream>>>(
+        st, mp, ep, tiles, ns, s0, b->chunk, b->nVmax, b->dObs, nullptr,
+        nullptr, b->dErr);
+  } else {
+    bulkStepKernel<T, false, 1><<<nT, b->blockThreads, smem, b->stream>>>(
+        st, mp, ep, tiles, ns, s0, b->chunk, b->nVmax, b->dObs, nullptr,
+        nullptr, b->dErr);
+  }
+  EMCG_CUDA(cudaGetLastError());
+  return EMCG_OK;
+}
+
+// src/srcEns: the first launch reads ensemble srcEns's start state from src
+// (the warp-asynchronous kernel only; nullptr: the device state)
+template <class T>
+static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHost,
+                         const StateK<T> *src = nullptr, int srcEns = -1) {
   if (b->coulomb) // set_coulomb and set_replay exclude each other
     return coulombStepTyped<T>(b, nSteps, step0, obsHost);
   if (b->autoBlock) {
@@ -1404,7 +1482,8 @@ static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHos
   const bool graph = b->useGraph && !b->replay && b->nTiles > 0;
   for (int done = 0; done < nSteps; done += per) {
     int ns = std::min(per, nSteps - done);
-    if (graph) {
+    const bool fromSrc = done == 0 && src != nullptr;
+    if (graph && !fromSrc) {
       const size_t qsmem = ((smem + 15) & ~size_t(15)) + blockStateBytes<T>(b->blockThreads);
       EMCG_TRY(graphFor<T>(b, ns, smem, qsmem));
       reinterpret_cast<StepArgs<T> *>(b->gArgs)->step0 = step0 + done;
@@ -1414,60 +1493,9 @@ static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHos
     } else {
       EMCG_CUDA(cudaMemsetAsync(b->dObs, 0, (size_t)b->nEns * ns * Q * sizeof(double), b->stream));
       EMCG_CUDA(cudaEventRecord(b->ev0, b->stream));
-      if (b->nTiles > 0) {
-        const ModelK<T> *mp = (const ModelK<T> *)b->dModels;
-        const EnsK<T> *ep = (const EnsK<T> *)b->dEns;
-        if (b->replay) {
-          if constexpr (sizeof(T) == 8)
-            bulkStepKernel<T, true, 1><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
-                st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dWords,
-                b->dOff, b->dErr);
-        } else if (async) {
-          if constexpr (sizeof(T) == 4) {
-            const size_t asmem = asyncSmemBytes(b->blockThreads / 32, ns, Q);
-            if (b->minBlocks >= 4 && b->blockThreads <= 256) {
-              EMCG_TRY(asyncSmemOptIn<4>(asmem));
-              asyncKernel<4>(b->nVmax == 1)<<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
-                  st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->passActions,
-                  b->dObs, b->dErr);
-            } else if (b->minBlocks == 3 && b->blockThreads <= 256) {
-              EMCG_TRY(asyncSmemOptIn<3>(asmem));
-              asyncKernel<3>(b->nVmax == 1)<<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
-                  st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->passActions,
-                  b->dObs, b->dErr);
-            } else {
-              EMCG_TRY(asyncSmemOptIn<1>(asmem));
-              asyncKernel<1>(b->nVmax == 1)<<<b->nTiles, b->blockThreads, asmem, b->stream>>>(
-                  st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->passActions,
-                  b->dObs, b->dErr);
-            }
-          }
-        } else if (b->queued) {
-          const size_t qsmem = ((smem + 15) & ~size_t(15)) + blockStateBytes<T>(b->blockThreads);
-          if (b->minBlocks >= 4 && b->blockThreads <= 256)
-            bulkStepQueuedKernel<T, 4><<<b->nTiles, b->blockThreads, qsmem, b->stream>>>(
-                st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
-          else if (b->minBlocks == 3 && b->blockThreads <= 256)
-            bulkStepQueuedKernel<T, 3><<<b->nTiles, b->blockThreads, qsmem, b->stream>>>(
-                st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
-          else
-            bulkStepQueuedKernel<T, 1><<<b->nTiles, b->blockThreads, qsmem, b->stream>>>(
-                st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, b->dErr);
-        } else if (b->minBlocks >= 4 && b->blockThreads <= 256) {
-          bulkStepKernel<T, false, 4><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
-              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, nullptr,
-              nullptr, b->dErr);
-        } else if (b->minBlocks == 3 && b->blockThreads <= 256) {
-          bulkStepKernel<T, false, 3><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
-              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, nullptr,
-              nullptr, b->dErr);
-        } else {
-          bulkStepKernel<T, false, 1><<<b->nTiles, b->blockThreads, smem, b->stream>>>(
-              st, mp, ep, b->dTiles, ns, step0 + done, b->chunk, b->nVmax, b->dObs, nullptr,
-              nullptr, b->dErr);
-        }
-        EMCG_CUDA(cudaGetLastError());
-      }
+      if (b->nTiles > 0)
+        EMCG_TRY(launchStepTiles<T>(b, st, ns, step0 + done, b->dTiles, b->nTiles, smem, async,
+                                    fromSrc ? *src : st, fromSrc ? srcEns : -1));
     }
     EMCG_CUDA(cudaEventRecord(b->ev1, b->stream));
     if (obsHost) {
@@ -1822,6 +1850,56 @@ extern "C" int32_t emcg_set_state_f32(emcg_handle *h, int32_t e, const emcg_stat
   b->count[e] = s->n;
   b->tilesDirty = true;
   return EMCG_OK;
+}
+
+extern "C" int32_t emcg_bulk_step_from_host(emcg_handle *h, int32_t e, const emcg_state_f32 *s,
+                                            int32_t n_steps, uint32_t step0, double *obs) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(s && e >= 0 && e < b->nEns, "bad ensemble or state");
+  EMCG_CHECK_ARG(n_steps >= 0, "n_steps must be >= 0");
+  EMCG_CHECK_ARG(s->n >= 0 && s->n <= b->cap[e], "ensemble %d: %lld particles exceed capacity %lld",
+                 e, (long long)s->n, (long long)b->cap[e]);
+  const float *f[9] = {s->kx, s->ky, s->kz, s->px, s->py, s->pz, s->energy, s->tau, s->grain_tau};
+  for (int i = 0; i < 9; i++)
+    EMCG_CHECK_ARG(f[i] != nullptr, "state field %d is NULL", i);
+  EMCG_CHECK_ARG(s->meta, "state meta array is NULL");
+  // The fused form: a float engine stepping with the warp-asynchronous kernel
+  // reads the start state straight from emcg_host_alloc blocks.
+  StateK<float> src{};
+  bool fused = b->precision == EMCG_FP32 && b->queued == 2 && !b->replay && !b->coulomb &&
+               n_steps > 0 && s->n > 0;
+  const int64_t n = s->n, base = b->begin[e];
+  if (fused) {
+    float **d[9] = {&src.kx, &src.ky, &src.kz, &src.px, &src.py, &src.pz, &src.E, &src.tau,
+                    &src.gtau};
+    for (int i = 0; i < 9 && fused; i++) {
+      const void *p = reinterpret_cast<uintptr_t>(f[i]) % alignof(float) == 0
+                          ? mappedHostRange(f[i], (size_t)n * sizeof(float))
+                          : nullptr;
+      fused = p != nullptr;
+      // indexed by the particle's place in the handle's arrays (base + i)
+      *d[i] = const_cast<float *>(static_cast<const float *>(p)) - base;
+    }
+    const void *m = reinterpret_cast<uintptr_t>(s->meta) % alignof(uint32_t) == 0
+                        ? mappedHostRange(s->meta, (size_t)n * sizeof(uint32_t))
+                        : nullptr;
+    fused = fused && m != nullptr;
+    src.meta = const_cast<uint32_t *>(static_cast<const uint32_t *>(m)) - base;
+  }
+  if (!fused) {
+    EMCG_TRY(emcg_set_state_f32(h, e, s));
+    return emcg_bulk_step(h, n_steps, step0, obs);
+  }
+  if (b->count[e] != n) {
+    b->count[e] = n;
+    b->tilesDirty = true;
+  }
+  const int32_t r = stepTyped<float>(b, n_steps, step0, obs, &src, e);
+  if (r == EMCG_ERR_ARG)
+    setError("ensemble %d: a particle's valley, subvalley or region is out of range; "
+             "its state is unspecified until set again", e);
+  return r;
 }
 
 extern "C" int32_t emcg_get_state_f32(emcg_handle *h, int32_t e, emcg_state_f32 *s) {

@@ -1,5 +1,9 @@
-// Error reporting and version of libemcgpu.
+// Error reporting, version and page-locked host blocks of libemcgpu.
 #include "emcg_host.h"
+
+#include <cstdint>
+#include <map>
+#include <mutex>
 
 namespace emcg {
 
@@ -28,6 +32,27 @@ const char *statusName(int32_t s) {
   return "unknown status";
 }
 
+// live emcg_host_alloc blocks: start address -> (bytes, device address)
+struct HostBlock {
+  size_t bytes;
+  char *dev;
+};
+static std::mutex g_hostMu;
+static std::map<uintptr_t, HostBlock> g_hostBlocks;
+
+const void *mappedHostRange(const void *p, size_t bytes) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  std::lock_guard<std::mutex> lk(g_hostMu);
+  auto it = g_hostBlocks.upper_bound(a);
+  if (it == g_hostBlocks.begin())
+    return nullptr;
+  --it;
+  const uintptr_t off = a - it->first;
+  if (off > it->second.bytes || bytes > it->second.bytes - off)
+    return nullptr;
+  return it->second.dev + off;
+}
+
 } // namespace emcg
 
 extern "C" const char *emcg_last_error(void) {
@@ -41,13 +66,28 @@ extern "C" int32_t emcg_host_alloc(int64_t bytes, void **ptr) {
   *ptr = nullptr;
   if (bytes == 0)
     return EMCG_OK;
-  EMCG_CUDA(cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocDefault));
+  EMCG_CUDA(cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocMapped));
+  void *dev = nullptr;
+  if (cudaHostGetDevicePointer(&dev, *ptr, 0) != cudaSuccess) {
+    cudaGetLastError();
+    dev = nullptr; // not readable by kernels: used through copies only
+  }
+  if (dev) {
+    std::lock_guard<std::mutex> lk(emcg::g_hostMu);
+    emcg::g_hostBlocks[reinterpret_cast<uintptr_t>(*ptr)] = {(size_t)bytes,
+                                                             static_cast<char *>(dev)};
+  }
   return EMCG_OK;
 }
 
 extern "C" int32_t emcg_host_free(void *ptr) {
-  if (ptr)
-    EMCG_CUDA(cudaFreeHost(ptr));
+  if (!ptr)
+    return EMCG_OK;
+  {
+    std::lock_guard<std::mutex> lk(emcg::g_hostMu);
+    emcg::g_hostBlocks.erase(reinterpret_cast<uintptr_t>(ptr));
+  }
+  EMCG_CUDA(cudaFreeHost(ptr));
   return EMCG_OK;
 }
 

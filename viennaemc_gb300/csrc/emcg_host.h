@@ -41,6 +41,11 @@ void setError(const char *fmt, ...);
 
 const char *statusName(int32_t s);
 
+// The device address of host bytes [p, p + bytes) when they lie inside one
+// live emcg_host_alloc block (page-locked, mapped into the device's address
+// space), else nullptr: only such ranges are read by kernels over the host link.
+const void *mappedHostRange(const void *p, size_t bytes);
+
 struct BulkImpl;
 struct DeviceImpl;
 
