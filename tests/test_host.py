@@ -149,3 +149,29 @@ def test_bulk_handler_field_and_observable_averaging():
     a = BulkBatch.averages(sums, [3])
     assert a["energy"][0, 0, 0] == 1.0 and a["drift_velocity"][0, 0, 0] == -2.0
     assert a["occupation"][0, 0, 0] == 1.0 and a["energy"][0, 1, 0] == 0.0
+
+
+def test_float_state_fields_are_fixed_views():
+    """ParticleStateF32 builds its C descriptor once: its fields are views of
+    one block, written in place; rebinding a field is refused (the descriptor
+    would point at the old array)."""
+    from viennaemc_gb300.bulk import STATE_F, ParticleStateF32
+    st = ParticleStateF32(5)
+    st.kx[:] = np.arange(5, dtype=np.float32)
+    st.meta[:] = 7
+    d = st.desc()
+    assert C.cast(d.kx, C.c_void_p).value == st.kx.ctypes.data
+    assert C.cast(d.meta, C.c_void_p).value == st.meta.ctypes.data and d.n == 5
+    assert d.kx[4] == 4.0 and d.meta[2] == 7
+    for f in STATE_F + ("meta",):
+        with pytest.raises(AttributeError, match="in place"):
+            setattr(st, f, np.zeros(5, np.float32))
+    st.note = "other attributes stay free"
+
+
+def test_step_from_host_checks_arguments_without_gpu():
+    """emcg_bulk_step_from_host refuses a NULL handle or state before any
+    CUDA call."""
+    from viennaemc_gb300 import _lib as L
+    lib = L.lib()
+    assert lib.emcg_bulk_step_from_host(None, 0, None, 1, 0, None) == -1

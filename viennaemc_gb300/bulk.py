@@ -101,6 +101,20 @@ class ParticleStateF32:
         for k, f in enumerate(STATE_F):
             setattr(self, f, raw[4 * k * self.n:4 * (k + 1) * self.n].view(np.float32))
         self.meta = raw[4 * len(STATE_F) * self.n:nb].view(np.uint32)
+        # the fields are views of one block and stay put: the descriptor is
+        # built once (a step call then costs no ctypes conversions)
+        d = L.StateF32Desc()
+        for f in STATE_F:
+            setattr(d, f, getattr(self, f).ctypes.data_as(C.POINTER(C.c_float)))
+        d.meta = self.meta.ctypes.data_as(C.POINTER(C.c_uint32))
+        d.n = self.n
+        self._desc = d
+
+    def __setattr__(self, k, val):
+        if k in STATE_F + ("meta",) and "_desc" in self.__dict__:
+            raise AttributeError(f"{k} is a view of the state's block: assign in place "
+                                 f"({k}[:] = ...)")
+        object.__setattr__(self, k, val)
 
     @classmethod
     def from_state(cls, st: "ParticleState", pinned: bool = False) -> "ParticleStateF32":
@@ -112,12 +126,7 @@ class ParticleStateF32:
         return s
 
     def desc(self) -> L.StateF32Desc:
-        d = L.StateF32Desc()
-        for f in STATE_F:
-            setattr(d, f, getattr(self, f).ctypes.data_as(C.POINTER(C.c_float)))
-        d.meta = self.meta.ctypes.data_as(C.POINTER(C.c_uint32))
-        d.n = self.n
-        return d
+        return self._desc
 
 
 def update_rates(lib, h, model: int, raw, particle_type) -> object:

@@ -1002,6 +1002,8 @@ struct BulkImpl {
   uint32_t *dMeta = nullptr;
   double *dObs = nullptr;
   size_t obsCap = 0;
+  double *hObs = nullptr; // page-locked copy of dObs (asynchronous readback)
+  int *hErr = nullptr;    // page-locked copy of dErr
   int *dErr = nullptr;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1167,16 +1169,22 @@ static int32_t ensureTiles(BulkImpl *b) {
   return EMCG_OK;
 }
 
-static int32_t readError(BulkImpl *b) {
-  int e = 0;
-  EMCG_CUDA(cudaMemcpyAsync(&e, b->dErr, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
-  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+// The error word already copied to hErr (the stream synchronised since).
+static int32_t takeError(BulkImpl *b) {
+  const int e = *b->hErr;
   if (e) {
+    *b->hErr = 0;
     EMCG_CUDA(cudaMemsetAsync(b->dErr, 0, sizeof(int), b->stream));
     setError("bulk kernel reported: %s", statusName(e));
     return e;
   }
   return EMCG_OK;
+}
+
+static int32_t readError(BulkImpl *b) {
+  EMCG_CUDA(cudaMemcpyAsync(b->hErr, b->dErr, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  return takeError(b);
 }
 
 static void dropGraph(BulkImpl *b) {
@@ -1188,6 +1196,24 @@ static void dropGraph(BulkImpl *b) {
   b->graph = nullptr;
   b->gKernel = nullptr;
   b->gNs = -1;
+}
+
+// The observable buffers (device sums and their page-locked readback) for at
+// least need doubles.
+static int32_t growObs(BulkImpl *b, size_t need) {
+  if (need <= b->obsCap)
+    return EMCG_OK;
+  EMCG_CUDA(cudaStreamSynchronize(b->stream));
+  dropGraph(b); // it holds the old buffer
+  cudaFree(b->dObs);
+  cudaFreeHost(b->hObs);
+  b->dObs = nullptr;
+  b->hObs = nullptr;
+  b->obsCap = 0;
+  EMCG_CUDA(cudaMalloc(&b->dObs, need * sizeof(double)));
+  EMCG_CUDA(cudaHostAlloc(&b->hObs, need * sizeof(double), cudaHostAllocDefault));
+  b->obsCap = need;
+  return EMCG_OK;
 }
 
 // the step kernel of the current launch configuration (Philox streams)
@@ -1330,13 +1356,7 @@ static int32_t coulombStepTyped(BulkImpl *b, int nSteps, uint32_t step0, double 
     EMCG_CUDA(cudaMemsetAsync(b->dCoulF, 0, (size_t)std::max<int64_t>(b->totalCap, 1) * 4 *
                                                  sizeof(double), b->stream));
   }
-  if ((size_t)b->nEns * Q > b->obsCap) {
-    dropGraph(b);
-    cudaFree(b->dObs);
-    b->dObs = nullptr;
-    EMCG_CUDA(cudaMalloc(&b->dObs, (size_t)b->nEns * Q * sizeof(double)));
-    b->obsCap = (size_t)b->nEns * Q;
-  }
+  EMCG_TRY(growObs(b, (size_t)b->nEns * Q));
   StateK<T> st = stateOf<T>(b);
   const T coulFactor = (T)(-kCoulombKe / b->coulEpsR);
   EMCG_CUDA(cudaEventRecord(b->ev0, b->stream));
@@ -1467,14 +1487,7 @@ static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHos
   const bool async = b->queued == 2 && sizeof(T) == 4 && !b->replay;
   if (async) // the block's step sums live in shared memory
     per = std::min(per, asyncMaxSteps(b->blockThreads / 32, Q));
-  size_t need = (size_t)b->nEns * per * Q;
-  if (need > b->obsCap) {
-    dropGraph(b); // it holds the old buffer
-    cudaFree(b->dObs);
-    b->dObs = nullptr;
-    EMCG_CUDA(cudaMalloc(&b->dObs, need * sizeof(double)));
-    b->obsCap = need;
-  }
+  EMCG_TRY(growObs(b, (size_t)b->nEns * per * Q));
   const int nWarps = b->blockThreads / 32;
   const size_t smem = (size_t)b->chunk * nWarps * Q * sizeof(T);
   StateK<T> st = stateOf<T>(b);
@@ -1498,23 +1511,28 @@ static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHos
                                     fromSrc ? *src : st, fromSrc ? srcEns : -1));
     }
     EMCG_CUDA(cudaEventRecord(b->ev1, b->stream));
-    if (obsHost) {
-      // gather [ens][ns][Q] of this launch into [ens][nSteps][Q]
-      for (int e = 0; e < b->nEns; e++)
-        EMCG_CUDA(cudaMemcpyAsync(obsHost + ((size_t)e * nSteps + done) * Q,
-                                  b->dObs + (size_t)e * ns * Q, (size_t)ns * Q * sizeof(double),
-                                  cudaMemcpyDeviceToHost, b->stream));
-    }
-    EMCG_CUDA(cudaEventSynchronize(b->ev1));
+    // the launch's sums and, after the last, the error word: one page-locked
+    // readback and one synchronisation per launch
+    const size_t nObs = (size_t)b->nEns * ns * Q;
+    if (obsHost)
+      EMCG_CUDA(cudaMemcpyAsync(b->hObs, b->dObs, nObs * sizeof(double), cudaMemcpyDeviceToHost,
+                                b->stream));
+    if (done + ns >= nSteps)
+      EMCG_CUDA(cudaMemcpyAsync(b->hErr, b->dErr, sizeof(int), cudaMemcpyDeviceToHost,
+                                b->stream));
+    EMCG_CUDA(cudaStreamSynchronize(b->stream));
     float ms = 0;
     EMCG_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
     totalMs += ms;
+    if (obsHost) // gather [ens][ns][Q] of this launch into [ens][nSteps][Q]
+      for (int e = 0; e < b->nEns; e++)
+        std::memcpy(obsHost + ((size_t)e * nSteps + done) * Q, b->hObs + (size_t)e * ns * Q,
+                    (size_t)ns * Q * sizeof(double));
   }
-  EMCG_CUDA(cudaStreamSynchronize(b->stream));
   b->lastMs = totalMs;
   if (b->replay)
     b->replay = false;
-  return readError(b);
+  return takeError(b);
 }
 
 static void freeBulk(BulkImpl *b) {
@@ -1531,7 +1549,9 @@ static void freeBulk(BulkImpl *b) {
     cudaFree(p);
   cudaFree(b->dMeta);
   cudaFree(b->dObs);
+  cudaFreeHost(b->hObs);
   cudaFree(b->dErr);
+  cudaFreeHost(b->hErr);
   cudaFree(b->dWords);
   cudaFree(b->dOff);
   freeRateScratch(b->rateScratch);
@@ -1661,11 +1681,13 @@ extern "C" int32_t emcg_bulk_create(const emcg_model_desc *models, int32_t n_mod
   if (cudaMalloc(&b->dMeta, n * sizeof(uint32_t)) != cudaSuccess ||
       cudaMalloc(&b->dErr, sizeof(int)) != cudaSuccess ||
       cudaMemset(b->dErr, 0, sizeof(int)) != cudaSuccess ||
+      cudaHostAlloc(&b->hErr, sizeof(int), cudaHostAllocDefault) != cudaSuccess ||
       cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
     setError("CUDA allocation failed: %s", cudaGetErrorString(cudaGetLastError()));
     return fail(EMCG_ERR_CUDA);
   }
+  *b->hErr = 0;
   emcg_handle *h = new emcg_handle();
   h->kind = 1;
   h->bulk = b;
