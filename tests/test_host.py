@@ -175,3 +175,15 @@ def test_step_from_host_checks_arguments_without_gpu():
     from viennaemc_gb300 import _lib as L
     lib = L.lib()
     assert lib.emcg_bulk_step_from_host(None, 0, None, 1, 0, None) == -1
+
+
+def test_poisson_exp_is_accurate(tmp_path):
+    """The Poisson residual's table-driven exp (emcg_exp.h, Tang's method)
+    agrees with libm's exp to about one unit in the last place over the range
+    it serves, and hands overflow, underflow and NaN to the library."""
+    exe = tmp_path / "exp_check"
+    subprocess.run(["g++", "-O2", "-std=c++17", f"-I{ROOT}/viennaemc_gb300/csrc",
+                    f"{ROOT}/tests/native/exp_check.cpp", "-o", str(exe)], check=True)
+    worst, _, specials = subprocess.run([str(exe)], check=True, capture_output=True,
+                                        text=True).stdout.split()
+    assert float(worst) < 5e-16 and specials == "1"

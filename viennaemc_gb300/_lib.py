@@ -17,7 +17,7 @@ INCLUDE = os.path.join(ROOT, "include")
 LIB_PATH = os.path.join(PKG, "libemcgpu.so")
 SOURCES = ["emcg_core.cu", "emcg_bulk.cu", "emcg_device.cu", "emcg_poisson.cu", "emcg_p2p.cu"]
 HEADERS = ["emcg_common.cuh", "emcg_host.h", "emcg_model.h", "emcg_poisson.cuh", "emcg_rates.cuh",
-           "emcg_p2p.cuh"]
+           "emcg_p2p.cuh", "emcg_exp.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 MAX_VALLEYS, MAX_DEG, MAX_MECH, MAX_NF, MAX_REGIONS = 4, 8, 32, 8, 16

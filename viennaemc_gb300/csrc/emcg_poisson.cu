@@ -11,6 +11,7 @@
 #include <cooperative_groups.h>
 
 #include "emcg_common.cuh"
+#include "emcg_exp.h"
 #include "emcg_host.h"
 #include "emcg_poisson.cuh"
 
@@ -67,8 +68,13 @@ __global__ void nonlinResidualKernel(const double *__restrict__ pot, const doubl
                                      int nx, int ny, double hF0, double hF1, double hP,
                                      MT *__restrict__ rhs, MT *__restrict__ rho, MT *__restrict__ d,
                                      double *__restrict__ stats, int withScale) {
+  __shared__ double tab[32]; // 2^(j/32) for expTab
+  if (threadIdx.x < 32)
+    tab[threadIdx.x] = exp2(threadIdx.x * (1.0 / 32));
+  __syncthreads();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double aF = 0., sc = 0.;
+  MT aF = 0;
+  double sc = 0.;
   if (i < nx * ny) {
     d[i] = MT(0);
     if (fixed[i]) {
@@ -77,8 +83,8 @@ __global__ void nonlinResidualKernel(const double *__restrict__ pot, const doubl
     } else {
       int x = i % nx, y = i / nx;
       double phi = pot[i];
-      double p = exp(-phi);
-      double n = conc ? conc[i] : exp(phi);
+      double p = expTab(-phi, tab);
+      double n = conc ? conc[i] : expTab(phi, tab);
       double w = x > 0 ? pot[i - 1] : pot[i + 1];
       double e = x < nx - 1 ? pot[i + 1] : pot[i - 1];
       double s = y > 0 ? pot[i - nx] : pot[i + nx];
@@ -86,20 +92,22 @@ __global__ void nonlinResidualKernel(const double *__restrict__ pot, const doubl
       double F = hF0 * (w + e - 2 * phi) + hF1 * (s + nn - 2 * phi) + hP * (p - n + C[i]) +
                  (gV[i] - gSum[i] * phi);
       int bd = (x == 0 || x == nx - 1) + (y == 0 || y == ny - 1);
-      double scale = bd == 0 ? 1.0 : (bd == 1 ? 0.5 : 0.25);
-      rhs[i] = (MT)(F * scale);
+      // the FV scale (1, 1/2, 1/4) and the maxima in the multigrid's type:
+      // exact scalings, and the maximum needs no more than float accuracy
+      const MT fF = (MT)F;
+      rhs[i] = fF * (bd == 0 ? MT(1) : (bd == 1 ? MT(0.5) : MT(0.25)));
       rho[i] = (MT)(conc ? p : p + n);
-      aF = fabs(F);
+      aF = fabs(fF);
       if (withScale)
         sc = hP * (fabs(C[i]) + n + p);
       // a NaN would vanish in the maxima (fmax drops it): a non-finite
       // residual or scale term counts as an infinite residual, which ends
       // the solve as not converged
-      if (!isfinite(F) || !isfinite(sc))
+      if (!isfinite(F) || !isfinite(sc) || !isfinite(fF))
         aF = INFINITY;
     }
   }
-  double m1 = blockMax(aF);
+  double m1 = blockMax((double)aF);
   __syncthreads();
   double m2 = withScale ? blockMax(sc) : 0.;
   if (threadIdx.x == 0) {
@@ -113,18 +121,19 @@ template <class MT>
 __global__ void updatePotKernel(double *__restrict__ pot, const MT *__restrict__ d,
                                 const uint8_t *__restrict__ fixed, int n, double *stats) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double a = 0.;
+  MT a = 0;
   if (i < n && !fixed[i]) {
-    double v = (double)d[i];
+    // clamped in the correction's own type (the bound is exact in float)
+    MT v = d[i];
     // the clamp would turn a NaN correction into -kMaxNewtonStep (fmax drops
     // NaN): a non-finite correction is passed on, so that the next residual
     // reports it
     if (isfinite(v))
-      v = fmin(kMaxNewtonStep, fmax(-kMaxNewtonStep, v));
-    pot[i] += v;
-    a = isfinite(v) ? fabs(v) : INFINITY;
+      v = fmin(MT(kMaxNewtonStep), fmax(MT(-kMaxNewtonStep), v));
+    pot[i] += (double)v;
+    a = isfinite(v) ? fabs(v) : MT(INFINITY);
   }
-  double m = blockMax(a);
+  double m = blockMax((double)a);
   if (threadIdx.x == 0)
     atomicMaxPos(&stats[2], m);
 }
@@ -887,6 +896,9 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
   // the level descriptors, read by every phase, from shared memory rather than
   // the parameter bank
   __shared__ __align__(16) int sM[sizeof(CMG<MT>) / sizeof(int)];
+  __shared__ double sExp[32]; // 2^(j/32) for expTab
+  if (threadIdx.x < 32)
+    sExp[threadIdx.x] = exp2(threadIdx.x * (1.0 / 32));
   for (int k = threadIdx.x; k < (int)(sizeof(CMG<MT>) / sizeof(int)); k += blockDim.x)
     sM[k] = reinterpret_cast<const int *>(&Mp)[k];
   __syncthreads();
@@ -896,38 +908,70 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
   if (threadIdx.x < ranks)
     sBase[threadIdx.x] = static_cast<char *>(cluster.map_shared_rank((void *)smem, threadIdx.x));
   // stage the class and transfer tables (every CTA) and this CTA's rows of
-  // class indices
-  for (int l = 0; l < M.nLev; l++) {
-    const CLevel<MT> &L = M.L[l];
+  // class indices.  The word tables go by asynchronous copies, all in flight
+  // at once (a plain copy loop per table waited for each table's loads in
+  // turn: 20 us per launch); the class bytes of every level by one loop.
+  {
+    const unsigned sBaseAddr = (unsigned)__cvta_generic_to_shared(smem);
     auto stage = [&](unsigned off, const void *src, int n) {
       const int *sp = static_cast<const int *>(src);
-      int *dp = reinterpret_cast<int *>(smem + off);
       for (int k = threadIdx.x; k < n; k += blockDim.x)
-        dp[k] = sp[k];
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sBaseAddr + off + 4u * k),
+                     "l"(sp + k)
+                     : "memory");
     };
-    stage(L.offTab, L.tab, 8 * L.nCls * (int)(sizeof(MT) / 4));
-    int r0, r1;
-    cOwnRows(CCtx{sBase, smem, rank}, L, r0, r1);
-    uint8_t *cl = reinterpret_cast<uint8_t *>(smem + L.offCls);
-    for (int k = threadIdx.x; k < L.nx * (r1 - r0); k += blockDim.x)
-      cl[k] = L.cls[(size_t)r0 * L.nx + k];
-    if (l + 1 < M.nLev) { // the residual of Dirichlet nodes stays 0
-      MT *res = reinterpret_cast<MT *>(smem + L.offRes);
-      for (int k = threadIdx.x; k < L.nx * (r1 - r0); k += blockDim.x)
-        res[k] = MT(0);
+    int clsEnd[16]; // prefix sums of this CTA's class bytes per level
+    int nCls = 0;
+    for (int l = 0; l < M.nLev; l++) {
+      const CLevel<MT> &L = M.L[l];
+      stage(L.offTab, L.tab, 8 * L.nCls * (int)(sizeof(MT) / 4));
+      int r0, r1;
+      cOwnRows(CCtx{sBase, smem, rank}, L, r0, r1);
+      nCls += L.nx * (r1 - r0);
+      clsEnd[l] = nCls;
+      if (l + 1 < M.nLev) { // the residual of Dirichlet nodes stays 0
+        MT *res = reinterpret_cast<MT *>(smem + L.offRes);
+        for (int k = threadIdx.x; k < L.nx * (r1 - r0); k += blockDim.x)
+          res[k] = MT(0);
+      }
+      if (L.ncx > 0) {
+        stage(L.offPxI, L.pxIdx, L.nx);
+        stage(L.offPxW, L.pxW, L.nx);
+        stage(L.offPyI, L.pyIdx, L.ny);
+        stage(L.offPyW, L.pyW, L.ny);
+        stage(L.offRxI, L.rxIdx, 3 * L.ncx);
+        stage(L.offRxW, L.rxW, 3 * L.ncx);
+        stage(L.offRyI, L.ryIdx, 3 * L.ncy);
+        stage(L.offRyW, L.ryW, 3 * L.ncy);
+        stage(L.offMapX, L.mapX, L.ncx);
+        stage(L.offMapY, L.mapY, L.ncy);
+      }
     }
-    if (L.ncx > 0) {
-      stage(L.offPxI, L.pxIdx, L.nx);
-      stage(L.offPxW, L.pxW, L.nx);
-      stage(L.offPyI, L.pyIdx, L.ny);
-      stage(L.offPyW, L.pyW, L.ny);
-      stage(L.offRxI, L.rxIdx, 3 * L.ncx);
-      stage(L.offRxW, L.rxW, 3 * L.ncx);
-      stage(L.offRyI, L.ryIdx, 3 * L.ncy);
-      stage(L.offRyW, L.ryW, 3 * L.ncy);
-      stage(L.offMapX, L.mapX, L.ncx);
-      stage(L.offMapY, L.mapY, L.ncy);
+    // four bytes per thread and pass: the loads first, then the stores
+    for (int t0 = threadIdx.x; t0 < nCls; t0 += 4 * blockDim.x) {
+      uint8_t v[4];
+      uint8_t *dst[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int t = t0 + j * (int)blockDim.x;
+        dst[j] = nullptr;
+        if (t < nCls) {
+          int l = 0;
+          while (t >= clsEnd[l])
+            l++;
+          const CLevel<MT> &L = M.L[l];
+          const int k = t - (l > 0 ? clsEnd[l - 1] : 0);
+          const int r0 = L.small ? 0 : min(L.ny, rank * L.rowsPer);
+          v[j] = L.cls[(size_t)r0 * L.nx + k];
+          dst[j] = reinterpret_cast<uint8_t *>(smem + L.offCls) + k;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (dst[j])
+          *dst[j] = v[j];
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
   }
   __syncthreads();
   CCtx c{sBase, smem, rank};
@@ -943,7 +987,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
   for (;; it++) {
     // F(phi), Jacobian reaction and FV-scaled right-hand side (nonlinResidualKernel);
     // the scale of the relative residual from the first iteration's state
-    double aF = 0., sc = 0.;
+    MT aFm = 0;
+    double sc = 0.;
     for (int t = threadIdx.x; t < nOwn; t += blockDim.x) {
       const int ly = L0.byNx.div(t), y = p0 + ly, x = t - ly * nx, i = y * nx + x;
       MT *d0 = cRowNearT<true, MT>(c, L0, L0.offD, ly);
@@ -956,8 +1001,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
         continue;
       }
       const double phi = pot[i];
-      const double p = exp(-phi);
-      const double n = conc ? conc[i] : exp(phi);
+      const double p = expTab(-phi, sExp);
+      const double n = conc ? conc[i] : expTab(phi, sExp);
       const double w = x > 0 ? pot[i - 1] : pot[i + 1];
       const double e = x < nx - 1 ? pot[i + 1] : pot[i - 1];
       const double s = y > 0 ? pot[i - nx] : pot[i + nx];
@@ -965,17 +1010,18 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
       const double F = hF0 * (w + e - 2 * phi) + hF1 * (s + nn - 2 * phi) + hP * (p - n + C[i]) +
                        (gV[i] - gSum[i] * phi);
       const int bd = (x == 0 || x == nx - 1) + (y == 0 || y == ny - 1);
-      const double scale = bd == 0 ? 1.0 : (bd == 1 ? 0.5 : 0.25);
-      r0[x] = (MT)(F * scale);
+      const MT fF = (MT)F;
+      r0[x] = fF * (bd == 0 ? MT(1) : (bd == 1 ? MT(0.5) : MT(0.25)));
       rho0[x] = (MT)(conc ? p : p + n);
-      aF = fmax(aF, fabs(F));
+      aFm = fmax(aFm, fabs(fF));
       if (it == 0)
         sc = fmax(sc, hP * (fabs(C[i]) + n + p));
       // a NaN would vanish in the maxima: non-finite values count as an
       // infinite residual, which ends the solve as not converged
-      if (!isfinite(F) || !isfinite(p) || !isfinite(n))
-        aF = INFINITY;
+      if (!isfinite(F) || !isfinite(p) || !isfinite(n) || !isfinite(fF))
+        aFm = MT(INFINITY);
     }
+    double aF = (double)aFm;
     // its cluster barrier also orders the writes above; the maxima are next
     // written after the V-cycle's barriers, when every CTA has read them
     cClusterMax2(c, M.offRed, aF, sc, sh);
@@ -1017,17 +1063,18 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     }
     // clamped Newton update of this CTA's rows (updatePotKernel); the cluster
     // barrier makes the new values visible to the neighbours' next residual
-    double upd = 0.;
+    MT updM = 0;
     for (int t = threadIdx.x; t < nOwn; t += blockDim.x) {
       const int ly = L0.byNx.div(t), x = t - ly * nx;
       if (cCoef(c, L0, cRowNearT<true, uint8_t>(c, L0, L0.offCls, ly)[x]).fixed != MT(0))
         continue;
-      double v = (double)cRowNearT<true, MT>(c, L0, L0.offD, ly)[x];
+      MT v = cRowNearT<true, MT>(c, L0, L0.offD, ly)[x];
       if (isfinite(v)) // a non-finite correction is passed on to the next residual
-        v = fmin(kMaxNewtonStep, fmax(-kMaxNewtonStep, v));
-      pot[(size_t)(p0 + ly) * nx + x] += v;
-      upd = isfinite(v) ? fmax(upd, fabs(v)) : INFINITY;
+        v = fmin(MT(kMaxNewtonStep), fmax(MT(-kMaxNewtonStep), v));
+      pot[(size_t)(p0 + ly) * nx + x] += (double)v;
+      updM = isfinite(v) ? fmax(updM, fabs(v)) : MT(INFINITY);
     }
+    double upd = (double)updM;
     if (updTol > 0.) {
       // the maxima of this rule use their own slot (offRed + 16)
       double none = 0.;
