@@ -8,9 +8,9 @@
 #include "emcg_exp.h"
 
 int main() {
-  double tab[32];
-  for (int j = 0; j < 32; j++)
-    tab[j] = std::exp2(j / 32.0);
+  double tab[emcg::kExpTab];
+  for (int j = 0; j < emcg::kExpTab; j++)
+    tab[j] = std::exp2(j / double(emcg::kExpTab));
   double worst = 0, worstX = 0;
   std::mt19937_64 g(7);
   std::uniform_real_distribution<double> u(-699.9, 699.9), s(-40.0, 40.0);
@@ -23,7 +23,7 @@ int main() {
       worstX = x;
     }
   }
-  for (double x : {0.0, -0.0, 1e-300, -1e-300, 0.5 * std::log(2.0) / 32, 699.99, -699.99}) {
+  for (double x : {0.0, -0.0, 1e-300, -1e-300, 0.5 * std::log(2.0) / emcg::kExpTab, 699.99, -699.99}) {
     const double rel = std::fabs(emcg::expTab(x, tab) - std::exp(x)) / std::exp(x);
     if (rel > worst) {
       worst = rel;

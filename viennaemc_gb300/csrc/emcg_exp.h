@@ -2,16 +2,17 @@
 // table-driven method (P. T. P. Tang, "Table-driven implementation of the
 // exponential function in IEEE floating-point arithmetic", ACM Trans. Math.
 // Softw. 15(2), 1989):
-//   x = (32 m + j) ln2/32 + r,  |r| <= ln2/64,
-//   exp(x) = 2^m * 2^(j/32) * (1 + p(r)),
-// p the Taylor polynomial of e^r - 1 to r^6 (truncation below
-// |r|^7/5040 < 4e-18 relative).  The reduction r = x - k ln2/32 takes two
-// fused multiply-adds with ln2/32 split into its nearest double and the
-// remainder, so r is accurate to an ulp of r.  tab[j] = 2^(j/32), j < 32.
-// |x| >= 700 and NaN go to the library's exp.  The residual is evaluated in
-// double precision on 16 SMs; the GPU's double-precision rate is a small
-// fraction of its single-precision one, and this form takes about half the
-// double instructions of a general-purpose exp.
+//   x = (256 m + j) ln2/256 + r,  |r| <= ln2/512,
+//   exp(x) = 2^m * 2^(j/256) * (1 + p(r)),
+// p the Taylor polynomial of e^r - 1 to r^4 (truncation below
+// |r|^5/120 < 4e-17 relative).  k = 256 m + j is rounded by adding 1.5 * 2^52
+// (the integer lands in the low bits of the sum); the reduction
+// r = x - k ln2/256 takes two fused multiply-adds with ln2/256 split into its
+// nearest double and the remainder, so r is accurate to an ulp of r.
+// tab[j] = 2^(j/256), j < 256.  |x| >= 700 and NaN go to the library's exp.
+// The residual is evaluated in double precision on 16 SMs, and the GPU's
+// double-precision rate is a small fraction of its single-precision one: this
+// form takes 9 double instructions.
 #pragma once
 
 #include <math.h>
@@ -26,25 +27,36 @@
 
 namespace emcg {
 
+constexpr int kExpTab = 256;
+
+EMCG_HD uint64_t dbits(double x) {
+  uint64_t b;
+  memcpy(&b, &x, sizeof b);
+  return b;
+}
+EMCG_HD double bitsd(uint64_t b) {
+  double x;
+  memcpy(&x, &b, sizeof x);
+  return x;
+}
+
 EMCG_HD double expTab(double x, const double *tab) {
-  if (!(fabs(x) < 700.0))
+  // |x| < 700 by the high word of |x| (700 = 0x4085E000 00000000); NaN fails
+  if ((uint32_t)(dbits(x) >> 32 & 0x7fffffffu) >= 0x4085E000u)
     return exp(x);
-  const double k = rint(x * 46.16624130844683); // 32 / ln 2
-  const double r = fma(-k, 7.247021293269686e-19, fma(-k, 0.02166084939249829, x));
-  const int n = (int)k;
-  const int j = n & 31;
-  const int m = (n - j) / 32;
-  double q = fma(r, 1.0 / 720, 1.0 / 120);
-  q = fma(r, q, 1.0 / 24);
-  q = fma(r, q, 1.0 / 6);
+  const double kMagic = 6755399441055744.0; // 1.5 * 2^52
+  const double t = fma(x, 369.3299304675746, kMagic); // x * 256 / ln 2, rounded
+  const int n = (int)(uint32_t)dbits(t);
+  const double k = t - kMagic;
+  const double r = fma(-k, 9.058776616587108e-20, fma(-k, 0.0027076061740622863, x));
+  const int j = n & (kExpTab - 1);
+  const int m = (n - j) / kExpTab;
+  double q = fma(r, 1.0 / 24, 1.0 / 6);
   q = fma(r, q, 0.5);
   const double p = fma(r * r, q, r);
-  double y = fma(tab[j], p, tab[j]);
-  uint64_t b;
-  memcpy(&b, &y, sizeof b);
-  b += (uint64_t)(int64_t)m << 52; // y * 2^m: y is near 1, the result stays normal
-  memcpy(&y, &b, sizeof b);
-  return y;
+  const double y = fma(tab[j], p, tab[j]);
+  // y * 2^m: y is near 1, the result stays normal
+  return bitsd(dbits(y) + ((uint64_t)(int64_t)m << 52));
 }
 
 } // namespace emcg

@@ -59,6 +59,59 @@ __global__ void resetBCKernel(double *pot, const uint8_t *mask, const double *va
     pot[i] = val[i];
 }
 
+// x is finite (neither an infinity nor a NaN), by its exponent bits: no
+// double-precision instruction
+__device__ __forceinline__ bool finiteBits(double x) {
+  return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000;
+}
+
+// max of two non-negative doubles (+0 to +inf; a NaN ranks above all) by
+// their bit patterns, which order like the values: integer instructions only
+__device__ __forceinline__ unsigned long long bitsMax(unsigned long long a, unsigned long long b) {
+  return a > b ? a : b;
+}
+__device__ __forceinline__ double dmaxPos(double a, double b) {
+  return __longlong_as_double(
+      (long long)bitsMax((unsigned long long)__double_as_longlong(a),
+                         (unsigned long long)__double_as_longlong(b)));
+}
+
+// F(phi) at node i = (x, y) of the reference equation (the SOR fixed point
+// of emcSORSolver.hpp:131-197 times the FV area), with p = exp(-phi) and n
+// (the concentration, or exp(phi) at equilibrium).  Both solve paths call this
+// one function, so they see the same values to the last bit.  Written for the
+// GPU's narrow double-precision pipes: the table exp, the stencil as three
+// fused multiply-adds, and the gate terms only where a gate contact is (their
+// sums are zero elsewhere, and adding zero changes nothing).
+struct NodeF {
+  double F, p, n;
+};
+__device__ __forceinline__ NodeF nodeResidual(const double *__restrict__ pot,
+                                              const double *__restrict__ conc,
+                                              const double *__restrict__ C,
+                                              const double *__restrict__ gSum,
+                                              const double *__restrict__ gV, int i, int x, int y,
+                                              int nx, int ny, double hF0, double hF1, double c2,
+                                              double hP, const double *tab) {
+  const double phi = pot[i];
+  const double w = x > 0 ? pot[i - 1] : pot[i + 1];
+  const double e = x < nx - 1 ? pot[i + 1] : pot[i - 1];
+  const double s = y > 0 ? pot[i - nx] : pot[i + nx];
+  const double nn = y < ny - 1 ? pot[i + nx] : pot[i - nx];
+  const double gs = gSum[i], gv = gV[i];
+  NodeF r;
+  r.p = expTab(-phi, tab);
+  r.n = conc ? conc[i] : expTab(phi, tab);
+  double F = hF0 * (w + e);
+  F = fma(hF1, s + nn, F);
+  F = fma(c2, phi, F); // c2 = -2 (hF0 + hF1)
+  F = fma(hP, (r.p - r.n) + C[i], F);
+  if (((__double_as_longlong(gs) | __double_as_longlong(gv)) << 1) != 0)
+    F += gv - gs * phi;
+  r.F = F;
+  return r;
+}
+
 // F(phi) of the reference equation, the Jacobian's reaction density and the
 // FV-scaled right-hand side of the correction equation on level 0.
 template <class MT>
@@ -68,9 +121,9 @@ __global__ void nonlinResidualKernel(const double *__restrict__ pot, const doubl
                                      int nx, int ny, double hF0, double hF1, double hP,
                                      MT *__restrict__ rhs, MT *__restrict__ rho, MT *__restrict__ d,
                                      double *__restrict__ stats, int withScale) {
-  __shared__ double tab[32]; // 2^(j/32) for expTab
-  if (threadIdx.x < 32)
-    tab[threadIdx.x] = exp2(threadIdx.x * (1.0 / 32));
+  __shared__ double tab[kExpTab]; // 2^(j/256) for expTab
+  for (int k = threadIdx.x; k < kExpTab; k += blockDim.x)
+    tab[k] = exp2(k * (1.0 / kExpTab));
   __syncthreads();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   MT aF = 0;
@@ -82,15 +135,9 @@ __global__ void nonlinResidualKernel(const double *__restrict__ pot, const doubl
       rho[i] = MT(0);
     } else {
       int x = i % nx, y = i / nx;
-      double phi = pot[i];
-      double p = expTab(-phi, tab);
-      double n = conc ? conc[i] : expTab(phi, tab);
-      double w = x > 0 ? pot[i - 1] : pot[i + 1];
-      double e = x < nx - 1 ? pot[i + 1] : pot[i - 1];
-      double s = y > 0 ? pot[i - nx] : pot[i + nx];
-      double nn = y < ny - 1 ? pot[i + nx] : pot[i - nx];
-      double F = hF0 * (w + e - 2 * phi) + hF1 * (s + nn - 2 * phi) + hP * (p - n + C[i]) +
-                 (gV[i] - gSum[i] * phi);
+      const NodeF q = nodeResidual(pot, conc, C, gSum, gV, i, x, y, nx, ny, hF0, hF1,
+                                   -2.0 * (hF0 + hF1), hP, tab);
+      const double F = q.F, p = q.p, n = q.n;
       int bd = (x == 0 || x == nx - 1) + (y == 0 || y == ny - 1);
       // the FV scale (1, 1/2, 1/4) and the maxima in the multigrid's type:
       // exact scalings, and the maximum needs no more than float accuracy
@@ -103,7 +150,7 @@ __global__ void nonlinResidualKernel(const double *__restrict__ pot, const doubl
       // a NaN would vanish in the maxima (fmax drops it): a non-finite
       // residual or scale term counts as an infinite residual, which ends
       // the solve as not converged
-      if (!isfinite(F) || !isfinite(sc) || !isfinite(fF))
+      if (!finiteBits(F) || !finiteBits(sc) || !isfinite(fF))
         aF = INFINITY;
     }
   }
@@ -849,36 +896,54 @@ template <class MT> __device__ void cCoarse(const CCtx &c, const CLevel<MT> &L, 
 // each CTA's two block maxima sit at byte offset offRed of its shared memory
 __device__ __forceinline__ void cClusterMax2(const CCtx &c, unsigned offRed, double &a,
                                              double &b, double *sh) {
+  // non-negative values: maxima of their bit patterns (integer instructions;
+  // the double-precision pipes are narrow)
+  unsigned long long ua = (unsigned long long)__double_as_longlong(a) & ~(1ull << 63);
+  unsigned long long ub = (unsigned long long)__double_as_longlong(b) & ~(1ull << 63);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
-    b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
+    ua = bitsMax(ua, __shfl_xor_sync(0xffffffffu, ua, o));
+    ub = bitsMax(ub, __shfl_xor_sync(0xffffffffu, ub, o));
   }
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nW = (int)(blockDim.x >> 5);
+  unsigned long long *shu = reinterpret_cast<unsigned long long *>(sh);
   if (lane == 0) {
-    sh[2 * w] = a;
-    sh[2 * w + 1] = b;
+    shu[2 * w] = ua;
+    shu[2 * w + 1] = ub;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double ma = 0., mb = 0.;
-    for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
-      ma = fmax(ma, sh[2 * k]);
-      mb = fmax(mb, sh[2 * k + 1]);
+  if (w == 0) {
+    ua = lane < nW ? shu[2 * lane] : 0ull;
+    ub = lane < nW ? shu[2 * lane + 1] : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ua = bitsMax(ua, __shfl_xor_sync(0xffffffffu, ua, o));
+      ub = bitsMax(ub, __shfl_xor_sync(0xffffffffu, ub, o));
     }
-    double *red = reinterpret_cast<double *>(c.smem + offRed);
-    red[0] = ma;
-    red[1] = mb;
+    if (lane == 0) {
+      unsigned long long *red = reinterpret_cast<unsigned long long *>(c.smem + offRed);
+      red[0] = ua;
+      red[1] = ub;
+    }
   }
   cg::this_cluster().sync();
+  // every warp: lane r reads rank r's maxima, then the warp reduces them
   const int ranks = (int)cg::this_cluster().num_blocks();
-  a = 0.;
-  b = 0.;
-  for (int r = 0; r < ranks; r++) {
-    const double *o = reinterpret_cast<const double *>(c.base[r] + offRed);
-    a = fmax(a, o[0]);
-    b = fmax(b, o[1]);
+  ua = 0ull;
+  ub = 0ull;
+  for (int r = lane; r < ranks; r += 32) {
+    const unsigned long long *o =
+        reinterpret_cast<const unsigned long long *>(c.base[r] + offRed);
+    ua = bitsMax(ua, o[0]);
+    ub = bitsMax(ub, o[1]);
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ua = bitsMax(ua, __shfl_xor_sync(0xffffffffu, ua, o));
+    ub = bitsMax(ub, __shfl_xor_sync(0xffffffffu, ub, o));
+  }
+  a = __longlong_as_double((long long)ua);
+  b = __longlong_as_double((long long)ub);
 }
 
 // out[0] = final relative residual, out[1] = Newton steps done, out[2] = 1 if the
@@ -896,9 +961,9 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
   // the level descriptors, read by every phase, from shared memory rather than
   // the parameter bank
   __shared__ __align__(16) int sM[sizeof(CMG<MT>) / sizeof(int)];
-  __shared__ double sExp[32]; // 2^(j/32) for expTab
-  if (threadIdx.x < 32)
-    sExp[threadIdx.x] = exp2(threadIdx.x * (1.0 / 32));
+  __shared__ double sExp[kExpTab]; // 2^(j/256) for expTab
+  for (int k = threadIdx.x; k < kExpTab; k += blockDim.x)
+    sExp[k] = exp2(k * (1.0 / kExpTab));
   for (int k = threadIdx.x; k < (int)(sizeof(CMG<MT>) / sizeof(int)); k += blockDim.x)
     sM[k] = reinterpret_cast<const int *>(&Mp)[k];
   __syncthreads();
@@ -984,6 +1049,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
   double rel = INFINITY, scale = 0.;
   int it = 0;
   bool stopped = false;
+  const double c2 = -2.0 * (hF0 + hF1);
   for (;; it++) {
     // F(phi), Jacobian reaction and FV-scaled right-hand side (nonlinResidualKernel);
     // the scale of the relative residual from the first iteration's state
@@ -1000,25 +1066,19 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
         rho0[x] = MT(0);
         continue;
       }
-      const double phi = pot[i];
-      const double p = expTab(-phi, sExp);
-      const double n = conc ? conc[i] : expTab(phi, sExp);
-      const double w = x > 0 ? pot[i - 1] : pot[i + 1];
-      const double e = x < nx - 1 ? pot[i + 1] : pot[i - 1];
-      const double s = y > 0 ? pot[i - nx] : pot[i + nx];
-      const double nn = y < ny - 1 ? pot[i + nx] : pot[i - nx];
-      const double F = hF0 * (w + e - 2 * phi) + hF1 * (s + nn - 2 * phi) + hP * (p - n + C[i]) +
-                       (gV[i] - gSum[i] * phi);
+      const NodeF q =
+          nodeResidual(pot, conc, C, gSum, gV, i, x, y, nx, ny, hF0, hF1, c2, hP, sExp);
+      const double F = q.F, p = q.p, n = q.n;
       const int bd = (x == 0 || x == nx - 1) + (y == 0 || y == ny - 1);
       const MT fF = (MT)F;
       r0[x] = fF * (bd == 0 ? MT(1) : (bd == 1 ? MT(0.5) : MT(0.25)));
       rho0[x] = (MT)(conc ? p : p + n);
       aFm = fmax(aFm, fabs(fF));
       if (it == 0)
-        sc = fmax(sc, hP * (fabs(C[i]) + n + p));
+        sc = dmaxPos(sc, hP * (fabs(C[i]) + n + p));
       // a NaN would vanish in the maxima: non-finite values count as an
       // infinite residual, which ends the solve as not converged
-      if (!isfinite(F) || !isfinite(p) || !isfinite(n) || !isfinite(fF))
+      if (!finiteBits(F) || !finiteBits(p) || !finiteBits(n) || !isfinite(fF))
         aFm = MT(INFINITY);
     }
     double aF = (double)aFm;
@@ -1218,7 +1278,8 @@ template <class MT> void clusterPlan(PoissonMG &P) {
       continue;
     size_t bytes = 0;
     clusterDesc<MT>(P, CL, &bytes);
-    if (bytes == 0 || bytes + sizeof(CMG<MT>) + 1024 > kClusterSmemMax)
+    // the static part: the level descriptors, the exp table and the reduction slots
+    if (bytes == 0 || bytes + sizeof(CMG<MT>) + kExpTab * sizeof(double) + 1024 > kClusterSmemMax)
       continue;
     auto k = poissonClusterKernel<MT>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
