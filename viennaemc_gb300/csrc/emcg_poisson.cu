@@ -164,6 +164,14 @@ __global__ void nonlinResidualKernel(const double *__restrict__ pot, const doubl
   }
 }
 
+// 2^(j/256), j < 256, for expTab: the same values as the multi-launch
+// residual kernel forms in its shared memory
+__global__ void expTableKernel(double *tab) {
+  const int k = threadIdx.x;
+  if (k < kExpTab)
+    tab[k] = exp2(k * (1.0 / kExpTab));
+}
+
 template <class MT>
 __global__ void updatePotKernel(double *__restrict__ pot, const MT *__restrict__ d,
                                 const uint8_t *__restrict__ fixed, int n, double *stats) {
@@ -954,16 +962,27 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
                          const double *__restrict__ C, const double *__restrict__ gSum,
                          const double *__restrict__ gV, double hF0, double hF1, double hP,
                          double rtol, int maxCycles, double updTol,
-                         double *__restrict__ out) {
+                         const double *__restrict__ expG, double *__restrict__ out) {
   extern __shared__ __align__(16) char smem[];
   __shared__ char *sBase[kMaxCluster];
   __shared__ double sh[2 * (kClusterThreads / 32)];
   // the level descriptors, read by every phase, from shared memory rather than
   // the parameter bank
   __shared__ __align__(16) int sM[sizeof(CMG<MT>) / sizeof(int)];
-  __shared__ double sExp[kExpTab]; // 2^(j/256) for expTab
-  for (int k = threadIdx.x; k < kExpTab; k += blockDim.x)
-    sExp[k] = exp2(k * (1.0 / kExpTab));
+  __shared__ __align__(16) double sExp[kExpTab]; // 2^(j/256) for expTab
+  // Staging.  Every table goes by asynchronous copies, all in flight at once
+  // (a plain copy loop per table waited for each table's loads in turn: 20 us
+  // per launch), in two groups: the exp table and level 0's coefficient
+  // classes, which the first residual needs, and then the rest, which lands
+  // while the first residual runs (it is first needed by the V-cycle).
+  const unsigned sBaseAddr = (unsigned)__cvta_generic_to_shared(smem);
+  {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(sExp);
+    for (int k = threadIdx.x; k < kExpTab / 2; k += blockDim.x)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(a + 16u * k),
+                   "l"(expG + 2 * k)
+                   : "memory");
+  }
   for (int k = threadIdx.x; k < (int)(sizeof(CMG<MT>) / sizeof(int)); k += blockDim.x)
     sM[k] = reinterpret_cast<const int *>(&Mp)[k];
   __syncthreads();
@@ -972,56 +991,57 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
   const int rank = (int)cluster.block_rank(), ranks = (int)cluster.num_blocks();
   if (threadIdx.x < ranks)
     sBase[threadIdx.x] = static_cast<char *>(cluster.map_shared_rank((void *)smem, threadIdx.x));
-  // stage the class and transfer tables (every CTA) and this CTA's rows of
-  // class indices.  The word tables go by asynchronous copies, all in flight
-  // at once (a plain copy loop per table waited for each table's loads in
-  // turn: 20 us per launch); the class bytes of every level by one loop.
+  auto stage = [&](unsigned off, const void *src, int n) {
+    const int *sp = static_cast<const int *>(src);
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sBaseAddr + off + 4u * k),
+                   "l"(sp + k)
+                   : "memory");
+  };
+  int clsEnd[16]; // prefix sums of this CTA's class bytes per level
   {
-    const unsigned sBaseAddr = (unsigned)__cvta_generic_to_shared(smem);
-    auto stage = [&](unsigned off, const void *src, int n) {
-      const int *sp = static_cast<const int *>(src);
-      for (int k = threadIdx.x; k < n; k += blockDim.x)
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sBaseAddr + off + 4u * k),
-                     "l"(sp + k)
-                     : "memory");
-    };
-    int clsEnd[16]; // prefix sums of this CTA's class bytes per level
     int nCls = 0;
     for (int l = 0; l < M.nLev; l++) {
       const CLevel<MT> &L = M.L[l];
-      stage(L.offTab, L.tab, 8 * L.nCls * (int)(sizeof(MT) / 4));
       int r0, r1;
       cOwnRows(CCtx{sBase, smem, rank}, L, r0, r1);
       nCls += L.nx * (r1 - r0);
       clsEnd[l] = nCls;
-      if (l + 1 < M.nLev) { // the residual of Dirichlet nodes stays 0
-        MT *res = reinterpret_cast<MT *>(smem + L.offRes);
-        for (int k = threadIdx.x; k < L.nx * (r1 - r0); k += blockDim.x)
-          res[k] = MT(0);
-      }
-      if (L.ncx > 0) {
-        stage(L.offPxI, L.pxIdx, L.nx);
-        stage(L.offPxW, L.pxW, L.nx);
-        stage(L.offPyI, L.pyIdx, L.ny);
-        stage(L.offPyW, L.pyW, L.ny);
-        stage(L.offRxI, L.rxIdx, 3 * L.ncx);
-        stage(L.offRxW, L.rxW, 3 * L.ncx);
-        stage(L.offRyI, L.ryIdx, 3 * L.ncy);
-        stage(L.offRyW, L.ryW, 3 * L.ncy);
-        stage(L.offMapX, L.mapX, L.ncx);
-        stage(L.offMapY, L.mapY, L.ncy);
-      }
     }
-    // four bytes per thread and pass: the loads first, then the stores
-    for (int t0 = threadIdx.x; t0 < nCls; t0 += 4 * blockDim.x) {
+  }
+  stage(M.L[0].offTab, M.L[0].tab, 8 * M.L[0].nCls * (int)(sizeof(MT) / 4));
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  for (int l = 0; l < M.nLev; l++) {
+    const CLevel<MT> &L = M.L[l];
+    if (l > 0)
+      stage(L.offTab, L.tab, 8 * L.nCls * (int)(sizeof(MT) / 4));
+    if (L.ncx > 0) {
+      stage(L.offPxI, L.pxIdx, L.nx);
+      stage(L.offPxW, L.pxW, L.nx);
+      stage(L.offPyI, L.pyIdx, L.ny);
+      stage(L.offPyW, L.pyW, L.ny);
+      stage(L.offRxI, L.rxIdx, 3 * L.ncx);
+      stage(L.offRxW, L.rxW, 3 * L.ncx);
+      stage(L.offRyI, L.ryIdx, 3 * L.ncy);
+      stage(L.offRyW, L.ryW, 3 * L.ncy);
+      stage(L.offMapX, L.mapX, L.ncx);
+      stage(L.offMapY, L.mapY, L.ncy);
+    }
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  // this CTA's class bytes of the levels [clsEnd[l0 - 1], clsEnd[l1 - 1]), four
+  // bytes per thread and pass: the loads first, then the stores
+  auto copyCls = [&](int l0, int l1) {
+    const int begin = l0 > 0 ? clsEnd[l0 - 1] : 0, end = clsEnd[l1 - 1];
+    for (int t0 = begin + (int)threadIdx.x; t0 < end; t0 += 4 * blockDim.x) {
       uint8_t v[4];
       uint8_t *dst[4];
 #pragma unroll
       for (int j = 0; j < 4; j++) {
         const int t = t0 + j * (int)blockDim.x;
         dst[j] = nullptr;
-        if (t < nCls) {
-          int l = 0;
+        if (t < end) {
+          int l = l0;
           while (t >= clsEnd[l])
             l++;
           const CLevel<MT> &L = M.L[l];
@@ -1036,16 +1056,18 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
         if (dst[j])
           *dst[j] = v[j];
     }
-    asm volatile("cp.async.wait_all;" ::: "memory");
-  }
+  };
+  copyCls(0, 1);
+  asm volatile("cp.async.wait_group 1;" ::: "memory"); // the exp table and level 0's classes
   __syncthreads();
+  // (no cluster barrier yet: the first access to another CTA's shared memory
+  // comes after the cluster barrier of the first residual's maxima)
   CCtx c{sBase, smem, rank};
   const CLevel<MT> &L0 = M.L[0];
   const int nx = L0.nx, ny = L0.ny;
   int p0, p1;
   cOwnRows(c, L0, p0, p1);
   const int nOwn = nx * (p1 - p0);
-  cluster.sync();
   double rel = INFINITY, scale = 0.;
   int it = 0;
   bool stopped = false;
@@ -1080,6 +1102,21 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
       // infinite residual, which ends the solve as not converged
       if (!finiteBits(F) || !finiteBits(p) || !finiteBits(n) || !isfinite(fF))
         aFm = MT(INFINITY);
+    }
+    if (it == 0) {
+      // the rest of the staging: the class bytes of the other levels, zero
+      // residuals (Dirichlet nodes keep them), the asynchronous copies; the
+      // barriers of the maxima below make them visible
+      copyCls(1, M.nLev);
+      for (int l = 0; l + 1 < M.nLev; l++) {
+        const CLevel<MT> &L = M.L[l];
+        int r0, r1;
+        cOwnRows(c, L, r0, r1);
+        MT *res = reinterpret_cast<MT *>(smem + L.offRes);
+        for (int k = threadIdx.x; k < L.nx * (r1 - r0); k += blockDim.x)
+          res[k] = MT(0);
+      }
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
     }
     double aF = (double)aFm;
     // its cluster barrier also orders the writes above; the maxima are next
@@ -1452,6 +1489,9 @@ int32_t poissonCreate(PoissonMG &P, const PoissonSetup &S, bool fp32, int smooth
   EMCG_TRY(upload(&P.resetEq, S.resetEq, st));
   EMCG_TRY(upload(&P.resetNe, S.resetNe, st));
   EMCG_CUDA(cudaMalloc(&P.stats, 3 * sizeof(double)));
+  EMCG_CUDA(cudaMalloc(&P.expTab, kExpTab * sizeof(double)));
+  expTableKernel<<<1, kExpTab, 0, st>>>(P.expTab);
+  EMCG_CUDA(cudaGetLastError());
   // level hierarchy (host)
   std::vector<double> X(nx), Y(ny);
   for (int i = 0; i < nx; i++)
@@ -1571,7 +1611,8 @@ void poissonFree(PoissonMG &P) {
       cudaFree(p);
   }
   P.L.clear();
-  void *ps[] = {P.C, P.gSum, P.gVeq, P.gVne, P.resetMask, P.resetEq, P.resetNe, P.stats};
+  void *ps[] = {P.C,       P.gSum,    P.gVeq,  P.gVne,  P.resetMask,
+                P.resetEq, P.resetNe, P.stats, P.expTab};
   for (void *p : ps)
     cudaFree(p);
   if (P.hStats)
@@ -1589,7 +1630,7 @@ static int32_t clusterLaunch(PoissonMG &P, double *pot, const double *conc, doub
   cudaLaunchConfig_t cfg = clusterConfig<MT>(P.clusterSize, bytes, st, &at);
   EMCG_CUDA(cudaLaunchKernelEx(&cfg, poissonClusterKernel<MT>, M, pot, conc, P.C, P.gSum,
                                conc ? P.gVne : P.gVeq, P.hF[0], P.hF[1], P.hP, rtol, maxCycles,
-                               P.updTol, P.stats));
+                               P.updTol, (const double *)P.expTab, P.stats));
   return EMCG_OK;
 }
 

@@ -68,6 +68,7 @@ struct PoissonMG {
   uint8_t *resetMask = nullptr;
   double *resetEq = nullptr, *resetNe = nullptr;
   double *stats = nullptr; // [max|F|, scale, max|d|] as ordered bits
+  double *expTab = nullptr; // 2^(j/256), j < 256, for the residual's exp
   // red-black sweeps before and after the coarse correction, and sweeps on
   // the coarsest level
   int pre = 3, post = 3, coarseSweeps = 16;
