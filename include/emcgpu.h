@@ -517,6 +517,13 @@ int32_t emcg_device_step_many(emcg_handle **h, int32_t n, int32_t n_steps, uint3
    -1 = leave as is.  *cluster_size (may be NULL) receives the CTAs per
    cluster of the solve in use, 0 for the multi-launch path. */
 int32_t emcg_device_poisson_mode(emcg_handle *h, int32_t mode, int32_t *cluster_size);
+/* Upper bound on the CTAs of the single-launch Poisson cluster (0: none; the
+   largest size whose layout fits is taken, 16, 14, 12, 10, 8, 4, 2 or 1).
+   The result does not depend on the size.  *cluster_size (may be NULL)
+   receives the size now in use (0 for the multi-launch path).
+   emcg_device_step_many plans its engines' clusters for the batch by itself:
+   sizes of which the device holds all n at once.  No reference counterpart. */
+int32_t emcg_device_set_poisson_cluster(emcg_handle *h, int32_t max_ctas, int32_t *cluster_size);
 /* Change the Poisson settings of a device engine (negative: keep):
    relative-residual target, Newton-step limit, update tolerance [V]. */
 int32_t emcg_device_set_poisson(emcg_handle *h, double rtol, int32_t max_cycles,

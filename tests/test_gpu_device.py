@@ -286,6 +286,46 @@ def test_poisson_cluster_equals_multilaunch(engine, case):
     assert np.max(np.abs(a[3] - b[3])) <= 1e-13 * max(1.0, np.abs(b[3]).max())
 
 
+@pytest.mark.parametrize("case", ["resistor_201x101", "resistor_401x201"])
+def test_poisson_cluster_size_does_not_change_the_solve(engine, case):
+    """Clusters of 16, 14, 12, 10 or 8 CTAs (the sizes a batch of engines may
+    be given so that all their solves fit at once) split the rows differently
+    but evaluate the same expressions: the same Newton steps and potential
+    (1e-13 thermal voltages) as the 16-CTA solve.  On 401 x 201 only 16 and 14
+    CTAs leave each CTA's share of the levels within its shared memory."""
+    from viennaemc_gb300 import _lib as L
+    from viennaemc_gb300 import device as D
+    from viennaemc_gb300 import physics as P
+    dev = _resistor_201x101(2 if case == "resistor_401x201" else 1)
+    pt = P.silicon_electron("refbulk", n_levels=1000, max_energy=4.0, regions=[0],
+                            coulomb=True, region_doping=dev.getDopingRegionDoping)
+    sim = D.DeviceSimulation(dev, pt, scheme=D.CIC, dt=1e-16, seed=5, precision="fp32",
+                             poisson_rtol=1e-10, poisson_max_cycles=200)
+    pot0 = np.arcsinh(0.5 * dev.doping / dev.material.Ni)
+    rs = np.random.default_rng(2)
+    conc = np.exp(pot0) * (1 + 0.05 * rs.standard_normal(pot0.size))
+    out = {}
+    for cap in (16, 14, 12, 10, 8):
+        cs = sim.set_poisson_cluster(cap)
+        if cs == 0 or cs in out:  # the layout does not fit, or the size was run
+            continue
+        sim.set_grid(L.GRID_POTENTIAL, pot0)
+        r1 = sim.poisson(equilibrium=True, reset_bc=True)
+        eq = sim.potential
+        sim.set_grid(L.GRID_CONC, conc)
+        r2 = sim.poisson(equilibrium=False, reset_bc=True)
+        out[cs] = (r1[1], r2[1], eq, sim.potential, r1[0], r2[0])
+    assert sim.set_poisson_cluster(0) == 16
+    sim.close()
+    assert sorted(out) == ([14, 16] if case == "resistor_401x201" else [8, 10, 12, 14, 16])
+    a = out[16]
+    for cs, b in out.items():
+        assert b[:2] == a[:2], (cs, b[:2], a[:2])
+        assert max(b[4], b[5]) <= 1e-10
+        for k in (2, 3):
+            assert np.max(np.abs(b[k] - a[k])) <= 1e-13 * max(1.0, np.abs(a[k]).max()), cs
+
+
 def test_step_many_equals_separate_steps(engine):
     """Stepping two engines concurrently gives what stepping each alone gives."""
     from viennaemc_gb300 import _lib as L

@@ -252,6 +252,7 @@ _EXTRA_DECLS.extend([
     ("emcg_device_timing", [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("emcg_device_poisson_counts", [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("emcg_device_poisson_mode", [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
+    ("emcg_device_set_poisson_cluster", [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     ("emcg_device_set_poisson", [C.c_void_p, C.c_double, C.c_int32, C.c_double]),
     ("emcg_device_step_many", [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_uint32,
                                C.POINTER(C.POINTER(C.c_int32))]),

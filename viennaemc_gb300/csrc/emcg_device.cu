@@ -1563,6 +1563,17 @@ extern "C" int32_t emcg_device_step_many(emcg_handle **hs, int32_t n, int32_t n_
   }
   int dev = 0;
   EMCG_CUDA(cudaGetDevice(&dev));
+  // Each engine's Poisson solve is one thread-block cluster of one CTA per SM.
+  // A batch plans the clusters so that all n fit on the device at once (16
+  // CTAs: 7 resident clusters on GB300; 12: 8), and restores each engine's
+  // own plan afterwards.  The cluster size does not change the result.
+  std::vector<std::pair<int, size_t>> ownPlan(n);
+  for (int i = 0; i < n; i++) {
+    PoissonMG &P = hs[i]->dev->mg;
+    ownPlan[i] = {P.clusterSize, P.clusterSmem};
+    if (n > 1 && P.useCluster && P.clusterSize > 0)
+      EMCG_TRY(poissonPlanCluster(P, n));
+  }
   // one host thread per engine: each drives its own stream, so the engines'
   // kernels (one Poisson cluster each, the particle kernels) run side by side
   std::vector<int32_t> status(n, EMCG_OK);
@@ -1582,6 +1593,11 @@ extern "C" int32_t emcg_device_step_many(emcg_handle **hs, int32_t n, int32_t n_
     });
   for (auto &w : workers)
     w.join();
+  for (int i = 0; i < n; i++) {
+    PoissonMG &P = hs[i]->dev->mg;
+    P.clusterSize = ownPlan[i].first;
+    P.clusterSmem = ownPlan[i].second;
+  }
   for (int i = 0; i < n; i++)
     if (status[i] != EMCG_OK) {
       setError("engine %d of the batch: %s", i, message[i].c_str());
@@ -1596,6 +1612,18 @@ extern "C" int32_t emcg_device_poisson_mode(emcg_handle *h, int32_t mode, int32_
   EMCG_CHECK_ARG(mode >= -1 && mode <= 1, "mode must be -1 (query), 0 or 1");
   if (mode >= 0)
     d->mg.useCluster = mode == 1;
+  if (cluster_size)
+    *cluster_size = d->mg.useCluster ? d->mg.clusterSize : 0;
+  return EMCG_OK;
+}
+
+extern "C" int32_t emcg_device_set_poisson_cluster(emcg_handle *h, int32_t max_ctas,
+                                                   int32_t *cluster_size) {
+  DeviceImpl *d;
+  EMCG_TRY(devOf(h, &d));
+  EMCG_CHECK_ARG(max_ctas >= 0 && max_ctas <= 16, "max_ctas must be 0 (no bound) to 16");
+  d->mg.clusterCap = max_ctas;
+  EMCG_TRY(poissonPlanCluster(d->mg, 1));
   if (cluster_size)
     *cluster_size = d->mg.useCluster ? d->mg.clusterSize : 0;
   return EMCG_OK;

@@ -1303,32 +1303,50 @@ template <class MT> cudaLaunchConfig_t clusterConfig(int CL, size_t bytes, cudaS
   return cfg;
 }
 
-// Largest cluster (16, 8, 4, 2 or 1 CTAs) whose layout fits in shared memory
-// and that the device can place; none: the multi-launch path serves the grid.
-template <class MT> void clusterPlan(PoissonMG &P) {
+// Largest cluster (16, 14, 12, 10, 8, 4, 2 or 1 CTAs, at most P.clusterCap
+// when that is set) whose layout fits in shared memory and of which the
+// device can hold `concurrent` at once (solves of engines stepped side by
+// side); none: the multi-launch path serves the grid.  On GB300 with one
+// 512-thread CTA per SM, 16 or 14 CTAs give 7 resident clusters, 12 give 8,
+// 10 give 13 and 8 give 15.
+template <class MT> void clusterPlan(PoissonMG &P, int concurrent) {
   P.clusterSize = 0;
   P.clusterSmem = 0;
   const int n = P.S.nx * P.S.ny;
-  const int cands[] = {16, 8, 4, 2, 1};
+  auto k = poissonClusterKernel<MT>;
+  // the kernel may take all the dynamic shared memory a block can have: the
+  // attribute is one per kernel, shared by every hierarchy (engines of other
+  // grid sizes), so it is set to the device's limit, not to one layout's size
+  cudaFuncAttributes fa;
+  int dev = 0, optin = 0;
+  if (cudaFuncGetAttributes(&fa, k) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+          cudaSuccess ||
+      optin <= (int)fa.sharedSizeBytes ||
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           optin - (int)fa.sharedSizeBytes) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  const size_t maxDyn = (size_t)(optin - (int)fa.sharedSizeBytes);
+  const bool bigOk =
+      cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+  if (!bigOk)
+    cudaGetLastError();
+  const int cands[] = {16, 14, 12, 10, 8, 4, 2, 1};
   for (int CL : cands) {
+    if (P.clusterCap > 0 && CL > P.clusterCap)
+      continue;
     if (CL > 1 && n <= kSmallNodes)
+      continue;
+    if (CL > 8 && !bigOk)
       continue;
     size_t bytes = 0;
     clusterDesc<MT>(P, CL, &bytes);
     // the static part: the level descriptors, the exp table and the reduction slots
-    if (bytes == 0 || bytes + sizeof(CMG<MT>) + kExpTab * sizeof(double) + 1024 > kClusterSmemMax)
+    if (bytes == 0 || bytes > maxDyn ||
+        bytes + sizeof(CMG<MT>) + kExpTab * sizeof(double) + 1024 > kClusterSmemMax)
       continue;
-    auto k = poissonClusterKernel<MT>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
-        cudaSuccess) {
-      cudaGetLastError();
-      continue;
-    }
-    if (CL > 8 &&
-        cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
-      cudaGetLastError();
-      continue;
-    }
     cudaLaunchAttribute at;
     cudaLaunchConfig_t cfg = clusterConfig<MT>(CL, bytes, nullptr, &at);
     int nc = 0;
@@ -1336,13 +1354,34 @@ template <class MT> void clusterPlan(PoissonMG &P) {
       cudaGetLastError();
       continue;
     }
-    if (nc < 1)
+    if (nc < std::max(1, concurrent))
       continue;
     P.clusterSize = CL;
     P.clusterSmem = bytes;
     return;
   }
 }
+
+} // namespace
+
+int32_t poissonPlanCluster(PoissonMG &P, int concurrent) {
+  if (P.L.empty())
+    return EMCG_OK;
+  if (P.fp32)
+    clusterPlan<float>(P, concurrent);
+  else
+    clusterPlan<double>(P, concurrent);
+  // a cap or a concurrency that nothing meets: plan for one solve at a time
+  if (P.clusterSize == 0 && concurrent > 1) {
+    if (P.fp32)
+      clusterPlan<float>(P, 1);
+    else
+      clusterPlan<double>(P, 1);
+  }
+  return cudaGetLastError() == cudaSuccess ? EMCG_OK : EMCG_ERR_CUDA;
+}
+
+namespace {
 
 template <class MT> void vcycle(PoissonMG &P, int l, cudaStream_t st) {
   MGLevel &lv = P.L[l];
@@ -1594,11 +1633,7 @@ int32_t poissonCreate(PoissonMG &P, const PoissonSetup &S, bool fp32, int smooth
     ly = ncy;
   }
   EMCG_CUDA(cudaStreamSynchronize(st));
-  if (fp32)
-    clusterPlan<float>(P);
-  else
-    clusterPlan<double>(P);
-  return EMCG_OK;
+  return poissonPlanCluster(P, 1);
 }
 
 void poissonFree(PoissonMG &P) {

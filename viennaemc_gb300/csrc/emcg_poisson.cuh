@@ -91,6 +91,8 @@ struct PoissonMG {
   int clusterSize = 0;
   size_t clusterSmem = 0;
   bool useCluster = true;
+  // upper bound on clusterSize set by the caller (0: none)
+  int clusterCap = 0;
   // pinned copy of a cluster solve's [relative residual, Newton steps,
   // stopped by the update rule], written by the stream (poissonEnqueue)
   double *hStats = nullptr;
@@ -113,5 +115,9 @@ int32_t poissonEnqueue(PoissonMG &P, double *pot, const double *conc, bool reset
                        int maxCycles, cudaStream_t st, bool *queued, double *relRes,
                        int *cycles);
 int32_t poissonFinish(PoissonMG &P, double rtol, double *relRes, int *cycles);
+// Re-plan the cluster solve (clusterSize, clusterSmem) under P.clusterCap so
+// that `concurrent` solves of this size fit on the device at once (engines
+// stepped side by side); falls back to the plan for one solve at a time.
+int32_t poissonPlanCluster(PoissonMG &P, int concurrent);
 
 } // namespace emcg

@@ -399,6 +399,13 @@ class DeviceSimulation:
         L.check(self._lib.emcg_device_poisson_mode(self.h, int(mode), C.byref(cs)))
         return cs.value
 
+    def set_poisson_cluster(self, max_ctas=0):
+        """Bound the CTAs of the single-launch Poisson cluster (0: none);
+        returns the cluster size in use (0: multi-launch path)."""
+        cs = C.c_int32()
+        L.check(self._lib.emcg_device_set_poisson_cluster(self.h, int(max_ctas), C.byref(cs)))
+        return cs.value
+
     def set_poisson(self, rtol=None, max_cycles=None, update_tol=None):
         """Poisson settings: relative-residual target, Newton-step limit, and the
         reference SOR's update tolerance in volts (0: off)."""
