@@ -1656,16 +1656,18 @@ void poissonFree(PoissonMG &P) {
 }
 
 // the single-launch cluster solve, enqueued on st
+// out: where the kernel writes [relative residual, Newton steps, stopped by
+// the update rule] (device memory, or mapped page-locked host memory)
 template <class MT>
 static int32_t clusterLaunch(PoissonMG &P, double *pot, const double *conc, double rtol,
-                             int maxCycles, cudaStream_t st) {
+                             int maxCycles, cudaStream_t st, double *out) {
   size_t bytes = 0;
   const CMG<MT> M = clusterDesc<MT>(P, P.clusterSize, &bytes);
   cudaLaunchAttribute at;
   cudaLaunchConfig_t cfg = clusterConfig<MT>(P.clusterSize, bytes, st, &at);
   EMCG_CUDA(cudaLaunchKernelEx(&cfg, poissonClusterKernel<MT>, M, pot, conc, P.C, P.gSum,
                                conc ? P.gVne : P.gVeq, P.hF[0], P.hF[1], P.hP, rtol, maxCycles,
-                               P.updTol, (const double *)P.expTab, P.stats));
+                               P.updTol, (const double *)P.expTab, out));
   return EMCG_OK;
 }
 
@@ -1705,7 +1707,7 @@ static int32_t solveT(PoissonMG &P, double *pot, const double *conc, bool resetB
   bool updStop = false;
   const bool cluster = P.useCluster && P.clusterSize > 0;
   if (cluster) {
-    EMCG_TRY(clusterLaunch<MT>(P, pot, conc, rtol, maxCycles, st));
+    EMCG_TRY(clusterLaunch<MT>(P, pot, conc, rtol, maxCycles, st, P.stats));
     EMCG_CUDA(cudaMemcpyAsync(stats, P.stats, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     EMCG_CUDA(cudaStreamSynchronize(st));
     rel = stats[0];
@@ -1758,17 +1760,20 @@ int32_t poissonEnqueue(PoissonMG &P, double *pot, const double *conc, bool reset
   *queued = false;
   if (!(P.useCluster && P.clusterSize > 0))
     return poissonSolve(P, pot, conc, resetBC, rtol, maxCycles, st, relRes, cycles);
-  if (!P.hStats)
-    EMCG_CUDA(cudaMallocHost(&P.hStats, 3 * sizeof(double)));
+  if (!P.hStats) {
+    EMCG_CUDA(cudaHostAlloc(&P.hStats, 3 * sizeof(double), cudaHostAllocMapped));
+    EMCG_CUDA(cudaHostGetDevicePointer(&P.hStatsDev, P.hStats, 0));
+  }
   if (resetBC) {
     const int n = P.S.nx * P.S.ny;
     resetBCKernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(
         pot, P.resetMask, conc ? P.resetNe : P.resetEq, n);
     EMCG_CUDA(cudaGetLastError());
   }
-  EMCG_TRY(P.fp32 ? clusterLaunch<float>(P, pot, conc, rtol, maxCycles, st)
-                  : clusterLaunch<double>(P, pot, conc, rtol, maxCycles, st));
-  EMCG_CUDA(cudaMemcpyAsync(P.hStats, P.stats, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  // the kernel writes its statistics straight into the page-locked block: no
+  // copy follows it on the stream
+  EMCG_TRY(P.fp32 ? clusterLaunch<float>(P, pot, conc, rtol, maxCycles, st, P.hStatsDev)
+                  : clusterLaunch<double>(P, pot, conc, rtol, maxCycles, st, P.hStatsDev));
   *queued = true;
   return EMCG_OK;
 }

@@ -93,9 +93,10 @@ struct PoissonMG {
   bool useCluster = true;
   // upper bound on clusterSize set by the caller (0: none)
   int clusterCap = 0;
-  // pinned copy of a cluster solve's [relative residual, Newton steps,
-  // stopped by the update rule], written by the stream (poissonEnqueue)
-  double *hStats = nullptr;
+  // page-locked block, mapped into the device's address space, into which an
+  // enqueued cluster solve (poissonEnqueue) writes its [relative residual,
+  // Newton steps, stopped by the update rule]
+  double *hStats = nullptr, *hStatsDev = nullptr; // host and device addresses
 };
 
 int32_t poissonCreate(PoissonMG &P, const PoissonSetup &S, bool fp32, int smooth,
