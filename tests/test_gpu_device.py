@@ -350,6 +350,40 @@ def test_step_many_equals_separate_steps(engine):
         assert np.allclose(pa, pb, rtol=1e-9, atol=1e-9)
 
 
+def test_step_many_plans_clusters_for_the_batch(engine):
+    """Eight engines on 201 x 101 grids (16-CTA Poisson clusters alone; the
+    device holds seven of those at once) stepped as one batch, which plans
+    clusters of a size the device holds eight of: every engine lands where it
+    lands stepped alone (same contact counts, particles and potential), and
+    each engine's own 16-CTA plan is back after the batch."""
+    from viennaemc_gb300 import device as D
+    from viennaemc_gb300 import physics as P
+    dev = _resistor_201x101()
+    dev.setDeviceWidth(2e-6)  # about 1e4 electrons
+    pt = P.silicon_electron("refbulk", n_levels=1000, max_energy=4.0, regions=[0],
+                            coulomb=True, region_doping=dev.getDopingRegionDoping)
+    runs = []
+    for batch in (False, True):
+        sims = []
+        for seed in range(8):
+            sim = D.DeviceSimulation(dev, pt, scheme=D.CIC, dt=1e-16, seed=20 + seed,
+                                     precision="fp32", poisson_rtol=1e-8)
+            sim.calcEquilibriumCharacteristics()
+            assert sim.poisson_mode() == 16
+            sims.append(sim)
+        if batch:
+            nets = D.DeviceSimulation.performEMCStepMany(sims, 3)
+            assert all(s.poisson_mode() == 16 for s in sims)
+        else:
+            nets = [s.performEMCStep(3) for s in sims]
+        runs.append([(n, s.potential, s.num_particles()) for n, s in zip(nets, sims)])
+        for s in sims:
+            s.close()
+    for (na, pa, ca), (nb, pb, cb) in zip(*runs):
+        assert np.array_equal(na, nb) and ca == cb
+        assert np.max(np.abs(pa - pb)) <= 1e-13 * np.abs(pb).max()
+
+
 def test_execute_writes_reference_output_files(engine, tmp_path):
     """execute() with an output prefix writes the reference's file set: grids
     with their extent, the particle dump, the current table over the

@@ -1566,13 +1566,37 @@ extern "C" int32_t emcg_device_step_many(emcg_handle **hs, int32_t n, int32_t n_
   // Each engine's Poisson solve is one thread-block cluster of one CTA per SM.
   // A batch plans the clusters so that all n fit on the device at once (16
   // CTAs: 7 resident clusters on GB300; 12: 8), and restores each engine's
-  // own plan afterwards.  The cluster size does not change the result.
+  // own plan afterwards.  The cluster size does not change the result.  The
+  // plan for a batch size is kept until the batch size or the engine's bound
+  // changes (planning queries the runtime for every candidate size).
   std::vector<std::pair<int, size_t>> ownPlan(n);
   for (int i = 0; i < n; i++) {
     PoissonMG &P = hs[i]->dev->mg;
     ownPlan[i] = {P.clusterSize, P.clusterSmem};
-    if (n > 1 && P.useCluster && P.clusterSize > 0)
-      EMCG_TRY(poissonPlanCluster(P, n));
+  }
+  int32_t planStatus = EMCG_OK;
+  for (int i = 0; i < n && planStatus == EMCG_OK && n > 1; i++) {
+    PoissonMG &P = hs[i]->dev->mg;
+    if (!P.useCluster || P.clusterSize == 0)
+      continue;
+    if (P.batchFor != n || P.batchCap != P.clusterCap) {
+      planStatus = poissonPlanCluster(P, n);
+      P.batchFor = n;
+      P.batchCap = P.clusterCap;
+      P.batchSize = P.clusterSize;
+      P.batchSmem = P.clusterSmem;
+    }
+    P.clusterSize = P.batchSize;
+    P.clusterSmem = P.batchSmem;
+  }
+  if (planStatus != EMCG_OK) {
+    for (int i = 0; i < n; i++) {
+      PoissonMG &P = hs[i]->dev->mg;
+      P.clusterSize = ownPlan[i].first;
+      P.clusterSmem = ownPlan[i].second;
+      P.batchFor = 0;
+    }
+    return planStatus;
   }
   // one host thread per engine: each drives its own stream, so the engines'
   // kernels (one Poisson cluster each, the particle kernels) run side by side
@@ -1623,6 +1647,7 @@ extern "C" int32_t emcg_device_set_poisson_cluster(emcg_handle *h, int32_t max_c
   EMCG_TRY(devOf(h, &d));
   EMCG_CHECK_ARG(max_ctas >= 0 && max_ctas <= 16, "max_ctas must be 0 (no bound) to 16");
   d->mg.clusterCap = max_ctas;
+  d->mg.batchFor = 0; // a batch plans again under the new bound
   EMCG_TRY(poissonPlanCluster(d->mg, 1));
   if (cluster_size)
     *cluster_size = d->mg.useCluster ? d->mg.clusterSize : 0;

@@ -93,6 +93,10 @@ struct PoissonMG {
   bool useCluster = true;
   // upper bound on clusterSize set by the caller (0: none)
   int clusterCap = 0;
+  // the plan for batchFor solves side by side (emcg_device_step_many) under
+  // the bound batchCap; batchFor = 0: none yet
+  int batchFor = 0, batchCap = 0, batchSize = 0;
+  size_t batchSmem = 0;
   // page-locked block, mapped into the device's address space, into which an
   // enqueued cluster solve (poissonEnqueue) writes its [relative residual,
   // Newton steps, stopped by the update rule]
