@@ -333,34 +333,61 @@ def test_fp32_matches_fp64_within_one_percent(engine):
     assert vd64 < 0 and 4e4 < abs(vd64) < 2e5
 
 
+def _steady_occupancy(engine, n, steps, seed, tail, every, direction):
+    """FP64 engine: drift velocity and energy per step, and the subvalley
+    occupancy (fraction of electrons in each of the three subvalleys)
+    averaged over snapshots every `every` steps of the last `tail` steps."""
+    pt = engine.physics.silicon_electron("jacoboni", temperature=300.0)
+    spec = engine.EnsembleSpec(0, n, 1e6, direction, (1e-6,) * 3, 1e-15, seed, 0, 300.0)
+    b = engine.BulkBatch([pt], [spec], "fp64")
+    b.init_particles(0)
+    obs, occ = [b.step(steps - tail)], []
+    for _ in range(tail // every):
+        obs.append(b.step(every))
+        occ.append(np.bincount(b.get_state(0).sub, minlength=3)[:3] / n)
+    b.close()
+    a = engine.BulkBatch.averages(np.concatenate(obs, axis=1), [n])
+    return a["drift_velocity"][0, :, 0], a["energy"][0, :, 0], np.mean(occ, axis=0)
+
+
 def test_ensemble_statistics_match_reference_16_seeds(engine, oracle):
     """FP64 engine (Philox) vs the reference algorithm with mt19937_64 (oracle,
-    bit-identical to the reference) over 16 seeds: steady drift velocity and
-    energy agree within 3 sigma of the seed-to-seed spread."""
-    n, steps, tail = 1000, 600, 300
+    bit-identical to the reference) over 16 seeds: steady drift velocity,
+    energy and the occupancy of each subvalley (the three X-valley pairs; one
+    valley, so the valley occupancy itself is 1) agree within 3 sigma of the
+    seed-to-seed spread."""
+    n, steps, tail, every = 1000, 600, 300, 100
     m = oracle.silicon_model("jacoboni")
-    ref_v, ref_e, gpu_v, gpu_e = [], [], [], []
+    ref_v, ref_e, ref_o, gpu_v, gpu_e, gpu_o = [], [], [], [], [], []
     for seed in range(1, 17):
         rng = oracle.RngState(oracle.RNG_MT, seed)
         st = m.bulk_init([1e-6] * 3, [2e-7] * 3, 1e21, rng)
         st = st.resize(n) if st.n > n else st
         force = [1.60219e-19 * 1e6, 0, 0]
-        vs, es = [], []
+        vs, es, occ = [], [], []
         for s in range(steps):
             m.bulk_step(st, 1e-15, force, [1e-6] * 3, rng, s)
             if s >= steps - tail:
                 o = m.observables(st, [-1.0, 0, 0])
                 es.append(o[0, 0])
                 vs.append(o[0, 1])
+                if (s + 1 - (steps - tail)) % every == 0:
+                    occ.append(np.bincount(st.sub[:st.n], minlength=3)[:3] / st.n)
         ref_v.append(np.mean(vs))
         ref_e.append(np.mean(es))
-        v, e = _steady(engine, "fp64", st.n, steps, 1000 + seed, direction=(-1, 0, 0))
+        ref_o.append(np.mean(occ, axis=0))
+        v, e, o = _steady_occupancy(engine, st.n, steps, 1000 + seed, tail, every, (-1, 0, 0))
         gpu_v.append(v[-tail:].mean())
         gpu_e.append(e[-tail:].mean())
-    for ref, gpu in ((ref_v, gpu_v), (ref_e, gpu_e)):
+        gpu_o.append(o)
+    ref_o, gpu_o = np.array(ref_o), np.array(gpu_o)
+    pairs = [(ref_v, gpu_v), (ref_e, gpu_e)] + [(ref_o[:, k], gpu_o[:, k]) for k in range(3)]
+    for ref, gpu in pairs:
         ref, gpu = np.array(ref), np.array(gpu)
         sigma = np.sqrt(ref.var(ddof=1) / len(ref) + gpu.var(ddof=1) / len(gpu))
         assert abs(ref.mean() - gpu.mean()) <= 3 * sigma, (ref.mean(), gpu.mean(), sigma)
+    # the field along x lifts the occupancy of one pair above the other two
+    assert gpu_o.mean(axis=0).max() - gpu_o.mean(axis=0).min() > 0.01
 
 
 def test_uneven_batch_equals_separate_runs(engine):
