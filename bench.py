@@ -627,6 +627,8 @@ def _device_bench(args, rank):
            "poisson": "double Newton steps, each with 3 float multigrid V-cycles; stop at 1e-8 "
                       "relative residual",
            "wall_s": wall, "current_A": [float(c) for c in cur]}
+    out.update(_device_rooflines(out["value"], pois_ms / K, cycles / max(solves, 1),
+                                 dev.nx * dev.ny))
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_reference_sor"] = _cpu_sor(dev, sim.potential, sim.concentration)
     # the same steps with the reference SOR's stopping rule (no update above 1e-4 V)
@@ -642,6 +644,30 @@ def _device_bench(args, rank):
                                      "1e-4 V (the reference SOR's rule at its accuracy)"}
     sim.close()
     return out
+
+
+def _device_rooflines(psteps, pois_ms, newton, nodes, pre=3, post=3, vcycles=3):
+    """The device step's two bounds: the particle kernels against HBM
+    (64 B per particle-step, the 2-D float state read and written once) and
+    the Poisson solve's algorithmic bytes (per V-cycle and level, pre + post
+    sweeps and one residual of 16 B per node, levels adding a third) against
+    the same peak: the grids stay in shared memory and L2, so both report how
+    far the step is from a bandwidth bound, not the bound itself (launch and
+    barrier latency)."""
+    peak, src = _peaks()
+    pbytes = (pre + post + 1) * 16.0 * nodes * 4.0 / 3.0 * vcycles * newton
+    pgbs = pbytes / (pois_ms * 1e-3) / 1e9
+    agbs = psteps * 64.0 / 1e9
+    return {"particle_roofline": {"bound": "hbm", "bytes_per_unit": 64,
+                                  "unit_of_work": "particle-step", "achieved": agbs,
+                                  "peak": peak, "unit": "GB/s", "frac": agbs / peak,
+                                  "peak_source": src},
+            "poisson_roofline": {"bound": "latency", "algorithmic_bytes_per_solve": pbytes,
+                                 "achieved": pgbs, "peak": peak, "unit": "GB/s",
+                                 "frac": pgbs / peak, "peak_source": src,
+                                 "note": "grids resident in shared memory and L2; the solve "
+                                         "waits on barriers (profiles/poisson_cluster_"
+                                         "resistor_201x101_full.md)"}}
 
 
 def mosfet_device(D, P, vds, vgs=1.0, width=1.3e-6):
