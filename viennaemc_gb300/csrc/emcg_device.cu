@@ -1569,10 +1569,15 @@ extern "C" int32_t emcg_device_step_many(emcg_handle **hs, int32_t n, int32_t n_
   // own plan afterwards.  The cluster size does not change the result.  The
   // plan for a batch size is kept until the batch size or the engine's bound
   // changes (planning queries the runtime for every candidate size).
-  std::vector<std::pair<int, size_t>> ownPlan(n);
+  struct Plan {
+    int size;
+    size_t smem;
+    bool even;
+  };
+  std::vector<Plan> ownPlan(n);
   for (int i = 0; i < n; i++) {
     PoissonMG &P = hs[i]->dev->mg;
-    ownPlan[i] = {P.clusterSize, P.clusterSmem};
+    ownPlan[i] = {P.clusterSize, P.clusterSmem, P.clusterEven};
   }
   int32_t planStatus = EMCG_OK;
   for (int i = 0; i < n && planStatus == EMCG_OK && n > 1; i++) {
@@ -1585,17 +1590,24 @@ extern "C" int32_t emcg_device_step_many(emcg_handle **hs, int32_t n, int32_t n_
       P.batchCap = P.clusterCap;
       P.batchSize = P.clusterSize;
       P.batchSmem = P.clusterSmem;
+      P.batchEven = P.clusterEven;
     }
     P.clusterSize = P.batchSize;
     P.clusterSmem = P.batchSmem;
+    P.clusterEven = P.batchEven;
   }
-  if (planStatus != EMCG_OK) {
+  auto restore = [&]() {
     for (int i = 0; i < n; i++) {
       PoissonMG &P = hs[i]->dev->mg;
-      P.clusterSize = ownPlan[i].first;
-      P.clusterSmem = ownPlan[i].second;
-      P.batchFor = 0;
+      P.clusterSize = ownPlan[i].size;
+      P.clusterSmem = ownPlan[i].smem;
+      P.clusterEven = ownPlan[i].even;
     }
+  };
+  if (planStatus != EMCG_OK) {
+    restore();
+    for (int i = 0; i < n; i++)
+      hs[i]->dev->mg.batchFor = 0;
     return planStatus;
   }
   // one host thread per engine: each drives its own stream, so the engines'
@@ -1617,11 +1629,7 @@ extern "C" int32_t emcg_device_step_many(emcg_handle **hs, int32_t n, int32_t n_
     });
   for (auto &w : workers)
     w.join();
-  for (int i = 0; i < n; i++) {
-    PoissonMG &P = hs[i]->dev->mg;
-    P.clusterSize = ownPlan[i].first;
-    P.clusterSmem = ownPlan[i].second;
-  }
+  restore();
   for (int i = 0; i < n; i++)
     if (status[i] != EMCG_OK) {
       setError("engine %d of the batch: %s", i, message[i].c_str());

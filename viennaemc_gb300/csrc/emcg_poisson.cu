@@ -1193,8 +1193,14 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
 }
 
 // Level layout of the cluster solve for CL CTAs; *bytes = dynamic shared memory,
-// 0 if some level has too many coefficient classes.
-template <class MT> CMG<MT> clusterDesc(const PoissonMG &P, int CL, size_t *bytes) {
+// 0 if some level has too many coefficient classes.  evenRows: a distributed
+// level followed by another gets an even number of rows per CTA, so that a
+// CTA's coarse rows lie under its fine rows; without it the bands of two
+// levels may be a row apart, and a restriction or prolongation then reaches a
+// neighbour's row through distributed shared memory (the same arithmetic, a
+// row less per CTA and level: the 401 x 201 grid fits in 12 CTAs).
+template <class MT>
+CMG<MT> clusterDesc(const PoissonMG &P, int CL, size_t *bytes, bool evenRows = true) {
   CMG<MT> M;
   std::memset(&M, 0, sizeof(M));
   M.nLev = (int)P.L.size();
@@ -1229,7 +1235,7 @@ template <class MT> CMG<MT> clusterDesc(const PoissonMG &P, int CL, size_t *byte
     int rows = even;
     if (l > 0 && M.L[l - 1].ny > 3 && M.L[l - 1].rowsPer / 2 * CL >= c.ny)
       rows = M.L[l - 1].rowsPer / 2;
-    if (l < B && (rows & 1))
+    if (evenRows && l < B && (rows & 1))
       rows++;
     c.rowsPer = rows;
   }
@@ -1341,12 +1347,20 @@ template <class MT> void clusterPlan(PoissonMG &P, int concurrent) {
       continue;
     if (CL > 8 && !bigOk)
       continue;
-    size_t bytes = 0;
-    clusterDesc<MT>(P, CL, &bytes);
     // the static part: the level descriptors, the exp table and the reduction slots
-    if (bytes == 0 || bytes > maxDyn ||
-        bytes + sizeof(CMG<MT>) + kExpTab * sizeof(double) + 1024 > kClusterSmemMax)
-      continue;
+    auto fits = [&](size_t b) {
+      return b != 0 && b <= maxDyn &&
+             b + sizeof(CMG<MT>) + kExpTab * sizeof(double) + 1024 <= kClusterSmemMax;
+    };
+    size_t bytes = 0;
+    bool even = true;
+    clusterDesc<MT>(P, CL, &bytes, true);
+    if (!fits(bytes)) {
+      even = false;
+      clusterDesc<MT>(P, CL, &bytes, false);
+      if (!fits(bytes))
+        continue;
+    }
     cudaLaunchAttribute at;
     cudaLaunchConfig_t cfg = clusterConfig<MT>(CL, bytes, nullptr, &at);
     int nc = 0;
@@ -1358,6 +1372,7 @@ template <class MT> void clusterPlan(PoissonMG &P, int concurrent) {
       continue;
     P.clusterSize = CL;
     P.clusterSmem = bytes;
+    P.clusterEven = even;
     return;
   }
 }
@@ -1662,7 +1677,7 @@ template <class MT>
 static int32_t clusterLaunch(PoissonMG &P, double *pot, const double *conc, double rtol,
                              int maxCycles, cudaStream_t st, double *out) {
   size_t bytes = 0;
-  const CMG<MT> M = clusterDesc<MT>(P, P.clusterSize, &bytes);
+  const CMG<MT> M = clusterDesc<MT>(P, P.clusterSize, &bytes, P.clusterEven);
   cudaLaunchAttribute at;
   cudaLaunchConfig_t cfg = clusterConfig<MT>(P.clusterSize, bytes, st, &at);
   EMCG_CUDA(cudaLaunchKernelEx(&cfg, poissonClusterKernel<MT>, M, pot, conc, P.C, P.gSum,

@@ -90,6 +90,7 @@ struct PoissonMG {
   // multi-launch path
   int clusterSize = 0;
   size_t clusterSmem = 0;
+  bool clusterEven = true; // the layout's bands have even rows (see clusterDesc)
   bool useCluster = true;
   // upper bound on clusterSize set by the caller (0: none)
   int clusterCap = 0;
@@ -97,6 +98,7 @@ struct PoissonMG {
   // the bound batchCap; batchFor = 0: none yet
   int batchFor = 0, batchCap = 0, batchSize = 0;
   size_t batchSmem = 0;
+  bool batchEven = true;
   // page-locked block, mapped into the device's address space, into which an
   // enqueued cluster solve (poissonEnqueue) writes its [relative residual,
   // Newton steps, stopped by the update rule]
