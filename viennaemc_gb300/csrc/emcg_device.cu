@@ -196,7 +196,7 @@ __device__ __forceinline__ int devParticleStep(const ModelK<T> &M, const DevK &G
 }
 
 template <class T, int SCHEME, bool REPLAY>
-__global__ void devMoveKernel(StateK<T> st, const ModelK<T> *__restrict__ models, DevK G,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) devMoveKernel(StateK<T> st, const ModelK<T> *__restrict__ models, DevK G,
                               const T *__restrict__ Ex, const T *__restrict__ Ey, T charge, T dt,
                               const int64_t *__restrict__ nPtr, uint32_t step, uint32_t key0,
                               uint32_t key1, uint32_t stream, uint8_t *__restrict__ drop,
