@@ -195,13 +195,16 @@ __device__ __forceinline__ int devParticleStep(const ModelK<T> &M, const DevK &G
   return err;
 }
 
+// the float instance is capped at 64 registers, 4 blocks of 256 per SM (72
+// registers gave 3; a one-step launch needs the warps to hide its loads)
 template <class T, int SCHEME, bool REPLAY>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) devMoveKernel(StateK<T> st, const ModelK<T> *__restrict__ models, DevK G,
-                              const T *__restrict__ Ex, const T *__restrict__ Ey, T charge, T dt,
-                              const int64_t *__restrict__ nPtr, uint32_t step, uint32_t key0,
-                              uint32_t key1, uint32_t stream, uint8_t *__restrict__ drop,
-                              int32_t *__restrict__ netto, const uint64_t *__restrict__ rw,
-                              const int64_t *__restrict__ roff, int *__restrict__ err) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1)
+    devMoveKernel(StateK<T> st, const ModelK<T> *__restrict__ models, DevK G,
+                  const T *__restrict__ Ex, const T *__restrict__ Ey, T charge, T dt,
+                  const int64_t *__restrict__ nPtr, uint32_t step, uint32_t key0, uint32_t key1,
+                  uint32_t stream, uint8_t *__restrict__ drop, int32_t *__restrict__ netto,
+                  const uint64_t *__restrict__ rw, const int64_t *__restrict__ roff,
+                  int *__restrict__ err) {
   const int64_t n = *nPtr;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n)
