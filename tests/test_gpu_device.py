@@ -318,6 +318,10 @@ def test_poisson_cluster_size_does_not_change_the_solve(engine, case):
         r2 = sim.poisson(equilibrium=False, reset_bc=True)
         out[cs] = (r1[1], r2[1], eq, sim.potential, r1[0], r2[0])
     assert sim.set_poisson_cluster(0) == 16
+    for bad in (-1, 17):
+        with pytest.raises(engine._lib.EmcgError):
+            sim.set_poisson_cluster(bad)
+    assert sim.poisson_mode() == 16
     sim.close()
     assert sorted(out) == ([12, 14, 16] if case == "resistor_401x201" else [8, 10, 12, 14, 16])
     a = out[16]
