@@ -290,6 +290,51 @@ def test_drift_known_answers(engine, precision, ktol, ptol):
     b.close()
 
 
+@pytest.mark.parametrize("name", ["X", "L"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_valley_frames_through_drift(engine, name, precision):
+    """The subvalley frames of the reference's tests/testValleyCoordinateTransformation
+    (an X valley of 6 subvalleys, an L valley of 8) through the engine's drift
+    with no force: k comes back unchanged from the ellipse frame, and the
+    displacement is R^T (vogt * R k) hbar dt / (m_c (1 + 2 alpha E)), which
+    holds only if the engine's R is the subvalley's normalised axes."""
+    from test_host import VALLEY_FRAMES
+    from viennaemc_gb300 import physics
+    hbar, me, dt = 1.05459e-34, 9.11e-31, 1e-15
+    masses, alpha, frames = VALLEY_FRAMES[name]
+    n = len(frames)
+    pt = physics.Electron(1000, 1.0)
+    v = physics.NonParabolicAnisotropValley(list(masses), me, n, alpha)
+    for s, (a, bb, c) in enumerate(frames):
+        v.setSubValleyEllipseCoordSystem(s, a, bb, c)
+    pt.addValley(v)
+    pt.addScatterMechanism([0], physics.AcousticScatterMechanism(0, 9.0, 300, 2329., 9040.))
+    pt.initScatterTables()
+    b = engine.BulkBatch([pt], [engine.EnsembleSpec(0, 1, 0.0, (1, 0, 0), (1e-6,) * 3, dt, 1)],
+                         precision)
+    k0 = np.array([1.0, 2.0, 3.0]) * 1e8
+    k = np.repeat(k0[:, None], n, axis=1).copy()
+    pos = np.zeros((3, n))
+    F = np.zeros((3, n))
+    E = np.zeros(n)
+    sub = np.arange(n, dtype=np.int32)
+    dts = np.full(n, dt)
+    L = engine._lib.lib()
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    engine._lib.check(L.emcg_drift_kat(b.h, 0, n, sub.ctypes.data_as(C.POINTER(C.c_int32)),
+                                       dp(dts), dp(F), dp(k), dp(pos), dp(E)))
+    b.close()
+    rtol = 1e-12 if precision == "fp64" else 2e-6
+    e0 = v.getEnergy(list(k0))
+    vogt = np.array(v.vogt)
+    for s, dirs in enumerate(frames):
+        R = np.array([np.array(d, float) / np.linalg.norm(d) for d in dirs])
+        dx = R.T @ (vogt * (R @ k0)) * hbar * dt / (v.eff_mass_cond * (1 + 2 * alpha * e0))
+        assert np.all(np.abs(k[:, s] - k0) <= rtol * np.abs(k0).max()), s
+        assert np.all(np.abs(pos[:, s] - dx) <= rtol * np.abs(dx).max() * 10), (s, pos[:, s], dx)
+        assert abs(E[s] - e0) <= rtol * 10 * e0, s
+
+
 def _steady(engine, precision, n, steps, seed, field=1e6, direction=(1, 0, 0), model="jacoboni",
             T=300.0):
     pt = engine.physics.silicon_electron(model, temperature=T)

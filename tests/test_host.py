@@ -187,3 +187,37 @@ def test_poisson_exp_is_accurate(tmp_path):
     worst, _, specials = subprocess.run([str(exe)], check=True, capture_output=True,
                                         text=True).stdout.split()
     assert float(worst) < 5e-16 and specials == "1"
+
+
+# the frames of the reference's tests/testValleyCoordinateTransformation: an
+# X valley with 6 subvalleys and an L valley with 8 (the last repeats the sixth)
+X_FRAMES = [((1, 0, 0), (0, 1, 0), (0, 0, 1)), ((-1, 0, 0), (0, 1, 0), (0, 0, 1)),
+            ((0, 1, 0), (1, 0, 0), (0, 0, 1)), ((0, -1, 0), (1, 0, 0), (0, 0, 1)),
+            ((0, 0, 1), (0, 1, 0), (1, 0, 0)), ((0, 0, -1), (0, 1, 0), (1, 0, 0))]
+L_FRAMES = [((1, 1, 1), (-1, 1, 0), (-1, -1, 2)), ((-1, -1, -1), (-1, 1, 0), (-1, -1, 2)),
+            ((-1, 1, 1), (1, 1, 0), (1, -1, 2)), ((1, -1, 1), (1, 1, 0), (-1, 1, 2)),
+            ((1, 1, -1), (1, 0, 1), (-1, 2, 1)), ((-1, -1, 1), (1, 0, 1), (-1, 2, 1)),
+            ((-1, 1, -1), (1, 1, 0), (-1, 1, 2)), ((-1, -1, 1), (1, 0, 1), (-1, 2, 1))]
+VALLEY_FRAMES = {"X": ((0.9, 0.1, 0.1), 0.5, X_FRAMES), "L": ((0.8, 0.2, 0.2), 0.3, L_FRAMES)}
+
+
+@pytest.mark.parametrize("name", sorted(VALLEY_FRAMES))
+def test_valley_coordinate_transformation_known_answers(name):
+    """tests/testValleyCoordinateTransformation of the reference: the ellipse
+    coordinates of (1, 2, 3) are its inner products with the subvalley's
+    normalised axes, and the way back gives (1, 2, 3) again (1e-9)."""
+    from viennaemc_gb300 import physics
+    masses, alpha, frames = VALLEY_FRAMES[name]
+    v = physics.NonParabolicAnisotropValley(list(masses), 9.11e-31, len(frames), alpha)
+    for s, (a, b, c) in enumerate(frames):
+        v.setSubValleyEllipseCoordSystem(s, a, b, c)
+    vec = np.array([1.0, 2.0, 3.0])
+    for s, dirs in enumerate(frames):
+        R = np.array(v.rot[s]).reshape(3, 3)
+        ell = R @ vec
+        for i, d in enumerate(dirs):
+            d = np.array(d, float) / np.linalg.norm(d)
+            assert abs(ell[i] - vec @ d) <= 1e-9
+        assert np.all(np.abs(R.T @ ell - vec) <= 1e-9)
+    with pytest.raises(ValueError):  # the reference refuses axes that are not orthogonal
+        v.setSubValleyEllipseCoordSystem(0, (1, 0, 0), (1, 1, 0), (0, 0, 1))
