@@ -123,6 +123,17 @@ typedef struct {
   const emcg_tableset_desc *tablesets;
   const double *tables;
   double region_doping[EMCG_MAX_REGIONS];
+  /* A grain mechanism (emcParticleType::setGrainScatterMechanism with an
+     emcGrainScatterMechanism(transmissionProb, scatterRate),
+     include/emcGrainScatterMechanism.hpp:27-80): grain = 1 scatters the
+     particle at every grain event (basicBulkParticleHandler.hpp:215-219,
+     emcBasicParticleHandler.hpp:131-138), reflected when a uniform draw
+     exceeds grain_transmission, else transmitted, with |k| and the energy
+     kept; grain_tau is then 1 / scatterRate.  grain = 0 (a zeroed
+     descriptor): no mechanism, grain events only redraw the timer. */
+  int32_t grain;
+  int32_t grain_pad_;
+  double grain_transmission;
 } emcg_model_desc;
 
 /* One bulk ensemble (basicBulkParticleHandler,
@@ -290,9 +301,10 @@ int32_t emcg_get_launch(emcg_handle *h, int32_t *block_threads, int32_t *steps_p
    boundaries, so a warp's lanes process their events together; per-step
    observables go through a per-warp window).  All follow the same
    per-particle algorithm; replay always uses the lockstep kernel.  In the
-   queued kernel the grain free-flight redraw takes its own Philox calls, so
-   its double-precision stream differs from the lockstep kernel and the
-   oracle in that (rare) event only.  The warp-asynchronous kernel adds its
+   queued kernel a grain event (the grain mechanism's draws and the timer
+   redraw) takes its own Philox calls, so its stream differs from the
+   lockstep kernel and the oracle in grain events only (without a grain
+   mechanism they are rare timer redraws).  The warp-asynchronous kernel adds its
    per-step sums in float in an order that varies from run to run: particle
    states are reproducible bit for bit, observables to float rounding. */
 int32_t emcg_set_scatter_mode(emcg_handle *h, int32_t queued);

@@ -60,6 +60,7 @@
 #include <ValleyTypes/emcNonParabolicAnistropValley.hpp>
 #include <emcBoundaryPos.hpp>
 #include <emcContact.hpp>
+#include <emcGrainScatterMechanism.hpp>
 #include <emcMessage.hpp>
 
 #include "emcgpu.h"
@@ -140,6 +141,19 @@ public:
     pt_.addScatterMechanism(regions, std::move(m));
   }
 
+  // emcParticleType::setGrainScatterMechanism with an
+  // emcGrainScatterMechanism(transmissionProb, scatterRate)
+  // (include/emcGrainScatterMechanism.hpp:27-29): forwarded to the particle
+  // type; its two parameters are kept for the engine, since the reference
+  // keeps them protected.
+  void setGrainScatterMechanism(T transmissionProb, T scatterRate) {
+    pt_.setGrainScatterMechanism(
+        std::make_unique<emcGrainScatterMechanism<T>>(transmissionProb, scatterRate));
+    grain_ = true;
+    grainProb_ = transmissionProb;
+    grainRate_ = scatterRate;
+  }
+
   // ---- engine descriptor (after all mechanisms are registered) ------------
   // Rates are the reference's getScatterRate at (L + 1) dE, accumulated and
   // normalised exactly as emcScatterHandler::renormalizeTables
@@ -181,7 +195,19 @@ public:
     d_.n_tablesets = (int32_t)sets_.size();
     d_.n_levels = (int32_t)nL;
     d_.max_energy = maxE_;
-    d_.grain_tau = pt_.getGrainTau();
+    // the grain free-flight constant: 1 / rate with a mechanism
+    // (include/emcScatterHandler.hpp:233-234), else the particle type's 1.  A
+    // mechanism set on the particle type directly (not through this builder)
+    // has parameters the engine cannot read: refuse it rather than run
+    // without its scattering.
+    if (!grain_ && pt_.getGrainTau() != T(1))
+      emcMessage::getInstance().addError(
+          "libemcgpu: a grain mechanism was set on the particle type directly; set it "
+          "with ModelBuilder::setGrainScatterMechanism so that the engine knows its "
+          "transmission probability");
+    d_.grain_tau = grain_ ? T(1) / grainRate_ : pt_.getGrainTau();
+    d_.grain = grain_ ? 1 : 0;
+    d_.grain_transmission = grain_ ? grainProb_ : T(0);
     d_.valleys = valleys_.data();
     d_.mechs = mechs_.data();
     d_.tablesets = sets_.data();
@@ -272,6 +298,8 @@ private:
   T regionDoping_[EMCG_MAX_REGIONS] = {1.45e16, 1.45e16, 1.45e16, 1.45e16, 1.45e16, 1.45e16,
                                        1.45e16, 1.45e16, 1.45e16, 1.45e16, 1.45e16, 1.45e16,
                                        1.45e16, 1.45e16, 1.45e16, 1.45e16};
+  bool grain_ = false;
+  T grainProb_ = 0, grainRate_ = 0;
   emcg_model_desc d_{};
 };
 

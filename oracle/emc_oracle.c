@@ -57,6 +57,10 @@ struct oc_model {
   double *raw[OC_MAX_VALLEYS][OC_MAX_REGIONS];
   double *norm[OC_MAX_VALLEYS][OC_MAX_REGIONS];
   double tau[OC_MAX_VALLEYS][OC_MAX_REGIONS];
+  /* grain mechanism (include/emcScatterHandler.hpp:61-62, 233-234):
+     grainTau = 1 / rate with one set, 1 without */
+  int32_t grain;
+  double grainProb, grainTau;
   int32_t built;
 };
 
@@ -243,6 +247,7 @@ oc_model *oc_model_new(double temperature, double rho, double vSound,
   m->Vt = C_KB / C_Q * temperature;
   for (int r = 0; r < OC_MAX_REGIONS; r++)
     m->regionDoping[r] = Ni;
+  m->grainTau = 1.;
   return m;
 }
 
@@ -399,6 +404,21 @@ int32_t oc_add_mech(oc_model *m, int32_t kind, int32_t valley,
   m->nM++;
   return idx;
 }
+
+/* emcScatterHandler::setGrainScatterMechanism with an
+   emcGrainScatterMechanism(transmissionProb, scatterRate)
+   (include/emcGrainScatterMechanism.hpp:27-29); the grain free-flight
+   constant becomes 1 / scatterRate (include/emcScatterHandler.hpp:233-234) */
+int32_t oc_set_grain(oc_model *m, double transmissionProb, double scatterRate) {
+  if (!(scatterRate > 0))
+    return -1;
+  m->grain = 1;
+  m->grainProb = transmissionProb;
+  m->grainTau = 1. / scatterRate;
+  return 0;
+}
+
+double oci_grain_tau(const oc_model *m) { return m->grainTau; }
 
 int32_t oc_set_region_doping(oc_model *m, int32_t region, double doping) {
   if (region < 0 || region >= OC_MAX_REGIONS)
@@ -681,6 +701,27 @@ static void random_direction_wrt_k(const double *k, double ct, double rnd,
   o[2] = -kxp * st0 + kzp * ct0;
 }
 
+/* emcGrainScatterMechanism::scatterParticle
+   (include/emcGrainScatterMechanism.hpp:41-80): reflected (into the opposite
+   hemisphere, cos(theta) <= 0) when a draw exceeds the transmission
+   probability, else transmitted (same hemisphere); |k| is kept and the
+   energy is not updated.  No mechanism: a no-op
+   (include/emcScatterHandler.hpp:193-196). */
+void oci_grain_scatter(const oc_model *m, double *k, dctx *d) {
+  if (!m->grain)
+    return;
+  const int reflect = oci_draw_u01(d) > m->grainProb;
+  double rnd = oci_draw_u01(d);
+  if (reflect) {
+    if (rnd < 0.5)
+      rnd += 0.5;
+  } else if (rnd > 0.5) {
+    rnd -= 0.5;
+  }
+  const double kin[3] = {k[0], k[1], k[2]};
+  random_direction_wrt_k(kin, 1 - 2 * rnd, oci_draw_u01(d), k);
+}
+
 /* include/emcScatterHandler.hpp:237-244 with the x86-64 size_t conversion of
    floor(E/dE) - 1 (-1 -> 0; other negatives and NaN wrap to the top level) */
 static int32_t energy_level(const oc_model *m, double E) {
@@ -811,8 +852,10 @@ static int32_t bulk_particle_step(const oc_model *m, oc_particles *p, int64_t i,
   }
   tau -= dt;
   gtau -= dt;
-  if (gtau <= 0) /* no grain mechanism: scatterParticleAtGrain is a no-op */
-    gtau = -log(oci_draw_ulog(d)) * 1.;
+  if (gtau <= 0) { /* basicBulkParticleHandler.hpp:215-219 */
+    oci_grain_scatter(m, k, d);
+    gtau = -log(oci_draw_ulog(d)) * m->grainTau;
+  }
   p->kx[i] = k[0];
   p->ky[i] = k[1];
   p->kz[i] = k[2];
@@ -1012,7 +1055,7 @@ void oci_init_particle(const oc_model *m, const int64_t *coord,
       k[i] *= -1;
   double tau = -log(oci_draw_ulog(d)) *
                oc_get_tau(m, valley, tauRegionIsValley ? valley : region);
-  double gtau = -log(oci_draw_ulog(d)) * 1.;
+  double gtau = -log(oci_draw_ulog(d)) * m->grainTau;
   p->kx[idx] = k[0];
   p->ky[idx] = k[1];
   p->kz[idx] = k[2];

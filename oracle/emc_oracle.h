@@ -108,6 +108,9 @@ int32_t oc_add_mech(oc_model *m, int32_t kind, int32_t valley,
                     const int32_t *finalSub, const int32_t *regions,
                     int32_t nRegions);
 int32_t oc_set_region_doping(oc_model *m, int32_t region, double doping);
+/* emcParticleType::setGrainScatterMechanism(emcGrainScatterMechanism(
+   transmissionProb, scatterRate)), include/emcGrainScatterMechanism.hpp */
+int32_t oc_set_grain(oc_model *m, double transmissionProb, double scatterRate);
 int32_t oc_build_tables(oc_model *m);
 /* replace the rates of one built (valley, region) table set and
    renormalise it (reinitScatterTables with caller-filled rates) */

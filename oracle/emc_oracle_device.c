@@ -333,8 +333,10 @@ int32_t oc_dev_move(const oc_model *m, const oc_dev *d, int32_t scheme,
       rem[i] = 1;
     }
     gtau -= dt;
-    if (gtau <= 0 && !removed)
-      gtau = -log(oci_draw_ulog(&dc)) * 1.;
+    if (gtau <= 0 && !removed) { /* emcBasicParticleHandler.hpp:131-138 */
+      oci_grain_scatter(m, k, &dc);
+      gtau = -log(oci_draw_ulog(&dc)) * oci_grain_tau(m);
+    }
     p->kx[i] = k[0];
     p->ky[i] = k[1];
     p->kz[i] = k[2];

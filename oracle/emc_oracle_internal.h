@@ -19,6 +19,8 @@ void oci_dctx_init(dctx *d, oc_rng *r, uint32_t pid, uint32_t step, uint32_t str
 uint64_t oci_draw_u64(dctx *d);
 double oci_draw_u01(dctx *d);
 double oci_draw_ulog(dctx *d);
+void oci_grain_scatter(const oc_model *m, double *k, dctx *d);
+double oci_grain_tau(const oc_model *m);
 uint32_t oci_draw_pick(dctx *d, uint32_t n);
 int32_t oci_handler_scatter(const oc_model *m, double *k, double *E, int32_t *valley,
                             int32_t *sub, int32_t region, dctx *d);

@@ -65,6 +65,8 @@ def _declare(L):
     L.oc_add_mech.argtypes = [vp, i32, i32, i32, d, d, i32, P(i32), P(i32), i32]
     L.oc_set_region_doping.restype = i32
     L.oc_set_region_doping.argtypes = [vp, i32, d]
+    L.oc_set_grain.restype = i32
+    L.oc_set_grain.argtypes = [vp, d, d]
     L.oc_build_tables.restype = i32
     L.oc_build_tables.argtypes = [vp]
     for fn in ("oc_get_raw_table", "oc_get_norm_table"):
@@ -259,6 +261,11 @@ class Model:
     def set_region_doping(self, region, doping):
         assert lib().oc_set_region_doping(self.h, region, doping) == 0
 
+    def set_grain(self, transmission_prob, scatter_rate):
+        """emcGrainScatterMechanism(transmissionProb, scatterRate) on the type
+        (include/emcGrainScatterMechanism.hpp:27-29)."""
+        assert lib().oc_set_grain(self.h, transmission_prob, scatter_rate) == 0
+
     def build_tables(self):
         assert lib().oc_build_tables(self.h) == 0
 
@@ -356,9 +363,13 @@ JACOBONI = [("G1", False, 140., 0.5e10), ("G2", False, 215., 0.8e10),
 
 
 def silicon_model(name="jacoboni", temperature=300.0, n_levels=1000, max_energy=1.0,
-                  mt=None, regions=(0,), coulomb=False) -> Model:
-    """Oracle twin of the silicon models used by the reference harness."""
+                  mt=None, regions=(0,), coulomb=False, grain=None) -> Model:
+    """Oracle twin of the silicon models used by the reference harness;
+    grain: (transmission probability, scatter rate [1/s]) of a grain
+    mechanism."""
     m = Model(temperature=temperature, n_levels=n_levels, max_energy=max_energy)
+    if grain is not None:
+        m.set_grain(*grain)
     if mt is None:
         mt = 0.196 if name == "refbulk" else 0.19
     m.add_valley([0.916, mt, mt], ME, 3, 0.5, 0.0, SI_FRAMES)

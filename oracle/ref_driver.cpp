@@ -225,7 +225,8 @@ static void dumpMt(const char *tag, const emcRNG &rng) {
 }
 
 // usage: ref_driver bulk <model> <T> <nLevels> <maxE> <box> <spacing>
-//                   <doping> <seed> <field> <dx> <dy> <dz> <dt> <nSteps>
+//                   <doping> <seed> <field> <dx> <dy> <dz> <dt> <nSteps> <mt>
+//                   [<grain transmission probability> <grain scatter rate>]
 static int runBulk(int argc, char **argv) {
   if (argc < 17) {
     std::fprintf(stderr, "bulk: missing arguments\n");
@@ -253,6 +254,9 @@ static int runBulk(int argc, char **argv) {
   auto el = std::make_unique<emcElectron<T, Dev3>>(spec.nLevels, spec.maxE, false);
   addValley(el, mt);
   addMechanisms(spec, el, device, {0});
+  if (argc > 18)
+    el->setGrainScatterMechanism(
+        std::make_unique<emcGrainScatterMechanism<T>>(std::atof(argv[17]), std::atof(argv[18])));
   types[0] = std::move(el);
   // tables are written to files by initScatterTables; keep them out of cwd
   Handler handler(device, types, dir, field, seed);

@@ -80,5 +80,16 @@ int main() {
   for (int k = 0; k < g.n_contacts; k++)
     std::printf("contact %d %d %a %a %a %a\n", k, g.contact_type[k], g.contact_voltage[k],
                 g.contact_param[3 * k], g.contact_param[3 * k + 1], g.contact_param[3 * k + 2]);
+  // a grain mechanism set through the builder (and forwarded to the type)
+  emcElectron<T, Dev3> el2(1000, 1., false);
+  std::unique_ptr<emcNonParabolicAnisotropValley<T>> v2(
+      new emcNonParabolicAnisotropValley<T>({0.916, 0.19, 0.19}, el2.getMass(), 3, 0.5));
+  el2.addValley(std::move(v2));
+  emcgpu::ModelBuilder<T, Dev3> mb2(el2, 1000, 1.);
+  mb2.addAcoustic(0, 9., device, {0});
+  mb2.setGrainScatterMechanism(0.3, 2e14);
+  const emcg_model_desc &d2 = mb2.desc();
+  std::printf("grain %d %a %a\n", d2.grain, d2.grain_transmission, d2.grain_tau);
+  std::printf("nograin %d %a\n", d.grain, d.grain_tau);
   return 0;
 }

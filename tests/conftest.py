@@ -22,7 +22,8 @@ def golden(name: str) -> dict:
         return {k: z[k] for k in z.files}
 
 
-BULK_CASES = ["bulk_jacoboni_300K.npz", "bulk_refbulk_300K.npz", "bulk_jacoboni_77K_111.npz"]
+BULK_CASES = ["bulk_jacoboni_300K.npz", "bulk_refbulk_300K.npz", "bulk_jacoboni_77K_111.npz",
+              "bulk_jacoboni_300K_grain.npz"]
 
 
 def case_model(g: dict):
@@ -30,6 +31,12 @@ def case_model(g: dict):
     T, nL, maxE, box, h, doping, seed, field, dt, steps, mt = g["params"]
     name = "refbulk" if g["raw"].shape[0] == 9 else "jacoboni"
     return name, float(T), int(nL), float(maxE), float(mt)
+
+
+def case_grain(g: dict):
+    """(transmission probability, scatter rate) of the fixture's grain
+    mechanism, None without one."""
+    return tuple(float(x) for x in g["grain"]) if "grain" in g else None
 
 
 @pytest.fixture(scope="session")

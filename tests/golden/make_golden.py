@@ -34,7 +34,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import pyoracle as po  # noqa: E402
 
-# (name, model, T, nLevels, maxE, box, spacing, doping, seed, field, dir, dt, steps, mt)
+# (name, model, T, nLevels, maxE, box, spacing, doping, seed, field, dir, dt, steps, mt
+#  [, grain mechanism (transmission probability, scatter rate [1/s])])
 CASES = [
     ("jacoboni_300K", "jacoboni", 300.0, 1000, 1.0, 5e-7, 1e-7, 6e20, 12345, 1e6,
      (-1, 0, 0), 1e-15, 24, 0.19),
@@ -42,13 +43,19 @@ CASES = [
      (-1, 0, 0), 5e-16, 24, 0.196),
     ("jacoboni_77K_111", "jacoboni", 77.0, 2000, 2.0, 5e-7, 1e-7, 6e20, 4242, 1e7,
      (1, 1, 1), 1e-15, 24, 0.19),
+    # an emcGrainScatterMechanism: a grain every 5 fs on average, half of the
+    # particles transmitted, half reflected
+    ("jacoboni_300K_grain", "jacoboni", 300.0, 1000, 1.0, 5e-7, 1e-7, 6e20, 2468, 1e6,
+     (-1, 0, 0), 1e-15, 24, 0.19, (0.5, 2e14)),
 ]
 
 
 def make_bulk(case):
-    (name, model, T, nL, maxE, box, h, doping, seed, field, dirn, dt, steps, mt) = case
-    d = po.run_ref("bulk", model, T, nL, maxE, box, h, doping, seed, field, *dirn, dt, steps, mt)
-    m = po.silicon_model(model, temperature=T, n_levels=nL, max_energy=maxE, mt=mt)
+    (name, model, T, nL, maxE, box, h, doping, seed, field, dirn, dt, steps, mt) = case[:14]
+    grain = case[14] if len(case) > 14 else None
+    d = po.run_ref("bulk", model, T, nL, maxE, box, h, doping, seed, field, *dirn, dt, steps, mt,
+                   *(grain or ()))
+    m = po.silicon_model(model, temperature=T, n_levels=nL, max_energy=maxE, mt=mt, grain=grain)
     nT = m.n_tables(0, 0)
     raw = np.stack([d[f"raw_v0_r0_t{t}"] for t in range(nT)])
     norm = np.stack([d[f"norm_v0_r0_t{t}"] for t in range(nT)])
@@ -60,6 +67,8 @@ def make_bulk(case):
            "applied_field": d["appliedField"], "field_dir": d["appliedFieldDir"],
            "mt0": d["mt0"], "dt": np.array(dt), "box": np.array(box),
            "params": np.array([T, nL, maxE, box, h, doping, seed, field, dt, steps, mt])}
+    if grain is not None:
+        out["grain"] = np.array(grain, dtype=np.float64)
     st = po.state_from_ref(d, "s0")
     for f in po.STATE_F + po.STATE_I:
         out[f"s0_{f}"] = getattr(st, f)

@@ -57,6 +57,13 @@ def test_adapter_descriptor_matches_host_builder(tmp_path):
         if line.startswith("table"):
             i, v = line.split()[1:]
             assert float.fromhex(v) == tab[int(i)]
+    # the grain mechanism: descriptor fields as the Python builder sets them
+    g = physics.silicon_electron("jacoboni", grain=(0.3, 2e14)).model_desc()
+    flag, prob, gtau = [l for l in out if l.startswith("grain ")][0].split()[1:]
+    assert (int(flag), float.fromhex(prob), float.fromhex(gtau)) == \
+        (g.grain, g.grain_transmission, g.grain_tau)
+    flag, gtau = [l for l in out if l.startswith("nograin ")][0].split()[1:]
+    assert (int(flag), float.fromhex(gtau)) == (d.grain, d.grain_tau) == (0, 1.0)
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include")),

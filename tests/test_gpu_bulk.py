@@ -13,7 +13,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import BULK_CASES, case_model, golden
+from conftest import BULK_CASES, case_grain, case_model, golden
 
 pytestmark = pytest.mark.gpu
 
@@ -28,7 +28,8 @@ def _eng_field(f):
 
 def _batch(engine, g, precision="fp64", n=None, seed=1, stream=0, float_draws=False):
     name, T, nL, maxE, mt = case_model(g)
-    pt = engine.physics.silicon_electron(name, temperature=T, n_levels=nL, max_energy=maxE, mt=mt)
+    pt = engine.physics.silicon_electron(name, temperature=T, n_levels=nL, max_energy=maxE,
+                                         mt=mt, grain=case_grain(g) if "grain" in g else None)
     fld = g["applied_field"]
     strength = float(np.sqrt(np.sum(fld * fld)))
     spec = engine.EnsembleSpec(0, n if n is not None else len(g["s0_E"]), strength,
@@ -114,16 +115,21 @@ def _oracle_state_to_engine(engine, st):
     return engine.ParticleState.from_arrays(**kw)
 
 
-def test_philox_fp64_matches_oracle(engine, oracle):
+@pytest.mark.parametrize("grain", [None, (0.3, 2e14)])
+def test_philox_fp64_matches_oracle(engine, oracle, grain):
     """Same Philox stream in engine and oracle: states within 1e-12 after 100 steps
-    (particles whose path branched on a last-ulp difference are counted)."""
-    m = oracle.silicon_model("jacoboni")
+    (particles whose path branched on a last-ulp difference are counted); also
+    with a grain mechanism (a grain every 5 fs, 30 % transmitted)."""
+    m = oracle.silicon_model("jacoboni", grain=grain)
     rng = oracle.RngState(oracle.RNG_MT, 99)
     st = m.bulk_init([2e-6] * 3, [2e-7] * 3, 4e20, rng)
     assert st.n > 2000
     g = {"applied_field": np.array([-1e6, 0, 0]), "field_dir": np.array([-1.0, 0, 0]),
          "box": np.array(2e-6), "dt": np.array(1e-15), "s0_E": st.E,
          "raw": np.zeros((13, 1)), "params": np.array([300, 1000, 1.0, 0, 0, 0, 0, 0, 0, 0, 0.19])}
+    if grain is not None:
+        g["grain"] = np.array(grain)
+        assert st.gtau.mean() < 1e-14  # the initial grain timers use 1 / rate
     seed, stream, steps = 0x1234_5678_9ABC, 3, 100
     b = _batch(engine, g, seed=seed, stream=stream)
     b.set_state(0, _oracle_state_to_engine(engine, st))
@@ -500,6 +506,48 @@ def test_queued_kernel_equals_lockstep_kernel(engine, precision, mode):
     assert bad.sum() <= a.n // 200, bad.sum()
     assert np.allclose(oa[..., 2], oq[..., 2])
     assert np.allclose(oa[..., 0], oq[..., 0], rtol=1e-3)
+
+
+@pytest.mark.parametrize("precision,mode", [("fp32", 2), ("fp64", 0)])
+def test_grain_mechanism_in_the_step_kernels(engine, precision, mode):
+    """A grain mechanism (basicBulkParticleHandler.hpp:215-219): the
+    warp-asynchronous kernel's grain instance follows the lockstep kernel's
+    trajectories (same Philox counters), and the block-queued kernel, which
+    draws its grain events from a counter block of their own, the lockstep
+    kernel's observables.  Grains every 5 fs slow the drift velocity against
+    the same electrons without them, and leave the energy gain of the field
+    (no energy change at a grain) far less touched."""
+    grain = (0.5, 2e14)
+    pt = engine.physics.silicon_electron("jacoboni", grain=grain)
+    pt0 = engine.physics.silicon_electron("jacoboni")
+    spec = engine.EnsembleSpec(0, 20000, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 23, 0)
+    runs = {}
+    for label, model, queued in (("lock", pt, 0), ("alt", pt, mode), ("queued", pt, 1),
+                                 ("none", pt0, 0)):
+        b = engine.BulkBatch([model], [spec], precision)
+        b.set_launch(queued=queued, min_blocks=1, steps_per_launch=50)
+        b.init_particles(0)
+        obs = b.step(300)
+        runs[label] = (b.get_state(0), engine.BulkBatch.averages(obs, [20000]))
+        b.close()
+    (a, A), (q, Q) = runs["lock"], runs["alt"]
+    tol = 1e-12 if precision == "fp64" else 2e-5
+    bad = np.zeros(a.n, bool)
+    for f in ("kx", "ky", "kz", "energy", "tau", "grain_tau", "px"):
+        x, y = getattr(a, f), getattr(q, f)
+        bad |= np.abs(x - y) > tol * np.max(np.abs(x))
+    bad |= a.sub != q.sub
+    assert bad.sum() <= a.n // 100, bad.sum()
+    # the grain timers: drawn with 1 / rate, redrawn at every grain event
+    assert abs(a.grain_tau.mean() - 5e-15) < 0.5e-15, a.grain_tau.mean()
+    v = {k: runs[k][1]["drift_velocity"][0, -100:, 0].mean() for k in runs}
+    e = {k: runs[k][1]["energy"][0, -100:, 0].mean() for k in runs}
+    # grains every 5 fs cut the drift velocity to a few percent of its value
+    # without them; the queued kernel's (other draws) agrees within the
+    # sampling noise, a small fraction of what a missing grain would change
+    assert abs(v["lock"]) < 0.2 * abs(v["none"]), v
+    assert abs(v["queued"] - v["lock"]) <= 0.03 * abs(v["none"]), v
+    assert abs(e["queued"] - e["lock"]) <= 0.03 * e["lock"], e
 
 
 def _sweep_batch(engine, precision="fp32", seed=41):

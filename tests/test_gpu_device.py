@@ -22,9 +22,10 @@ FIELDS_F = ("kx", "ky", "kz", "px", "py", "E", "tau", "gtau")
 ENG = {"E": "energy", "gtau": "grain_tau"}
 
 
-def _electron(engine, dev):
+def _electron(engine, dev, grain=None):
     """The harness's particle type: acoustic, Coulomb, zero-order f/g
-    absorption/emission, in that registration order, 4 eV tables."""
+    absorption/emission, in that registration order, 4 eV tables; grain: a
+    grain mechanism (transmission probability, scatter rate)."""
     from viennaemc_gb300 import physics as P
     mat = P.silicon_material()
     pt = P.Electron(1000, 4.0)
@@ -38,15 +39,17 @@ def _electron(engine, dev):
             sfx, 0, fs, 5.23e10, 0.06, 300.0, mat.rho))
         pt.addScatterMechanism(regs, P.ZeroOrderInterValleyEmissionScatterMechanism(
             sfx, 0, fs, 5.23e10, 0.06, 300.0, mat.rho))
+    if grain is not None:
+        pt.setGrainScatterMechanism(P.GrainScatterMechanism(*grain))
     pt.initScatterTables()
     return pt
 
 
-def _sim(engine, g, case, precision="fp64", seed=1, **kw):
+def _sim(engine, g, case, precision="fp64", seed=1, grain=None, **kw):
     from viennaemc_gb300 import device as D
     scheme, pot_init, vwd = flavour(g)
     dev = _host_device(g, pot_init)
-    pt = _electron(engine, dev)
+    pt = _electron(engine, dev, grain)
     return D.DeviceSimulation(dev, pt, scheme=scheme, dt=float(g["params"][1]),
                               seed=seed, capacity=1 << 15, precision=precision,
                               potential_init=pot_init, round_counts=vwd,
@@ -146,22 +149,32 @@ def test_poisson_matches_converged_sor(engine, oracle, case, fp32):
     sim.close()
 
 
-@pytest.mark.parametrize("case", DEVICE_CASES)
-def test_philox_step_matches_oracle(engine, oracle, case):
+@pytest.mark.parametrize("case,grain", [(c, None) for c in DEVICE_CASES] +
+                         [(DEVICE_CASES[0], (0.4, 5e14)), (DEVICE_CASES[1], (0.6, 5e14))])
+def test_philox_step_matches_oracle(engine, oracle, case, grain):
     """Same potential, same Philox counters: E field, move, contacts and
-    assignment of the FP64 engine equal the oracle's (1e-12)."""
+    assignment of the FP64 engine equal the oracle's (1e-12); also with a
+    grain mechanism (emcBasicParticleHandler.hpp:131-138), the grain timers
+    set below one step so that most particles meet a grain."""
     from viennaemc_gb300 import _lib as L
     g = golden(case)
     seed, stream = 0xBEEF, 0
-    sim, dev, pt = _sim(engine, g, case, seed=seed)
+    sim, dev, pt = _sim(engine, g, case, seed=seed, grain=grain)
     odev = _oracle_device(oracle, g)
     m, regs = _oracle_model(oracle, g)
+    if grain is not None:
+        m.set_grain(*grain)
     scheme, _, vwd = flavour(g)
     dt = float(g["params"][1])
     cur = oracle.State.from_dict({f: g[f"s0_{f}"] for f in oracle.STATE_F + oracle.STATE_I})
+    if grain is not None:
+        cur.gtau[:] = np.linspace(0.05, 0.95, cur.n) * dt
     cur = cur.resize(1 << 15)
     cur.n = len(g["s0_E"])
-    sim.set_state(_engine_state(engine, g, 0))
+    est = _engine_state(engine, g, 0)
+    if grain is not None:
+        est.grain_tau[:] = cur.gtau[:cur.n]
+    sim.set_state(est)
     rng = oracle.RngState(oracle.RNG_PHILOX, seed, stream)
     expnr = odev.exp_nr(vwd)
     for s in range(1, 4):

@@ -9,7 +9,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import BULK_CASES, ROOT, case_model, golden
+from conftest import BULK_CASES, ROOT, case_grain, case_model, golden
 
 
 def header_symbols():
@@ -42,12 +42,23 @@ def test_host_model_builder_matches_reference_tables(case):
     from viennaemc_gb300 import physics
     g = golden(case)
     name, T, nL, maxE, mt = case_model(g)
-    pt = physics.silicon_electron(name, temperature=T, n_levels=nL, max_energy=maxE, mt=mt)
+    pt = physics.silicon_electron(name, temperature=T, n_levels=nL, max_energy=maxE, mt=mt,
+                                  grain=case_grain(g))
     raw = pt.scatterHandler.raw[(0, 0)]
     assert np.array_equal(raw, g["raw"])
     assert pt.getTau(0, 0) == g["tau"][0]
     names = [m.getName() for m in pt.scatterHandler.mechanisms]
     assert names == [str(x) for x in g["names"]]
+    # the grain mechanism: the reference's initial particles draw their grain
+    # timers with 1 / rate (mean of the fixture's s0 timers within 3 sigma)
+    d = pt.model_desc()
+    grain = case_grain(g)
+    if grain is None:
+        assert (d.grain, d.grain_tau) == (0, 1.0)
+    else:
+        assert (d.grain, d.grain_transmission, d.grain_tau) == (1, grain[0], 1.0 / grain[1])
+        gt = g["s0_gtau"]
+        assert abs(gt.mean() - d.grain_tau) < 3 * d.grain_tau / np.sqrt(len(gt))
 
 
 def _desc(**over):
@@ -87,6 +98,8 @@ def _ens(**over):
     (dict(n_levels=0), "n_levels"),
     (dict(max_energy=-1.0), "max_energy"),
     (dict(grain_tau=0.0), "grain_tau"),
+    (dict(grain=2), "grain must be 0 or 1"),
+    (dict(grain=1, grain_transmission=float("nan")), "grain_transmission"),
 ])
 def test_create_rejects_bad_model_without_gpu(bad, msg):
     pt, d = _desc(**bad)

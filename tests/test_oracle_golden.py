@@ -7,7 +7,7 @@ bit-exact: the oracle restates the reference operation by operation.
 import numpy as np
 import pytest
 
-from conftest import BULK_CASES, case_model, golden
+from conftest import BULK_CASES, case_grain, case_model, golden
 
 pytestmark = []
 
@@ -66,7 +66,8 @@ def test_philox4x32_10_known_answers(oracle, ctr, key, expect):
 def test_rate_tables_match_reference(oracle, case):
     g = golden(case)
     name, T, nL, maxE, mt = case_model(g)
-    m = oracle.silicon_model(name, temperature=T, n_levels=nL, max_energy=maxE, mt=mt)
+    m = oracle.silicon_model(name, temperature=T, n_levels=nL, max_energy=maxE, mt=mt,
+                            grain=case_grain(g))
     assert m.n_tables(0, 0) == g["raw"].shape[0]
     for t in range(g["raw"].shape[0]):
         assert np.array_equal(m.raw_table(0, 0, t), g["raw"][t]), t
@@ -82,7 +83,8 @@ def test_initial_particles_match_reference(oracle, case):
     g = golden(case)
     name, T, nL, maxE, mt = case_model(g)
     box, h, doping, seed = g["params"][3:7]
-    m = oracle.silicon_model(name, temperature=T, n_levels=nL, max_energy=maxE, mt=mt)
+    m = oracle.silicon_model(name, temperature=T, n_levels=nL, max_energy=maxE, mt=mt,
+                            grain=case_grain(g))
     rng = oracle.RngState(oracle.RNG_MT, int(seed))
     st = m.bulk_init([box] * 3, [h] * 3, doping, rng)
     assert st.n == len(g["s0_E"])
@@ -101,7 +103,8 @@ def _state(oracle, g, s):
 def test_trajectories_match_reference(oracle, case, mode):
     g = golden(case)
     name, T, nL, maxE, mt = case_model(g)
-    m = oracle.silicon_model(name, temperature=T, n_levels=nL, max_energy=maxE, mt=mt)
+    m = oracle.silicon_model(name, temperature=T, n_levels=nL, max_energy=maxE, mt=mt,
+                            grain=case_grain(g))
     dt, box = float(g["dt"]), float(g["box"])
     force = -oracle.Q * g["applied_field"]
     steps = g["offsets"].shape[0]

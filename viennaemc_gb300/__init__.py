@@ -11,7 +11,7 @@ from .physics import (Electron, NonParabolicAnisotropValley, AcousticScatterMech
                       ZeroOrderInterValleyEmissionScatterMechanism,
                       FirstOrderInterValleyAbsorptionScatterMechanism,
                       FirstOrderInterValleyEmissionScatterMechanism, CoulombScatterMechanism,
-                      silicon_electron, silicon_material, thermal_voltage)
+                      GrainScatterMechanism, silicon_electron, silicon_material, thermal_voltage)
 from .bulk import (BulkBatch, BulkParticleHandler, EnsembleSpec, FMMBulkParticleHandler,
                    ParticleState, ParticleStateF32)
 
@@ -21,6 +21,6 @@ __all__ = ["Electron", "NonParabolicAnisotropValley", "AcousticScatterMechanism"
            "ZeroOrderInterValleyEmissionScatterMechanism",
            "FirstOrderInterValleyAbsorptionScatterMechanism",
            "FirstOrderInterValleyEmissionScatterMechanism", "CoulombScatterMechanism",
-           "silicon_electron", "silicon_material", "thermal_voltage", "BulkBatch",
+           "GrainScatterMechanism", "silicon_electron", "silicon_material", "thermal_voltage", "BulkBatch",
            "BulkParticleHandler", "EnsembleSpec", "FMMBulkParticleHandler", "ParticleState",
            "build"]

@@ -101,7 +101,8 @@ class ModelDesc(C.Structure):
                 ("n_levels", C.c_int32), ("max_energy", C.c_double), ("grain_tau", C.c_double),
                 ("valleys", C.POINTER(ValleyDesc)), ("mechs", C.POINTER(MechDesc)),
                 ("tablesets", C.POINTER(TablesetDesc)), ("tables", C.POINTER(C.c_double)),
-                ("region_doping", C.c_double * MAX_REGIONS)]
+                ("region_doping", C.c_double * MAX_REGIONS), ("grain", C.c_int32),
+                ("grain_pad_", C.c_int32), ("grain_transmission", C.c_double)]
 
 
 class EnsembleDesc(C.Structure):

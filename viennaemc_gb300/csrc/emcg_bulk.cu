@@ -66,8 +66,13 @@ __device__ __forceinline__ int bulkParticleStep(const ModelK<T> &M, const EnsK<T
   }
   tau -= dt;
   gtau -= dt;
-  if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
+  if (gtau <= T(0)) { // basicBulkParticleHandler.hpp:215-219
+    if (M.grain) {
+      grainScatter(M, k, rng);
+      toEcs(M.v[valley].rot[sub], k[0], k[1], k[2], kN);
+    }
     gtau = -m_log(rng.ulog()) * M.grainTau;
+  }
   return err;
 }
 
@@ -112,8 +117,13 @@ __device__ __forceinline__ int bulkParticleStepF(const ModelK<T> &M, const EnsK<
   }
   tau -= dt;
   gtau -= dt;
-  if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
+  if (gtau <= T(0)) { // basicBulkParticleHandler.hpp:215-219
+    if (M.grain) {
+      grainScatter(M, k, rng);
+      toEcs(M.v[valley].rot[sub], k[0], k[1], k[2], kN);
+    }
     gtau = -m_log(rng.ulog()) * M.grainTau;
+  }
   return err;
 }
 
@@ -487,6 +497,17 @@ __global__ void __launch_bounds__(256, MINB)
         PhiloxSrc<T> rng;
         rng.init((uint32_t)(gi - EK.begin), step, EK.stream, EK.key0, EK.key1, EK.floatDraws);
         rng.c2 = 0x40000000u;
+        if (M.grain) { // the step's new k and its ellipse-frame copy for the sums
+          T k[3] = {B.k0[me], B.k1[me], B.k2[me]}, kN[3];
+          grainScatter(M, k, rng);
+          toEcs(M.v[valley].rot[sub], k[0], k[1], k[2], kN);
+          B.k0[me] = k[0];
+          B.k1[me] = k[1];
+          B.k2[me] = k[2];
+          B.n0[me] = kN[0];
+          B.n1[me] = kN[1];
+          B.n2[me] = kN[2];
+        }
         gtau = -m_log(rng.ulog()) * M.grainTau;
       }
       B.gtau[me] = gtau;
@@ -724,7 +745,10 @@ __device__ __forceinline__ void flushPos(const float *R, const float vogt[3], fl
   }
 }
 
-template <int MINB, bool kOne>
+// kGrain: an instance for batches with a grain mechanism; the other keeps the
+// grain branch out of the register allocation of the step loop (64 registers
+// at 4 blocks per SM: the branch spilled 64 B there)
+template <int MINB, bool kOne, bool kGrain>
 __global__ void __launch_bounds__(256, MINB)
     bulkStepAsyncKernel(StateK<float> st, StateK<float> src, int srcEns,
                         const ModelK<float> *__restrict__ models,
@@ -887,8 +911,16 @@ __global__ void __launch_bounds__(256, MINB)
           } else { // end of step s: its observables, then step s + 1
             tau -= rem;
             gtau -= dt;
-            if (gtau <= T(0)) // no grain mechanism: only the free-flight time is redrawn
+            if (gtau <= T(0)) { // basicBulkParticleHandler.hpp:215-219
+              if (kGrain && M.grain) { // in the device frame; the subvalley (and dP's frame) stay
+                const T *R = M.v[vd].rot[sub];
+                T k[3];
+                toDev(R, kE[0], kE[1], kE[2], k);
+                grainScatter(M, k, rng);
+                toEcs(R, k[0], k[1], k[2], kE);
+              }
               gtau = -m_log(rng.ulog()) * M.grainTau;
+            }
             const int slot = ws * 32 + lane;
             winE[slot] = E;
             winD[slot] = vf * (gl[0] * kE[0] + gl[1] * kE[1] + gl[2] * kE[2]);
@@ -938,17 +970,19 @@ __global__ void __launch_bounds__(256, MINB)
 template <int MINB> int32_t asyncSmemOptIn(size_t bytes) {
   if (bytes <= 48 * 1024)
     return EMCG_OK;
-  EMCG_CUDA(cudaFuncSetAttribute(bulkStepAsyncKernel<MINB, false>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  EMCG_CUDA(cudaFuncSetAttribute(bulkStepAsyncKernel<MINB, true>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  for (auto k : {bulkStepAsyncKernel<MINB, false, false>, bulkStepAsyncKernel<MINB, true, false>,
+                 bulkStepAsyncKernel<MINB, false, true>, bulkStepAsyncKernel<MINB, true, true>})
+    EMCG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   return EMCG_OK;
 }
 
-// the warp-asynchronous kernel for a register cap; kOne: every ensemble of the
-// batch has one valley, so the drift reads that valley's constants once
-template <int MINB> static auto asyncKernel(bool one) {
-  return one ? bulkStepAsyncKernel<MINB, true> : bulkStepAsyncKernel<MINB, false>;
+// the warp-asynchronous kernel for a register cap; one: every ensemble of the
+// batch has one valley, so the drift reads that valley's constants once;
+// grain: some model of the batch has a grain mechanism
+template <int MINB> static auto asyncKernel(bool one, bool grain) {
+  if (grain)
+    return one ? bulkStepAsyncKernel<MINB, true, true> : bulkStepAsyncKernel<MINB, false, true>;
+  return one ? bulkStepAsyncKernel<MINB, true, false> : bulkStepAsyncKernel<MINB, false, false>;
 }
 
 // drift() known-answer kernel: independent particles, per-particle force/dt
@@ -984,6 +1018,7 @@ struct BulkImpl {
   int precision = EMCG_FP64;
   size_t tsz = 8;
   int nModels = 0, nEns = 0, nVmax = 1;
+  bool anyGrain = false; // some model has a grain mechanism
   std::vector<emcg_ensemble_desc> ens;
   std::vector<emcg_model_desc> modelDescs;       // shallow copies (valleys)
   std::vector<std::vector<emcg_valley_desc>> valleyCopies;
@@ -1223,10 +1258,10 @@ template <class T> static void *stepKernelFn(const BulkImpl *b, bool *queued) {
     if (b->queued == 2) {
       const bool one = b->nVmax == 1;
       if (b->minBlocks >= 4 && b->blockThreads <= 256)
-        return (void *)asyncKernel<4>(one);
+        return (void *)asyncKernel<4>(one, b->anyGrain);
       if (b->minBlocks == 3 && b->blockThreads <= 256)
-        return (void *)asyncKernel<3>(one);
-      return (void *)asyncKernel<1>(one);
+        return (void *)asyncKernel<3>(one, b->anyGrain);
+      return (void *)asyncKernel<1>(one, b->anyGrain);
     }
   }
   if (b->queued) {
@@ -1420,17 +1455,17 @@ static int32_t launchStepTiles(BulkImpl *b, const StateK<T> &st, int ns, uint32_
       const size_t asmem = asyncSmemBytes(b->blockThreads / 32, ns, Q);
       if (b->minBlocks >= 4 && b->blockThreads <= 256) {
         EMCG_TRY(asyncSmemOptIn<4>(asmem));
-        asyncKernel<4>(b->nVmax == 1)<<<nT, b->blockThreads, asmem, b->stream>>>(
+        asyncKernel<4>(b->nVmax == 1, b->anyGrain)<<<nT, b->blockThreads, asmem, b->stream>>>(
             st, src, srcEns, mp, ep, tiles, ns, s0, b->chunk, b->nVmax, b->passActions,
             b->dObs, b->dErr);
       } else if (b->minBlocks == 3 && b->blockThreads <= 256) {
         EMCG_TRY(asyncSmemOptIn<3>(asmem));
-        asyncKernel<3>(b->nVmax == 1)<<<nT, b->blockThreads, asmem, b->stream>>>(
+        asyncKernel<3>(b->nVmax == 1, b->anyGrain)<<<nT, b->blockThreads, asmem, b->stream>>>(
             st, src, srcEns, mp, ep, tiles, ns, s0, b->chunk, b->nVmax, b->passActions,
             b->dObs, b->dErr);
       } else {
         EMCG_TRY(asyncSmemOptIn<1>(asmem));
-        asyncKernel<1>(b->nVmax == 1)<<<nT, b->blockThreads, asmem, b->stream>>>(
+        asyncKernel<1>(b->nVmax == 1, b->anyGrain)<<<nT, b->blockThreads, asmem, b->stream>>>(
             st, src, srcEns, mp, ep, tiles, ns, s0, b->chunk, b->nVmax, b->passActions,
             b->dObs, b->dErr);
       }
@@ -1647,6 +1682,7 @@ extern "C" int32_t emcg_bulk_create(const emcg_model_desc *models, int32_t n_mod
     md.tablesets = nullptr;
     md.tables = nullptr;
     b->modelDescs.push_back(md);
+    b->anyGrain = b->anyGrain || md.grain != 0;
   }
   b->begin.resize(n_ens);
   b->count.assign(n_ens, 0);

@@ -45,8 +45,8 @@ template <class T> struct MechK {
 template <class T> struct ModelK {
   ValleyK<T> v[EMCG_MAX_VALLEYS];
   MechK<T> m[EMCG_MAX_MECH];
-  int32_t nV, nLevels, nTS, pad_;
-  T dE, invdE, grainTau, pad2_;
+  int32_t nV, nLevels, nTS, grain; // grain: a grain mechanism is set
+  T dE, invdE, grainTau, grainProb; // grainProb: its transmission probability
   int8_t tsIndex[EMCG_MAX_VALLEYS][EMCG_MAX_REGIONS]; // -1: no table set
   int32_t tsN[EMCG_MAX_TABLESETS];
   int64_t tsOff[EMCG_MAX_TABLESETS];   // offset of the set in `tables`
@@ -399,6 +399,26 @@ __device__ __forceinline__ void directionAboutK(T k[3], T ct, T rnd) {
   k[0] = kxp * cfi0 * ct0 - kyp * sfi0 + kzp * cfi0 * st0;
   k[1] = kxp * sfi0 * ct0 + kyp * cfi0 + kzp * sfi0 * st0;
   k[2] = -kxp * st0 + kzp * ct0;
+}
+
+// emcGrainScatterMechanism::scatterParticle (include/emcGrainScatterMechanism.hpp:
+// 41-80) with k in the device frame: reflected into the opposite hemisphere
+// (cos(theta) <= 0 about k) when a draw exceeds the transmission probability,
+// else transmitted into the same one; |k| is kept and the energy is not
+// updated.  Only with a grain mechanism set (M.grain): without one the
+// reference's scatterParticleAtGrain is a no-op (include/emcScatterHandler.hpp:
+// 193-196).
+template <class T, class R>
+__device__ __forceinline__ void grainScatter(const ModelK<T> &M, T k[3], R &rng) {
+  const bool reflect = rng.u01() > M.grainProb;
+  T rnd = rng.u01();
+  if (reflect) {
+    if (rnd < T(0.5))
+      rnd += T(0.5);
+  } else if (rnd > T(0.5)) {
+    rnd -= T(0.5);
+  }
+  directionAboutK(k, T(1) - T(2) * rnd, rng.u01());
 }
 
 // Selected mechanism's final state.

@@ -190,8 +190,11 @@ __device__ __forceinline__ int devParticleStep(const ModelK<T> &M, const DevK &G
   }
   tau -= dt;
   gtau -= dt;
-  if (gtau <= T(0) && !removed)
+  if (gtau <= T(0) && !removed) { // emcBasicParticleHandler.hpp:131-138
+    if (M.grain)
+      grainScatter(M, k, rng);
     gtau = -m_log(rng.ulog()) * M.grainTau;
+  }
   return err;
 }
 

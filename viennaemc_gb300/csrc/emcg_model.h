@@ -44,6 +44,9 @@ inline int32_t validateModel(const emcg_model_desc &m) {
                  "model: max_energy must be positive");
   EMCG_CHECK_ARG(m.grain_tau > 0 && std::isfinite(m.grain_tau),
                  "model: grain_tau must be positive");
+  EMCG_CHECK_ARG(m.grain == 0 || m.grain == 1, "model: grain must be 0 or 1");
+  EMCG_CHECK_ARG(m.grain == 0 || std::isfinite(m.grain_transmission),
+                 "model: grain_transmission must be finite");
   for (int v = 0; v < m.n_valleys; v++) {
     const emcg_valley_desc &V = m.valleys[v];
     EMCG_CHECK_ARG(V.deg >= 1 && V.deg <= EMCG_MAX_DEG, "valley %d: deg=%d out of [1,%d]", v,
@@ -110,6 +113,8 @@ int32_t buildModelK(const emcg_model_desc &m, ModelK<T> &K, std::vector<T> &tabl
   K.dE = (T)dE;
   K.invdE = (T)(1.0 / dE);
   K.grainTau = (T)m.grain_tau;
+  K.grain = m.grain;
+  K.grainProb = m.grain ? (T)m.grain_transmission : T(0);
   std::vector<double> mcOf(m.n_valleys);
   for (int v = 0; v < m.n_valleys; v++) {
     const emcg_valley_desc &V = m.valleys[v];

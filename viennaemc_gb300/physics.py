@@ -289,6 +289,14 @@ class ScatterHandler:
         self.raw: dict = {}
         self.norm: dict = {}
         self.tau: dict = {}
+        self.grainScatterMech = None
+        self.grainTau = 1.0  # include/emcScatterHandler.hpp:61-62
+
+    def setGrainScatterMechanism(self, mech):
+        self.grainScatterMech = mech
+
+    def getGrainTau(self):
+        return self.grainTau
 
     def addScatterMechanism(self, mech, regions):
         idx = len(self.mechanisms)
@@ -338,9 +346,26 @@ class ScatterHandler:
             mx = float(cum[-1].max())
             self.norm[key] = cum / mx
             self.tau[key] = 1.0 / mx
+        if self.grainScatterMech is not None:  # :233-234
+            self.grainTau = 1.0 / self.grainScatterMech.getScatterRate()
 
     def getTau(self, region, valley):
         return self.tau.get((valley, region), 2e-15)
+
+
+class GrainScatterMechanism:
+    """emcGrainScatterMechanism (include/emcGrainScatterMechanism.hpp:16-80):
+    grains met at a mean rate; a particle is transmitted (new direction in the
+    hemisphere of k) with the transmission probability, else reflected (the
+    opposite hemisphere), |k| kept.  The scattering itself runs in the engine
+    (grainScatter); this holds its two parameters."""
+
+    def __init__(self, transmissionProb=0.5, scatterRate=1e14):
+        self.transmissionProb = float(transmissionProb)
+        self.scatterRate = float(scatterRate)
+
+    def getScatterRate(self):
+        return self.scatterRate
 
 
 class Electron:
@@ -377,6 +402,14 @@ class Electron:
     def initScatterTables(self):
         self.scatterHandler.initScatterTables()
 
+    def setGrainScatterMechanism(self, mech):
+        """emcParticleType::setGrainScatterMechanism (emcParticleType.hpp:134-138);
+        the grain free-flight constant follows at the next table build."""
+        self.scatterHandler.setGrainScatterMechanism(mech)
+
+    def getGrainTau(self):
+        return self.scatterHandler.getGrainTau()
+
     def getTau(self, valley, region):
         return self.scatterHandler.getTau(region, valley)
 
@@ -412,7 +445,9 @@ class Electron:
         tables = np.ascontiguousarray(np.concatenate(chunks) if chunks else np.zeros(1))
         d = L.ModelDesc()
         d.n_valleys, d.n_mechs, d.n_tablesets = nV, nM, len(keys)
-        d.n_levels, d.max_energy, d.grain_tau = h.n_levels, h.max_energy, 1.0
+        d.n_levels, d.max_energy, d.grain_tau = h.n_levels, h.max_energy, h.getGrainTau()
+        if h.grainScatterMech is not None:
+            d.grain, d.grain_transmission = 1, h.grainScatterMech.transmissionProb
         d.valleys, d.mechs, d.tablesets = va, ma, ta
         d.tables = tables.ctypes.data_as(C.POINTER(C.c_double))
         for r in range(L.MAX_REGIONS):
@@ -447,13 +482,17 @@ def add_x_valley(pt: Electron, mt: float = 0.196, ml: float = 0.916, alpha: floa
 
 def silicon_electron(model: str = "jacoboni", temperature: float = 300.0, n_levels: int = 1000,
                      max_energy: float = 1.0, regions=(0,), mt=None, coulomb: bool = False,
-                     region_doping=None, zero_order=True, first_order=True) -> Electron:
+                     region_doping=None, zero_order=True, first_order=True,
+                     grain=None) -> Electron:
     """Silicon electrons with one of two mechanism sets:
 
     "refbulk":  the reference bulk example (acoustic + zero-order f/g at 60 meV
                 + first-order f/g; m_t = 0.196), SiliconFunctions.hpp:224-333.
     "jacoboni": acoustic (9 eV) + 3 g + 3 f zero-order phonons of the
                 Jacoboni-Reggiani table; m_t = 0.19.
+
+    grain: (transmission probability, scatter rate [1/s]) of a grain
+    mechanism (GrainScatterMechanism), none by default.
     """
     mat = silicon_material()
     pt = Electron(n_levels, max_energy)
@@ -489,5 +528,7 @@ def silicon_electron(model: str = "jacoboni", temperature: float = 300.0, n_leve
             raise ValueError("Coulomb scattering needs region_doping")
         pt.addScatterMechanism(regs, CoulombScatterMechanism(0, mat.epsR, temperature,
                                                              region_doping))
+    if grain is not None:
+        pt.setGrainScatterMechanism(GrainScatterMechanism(*grain))
     pt.initScatterTables()
     return pt
