@@ -57,6 +57,10 @@ extern "C" {
 #define EMCG_MECH_FIRST_IV_ABS 3 /* emcFirstOrderInterValleyScatterMechanism.hpp:121-131 */
 #define EMCG_MECH_FIRST_IV_EMI 4 /* emcFirstOrderInterValleyScatterMechanism.hpp:269-279 */
 #define EMCG_MECH_COULOMB 5      /* emcCoulombScatterMechanism.hpp:48-59 */
+/* surface mechanisms at device boundaries (emcg_model_desc.surface_kind) */
+#define EMCG_SURFACE_SPECULAR 0
+#define EMCG_SURFACE_CONSTANT 1
+#define EMCG_SURFACE_ROUGHNESS 2
 
 /* ---- random-number modes ----------------------------------------------- */
 #define EMCG_RNG_PHILOX 0 /* counter-based Philox4x32-10                   */
@@ -134,6 +138,18 @@ typedef struct {
   int32_t grain;
   int32_t grain_pad_;
   double grain_transmission;
+  /* Surface mechanism per boundary of a device (XMIN, XMAX, YMIN, YMAX;
+     emcParticleType::setSurfaceScatterMechanism, include/emcScatterHandler.hpp:
+     114-124, 172-191): EMCG_SURFACE_SPECULAR (0, a zeroed descriptor) reflects
+     specularly, the reference's default; EMCG_SURFACE_CONSTANT scatters
+     diffusely with probability 1 - surface_param (the specularity,
+     emcConstantSurfaceScatterMechanism); EMCG_SURFACE_ROUGHNESS with
+     probability 1 - exp(-(2 surface_param k_perp)^2) (surface_param: the
+     roughness height [m], emcMomentumDependentSurfaceScatterMechanism, its
+     polar angle from the reference's fixed-point iteration of at most 10000
+     steps).  Bulk engines ignore them. */
+  int32_t surface_kind[4];
+  double surface_param[4];
 } emcg_model_desc;
 
 /* One bulk ensemble (basicBulkParticleHandler,

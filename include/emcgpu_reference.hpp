@@ -61,6 +61,8 @@
 #include <emcBoundaryPos.hpp>
 #include <emcContact.hpp>
 #include <emcGrainScatterMechanism.hpp>
+#include <SurfaceScatterMechanisms/emcConstantSurfaceScatterMechanism.hpp>
+#include <SurfaceScatterMechanisms/emcMomentumDependentSurfaceScatterMechanism.hpp>
 #include <emcMessage.hpp>
 
 #include "emcgpu.h"
@@ -154,6 +156,28 @@ public:
     grainRate_ = scatterRate;
   }
 
+  // emcParticleType::setSurfaceScatterMechanism(boundary, mechanism)
+  // (include/ParticleType/emcParticleType.hpp:155-166) with an
+  // emcConstantSurfaceScatterMechanism(specularity, maxPos) or an
+  // emcMomentumDependentSurfaceScatterMechanism(roughnessHeight, maxPos):
+  // forwarded to the particle type, the kind and parameter kept for the
+  // engine (device simulations; the reference keeps them private).
+  void setConstantSurfaceScatterMechanism(emcBoundaryPos boundary, T specularity,
+                                          const std::array<T, DeviceType::Dimension> &maxPos) {
+    pt_.setSurfaceScatterMechanism(
+        boundary,
+        std::make_unique<emcConstantSurfaceScatterMechanism<T, DeviceType>>(specularity, maxPos));
+    surface(boundary, EMCG_SURFACE_CONSTANT, specularity);
+  }
+  void setMomentumDependentSurfaceScatterMechanism(
+      emcBoundaryPos boundary, T roughnessHeight,
+      const std::array<T, DeviceType::Dimension> &maxPos) {
+    pt_.setSurfaceScatterMechanism(
+        boundary, std::make_unique<emcMomentumDependentSurfaceScatterMechanism<T, DeviceType>>(
+                      roughnessHeight, maxPos));
+    surface(boundary, EMCG_SURFACE_ROUGHNESS, roughnessHeight);
+  }
+
   // ---- engine descriptor (after all mechanisms are registered) ------------
   // Rates are the reference's getScatterRate at (L + 1) dE, accumulated and
   // normalised exactly as emcScatterHandler::renormalizeTables
@@ -208,6 +232,10 @@ public:
     d_.grain_tau = grain_ ? T(1) / grainRate_ : pt_.getGrainTau();
     d_.grain = grain_ ? 1 : 0;
     d_.grain_transmission = grain_ ? grainProb_ : T(0);
+    for (int b = 0; b < 4; b++) {
+      d_.surface_kind[b] = surfKind_[b];
+      d_.surface_param[b] = surfParam_[b];
+    }
     d_.valleys = valleys_.data();
     d_.mechs = mechs_.data();
     d_.tablesets = sets_.data();
@@ -300,7 +328,21 @@ private:
                                        1.45e16, 1.45e16, 1.45e16, 1.45e16};
   bool grain_ = false;
   T grainProb_ = 0, grainRate_ = 0;
+  int32_t surfKind_[4] = {EMCG_SURFACE_SPECULAR, EMCG_SURFACE_SPECULAR, EMCG_SURFACE_SPECULAR,
+                          EMCG_SURFACE_SPECULAR};
+  T surfParam_[4] = {0, 0, 0, 0};
   emcg_model_desc d_{};
+
+  void surface(emcBoundaryPos boundary, int32_t kind, T param) {
+    const int b = (int)toUnderlying(boundary);
+    if (b < 0 || b > 3) {
+      emcMessage::getInstance().addError("libemcgpu: a surface mechanism needs a 2-D boundary "
+                                         "(XMIN, XMAX, YMIN or YMAX)");
+      return;
+    }
+    surfKind_[b] = kind;
+    surfParam_[b] = param;
+  }
 };
 
 // basicBulkParticleHandler on the GPU (one particle type, index 0).

@@ -61,6 +61,10 @@ struct oc_model {
      grainTau = 1 / rate with one set, 1 without */
   int32_t grain;
   double grainProb, grainTau;
+  /* surface mechanism per boundary (XMIN, XMAX, YMIN, YMAX):
+     include/emcScatterHandler.hpp:63-65, 114-124; OC_SURFACE_* */
+  int32_t surfKind[4];
+  double surfParam[4];
   int32_t built;
 };
 
@@ -419,6 +423,24 @@ int32_t oc_set_grain(oc_model *m, double transmissionProb, double scatterRate) {
 }
 
 double oci_grain_tau(const oc_model *m) { return m->grainTau; }
+
+/* emcScatterHandler::setSurfaceScatterMechanism (include/emcScatterHandler.hpp:
+   114-124) for one boundary: OC_SURFACE_CONSTANT with the specularity
+   parameter (emcConstantSurfaceScatterMechanism), OC_SURFACE_ROUGHNESS with
+   the roughness height [m] (emcMomentumDependentSurfaceScatterMechanism),
+   OC_SURFACE_SPECULAR for none */
+int32_t oc_set_surface(oc_model *m, int32_t boundary, int32_t kind, double param) {
+  if (boundary < 0 || boundary > 3 || kind < OC_SURFACE_SPECULAR || kind > OC_SURFACE_ROUGHNESS)
+    return -1;
+  m->surfKind[boundary] = kind;
+  m->surfParam[boundary] = param;
+  return 0;
+}
+
+int32_t oci_surface(const oc_model *m, int32_t boundary, double *param) {
+  *param = m->surfParam[boundary];
+  return m->surfKind[boundary];
+}
 
 int32_t oc_set_region_doping(oc_model *m, int32_t region, double doping) {
   if (region < 0 || region >= OC_MAX_REGIONS)

@@ -111,6 +111,15 @@ int32_t oc_set_region_doping(oc_model *m, int32_t region, double doping);
 /* emcParticleType::setGrainScatterMechanism(emcGrainScatterMechanism(
    transmissionProb, scatterRate)), include/emcGrainScatterMechanism.hpp */
 int32_t oc_set_grain(oc_model *m, double transmissionProb, double scatterRate);
+/* surface scattering at a device boundary (XMIN 0, XMAX 1, YMIN 2, YMAX 3):
+   emcParticleType::setSurfaceScatterMechanism with
+   emcConstantSurfaceScatterMechanism(specularity) or
+   emcMomentumDependentSurfaceScatterMechanism(roughness height)
+   (include/SurfaceScatterMechanisms/) */
+#define OC_SURFACE_SPECULAR 0
+#define OC_SURFACE_CONSTANT 1
+#define OC_SURFACE_ROUGHNESS 2
+int32_t oc_set_surface(oc_model *m, int32_t boundary, int32_t kind, double param);
 int32_t oc_build_tables(oc_model *m);
 /* replace the rates of one built (valley, region) table set and
    renormalise it (reinitScatterTables with caller-filled rates) */

@@ -226,7 +226,83 @@ void oc_dev_force(const oc_dev *d, int32_t scheme, const double *Ex,
 
 /* ---- boundary (include/emcParticleDrift.hpp:41-66 with the default specular
    reflection of include/emcScatterHandler.hpp:172-191) ------------------ */
-static int at_boundary(const oc_dev *d, double *pos, double *k) {
+/* emcSurfaceScatterMechanism::scatterParticleSpecularly
+   (include/SurfaceScatterMechanisms/emcSurfaceScatterMechanism.hpp:75-86):
+   back into the device, k turned inwards only where it points out */
+static void surface_specular(const oc_dev *d, double *pos, double *k) {
+  const double mx[2] = {d->maxX, d->maxY};
+  for (int i = 0; i < 2; i++)
+    if (pos[i] < 0) {
+      pos[i] *= -1;
+      if (k[i] < 0)
+        k[i] *= -1;
+    } else if (pos[i] > mx[i]) {
+      pos[i] = 2 * mx[i] - pos[i];
+      if (k[i] > 0)
+        k[i] *= -1;
+    }
+}
+
+/* emcMomentumDependentSurfaceScatterMechanism::solveForTheta
+   (include/SurfaceScatterMechanisms/emcMomentumDependentSurfaceScatterMechanism.hpp:
+   38-66), the reference's fixed-point iteration as it stands (at most 10000
+   steps, stopping below 1e-10) */
+static double solve_for_theta(double r, double height, double speed) {
+  const double c = pow(2 * height * speed, 2);
+  const double e = exp(-c);
+  const double start = sqrt(r * (1 / (1 - e) - 1 / c));
+  double error = 1, x = start, x1;
+  const double tol = 1e-10;
+  int it = 0;
+  const int maxIt = 10000;
+  while (error > tol && it < maxIt) {
+    const double co = cos(x), si = sin(x);
+    const double ecos = exp(-c * pow(co, 2));
+    const double esin = exp(-c * pow(si, 2));
+    x1 = x - (((e - ecos) / c + pow(si, 2) - r * (1 - (1 - e) / c)) *
+              (2 * esin * c * si * co * (ecos - 1)) / (e * (c - 1) - 1));
+    error = fabs(x1 - x);
+    x = x1;
+    it++;
+  }
+  return x;
+}
+
+/* emcScatterHandler::scatterParticleAtBoundary (include/emcScatterHandler.hpp:
+   172-191) with a surface mechanism at boundary b
+   (emcSurfaceScatterMechanism::scatterParticle, :38-44, and
+   calculateAndAssignKAndPos, :128-148): diffuse with the mechanism's
+   probability (new direction into the device at polar angle theta from the
+   normal), else specular */
+static void surface_scatter(const oc_model *m, const oc_dev *d, int b, double *pos, double *k,
+                            dctx *dc) {
+  double param;
+  const int kind = oci_surface(m, b, &param);
+  const int perp = b / 2;
+  double pDiff;
+  if (kind == OC_SURFACE_CONSTANT) /* emcConstantSurfaceScatterMechanism.hpp:33 */
+    pDiff = 1 - param;
+  else /* emcMomentumDependentSurfaceScatterMechanism.hpp:23-27 */
+    pDiff = 1 - (exp(-pow(2 * param * k[perp], 2)));
+  if (oci_draw_u01(dc) < pDiff) {
+    double theta;
+    if (kind == OC_SURFACE_CONSTANT)
+      theta = asin(sqrt(oci_draw_u01(dc)));
+    else {
+      const double sp = sqrt(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
+      theta = solve_for_theta(oci_draw_u01(dc), param, sp);
+    }
+    const double phi = 2 * 3.14159265358979323846 * oci_draw_u01(dc); /* constants::pi */
+    const double speed = sqrt(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
+    const double sign = (b % 2 == 1) ? -1. : 1.;
+    k[perp] = speed * cos(theta) * sign;
+    k[(perp + 1) % 3] = speed * sin(theta) * cos(phi);
+    k[(perp + 2) % 3] = speed * sin(theta) * sin(phi);
+  }
+  surface_specular(d, pos, k);
+}
+
+static int at_boundary(const oc_model *m, const oc_dev *d, double *pos, double *k, dctx *dc) {
   const double mx[2] = {d->maxX, d->maxY};
   int out = 0;
   for (int i = 0; i < 2; i++)
@@ -246,6 +322,12 @@ static int at_boundary(const oc_dev *d, double *pos, double *k) {
     pos[1] = pb[1];
     return 1;
   }
+  double sp;
+  const int b = boundary_pos(d, (int)c[0], (int)c[1]);
+  if (b >= 0 && oci_surface(m, b, &sp) != OC_SURFACE_SPECULAR) {
+    surface_scatter(m, d, b, pos, k, dc);
+    return 0;
+  }
   for (int i = 0; i < 2; i++) {
     if (pos[i] < 0) {
       pos[i] = -pos[i];
@@ -261,9 +343,9 @@ static int at_boundary(const oc_dev *d, double *pos, double *k) {
 /* emcAbstractParticleHandler::driftParticle (:238-249) */
 static int dev_drift(const oc_model *m, const oc_dev *d, double dt, double *k,
                      double *E, int32_t valley, int32_t sub, int32_t *region,
-                     double *pos, const double *F) {
+                     double *pos, const double *F, dctx *dc) {
   oc_drift(m, dt, k, E, valley, sub, pos, 2, F);
-  int removed = at_boundary(d, pos, k);
+  int removed = at_boundary(m, d, pos, k, dc);
   if (!removed) {
     int64_t c[2];
     pos_to_coord(d, pos, c);
@@ -307,9 +389,9 @@ int32_t oc_dev_move(const oc_model *m, const oc_dev *d, int32_t scheme,
     oc_dev_force(d, scheme, Ex, Ey, pos[0], pos[1], charge, F);
     int removed = 0;
     if (tau >= dt) {
-      removed = dev_drift(m, d, dt, k, &E, valley, sub, &region, pos, F);
+      removed = dev_drift(m, d, dt, k, &E, valley, sub, &region, pos, F, &dc);
     } else {
-      removed = dev_drift(m, d, tau, k, &E, valley, sub, &region, pos, F);
+      removed = dev_drift(m, d, tau, k, &E, valley, sub, &region, pos, F, &dc);
       double tRem = dt - tau;
       while (tRem > 0 && !removed) {
         if (oci_handler_scatter(m, k, &E, &valley, &sub, region, &dc) < 0) {
@@ -319,7 +401,8 @@ int32_t oc_dev_move(const oc_model *m, const oc_dev *d, int32_t scheme,
         double nt = oci_new_tau(m, valley, region, &dc);
         tau += nt;
         oc_dev_force(d, scheme, Ex, Ey, pos[0], pos[1], charge, F);
-        removed = dev_drift(m, d, (nt < tRem) ? nt : tRem, k, &E, valley, sub, &region, pos, F);
+        removed = dev_drift(m, d, (nt < tRem) ? nt : tRem, k, &E, valley, sub, &region, pos, F,
+                            &dc);
         tRem -= nt;
       }
     }

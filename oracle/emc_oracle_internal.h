@@ -21,6 +21,7 @@ double oci_draw_u01(dctx *d);
 double oci_draw_ulog(dctx *d);
 void oci_grain_scatter(const oc_model *m, double *k, dctx *d);
 double oci_grain_tau(const oc_model *m);
+int32_t oci_surface(const oc_model *m, int32_t boundary, double *param);
 uint32_t oci_draw_pick(dctx *d, uint32_t n);
 int32_t oci_handler_scatter(const oc_model *m, double *k, double *E, int32_t *valley,
                             int32_t *sub, int32_t region, dctx *d);

@@ -67,6 +67,8 @@ def _declare(L):
     L.oc_set_region_doping.argtypes = [vp, i32, d]
     L.oc_set_grain.restype = i32
     L.oc_set_grain.argtypes = [vp, d, d]
+    L.oc_set_surface.restype = i32
+    L.oc_set_surface.argtypes = [vp, i32, i32, d]
     L.oc_build_tables.restype = i32
     L.oc_build_tables.argtypes = [vp]
     for fn in ("oc_get_raw_table", "oc_get_norm_table"):
@@ -261,6 +263,11 @@ class Model:
     def set_region_doping(self, region, doping):
         assert lib().oc_set_region_doping(self.h, region, doping) == 0
 
+    def set_surface(self, boundary, kind, param):
+        """A surface mechanism at one device boundary (XMIN 0 .. YMAX 3): kind
+        SURFACE_CONSTANT (specularity) or SURFACE_ROUGHNESS (height [m])."""
+        assert lib().oc_set_surface(self.h, boundary, kind, param) == 0
+
     def set_grain(self, transmission_prob, scatter_rate):
         """emcGrainScatterMechanism(transmissionProb, scatterRate) on the type
         (include/emcGrainScatterMechanism.hpp:27-29)."""
@@ -360,6 +367,9 @@ KB, Q = 1.38066e-23, 1.60219e-19
 JACOBONI = [("G1", False, 140., 0.5e10), ("G2", False, 215., 0.8e10),
             ("G3", False, 720., 11.e10), ("F1", True, 220., 0.3e10),
             ("F2", True, 550., 2.0e10), ("F3", True, 685., 2.0e10)]
+
+
+SURFACE_SPECULAR, SURFACE_CONSTANT, SURFACE_ROUGHNESS = 0, 1, 2
 
 
 def silicon_model(name="jacoboni", temperature=300.0, n_levels=1000, max_energy=1.0,

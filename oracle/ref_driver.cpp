@@ -38,6 +38,8 @@
 #include <ScatterMechanisms/emcFirstOrderInterValleyScatterMechanism.hpp>
 #include <ScatterMechanisms/emcZeroOrderInterValleyScatterMechanism.hpp>
 #include <ValleyTypes/emcNonParabolicAnistropValley.hpp>
+#include <SurfaceScatterMechanisms/emcConstantSurfaceScatterMechanism.hpp>
+#include <SurfaceScatterMechanisms/emcMomentumDependentSurfaceScatterMechanism.hpp>
 #include <ScatterMechanisms/emcHotPhononFroehlichMechanism.hpp>
 #include <emcPhononBath.hpp>
 #include <ParticleHandler/FMM/FP2PRCutoff.hpp>
@@ -358,6 +360,7 @@ template <class PH> static void dumpDevState(const char *tag, PH &ph) {
 // usage: ref_driver device <resistor|mosfet|resistor_nec|mosfet_vwd> <seed> <dt> <nSteps>
 //                          <accV> <width> [outDir]
 // resistor: NGP, mosfet: CIC, resistor_nec: emcNECScheme, all with emcElectron;
+// resistor_surface: the NGP resistor with surface mechanisms on YMIN and YMAX;
 // mosfet_vwd: the mosfet2D example's NEC-VWD scheme with its electronVWD
 // With outDir, the reference's own writers put their files there after the
 // last step (emcSimulationResults::writeCurrentResults with suffix "Step",
@@ -417,6 +420,15 @@ static int runDeviceT(const std::string &kind, unsigned long seed, double dt, in
   el->addScatterMechanism(regions, std::make_unique<ZE>("F", 0, kF, 5.23e10, 0.06, device));
   el->addScatterMechanism(regions, std::make_unique<ZA>("G", 0, kG, 5.23e10, 0.06, device));
   el->addScatterMechanism(regions, std::make_unique<ZE>("G", 0, kG, 5.23e10, 0.06, device));
+  if (kind == "resistor_surface") {
+    // surface mechanisms on the two artificial boundaries of the resistor
+    el->setSurfaceScatterMechanism(
+        emcBoundaryPos::YMIN,
+        std::make_unique<emcConstantSurfaceScatterMechanism<T, Dev2>>(0.3, maxPos));
+    el->setSurfaceScatterMechanism(
+        emcBoundaryPos::YMAX,
+        std::make_unique<emcMomentumDependentSurfaceScatterMechanism<T, Dev2>>(0.5e-9, maxPos));
+  }
   param.addParticleType(std::move(el));
   Sim sim(param, device, solver, pm);
   // device description

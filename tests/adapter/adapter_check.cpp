@@ -88,8 +88,14 @@ int main() {
   emcgpu::ModelBuilder<T, Dev3> mb2(el2, 1000, 1.);
   mb2.addAcoustic(0, 9., device, {0});
   mb2.setGrainScatterMechanism(0.3, 2e14);
+  mb2.setConstantSurfaceScatterMechanism(emcBoundaryPos::YMIN, 0.3, {5e-7, 5e-7, 5e-7});
+  mb2.setMomentumDependentSurfaceScatterMechanism(emcBoundaryPos::YMAX, 0.5e-9,
+                                                  {5e-7, 5e-7, 5e-7});
   const emcg_model_desc &d2 = mb2.desc();
   std::printf("grain %d %a %a\n", d2.grain, d2.grain_transmission, d2.grain_tau);
+  std::printf("surface %d %d %d %d %a %a %a %a\n", d2.surface_kind[0], d2.surface_kind[1],
+              d2.surface_kind[2], d2.surface_kind[3], d2.surface_param[0], d2.surface_param[1],
+              d2.surface_param[2], d2.surface_param[3]);
   std::printf("nograin %d %a\n", d.grain, d.grain_tau);
   return 0;
 }

@@ -104,14 +104,20 @@ def make_bulk(case):
 DEVICE_CASES = [("resistor_ngp", "resistor", 42, 1e-15, 3, 1e-4, 3e-7),
                 ("mosfet_cic", "mosfet", 7, 1e-15, 3, 1e-4, 3e-8),
                 ("resistor_nec", "resistor_nec", 42, 1e-15, 3, 1e-4, 3e-7),
-                ("mosfet_necvwd", "mosfet_vwd", 7, 1e-15, 3, 1e-4, 3e-8)]
+                ("mosfet_necvwd", "mosfet_vwd", 7, 1e-15, 3, 1e-4, 3e-8),
+                ("resistor_surface", "resistor_surface", 4242, 4e-15, 6, 1e-4, 3e-7)]
+
+# surface mechanisms of a harness device kind: (boundary XMIN 0 .. YMAX 3,
+# oracle kind, parameter), as the harness sets them
+DEVICE_SURFACES = {"resistor_surface": [(2, po.SURFACE_CONSTANT, 0.3),
+                                        (3, po.SURFACE_ROUGHNESS, 0.5e-9)]}
 
 
 def device_flavour(kind):
     """PM scheme, potential-based initial counts, electronVWD (rounded counts,
     tau drawn with the valley as the region) of a harness device kind."""
     scheme = {"resistor": po.NGP, "mosfet": po.CIC, "resistor_nec": po.NEC,
-              "mosfet_vwd": po.NEC_VWD}[kind]
+              "mosfet_vwd": po.NEC_VWD, "resistor_surface": po.NGP}[kind]
     return scheme, kind.startswith("mosfet"), kind == "mosfet_vwd"
 
 
@@ -125,9 +131,10 @@ def device_of(d):
     return dev
 
 
-def device_model(d):
+def device_model(d, kind=""):
     """Oracle model of the device harness: acoustic, Coulomb and zero-order f/g
-    intervalley phonons on every doping region (4 eV tables)."""
+    intervalley phonons on every doping region (4 eV tables), and the kind's
+    surface mechanisms."""
     nreg = int(d["region"].max()) + 1
     m = po.Model(n_levels=1000, max_energy=4.0)
     m.add_valley([0.916, 0.196, 0.196], po.ME, 3, 0.5, 0.0, po.SI_FRAMES)
@@ -139,6 +146,8 @@ def device_model(d):
     for fs in (po.F_SUB, po.G_SUB):
         m.add_mech(po.ZERO_IV_ABS, 0, regs, 5.23e10, 0.06, 0, fs)
         m.add_mech(po.ZERO_IV_EMI, 0, regs, 5.23e10, 0.06, 0, fs)
+    for b, sk, par in DEVICE_SURFACES.get(kind, []):
+        m.set_surface(b, sk, par)
     m.build_tables()
     return m, regs
 
@@ -147,7 +156,7 @@ def make_device(case):
     name, kind, seed, dt, steps, acc, width = case
     d = po.run_ref("device", kind, seed, dt, steps, acc, width)
     dev = device_of(d)
-    m, regs = device_model(d)
+    m, regs = device_model(d, kind)
     for r in regs:
         for t in range(6):
             assert np.array_equal(m.raw_table(0, r, t), d[f"raw_v0_r{r}_t{t}"])
@@ -158,6 +167,8 @@ def make_device(case):
     out["raw_coulomb"] = np.stack([d[f"raw_v0_r{r}_t1"] for r in regs])
     out["params"] = np.array([seed, dt, steps, acc, width])
     out["kind"] = np.array(kind)
+    if kind in DEVICE_SURFACES:
+        out["surface"] = np.array(DEVICE_SURFACES[kind], dtype=np.float64)
     scheme, pot_init, vwd = device_flavour(kind)
     pot, _ = dev.sor(d["pot_init"], None, 1.8, acc, True)
     assert np.array_equal(pot, d["pot_eq"])

@@ -62,6 +62,13 @@ def test_adapter_descriptor_matches_host_builder(tmp_path):
     flag, prob, gtau = [l for l in out if l.startswith("grain ")][0].split()[1:]
     assert (int(flag), float.fromhex(prob), float.fromhex(gtau)) == \
         (g.grain, g.grain_transmission, g.grain_tau)
+    sf = [l for l in out if l.startswith("surface ")][0].split()[1:]
+    pt2 = physics.silicon_electron("jacoboni")
+    pt2.setSurfaceScatterMechanism(2, physics.ConstantSurfaceScatterMechanism(0.3))
+    pt2.setSurfaceScatterMechanism(3, physics.MomentumDependentSurfaceScatterMechanism(0.5e-9))
+    g2 = pt2.model_desc()
+    assert [int(x) for x in sf[:4]] == list(g2.surface_kind) == [0, 0, 1, 2]
+    assert [float.fromhex(x) for x in sf[4:]] == list(g2.surface_param)
     flag, gtau = [l for l in out if l.startswith("nograin ")][0].split()[1:]
     assert (int(flag), float.fromhex(gtau)) == (d.grain, d.grain_tau) == (0, 1.0)
 

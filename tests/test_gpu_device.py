@@ -14,7 +14,7 @@ import pytest
 
 from conftest import golden
 from test_oracle_device_golden import (DEVICE_CASES, _host_device, _oracle_device, _oracle_model,
-                                       flavour)
+                                       flavour, surfaces)
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-12
@@ -22,10 +22,11 @@ FIELDS_F = ("kx", "ky", "kz", "px", "py", "E", "tau", "gtau")
 ENG = {"E": "energy", "gtau": "grain_tau"}
 
 
-def _electron(engine, dev, grain=None):
+def _electron(engine, dev, grain=None, surface=()):
     """The harness's particle type: acoustic, Coulomb, zero-order f/g
     absorption/emission, in that registration order, 4 eV tables; grain: a
-    grain mechanism (transmission probability, scatter rate)."""
+    grain mechanism (transmission probability, scatter rate); surface: the
+    fixture's surface mechanisms (boundary, kind, parameter)."""
     from viennaemc_gb300 import physics as P
     mat = P.silicon_material()
     pt = P.Electron(1000, 4.0)
@@ -41,6 +42,10 @@ def _electron(engine, dev, grain=None):
             sfx, 0, fs, 5.23e10, 0.06, 300.0, mat.rho))
     if grain is not None:
         pt.setGrainScatterMechanism(P.GrainScatterMechanism(*grain))
+    for b, kind, par in surface:
+        cls = (P.ConstantSurfaceScatterMechanism if kind == 1
+               else P.MomentumDependentSurfaceScatterMechanism)
+        pt.setSurfaceScatterMechanism(b, cls(par))
     pt.initScatterTables()
     return pt
 
@@ -49,7 +54,7 @@ def _sim(engine, g, case, precision="fp64", seed=1, grain=None, **kw):
     from viennaemc_gb300 import device as D
     scheme, pot_init, vwd = flavour(g)
     dev = _host_device(g, pot_init)
-    pt = _electron(engine, dev, grain)
+    pt = _electron(engine, dev, grain, surfaces(g))
     return D.DeviceSimulation(dev, pt, scheme=scheme, dt=float(g["params"][1]),
                               seed=seed, capacity=1 << 15, precision=precision,
                               potential_init=pot_init, round_counts=vwd,

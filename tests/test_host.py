@@ -99,6 +99,8 @@ def _ens(**over):
     (dict(max_energy=-1.0), "max_energy"),
     (dict(grain_tau=0.0), "grain_tau"),
     (dict(grain=2), "grain must be 0 or 1"),
+    (dict(surface_kind=(C.c_int32 * 4)(0, 0, 3, 0)), "surface_kind"),
+    (dict(surface_kind=(C.c_int32 * 4)(0, 0, 0, 2)), "roughness height"),
     (dict(grain=1, grain_transmission=float("nan")), "grain_transmission"),
 ])
 def test_create_rejects_bad_model_without_gpu(bad, msg):

@@ -7,17 +7,19 @@ import pytest
 from conftest import golden
 
 DEVICE_CASES = ["device_resistor_ngp.npz", "device_mosfet_cic.npz", "device_resistor_nec.npz",
-                "device_mosfet_necvwd.npz"]
+                "device_mosfet_necvwd.npz", "device_resistor_surface.npz"]
 
 
 def flavour(g):
     """(PM scheme, potential-based initial counts, electronVWD) of a fixture:
     resistor NGP, MOSFET CIC, resistor with the NEC scheme, and the mosfet2D
     example's NEC-VWD scheme with its electronVWD particle type (rounded counts,
-    tau drawn with the valley as the region).  Scheme numbers are shared by the
+    tau drawn with the valley as the region); the NGP resistor with surface
+    mechanisms on its artificial boundaries.  Scheme numbers are shared by the
     oracle and the engine."""
     kind = str(g["kind"])
-    scheme = {"resistor": 0, "mosfet": 1, "resistor_nec": 2, "mosfet_vwd": 3}[kind]
+    scheme = {"resistor": 0, "mosfet": 1, "resistor_nec": 2, "mosfet_vwd": 3,
+              "resistor_surface": 0}[kind]
     return scheme, kind.startswith("mosfet"), kind == "mosfet_vwd"
 
 
@@ -43,8 +45,17 @@ def _oracle_model(oracle, g):
     for fs in (oracle.F_SUB, oracle.G_SUB):
         m.add_mech(oracle.ZERO_IV_ABS, 0, regs, 5.23e10, 0.06, 0, fs)
         m.add_mech(oracle.ZERO_IV_EMI, 0, regs, 5.23e10, 0.06, 0, fs)
+    for b, kind, par in surfaces(g):
+        m.set_surface(b, kind, par)
     m.build_tables()
     return m, regs
+
+
+def surfaces(g):
+    """(boundary, kind, parameter) of the fixture's surface mechanisms; the
+    kinds are shared by the oracle and the engine (0 specular, 1 constant
+    specularity, 2 momentum-dependent roughness)."""
+    return [(int(b), int(k), float(p)) for b, k, p in g["surface"]] if "surface" in g else []
 
 
 def _state(oracle, g, s):

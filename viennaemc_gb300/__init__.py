@@ -11,7 +11,8 @@ from .physics import (Electron, NonParabolicAnisotropValley, AcousticScatterMech
                       ZeroOrderInterValleyEmissionScatterMechanism,
                       FirstOrderInterValleyAbsorptionScatterMechanism,
                       FirstOrderInterValleyEmissionScatterMechanism, CoulombScatterMechanism,
-                      GrainScatterMechanism, silicon_electron, silicon_material, thermal_voltage)
+                      GrainScatterMechanism, ConstantSurfaceScatterMechanism,
+                      MomentumDependentSurfaceScatterMechanism, silicon_electron, silicon_material, thermal_voltage)
 from .bulk import (BulkBatch, BulkParticleHandler, EnsembleSpec, FMMBulkParticleHandler,
                    ParticleState, ParticleStateF32)
 
@@ -21,6 +22,7 @@ __all__ = ["Electron", "NonParabolicAnisotropValley", "AcousticScatterMechanism"
            "ZeroOrderInterValleyEmissionScatterMechanism",
            "FirstOrderInterValleyAbsorptionScatterMechanism",
            "FirstOrderInterValleyEmissionScatterMechanism", "CoulombScatterMechanism",
-           "GrainScatterMechanism", "silicon_electron", "silicon_material", "thermal_voltage", "BulkBatch",
+           "GrainScatterMechanism", "ConstantSurfaceScatterMechanism",
+           "MomentumDependentSurfaceScatterMechanism", "silicon_electron", "silicon_material", "thermal_voltage", "BulkBatch",
            "BulkParticleHandler", "EnsembleSpec", "FMMBulkParticleHandler", "ParticleState",
            "build"]

@@ -96,13 +96,17 @@ class TablesetDesc(C.Structure):
                 ("pad_", C.c_int32), ("mech", C.c_int32 * MAX_MECH), ("tau_max", C.c_double)]
 
 
+SURFACE_SPECULAR, SURFACE_CONSTANT, SURFACE_ROUGHNESS = 0, 1, 2  # emcg_model_desc.surface_kind
+
+
 class ModelDesc(C.Structure):
     _fields_ = [("n_valleys", C.c_int32), ("n_mechs", C.c_int32), ("n_tablesets", C.c_int32),
                 ("n_levels", C.c_int32), ("max_energy", C.c_double), ("grain_tau", C.c_double),
                 ("valleys", C.POINTER(ValleyDesc)), ("mechs", C.POINTER(MechDesc)),
                 ("tablesets", C.POINTER(TablesetDesc)), ("tables", C.POINTER(C.c_double)),
                 ("region_doping", C.c_double * MAX_REGIONS), ("grain", C.c_int32),
-                ("grain_pad_", C.c_int32), ("grain_transmission", C.c_double)]
+                ("grain_pad_", C.c_int32), ("grain_transmission", C.c_double),
+                ("surface_kind", C.c_int32 * 4), ("surface_param", C.c_double * 4)]
 
 
 class EnsembleDesc(C.Structure):

@@ -53,6 +53,8 @@ template <class T> struct ModelK {
   T tauMax[EMCG_MAX_TABLESETS];
   uint8_t tsMech[EMCG_MAX_TABLESETS][EMCG_MAX_MECH];
   const T *tables; // level-major per set: tables[tsOff + L * nT + t]
+  int32_t surfKind[4]; // EMCG_SURFACE_* per device boundary (XMIN, XMAX, YMIN, YMAX)
+  T surfParam[4];      // its specularity or roughness height [m]
 };
 
 // per-ensemble constants of a bulk launch
@@ -99,6 +101,10 @@ __device__ __forceinline__ double m_log(double x) { return log(x); }
 __device__ __forceinline__ float m_log(float x) { return __logf(x); }
 __device__ __forceinline__ double m_floor(double x) { return floor(x); }
 __device__ __forceinline__ float m_floor(float x) { return floorf(x); }
+__device__ __forceinline__ double m_exp(double x) { return exp(x); }
+__device__ __forceinline__ float m_exp(float x) { return expf(x); }
+__device__ __forceinline__ void m_sincos(double x, double *s, double *c) { sincos(x, s, c); }
+__device__ __forceinline__ void m_sincos(float x, float *s, float *c) { sincosf(x, s, c); }
 __device__ __forceinline__ void m_sincos2pi(double u, double *s, double *c) {
   double phi = 2 * kPI * u; // 2 * emcPi<T>() * rand (include/emcUtil.hpp:132)
   *s = sin(phi);

@@ -104,14 +104,90 @@ __device__ __forceinline__ void interpForce(const DevK &G, const T *Ex, const T 
   }
 }
 
+// emcMomentumDependentSurfaceScatterMechanism::solveForTheta
+// (include/SurfaceScatterMechanisms/emcMomentumDependentSurfaceScatterMechanism.hpp:
+// 38-66): the reference's fixed-point iteration as it stands, at most 10000
+// steps, stopping once a step moves theta by at most 1e-10 (it often runs to
+// the cap; the capped result is insensitive to rounding, ~1e-15 relative).
+template <class T> __device__ __noinline__ T solveForTheta(T r, T height, T speed) {
+  const T c = (T(2) * height * speed) * (T(2) * height * speed);
+  const T e = m_exp(-c);
+  T x = m_sqrt(r * (T(1) / (T(1) - e) - T(1) / c));
+  T error = T(1);
+  for (int it = 0; error > T(1e-10) && it < 10000; it++) {
+    T si, co;
+    m_sincos(x, &si, &co);
+    const T ecos = m_exp(-c * (co * co));
+    const T esin = m_exp(-c * (si * si));
+    const T x1 = x - (((e - ecos) / c + si * si - r * (T(1) - (T(1) - e) / c)) *
+                      (T(2) * esin * c * si * co * (ecos - T(1))) / (e * (c - T(1)) - T(1)));
+    error = fabs(x1 - x);
+    x = x1;
+  }
+  return x;
+}
+
+// emcScatterHandler::scatterParticleAtBoundary (include/emcScatterHandler.hpp:
+// 172-191) with the surface mechanism of boundary b
+// (emcSurfaceScatterMechanism::scatterParticle, :38-44): diffuse with the
+// mechanism's probability (calculateAndAssignKAndPos, :128-148: |k| kept, k at
+// polar angle theta from the inward normal), else specular; either way the
+// position goes back into the device and k is turned inwards where it points
+// out (scatterParticleSpecularly, :75-86).  The energy is not updated.
+template <class T, class Src>
+__device__ __forceinline__ void surfaceScatter(const ModelK<T> &M, const DevK &G, int b,
+                                               T pos[2], T k[3], Src &rng) {
+  const int kind = M.surfKind[b], perp = b >> 1;
+  const T par = M.surfParam[b];
+  const T pDiff = kind == EMCG_SURFACE_CONSTANT
+                      ? T(1) - par // emcConstantSurfaceScatterMechanism.hpp:33
+                      : T(1) - m_exp(-((T(2) * par * k[perp]) * (T(2) * par * k[perp])));
+  if (rng.u01() < pDiff) {
+    T theta;
+    if (kind == EMCG_SURFACE_CONSTANT)
+      theta = asin(m_sqrt(rng.u01()));
+    else
+      theta = solveForTheta(rng.u01(), par, m_sqrt(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]));
+    const T phi = T(2) * T(3.14159265358979323846) * rng.u01(); // constants::pi
+    const T speed = m_sqrt(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
+    T st, ct, sp, cp;
+    m_sincos(theta, &st, &ct);
+    m_sincos(phi, &sp, &cp);
+    k[perp] = speed * ct * ((b & 1) ? T(-1) : T(1));
+    k[(perp + 1) % 3] = speed * st * cp;
+    k[(perp + 2) % 3] = speed * st * sp;
+  }
+  const T mx[2] = {(T)G.maxX, (T)G.maxY};
+#pragma unroll
+  for (int i = 0; i < 2; i++) {
+    if (pos[i] < T(0)) {
+      pos[i] *= T(-1);
+      if (k[i] < T(0))
+        k[i] *= T(-1);
+    } else if (pos[i] > mx[i]) {
+      pos[i] = T(2) * mx[i] - pos[i];
+      if (k[i] > T(0))
+        k[i] *= T(-1);
+    }
+  }
+}
+
+// the first boundary (XMIN, XMAX, YMIN, YMAX) holding node (x, y)
+// (emcSurface::getBoundaryPos, include/emcSurface.hpp:338-349)
+__device__ __forceinline__ int boundaryOf(const DevK &G, int x, int y) {
+  return x == 0 ? 0 : x == G.nx - 1 ? 1 : y == 0 ? 2 : 3;
+}
+
 // free flight under force F, then the boundary treatment of
-// include/emcParticleDrift.hpp:41-66 (removal at ohmic contacts, specular
-// reflection elsewhere) and the region update of
-// include/ParticleHandler/emcAbstractParticleHandler.hpp:238-249.
-template <class T>
+// include/emcParticleDrift.hpp:41-66 (removal at ohmic contacts, a surface
+// mechanism or specular reflection elsewhere) and the region update of
+// include/ParticleHandler/emcAbstractParticleHandler.hpp:238-249.  kSurf: the
+// instance for models with surface mechanisms (the others keep the plain
+// reflection and their register allocation).
+template <class T, bool kSurf, class Src>
 __device__ __forceinline__ bool devDrift(const ModelK<T> &M, const DevK &G, int valley, int sub,
                                          const T F[2], T dt, T k[3], T &E, T pos[2],
-                                         int &region) {
+                                         int &region, Src &rng) {
   const ValleyK<T> &V = M.v[valley];
   T fE[3];
   toEcs(V.rot[sub], F[0], F[1], T(0), fE);
@@ -133,14 +209,19 @@ __device__ __forceinline__ bool devDrift(const ModelK<T> &M, const DevK &G, int 
       pos[1] = pb[1];
       return true;
     }
+    const int b = boundaryOf(G, cx, cy);
+    if (kSurf && M.surfKind[b] != EMCG_SURFACE_SPECULAR) {
+      surfaceScatter(M, G, b, pos, k, rng);
+    } else {
 #pragma unroll
-    for (int i = 0; i < 2; i++) {
-      if (pos[i] < T(0)) {
-        pos[i] = -pos[i];
-        k[i] = -k[i];
-      } else if (pos[i] > mx[i]) {
-        pos[i] = T(2) * mx[i] - pos[i];
-        k[i] = -k[i];
+      for (int i = 0; i < 2; i++) {
+        if (pos[i] < T(0)) {
+          pos[i] = -pos[i];
+          k[i] = -k[i];
+        } else if (pos[i] > mx[i]) {
+          pos[i] = T(2) * mx[i] - pos[i];
+          k[i] = -k[i];
+        }
       }
     }
   }
@@ -157,7 +238,7 @@ __device__ __forceinline__ void recordErr(int *err, int code) {
 
 // driftScatterParticles for one particle
 // (include/ParticleHandler/emcBasicParticleHandler.hpp:93-139)
-template <class T, int SCHEME, class Src>
+template <class T, int SCHEME, bool kSurf, class Src>
 __device__ __forceinline__ int devParticleStep(const ModelK<T> &M, const DevK &G, const T *Ex,
                                                const T *Ey, T charge, T dt, T k[3], T pos[2],
                                                T &E, T &tau, T &gtau, int &valley, int &sub,
@@ -166,9 +247,9 @@ __device__ __forceinline__ int devParticleStep(const ModelK<T> &M, const DevK &G
   T F[2];
   interpForce<T, SCHEME>(G, Ex, Ey, pos[0], pos[1], charge, F);
   if (tau >= dt) {
-    removed = devDrift(M, G, valley, sub, F, dt, k, E, pos, region);
+    removed = devDrift<T, kSurf>(M, G, valley, sub, F, dt, k, E, pos, region, rng);
   } else {
-    removed = devDrift(M, G, valley, sub, F, tau, k, E, pos, region);
+    removed = devDrift<T, kSurf>(M, G, valley, sub, F, tau, k, E, pos, region, rng);
     T tRem = dt - tau;
     int guard = 0;
     while (tRem > T(0) && !removed) {
@@ -184,7 +265,8 @@ __device__ __forceinline__ int devParticleStep(const ModelK<T> &M, const DevK &G
       T nt = -m_log(rng.ulog()) * tauOf(M, valley, region);
       tau += nt;
       interpForce<T, SCHEME>(G, Ex, Ey, pos[0], pos[1], charge, F);
-      removed = devDrift(M, G, valley, sub, F, nt < tRem ? nt : tRem, k, E, pos, region);
+      removed = devDrift<T, kSurf>(M, G, valley, sub, F, nt < tRem ? nt : tRem, k, E, pos,
+                                       region, rng);
       tRem -= nt;
     }
   }
@@ -200,7 +282,7 @@ __device__ __forceinline__ int devParticleStep(const ModelK<T> &M, const DevK &G
 
 // the float instance is capped at 64 registers, 4 blocks of 256 per SM (72
 // registers gave 3; a one-step launch needs the warps to hide its loads)
-template <class T, int SCHEME, bool REPLAY>
+template <class T, int SCHEME, bool REPLAY, bool kSurf>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1)
     devMoveKernel(StateK<T> st, const ModelK<T> *__restrict__ models, DevK G,
                   const T *__restrict__ Ex, const T *__restrict__ Ey, T charge, T dt,
@@ -222,15 +304,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1)
   int e;
   if constexpr (REPLAY) {
     ReplaySrc src{rw, roff[i], roff[i + 1], 0};
-    e = devParticleStep<T, SCHEME>(M, G, Ex, Ey, charge, dt, k, pos, E, tau, gtau, valley, sub,
-                                   region, src, removed);
+    e = devParticleStep<T, SCHEME, kSurf>(M, G, Ex, Ey, charge, dt, k, pos, E, tau, gtau, valley,
+                                          sub, region, src, removed);
     if (!e && (src.bad || src.pos != src.end))
       e = EMCG_ERR_REPLAY;
   } else {
     PhiloxSrc<T> src;
     src.init((uint32_t)i, step, stream, key0, key1);
-    e = devParticleStep<T, SCHEME>(M, G, Ex, Ey, charge, dt, k, pos, E, tau, gtau, valley, sub,
-                                   region, src, removed);
+    e = devParticleStep<T, SCHEME, kSurf>(M, G, Ex, Ey, charge, dt, k, pos, E, tau, gtau, valley,
+                                          sub, region, src, removed);
   }
   recordErr(err, e);
   st.kx[i] = k[0];
@@ -786,6 +868,7 @@ __global__ void efieldKernel(DevK G, const double *__restrict__ pot, T *__restri
 // ---------------------------------------------------------------------------
 struct DeviceImpl {
   int precision = EMCG_FP64;
+  bool surfaces = false; // the model has a surface mechanism (devMoveKernel's kSurf)
   size_t tsz = 8;
   emcg_device_config cfg;
   int nx = 0, ny = 0, nContacts = 0;
@@ -969,6 +1052,9 @@ template <class T> static int32_t createModel(DeviceImpl *d, const emcg_model_de
   std::vector<T> tab;
   EMCG_TRY(buildModelK<T>(m, K, tab));
   d->rates = rateLayoutOf(m);
+  d->surfaces = false;
+  for (int b = 0; b < 4; b++)
+    d->surfaces = d->surfaces || m.surface_kind[b] != EMCG_SURFACE_SPECULAR;
   EMCG_TRY(up((T **)&d->dTables, tab.data(), tab.size(), d->stream));
   K.tables = (const T *)d->dTables;
   EMCG_TRY(up((ModelK<T> **)&d->dModel, &K, 1, d->stream));
@@ -1272,9 +1358,10 @@ template <class T> static int32_t moveT(DeviceImpl *d, uint32_t step, bool compa
     return EMCG_ERR_ARG;
   }
 #define EMCG_MOVE(SCH, REP)                                                                      \
-  devMoveKernel<T, SCH, REP><<<nb, 256, 0, d->stream>>>(                                         \
-      st, M, G, Ex, Ey, (T)c.charge, (T)c.dt, d->dN, step, k0, k1, c.stream, d->dDrop, d->dNetto, \
-      d->dWords[0], d->dOff[0], d->dErr)
+  (d->surfaces ? devMoveKernel<T, SCH, REP, true> : devMoveKernel<T, SCH, REP, false>)           \
+      <<<nb, 256, 0, d->stream>>>(st, M, G, Ex, Ey, (T)c.charge, (T)c.dt, d->dN, step, k0, k1,    \
+                                  c.stream, d->dDrop, d->dNetto, d->dWords[0], d->dOff[0],        \
+                                  d->dErr)
   if (rep) {
     if constexpr (sizeof(T) == 8) {
       if (c.pm_scheme == EMCG_PM_NGP)

@@ -47,6 +47,17 @@ inline int32_t validateModel(const emcg_model_desc &m) {
   EMCG_CHECK_ARG(m.grain == 0 || m.grain == 1, "model: grain must be 0 or 1");
   EMCG_CHECK_ARG(m.grain == 0 || std::isfinite(m.grain_transmission),
                  "model: grain_transmission must be finite");
+  for (int b = 0; b < 4; b++) {
+    EMCG_CHECK_ARG(m.surface_kind[b] >= EMCG_SURFACE_SPECULAR &&
+                       m.surface_kind[b] <= EMCG_SURFACE_ROUGHNESS,
+                   "model: surface_kind[%d]=%d unknown", b, m.surface_kind[b]);
+    EMCG_CHECK_ARG(m.surface_kind[b] != EMCG_SURFACE_ROUGHNESS ||
+                       (m.surface_param[b] > 0 && std::isfinite(m.surface_param[b])),
+                   "model: surface_param[%d] (roughness height) must be positive", b);
+    EMCG_CHECK_ARG(m.surface_kind[b] != EMCG_SURFACE_CONSTANT ||
+                       std::isfinite(m.surface_param[b]),
+                   "model: surface_param[%d] (specularity) must be finite", b);
+  }
   for (int v = 0; v < m.n_valleys; v++) {
     const emcg_valley_desc &V = m.valleys[v];
     EMCG_CHECK_ARG(V.deg >= 1 && V.deg <= EMCG_MAX_DEG, "valley %d: deg=%d out of [1,%d]", v,
@@ -115,6 +126,10 @@ int32_t buildModelK(const emcg_model_desc &m, ModelK<T> &K, std::vector<T> &tabl
   K.grainTau = (T)m.grain_tau;
   K.grain = m.grain;
   K.grainProb = m.grain ? (T)m.grain_transmission : T(0);
+  for (int b = 0; b < 4; b++) {
+    K.surfKind[b] = m.surface_kind[b];
+    K.surfParam[b] = (T)m.surface_param[b];
+  }
   std::vector<double> mcOf(m.n_valleys);
   for (int v = 0; v < m.n_valleys; v++) {
     const emcg_valley_desc &V = m.valleys[v];

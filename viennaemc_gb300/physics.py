@@ -291,6 +291,7 @@ class ScatterHandler:
         self.tau: dict = {}
         self.grainScatterMech = None
         self.grainTau = 1.0  # include/emcScatterHandler.hpp:61-62
+        self.surfaceScatterMechanisms = [None] * 4  # per boundary, :63-65, 114-124
 
     def setGrainScatterMechanism(self, mech):
         self.grainScatterMech = mech
@@ -368,6 +369,31 @@ class GrainScatterMechanism:
         return self.scatterRate
 
 
+class ConstantSurfaceScatterMechanism:
+    """emcConstantSurfaceScatterMechanism (include/SurfaceScatterMechanisms/
+    emcConstantSurfaceScatterMechanism.hpp): at its boundary a particle is
+    reflected specularly with the specularity parameter's probability, else
+    diffusely (polar angle asin(sqrt(u)) from the inward normal).  max_pos is
+    the reference constructor's; the engine takes the device's extent."""
+
+    kind = L.SURFACE_CONSTANT
+
+    def __init__(self, specularityParam, max_pos=None):
+        self.param = float(specularityParam)
+
+
+class MomentumDependentSurfaceScatterMechanism:
+    """emcMomentumDependentSurfaceScatterMechanism (include/
+    SurfaceScatterMechanisms/emcMomentumDependentSurfaceScatterMechanism.hpp):
+    diffuse with probability 1 - exp(-(2 h k_perp)^2) for roughness height h
+    [m], else specular."""
+
+    kind = L.SURFACE_ROUGHNESS
+
+    def __init__(self, roughnessHeight, max_pos=None):
+        self.param = float(roughnessHeight)
+
+
 class Electron:
     """Electron particle type (include/ParticleType/emcElectron.hpp:15-105):
     valleys + scatter handler; charge -q, mass m0."""
@@ -410,6 +436,14 @@ class Electron:
     def getGrainTau(self):
         return self.scatterHandler.getGrainTau()
 
+    def setSurfaceScatterMechanism(self, boundary, mech):
+        """emcParticleType::setSurfaceScatterMechanism(boundaryPosition,
+        mechanism) (emcParticleType.hpp:155-166); boundary 0..3 = XMIN, XMAX,
+        YMIN, YMAX.  Used by device simulations."""
+        if not 0 <= int(boundary) < 4:
+            raise ValueError("boundary must be XMIN, XMAX, YMIN or YMAX")
+        self.scatterHandler.surfaceScatterMechanisms[int(boundary)] = mech
+
     def getTau(self, valley, region):
         return self.scatterHandler.getTau(region, valley)
 
@@ -448,6 +482,9 @@ class Electron:
         d.n_levels, d.max_energy, d.grain_tau = h.n_levels, h.max_energy, h.getGrainTau()
         if h.grainScatterMech is not None:
             d.grain, d.grain_transmission = 1, h.grainScatterMech.transmissionProb
+        for b, sm in enumerate(h.surfaceScatterMechanisms):
+            if sm is not None:
+                d.surface_kind[b], d.surface_param[b] = sm.kind, sm.param
         d.valleys, d.mechs, d.tablesets = va, ma, ta
         d.tables = tables.ctypes.data_as(C.POINTER(C.c_double))
         for r in range(L.MAX_REGIONS):
