@@ -509,6 +509,14 @@ int32_t emcg_device_poisson(emcg_handle *h, int32_t equilibrium, int32_t reset_b
                             double *rel_residual, int32_t *cycles);
 /* emcAbstractPMScheme::calcEField (include/PMSchemes/emcEFieldCalculation.hpp:13-81) */
 int32_t emcg_device_efield(emcg_handle *h);
+/* emcScatterHandler::scatterParticleAtBoundary (include/emcScatterHandler.hpp:
+   172-191) at boundary b (0 XMIN, 1 XMAX, 2 YMIN, 3 YMAX) for n independent
+   particles outside the device: the model's surface mechanism there, else
+   the plain reflection.  k (3 x n) and pos (2 x n) SoA, in/out; Philox draws
+   of the engine's seed and stream at `step`.  For known-answer tests of the
+   reference (tests/testSurfaceScatterMechanisms). */
+int32_t emcg_device_surface_kat(emcg_handle *h, int32_t boundary, int64_t n, double *k,
+                                double *pos, uint32_t step);
 /* driftScatterParticles (include/ParticleHandler/emcBasicParticleHandler.hpp:76-145):
    netto[c] += particles that left through contact c. */
 int32_t emcg_device_move(emcg_handle *h, uint32_t step, int32_t *netto);

@@ -542,3 +542,62 @@ def test_deposition_is_reproducible_bit_for_bit(engine):
     # the float engine forms its weights in float
     assert np.allclose(nr.reshape(101, 201), ref, rtol=0, atol=2e-6), \
         np.abs(nr.reshape(101, 201) - ref).max()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_surface_mechanisms_reference_kat(engine, precision):
+    """The reference's surface-scattering test (tests/testSurfaceScatterMechanisms/
+    testSurfaceScatterMechanisms.cpp:16-118) through the engine's boundary
+    routine, 1000 particles per case, on a 2-D device of the same 1 um extent
+    (the z positions of the 3-D original drop out): a smooth surface
+    (specularity 1) reflects, a rough one (specularity 0) and a
+    momentum-dependent one at |2 h k_perp| = 6 scatter diffusely into the
+    device, a boundary without mechanism reflects; |k| is kept."""
+    from viennaemc_gb300 import device as D
+    from viennaemc_gb300 import physics as P
+    mat = P.silicon_material()
+    dev = D.Device(mat, (1e-6, 1e-6), (1e-7, 1e-7))
+    dev.addConstantDopingRegion((0, 0), (1e-6, 1e-6), 1e22)
+    pt = P.silicon_electron("jacoboni", n_levels=1000, max_energy=4.0)
+    pt.setSurfaceScatterMechanism(D.YMAX, P.ConstantSurfaceScatterMechanism(1.0))
+    pt.setSurfaceScatterMechanism(D.XMIN, P.ConstantSurfaceScatterMechanism(0.0))
+    pt.setSurfaceScatterMechanism(D.XMAX, P.MomentumDependentSurfaceScatterMechanism(3e-10))
+    sim = D.DeviceSimulation(dev, pt, scheme=D.NGP, dt=1e-15, seed=1, capacity=1 << 12,
+                             precision=precision)
+    n, mx = 1000, 1e-6
+    rtol = 1e-10 if precision == "fp64" else 1e-6
+
+    def run(b, k0, p0):
+        k, p = sim.surface_kat(b, np.tile(k0, (n, 1)), np.tile(p0, (n, 1)))
+        assert np.allclose(np.linalg.norm(k, axis=1), np.linalg.norm(k0), rtol=rtol, atol=0)
+        return k, p
+
+    # YMAX, smooth: specular
+    k, p = run(D.YMAX, [1, 1, 1], [1e-6, 1.1e-6])
+    assert np.all(k[:, 1] < 0) and np.all(k[:, 0] == 1) and np.all(k[:, 2] == 1)
+    assert np.allclose(p[:, 1], 2 * mx - 1.1e-6, rtol=rtol)
+    assert np.allclose(p[:, 0], 1e-6, rtol=rtol)
+    # XMIN, rough: diffuse into the device
+    k, p = run(D.XMIN, [-1, 1, 1], [-0.1e-6, 1e-6])
+    assert np.all(k[:, 0] > 0) and np.all(k[:, 1] != 1) and np.all(k[:, 2] != 1)
+    assert np.allclose(p[:, 0], 0.1e-6, rtol=rtol) and np.allclose(p[:, 1], 1e-6, rtol=rtol)
+    # XMAX, momentum-dependent: diffuse (1 - exp(-36))
+    k, p = run(D.XMAX, [1e10, 1e10, 1e10], [1.1e-6, 5e-7])
+    assert np.all(k[:, 0] < 0) and np.all(k[:, 1] != 1e10) and np.all(k[:, 2] != 1e10)
+    assert np.allclose(p[:, 0], 2 * mx - 1.1e-6, rtol=rtol)
+    assert np.allclose(p[:, 1], 5e-7, rtol=rtol)
+    # XMIN, far outside in both directions: diffuse, then every coordinate back
+    # inside with k pointing inwards
+    k, p = run(D.XMIN, [-1, -1, -1], [-0.1, -0.1])
+    assert np.all(k[:, 0] > 0) and np.all(k[:, 1] > 0)
+    assert np.allclose(p, 0.1, rtol=rtol)
+    # YMIN, no mechanism: plain reflection
+    k, p = run(D.YMIN, [1, -1, 1], [5e-7, -0.1])
+    assert np.all(k[:, 1] > 0) and np.all(k[:, 0] == 1) and np.all(k[:, 2] == 1)
+    assert np.allclose(p[:, 1], 0.1, rtol=rtol) and np.allclose(p[:, 0], 5e-7, rtol=rtol)
+    # the diffuse directions: a cosine law about the inward normal (mean of
+    # cos(theta) = 2/3 for the constant mechanism)
+    k, _ = run(D.XMIN, [-1, 1, 1], [-0.1e-6, 1e-6])
+    ct = k[:, 0] / np.linalg.norm(k, axis=1)
+    assert abs(ct.mean() - 2 / 3) < 0.03, ct.mean()
+    sim.close()

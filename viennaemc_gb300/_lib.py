@@ -247,6 +247,8 @@ _EXTRA_DECLS.extend([
     ("emcg_device_poisson", [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_double),
                              C.POINTER(C.c_int32)]),
     ("emcg_device_efield", [C.c_void_p]),
+    ("emcg_device_surface_kat", [C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double), C.c_uint32]),
     ("emcg_device_move", [C.c_void_p, C.c_uint32, C.POINTER(C.c_int32)]),
     ("emcg_device_contacts", [C.c_void_p, C.c_uint32, C.POINTER(C.c_int32)]),
     ("emcg_device_assign", [C.c_void_p]),

@@ -1543,6 +1543,76 @@ extern "C" int32_t emcg_device_poisson(emcg_handle *h, int32_t equilibrium, int3
   return s;
 }
 
+namespace emcg {
+// scatterParticleAtBoundary (include/emcScatterHandler.hpp:172-191) at boundary
+// b for n independent particles: the model's surface mechanism there, else the
+// plain reflection (known-answer tests of the reference)
+template <class T>
+__global__ void surfaceKatKernel(const ModelK<T> *__restrict__ models, DevK G, int b, int64_t n,
+                                 double *__restrict__ k, double *__restrict__ pos, uint32_t step,
+                                 uint32_t key0, uint32_t key1, uint32_t stream) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const ModelK<T> &M = models[0];
+  T kk[3] = {(T)k[i], (T)k[n + i], (T)k[2 * n + i]}, p[2] = {(T)pos[i], (T)pos[n + i]};
+  PhiloxSrc<T> rng;
+  rng.init((uint32_t)i, step, stream, key0, key1);
+  if (M.surfKind[b] != EMCG_SURFACE_SPECULAR) {
+    surfaceScatter(M, G, b, p, kk, rng);
+  } else {
+    const T mx[2] = {(T)G.maxX, (T)G.maxY};
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      if (p[j] < T(0)) {
+        p[j] = -p[j];
+        kk[j] = -kk[j];
+      } else if (p[j] > mx[j]) {
+        p[j] = T(2) * mx[j] - p[j];
+        kk[j] = -kk[j];
+      }
+    }
+  }
+  for (int j = 0; j < 3; j++)
+    k[j * n + i] = (double)kk[j];
+  pos[i] = (double)p[0];
+  pos[n + i] = (double)p[1];
+}
+} // namespace emcg
+
+extern "C" int32_t emcg_device_surface_kat(emcg_handle *h, int32_t boundary, int64_t n,
+                                           double *k, double *pos, uint32_t step) {
+  DeviceImpl *d;
+  EMCG_TRY(devOf(h, &d));
+  EMCG_CHECK_ARG(boundary >= 0 && boundary < 4 && n >= 0 && k && pos, "bad surface arguments");
+  if (n == 0)
+    return EMCG_OK;
+  double *buf = nullptr;
+  EMCG_CUDA(cudaMalloc(&buf, 5 * n * sizeof(double)));
+  EMCG_CUDA(cudaMemcpy(buf, k, 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+  EMCG_CUDA(cudaMemcpy(buf + 3 * n, pos, 2 * n * sizeof(double), cudaMemcpyHostToDevice));
+  const uint32_t k0 = (uint32_t)d->cfg.seed, k1 = (uint32_t)(d->cfg.seed >> 32);
+  const int blocks = (int)((n + 127) / 128);
+  if (d->precision == EMCG_FP64)
+    surfaceKatKernel<double><<<blocks, 128, 0, d->stream>>>(
+        (const ModelK<double> *)d->dModel, devK(d), boundary, n, buf, buf + 3 * n, step, k0, k1,
+        d->cfg.stream);
+  else
+    surfaceKatKernel<float><<<blocks, 128, 0, d->stream>>>(
+        (const ModelK<float> *)d->dModel, devK(d), boundary, n, buf, buf + 3 * n, step, k0, k1,
+        d->cfg.stream);
+  int32_t st = EMCG_OK;
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(d->stream) != cudaSuccess ||
+      cudaMemcpy(k, buf, 3 * n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(pos, buf + 3 * n, 2 * n * sizeof(double), cudaMemcpyDeviceToHost) !=
+          cudaSuccess) {
+    setError("surface known-answer kernel failed");
+    st = EMCG_ERR_CUDA;
+  }
+  cudaFree(buf);
+  return st;
+}
+
 extern "C" int32_t emcg_device_efield(emcg_handle *h) {
   DeviceImpl *d;
   EMCG_TRY(devOf(h, &d));

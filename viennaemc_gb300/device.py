@@ -261,6 +261,15 @@ class DeviceSimulation:
     def efield(self):
         L.check(self._lib.emcg_device_efield(self.h))
 
+    def surface_kat(self, boundary, k, pos, step=0):
+        """scatterParticleAtBoundary at one boundary for independent particles
+        (k: n x 3, pos: n x 2); returns the new (k, pos)."""
+        kk = np.ascontiguousarray(np.asarray(k, np.float64).T).copy()
+        pp = np.ascontiguousarray(np.asarray(pos, np.float64).T).copy()
+        L.check(self._lib.emcg_device_surface_kat(self.h, int(boundary), kk.shape[1], _dp(kk),
+                                                  _dp(pp), int(step)))
+        return kk.T.copy(), pp.T.copy()
+
     def move(self, step=None):
         netto = np.zeros(max(self.nc, 1), np.int32)
         s = self.step_index if step is None else step
