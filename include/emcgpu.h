@@ -424,6 +424,11 @@ int32_t emcg_bulk_set_fixed_charges(emcg_handle *h, int32_t e, const double *pos
 int32_t emcg_bulk_get_coulomb(emcg_handle *h, int32_t e, double *force, double *potential);
 
 /* ---- single-particle kernels (known-answer tests of the reference) ----- */
+/* emcGrainScatterMechanism::scatterParticle (include/emcGrainScatterMechanism.hpp:
+   41-80) of model 0's grain mechanism for n independent wave vectors: k
+   (3 x n, SoA) in/out, Philox draws of a fixed key at `step`.  Runs in the
+   handle's precision; model 0 must have a grain mechanism. */
+int32_t emcg_grain_kat(emcg_handle *h, int64_t n, double *k, uint32_t step);
 /* drift() of include/emcParticleDrift.hpp:11-36 for n independent
    particles of valley v of model 0: k, pos (3 x n, SoA) and energy in/out,
    force 3 x n, dt per particle.  Runs in the handle's precision. */

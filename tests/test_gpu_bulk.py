@@ -882,3 +882,33 @@ def test_step_from_host_equals_upload_then_step(engine, steps_per_launch):
             assert np.array_equal(getattr(s0, f), getattr(ref[1], f)), f
             assert np.array_equal(getattr(s1, f), getattr(ref[2], f)), f
     assert ref[0][1, :, 0, 2].min() == st1.n
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_grain_mechanism_reference_kat(engine, precision):
+    """The reference's grain test (tests/testGrainScatterMechanism/
+    testGrainScatterMechanism.cpp:10-36) through the engine's grainScatter:
+    for its four initial wave vectors, 1000 draws each, a transmitted particle
+    keeps k . k0 >= 0 and a reflected one k . k0 <= 0, |k| unchanged (1e-10
+    relative; float rounding in FP32)."""
+    C_ = C
+    L = engine._lib.lib()
+    init = np.array([[1, 0, 0], [1, 1, 1], [-5, 6, 7], [-1, -2, -3]], float)
+    rtol = 1e-10 if precision == "fp64" else 1e-6
+    for prob, sign in ((1.0, 1), (0.0, -1)):  # always transmitted / always reflected
+        pt = engine.physics.silicon_electron("jacoboni", grain=(prob, 1e14))
+        spec = engine.EnsembleSpec(0, 16, 1e6, (1, 0, 0), (1e-6,) * 3, 1e-15, 5, 0)
+        b = engine.BulkBatch([pt], [spec], precision)
+        k0 = np.repeat(init, 1000, axis=0)
+        k = np.ascontiguousarray(k0.T).copy()
+        engine._lib.check(L.emcg_grain_kat(b.h, k.shape[1],
+                                           k.ctypes.data_as(C_.POINTER(C_.c_double)), 3))
+        k = k.T
+        dot = np.sum(k * k0, axis=1)
+        assert np.all(sign * dot >= 0), (prob, np.min(sign * dot))
+        n0, n1 = np.linalg.norm(k0, axis=1), np.linalg.norm(k, axis=1)
+        assert np.allclose(n1, n0, rtol=rtol, atol=0)
+        # the new directions spread over the hemisphere: cos uniform in [0, 1]
+        ct = sign * dot / (n0 * n1)
+        assert abs(ct.mean() - 0.5) < 0.03, ct.mean()
+        b.close()

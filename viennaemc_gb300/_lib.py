@@ -192,6 +192,8 @@ def _declare(L):
     L.emcg_host_free.argtypes = [vp]
     L.emcg_drift_kat.restype = i32
     L.emcg_drift_kat.argtypes = [vp, i32, i64, P(i32), P(d), P(d), P(d), P(d), P(d)]
+    L.emcg_grain_kat.restype = i32
+    L.emcg_grain_kat.argtypes = [vp, i64, P(d), u32]
     for name, args in _EXTRA_DECLS:
         if hasattr(L, name):
             fn = getattr(L, name)

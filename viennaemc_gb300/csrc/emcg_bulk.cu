@@ -2358,6 +2358,52 @@ extern "C" int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint3
   return EMCG_OK;
 }
 
+// grainScatter (emcGrainScatterMechanism::scatterParticle) of model 0 for n
+// independent wave vectors (known-answer tests of the reference)
+template <class T>
+__global__ void grainKatKernel(const ModelK<T> *__restrict__ models, int64_t n,
+                               double *__restrict__ k, uint32_t step) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  PhiloxSrc<T> rng;
+  rng.init((uint32_t)i, step, 0x47524149u, 0x5eedu, 0u);
+  T kk[3] = {(T)k[i], (T)k[n + i], (T)k[2 * n + i]};
+  grainScatter(models[0], kk, rng);
+  for (int j = 0; j < 3; j++)
+    k[j * n + i] = (double)kk[j];
+}
+
+extern "C" int32_t emcg_grain_kat(emcg_handle *h, int64_t n, double *k, uint32_t step) {
+  BulkImpl *b;
+  EMCG_TRY(bulkOf(h, &b));
+  EMCG_CHECK_ARG(n >= 0 && k, "bad grain arguments");
+  EMCG_CHECK_ARG(b->modelDescs[0].grain, "model 0 has no grain mechanism");
+  if (n == 0)
+    return EMCG_OK;
+  double *dK = nullptr;
+  EMCG_CUDA(cudaMalloc(&dK, 3 * n * sizeof(double)));
+  int32_t st = EMCG_OK;
+  if (cudaMemcpy(dK, k, 3 * n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+    st = EMCG_ERR_CUDA;
+  } else {
+    const int blocks = (int)((n + 127) / 128);
+    if (b->precision == EMCG_FP64)
+      grainKatKernel<double><<<blocks, 128, 0, b->stream>>>((const ModelK<double> *)b->dModels, n,
+                                                            dK, step);
+    else
+      grainKatKernel<float><<<blocks, 128, 0, b->stream>>>((const ModelK<float> *)b->dModels, n,
+                                                           dK, step);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(b->stream) != cudaSuccess ||
+        cudaMemcpy(k, dK, 3 * n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+      st = EMCG_ERR_CUDA;
+  }
+  if (st)
+    setError("grain known-answer kernel failed");
+  cudaFree(dK);
+  return st;
+}
+
 extern "C" int32_t emcg_drift_kat(emcg_handle *h, int32_t valley, int64_t n, const int32_t *sub,
                                   const double *dt, const double *force, double *k, double *pos,
                                   double *energy) {
