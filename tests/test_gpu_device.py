@@ -601,3 +601,36 @@ def test_surface_mechanisms_reference_kat(engine, precision):
     ct = k[:, 0] / np.linalg.norm(k, axis=1)
     assert abs(ct.mean() - 2 / 3) < 0.03, ct.mean()
     sim.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_grid_layout_through_the_field(engine, precision):
+    """The grid index layout of the reference's tests/testGrid (x fastest,
+    neighbours at +-1 and +-nx) seen through the E field
+    (include/PMSchemes/emcEFieldCalculation.hpp:13-81): with the potential
+    phi = y nx + x (thermal voltages), the interior field is -Vt / hx and
+    -nx Vt / hy; at the ohmic contacts (XMIN, XMAX) the normal field repeats
+    the neighbour's, at the artificial boundaries (YMIN, YMAX) it is 0."""
+    from viennaemc_gb300 import _lib as L
+    from viennaemc_gb300 import device as D
+    from viennaemc_gb300 import physics as P
+    dev = D.Device(P.silicon_material(), (20e-9, 10e-9), (1e-9, 2e-9))
+    dev.addConstantDopingRegion((0, 0), (20e-9, 10e-9), 1e24)
+    dev.addOhmicContact(D.XMIN, 0.0, (0,), (10e-9,))
+    dev.addOhmicContact(D.XMAX, 0.1, (0,), (10e-9,))
+    pt = P.silicon_electron("refbulk", n_levels=1000, max_energy=4.0)
+    sim = D.DeviceSimulation(dev, pt, scheme=D.NGP, dt=1e-15, seed=1, capacity=1 << 12,
+                             precision=precision)
+    nx, ny = dev.nx, dev.ny
+    assert (nx, ny) == (21, 6)
+    sim.set_grid(L.GRID_POTENTIAL, np.arange(nx * ny, dtype=float))
+    sim.efield()
+    ex = sim.get_grid(L.GRID_EX).reshape(ny, nx)
+    ey = sim.get_grid(L.GRID_EY).reshape(ny, nx)
+    Vt = dev.getThermalVoltage()
+    rtol = 1e-12 if precision == "fp64" else 1e-6
+    assert np.allclose(ex[:, 1:-1], -Vt / 1e-9, rtol=rtol, atol=0)
+    assert np.allclose(ey[1:-1, :], -nx * Vt / 2e-9, rtol=rtol, atol=0)
+    assert np.allclose(ex[:, 0], ex[:, 1], rtol=rtol) and np.allclose(ex[:, -1], ex[:, -2], rtol=rtol)
+    assert np.all(ey[0, 1:-1] == 0) and np.all(ey[-1, 1:-1] == 0)
+    sim.close()

@@ -126,3 +126,27 @@ def test_gpu_no_cutoff_and_edge_cases(engine, oracle):
         p2p.coulomb(pos, q, 1e9, box=0.0, images=1)
     with pytest.raises(_lib.EmcgError):
         p2p.coulomb(pos, q, -1.0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 1e-3)])
+def test_gpu_cutoff_radius_reference_kat(engine, precision, tol):
+    """The reference's cutoff test (tests/testCutOffRadius/testCutOffRadius.cpp:
+    46-116): two unit charges 0.17, 0.52 and 5.4 nm apart; below 1 nm the
+    distance is taken as 1 nm along the same direction.  Potential q / r and
+    force magnitudes |q^2 d / r^3| per component on both particles (1e-10
+    relative in FP64; float positions in FP32)."""
+    from viennaemc_gb300 import p2p
+    a = np.array([50e-9, 50e-9, 50e-9])
+    for b in ([50.1e-9, 50.1e-9, 50.1e-9], [50.5e-9, 50.1e-9, 50.1e-9],
+              [52e-9, 53e-9, 54e-9]):
+        b = np.array(b)
+        f, p = p2p.coulomb(np.stack([a, b], axis=1), np.ones(2), 1e9, precision=precision)
+        d = a - b
+        r = np.linalg.norm(d)
+        if r < 1e-9:
+            d, r = d * (1e-9 / r), 1e-9
+        exp_f, exp_p = np.abs(d) / r ** 3, 1.0 / r
+        for i in range(2):
+            assert abs(p[i] - exp_p) <= tol * exp_p, (b, i, p[i], exp_p)
+            assert np.allclose(np.abs(f[:, i]), exp_f, rtol=tol, atol=0), (b, i, f[:, i], exp_f)
