@@ -202,12 +202,14 @@ def test_philox_step_matches_oracle(engine, oracle, case, grain):
     sim.close()
 
 
-def test_full_device_steps_run_and_conserve_count(engine):
+@pytest.mark.parametrize("case", [DEVICE_CASES[0], "device_resistor_surface.npz"])
+def test_full_device_steps_run_and_conserve_count(engine, case):
     """performEMCStep end to end (Poisson -> E -> move -> contacts -> assign),
-    FP64 and FP32: particle count changes only by the contact flux."""
-    g = golden(DEVICE_CASES[0])
+    FP64 and FP32, also with surface mechanisms (the move kernels' surface
+    instances): particle count changes only by the contact flux."""
+    g = golden(case)
     for precision in ("fp64", "fp32"):
-        sim, dev, pt = _sim(engine, g, DEVICE_CASES[0], precision=precision, seed=3)
+        sim, dev, pt = _sim(engine, g, case, precision=precision, seed=3)
         sim.calcEquilibriumCharacteristics()
         n0 = sim.num_particles()
         netto = sim.performEMCStep(20)
