@@ -20,8 +20,8 @@ Q = 1.60219e-19
 EPS_R = 11.8
 
 
-def _setup(engine, oracle, n_el=1200, box=1e-7, seed=17):
-    m = oracle.silicon_model("jacoboni")
+def _setup(engine, oracle, n_el=1200, box=1e-7, seed=17, grain=None):
+    m = oracle.silicon_model("jacoboni", grain=grain)
     rng = oracle.RngState(oracle.RNG_MT, seed)
     # 1.2e24 m^-3 electrons on a (box / 8) grid
     st = m.bulk_init([box] * 3, [box / 8] * 3, n_el / box ** 3, rng)
@@ -39,17 +39,20 @@ def _engine_state(engine, st):
     return engine.ParticleState.from_arrays(**kw)
 
 
-def _batch(engine, n, box, precision, seed=321, stream=2, field=1e6):
-    pt = engine.physics.silicon_electron("jacoboni")
+def _batch(engine, n, box, precision, seed=321, stream=2, field=1e6, grain=None):
+    pt = engine.physics.silicon_electron("jacoboni", grain=grain)
     spec = engine.EnsembleSpec(0, n, field, (1, 0, 0), (box,) * 3, 1e-15, seed, stream)
     return engine.BulkBatch([pt], [spec], precision)
 
 
-def test_fp64_coulomb_steps_match_oracle(engine, oracle):
+@pytest.mark.parametrize("grain", [None, (0.5, 3e14)])
+def test_fp64_coulomb_steps_match_oracle(engine, oracle, grain):
+    """Also with a grain mechanism (grain events in the per-particle-force
+    steps of the Coulomb kernel)."""
     box = 1e-7
-    m, st, fixed, fq = _setup(engine, oracle)
+    m, st, fixed, fq = _setup(engine, oracle, grain=grain)
     assert st.n > 800
-    b = _batch(engine, st.n, box, "fp64")
+    b = _batch(engine, st.n, box, "fp64", grain=grain)
     b.set_state(0, _engine_state(engine, st))
     b.set_fixed_charges(0, fixed, fq)
     b.set_coulomb(EPS_R, 1e9, 0)
