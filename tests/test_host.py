@@ -236,3 +236,37 @@ def test_valley_coordinate_transformation_known_answers(name):
         assert np.all(np.abs(R.T @ ell - vec) <= 1e-9)
     with pytest.raises(ValueError):  # the reference refuses axes that are not orthogonal
         v.setSubValleyEllipseCoordSystem(0, (1, 0, 0), (1, 1, 0), (0, 0, 1))
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    """Every struct of include/emcgpu.h that the Python host fills has the
+    header's size and field offsets (a C program compiled against the header
+    prints them)."""
+    import subprocess
+    from viennaemc_gb300 import _lib
+    pairs = {"emcg_valley_desc": _lib.ValleyDesc, "emcg_mech_desc": _lib.MechDesc,
+             "emcg_tableset_desc": _lib.TablesetDesc, "emcg_model_desc": _lib.ModelDesc,
+             "emcg_ensemble_desc": _lib.EnsembleDesc, "emcg_state": _lib.StateDesc,
+             "emcg_state_f32": _lib.StateF32Desc, "emcg_device_desc": _lib.DeviceDesc,
+             "emcg_device_config": _lib.DeviceConfig}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "emcgpu.h"',
+             "int main(void) {"]
+    for cname, py in pairs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", f"-I{os.path.join(ROOT, 'include')}", str(src), "-o",
+                    str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    got = {}
+    for line in out.splitlines():
+        cname, f, v = line.split()
+        got[(cname, f)] = int(v)
+    for cname, py in pairs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
