@@ -325,8 +325,10 @@ int32_t emcg_get_launch(emcg_handle *h, int32_t *block_threads, int32_t *steps_p
    states are reproducible bit for bit, observables to float rounding. */
 int32_t emcg_set_scatter_mode(emcg_handle *h, int32_t queued);
 /* Tuning of the warp-asynchronous kernel: free flights a lane may take in one
-   drift pass before the warp checks its waiting lanes again, in [1, 20]
-   (default 6).  Only the schedule changes: particle states are the same bit
+   drift pass before the warp checks its waiting lanes again, in [1, 20]; 0
+   (the default) chooses by launch length: 5 below 100 steps per launch, 6
+   from there.  emcg_get_pass_actions gives the value of the last launch (or
+   the setting).  Only the schedule changes: particle states are the same bit
    for bit.  No reference counterpart. */
 int32_t emcg_set_pass_actions(emcg_handle *h, int32_t n);
 int32_t emcg_get_pass_actions(emcg_handle *h, int32_t *n);

@@ -605,7 +605,7 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(engine):
     cfg = b.autotune(10)
     assert cfg["steps_used"] == 260  # 13 float shapes x 10 steps, forward and backward
     assert cfg["block_threads"] in (128, 256) and cfg["min_blocks"] in (1, 3, 4)
-    assert cfg["queued"] in (0, 1, 2) and cfg["pass_actions"] in (3, 6)
+    assert cfg["queued"] in (0, 1, 2) and cfg["pass_actions"] in (3, 5, 6)
     o = b.step(20)
     b.close()
     b2 = _sweep_batch(engine)
@@ -736,9 +736,10 @@ def test_two_valley_kernels_equal_lockstep(engine, mode):
 
 
 def test_pass_actions_change_only_the_schedule(engine):
-    """Free flights per drift pass of the warp-asynchronous kernel (1, 5, the
-    default 6, 20): the same particle states bit for bit, the same counts, and
-    step sums equal to float rounding; out-of-range settings are refused."""
+    """Free flights per drift pass of the warp-asynchronous kernel (1, 5, 6,
+    20): the same particle states bit for bit, the same counts, and step sums
+    equal to float rounding; out-of-range settings are refused, and 0 returns
+    to the choice by launch length."""
     outs = []
     for n in (1, 5, 6, 20):
         b = _sweep_batch(engine)
@@ -756,9 +757,16 @@ def test_pass_actions_change_only_the_schedule(engine):
             for f in ("kx", "ky", "kz", "energy", "px", "py", "pz", "tau"):
                 assert np.array_equal(getattr(a, f), getattr(r, f)), f
     b = _sweep_batch(engine)
-    for bad in (0, 21):
+    for bad in (-1, 21):
         with pytest.raises(engine._lib.EmcgError):
             b.set_launch(pass_actions=bad)
+    # 0: chosen by launch length again (5 below 100 steps per launch, else 6)
+    b.set_launch(256, 20, 4, queued=2, pass_actions=0)
+    b.step(20)
+    assert b.pass_actions() == 5
+    b.set_launch(256, 200)
+    b.step(200)
+    assert b.pass_actions() == 6
     b.close()
 
 

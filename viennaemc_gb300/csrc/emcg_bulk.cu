@@ -674,6 +674,11 @@ constexpr int kEventBatch = 7;
 // 9.34e10, 7 9.28e10.  On the 64-ensemble sweep 5 was 3.6 % slower than 3, so
 // the autotuner tries 3 and 6.
 constexpr int kPassActions = 6;
+// the default for launches shorter than kShortLaunchSteps: measured on 2^20
+// electrons, one 20-step launch, L2 flushed (ms; 64 / 128 / 256 threads): 4
+// 0.3155 / 0.3159 / 0.3171, 5 0.3116 / 0.3108 / 0.3149, 6 0.3133 / 0.3128 /
+// 0.3170, 8 0.3256 / 0.3236 / 0.3278
+constexpr int kPassActionsShort = 5;
 // fixed-point scales of a warp's step sums: energy 2^-20 eV, velocity
 // 0.25 m/s per unit; below kFixMax per lane, 32 lanes stay within int32
 constexpr float kFixE = 1048576.f;
@@ -1047,6 +1052,7 @@ struct BulkImpl {
   int minBlocks = 1; // register cap variant of the step kernel (1, 3 or 4)
   int queued = 0; // step kernel: 0 lockstep, 1 block-queued, 2 warp-asynchronous (float)
   int passActions = kPassActions; // warp-asynchronous kernel: free flights per drift pass
+  bool passAuto = true;           // not set by the caller or the autotuner: by launch length
   int stepsPerLaunch = 0;
   int chunk = 16;
   uint64_t *dWords = nullptr;
@@ -1513,6 +1519,10 @@ static int32_t stepTyped(BulkImpl *b, int nSteps, uint32_t step0, double *obsHos
       b->blockThreads = want;
       b->tilesDirty = true;
     }
+  }
+  if (b->passAuto) {
+    const int first = std::min(b->stepsPerLaunch > 0 ? b->stepsPerLaunch : nSteps, nSteps);
+    b->passActions = first < kShortLaunchSteps ? kPassActionsShort : kPassActions;
   }
   EMCG_TRY(ensureTiles(b));
   const int Q = b->nVmax * 3;
@@ -2161,8 +2171,10 @@ extern "C" int32_t emcg_set_scatter_mode(emcg_handle *h, int32_t queued) {
 extern "C" int32_t emcg_set_pass_actions(emcg_handle *h, int32_t n) {
   BulkImpl *b;
   EMCG_TRY(bulkOf(h, &b));
-  EMCG_CHECK_ARG(n >= 1 && n <= kAsyncWindow, "pass actions must be in [1, %d]", kAsyncWindow);
-  b->passActions = n;
+  EMCG_CHECK_ARG(n >= 0 && n <= kAsyncWindow, "pass actions must be in [0, %d]", kAsyncWindow);
+  b->passAuto = n == 0;
+  if (n > 0)
+    b->passActions = n;
   return EMCG_OK;
 }
 
@@ -2312,7 +2324,9 @@ extern "C" int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint3
   constexpr int kCands = sizeof(cands) / sizeof(cands[0]);
   const int nCands = b->precision == EMCG_FP32 ? kCands : 8; // mode 2 is float only
   const int keepPer = b->stepsPerLaunch, keepPass = b->passActions;
+  const bool keepPassAuto = b->passAuto;
   b->autoBlock = false; // the tuner sets the block size
+  b->passAuto = false;  // and the free flights per pass of each shape
   b->stepsPerLaunch = trial_steps;
   double ms[kCands] = {};
   uint32_t s = step0;
@@ -2331,6 +2345,7 @@ extern "C" int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint3
     if (st != EMCG_OK) {
       b->stepsPerLaunch = keepPer;
       b->passActions = keepPass;
+      b->passAuto = keepPassAuto;
       return st;
     }
     ms[ci] += b->lastMs;
@@ -2346,6 +2361,7 @@ extern "C" int32_t emcg_bulk_autotune(emcg_handle *h, int32_t trial_steps, uint3
   b->minBlocks = bestC.minb;
   b->queued = bestC.queued;
   b->passActions = bestC.pass ? bestC.pass : keepPass;
+  b->passAuto = bestC.pass ? false : keepPassAuto;
   b->stepsPerLaunch = keepPer;
   if (steps_used)
     *steps_used = (int32_t)(s - step0);
