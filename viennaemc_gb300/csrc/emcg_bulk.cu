@@ -646,8 +646,8 @@ __global__ void bulkInitKernel(StateK<T> st, const ModelK<T> *__restrict__ model
 // go on flies freely to whichever comes first, the end of its current step
 // (then the end-of-step bookkeeping and its observables) or its next event
 // (then it waits); all of them run the drift together.  Once kEventBatch
-// lanes wait at events, or no lane can go on, a scatter pass scatters the
-// waiting lanes together.  The physics and the random numbers are those of
+// lanes wait at events (one, by measurement), or no lane can go on, a scatter
+// pass scatters the waiting lanes together.  The physics and the random numbers are those of
 // the lockstep kernel: the same free flights, the Philox counter (pid, step,
 // call) restarted at each step, the grain timer at each step end.
 // Observables: a lane writes its per-step values into its own column of a
@@ -663,10 +663,15 @@ __global__ void bulkInitKernel(StateK<T> st, const ModelK<T> *__restrict__ model
 // electrons, +1.4 % on the sweep against 20)
 constexpr int kAsyncWindow = 20;
 constexpr int kAsyncWindowOne = 24;
-// lanes of a warp that wait at an event before the warp scatters them together
-// (with five free flights per pass, 7 ran 0.9 % faster than 8 on 2^20
-// electrons and the same on the 64-ensemble sweep)
-constexpr int kEventBatch = 7;
+// lanes of a warp that wait at an event before the warp scatters them together.
+// With six free flights per pass and the 24-step window one is best: the warp
+// scatters as soon as a lane waits.  Measured on 2^20 electrons (ms per
+// launch, 20 steps / 500 steps) and the 64-ensemble sweep (500 steps, 3
+// flights per pass): 1 lane 0.3029 / 5.514 / 82.60, 2 0.3035 / 5.529, 3
+// 0.3049 / 5.527 / 83.03, 4 0.3052 / 5.520, 5 0.3076 / 5.531, 6 0.3100 /
+// 5.543, 7 0.3116 / 5.565 / 83.08 (7 was best with one or five flights per
+// pass and shorter windows)
+constexpr int kEventBatch = 1;
 // free flights a lane may take in one drift pass, by default (set per handle:
 // emcg_set_pass_actions).  Measured on 2^20 electrons, 2000 steps, 20-step
 // window: 3 gave 8.90e10, 4 9.00e10, 5 9.06e10, 6 9.02e10, 8 8.70e10, 20
